@@ -1,0 +1,285 @@
+"""Benchmark of the GB300 visibility pipeline (one JSON line on rank 0).
+
+Workload: the plain large configuration -- 4,096 instances of 8 seeded
+procedural meshes (~50M triangles before culling), 16 textured materials,
+one 1920x1080 main view + 4 shadow cascades, full frame: instance cull +
+prefix sum, meshlet cull, visibility raster, depth reduction, cascade fit,
+shadow cull + raster, lighting resolve.  A step is one frame.
+
+  value  device time of one frame (CUDA events on the frame's stream), L2
+         flushed between frames by writing a 256 MiB buffer (untimed)
+  e2e    the same frame through the C ABI with host buffers: per-frame
+         uniforms copied from pinned host memory, the HDR image read back to
+         pinned host memory, wall clock around both
+  cpu_baseline  the CPU oracle (C++ restatement of the reference shaders) on
+         the host cores, same scene, median of a few frames
+
+`--impl reference` times the reference's CPU path instead: the reference is a
+Vulkan renderer that cannot run here, so its shaders' CPU restatement (the
+oracle) stands in for it, with every host thread.
+
+Multi-GPU: the path does not shard (one view set per frame); under torchrun
+each rank renders an independent replica and value is the frame time
+(max over ranks).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "1080p frame ms (cull+raster+resolve)"
+
+# Algorithmic bytes per unit (per-stage rooflines).
+INSTANCE_BYTES = 112
+MESHLET_BYTES = 56
+PREFIX_ENTRY_BYTES = 8
+DRAW_WRITE_BYTES = 8 + 16
+VIS_PIXEL_BYTES = 8
+HDR_PIXEL_BYTES = 16
+
+
+def _env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def _clock_sampler():
+    """Sample SM clocks and throttle reasons during the timed region."""
+    q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+    try:
+        return subprocess.Popen(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits", "-lms", "200"],
+                                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+    except Exception:
+        return None
+
+
+def _clock_summary(proc, gpu_index):
+    if proc is None:
+        return None
+    try:
+        proc.terminate()
+        out, _ = proc.communicate(timeout=5)
+    except Exception:
+        return None
+    sms, maxes, reasons = [], [], set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for line in out.splitlines():
+        f = [x.strip() for x in line.split(",")]
+        if len(f) < 9 or f[0] != str(gpu_index):
+            continue
+        try:
+            sms.append(float(f[1]))
+            maxes.append(float(f[2]))
+        except ValueError:
+            continue
+        for n, v in zip(names, f[5:9]):
+            if v.lower() == "active":
+                reasons.add(n)
+    if not sms:
+        return None
+    sms.sort()
+    return {"sm_mhz": sms[len(sms) // 2], "sm_max_mhz": max(maxes), "reasons": sorted(reasons), "samples": len(sms)}
+
+
+def _measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_oracle_frames(scene, frames, threads=0):
+    from oracle import binding as ob
+    d = scene.desc
+    times, stages = [], []
+    for _ in range(frames):
+        fr = ob.run_scene(scene, shadow_size=d.shadow_size, max_instances=max(1024, d.n_instances), threads=threads)
+        times.append(fr.stage_ms["total"])
+        stages.append(fr.stage_ms)
+    n_threads = int(stages[-1]["threads"]) if stages else 0
+    s = sorted(times)
+    return s[len(s) // 2], n_threads, stages[-1] if stages else {}
+
+
+def run_reference(args):
+    rank, world, _ = _env_rank()
+    if rank != 0:
+        return 0
+    import lighthugger_gb300 as lh
+    from oracle import binding as ob
+    ob.lib()
+    scene = lh.Scene(args.config, seed=args.seed)
+    d = scene.desc
+    for _ in range(args.warmup):
+        ob.run_scene(scene, shadow_size=d.shadow_size, max_instances=max(1024, d.n_instances))
+    times = []
+    last = None
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        last = ob.run_scene(scene, shadow_size=d.shadow_size, max_instances=max(1024, d.n_instances))
+        times.append((time.perf_counter() - t0) * 1e3)
+    ms = sum(times) / len(times)
+    threads = int(last.stage_ms["threads"])
+    line = {
+        "impl": "reference", "metric": METRIC, "value": ms, "unit": "ms", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+        "config": {"workload": _workload_name(args.config, d), "seed": scene.seed},
+        "cpu_baseline": {"value": ms, "unit": "ms", "cores": threads, "kind": "port",
+                         "sample": "%d full frames of the workload on %d host threads" % (args.steps, threads)},
+        "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "stage_ms": {k: round(v, 3) for k, v in last.stage_ms.items() if k not in ("threads",)},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def _workload_name(cfg, d):
+    names = {1: "plain-small", 2: "plain-large", 3: "batched-views", 4: "differentiable-resolve", 5: "stress"}
+    return "%s: %d instances, %.1fM triangles before culling, %dx%d + 4 cascades %d^2" % (
+        names.get(cfg, str(cfg)), d.n_instances, d.total_triangles / 1e6, d.width, d.height, d.shadow_size)
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+    import lighthugger_gb300 as lh
+    from lighthugger_gb300 import build as native_build
+    rank, world, local_rank = _env_rank()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local_rank)
+    native_build.build()
+    scene = lh.Scene(args.config, seed=args.seed).upload(local_rank)
+    d = scene.desc
+    cap = max(1024, d.n_instances)
+    cfg = lh.Config(width=d.width, height=d.height, shadow_size=d.shadow_size, max_instances=cap, max_draws=2000000,
+                    device=local_rank)
+    r = lh.Renderer(cfg)
+    r.set_scene(scene)
+    stream = torch.cuda.Stream()
+    sptr = stream.cuda_stream
+    u = scene.uniforms
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(max(3, args.warmup)):
+        r.frame(u, stream=sptr)
+    torch.cuda.synchronize()
+    st = r.status()
+    # per-stage times (device events on the frame stream), one profiled frame per step
+    r.set_profiling(True)
+    stage_acc = {k: 0.0 for k in lh.STAGES}
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = _clock_sampler()
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(i))
+            ev[i][0].record(stream)
+        r.frame(u, stream=sptr)
+        with torch.cuda.stream(stream):
+            ev[i][1].record(stream)
+        for k, v in r.stage_times().items():
+            stage_acc[k] += v
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clk = _clock_summary(clocks, local_rank)
+    ms_steps = [a.elapsed_time(b) for a, b in ev]
+    ms = sum(ms_steps) / len(ms_steps)
+    stage_ms = {k: v / args.steps for k, v in stage_acc.items()}
+    r.set_profiling(False)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # e2e through the C ABI with host buffers
+    npx = d.width * d.height
+    host_hdr = torch.empty(npx * 16, dtype=torch.uint8, pin_memory=True)
+    e2e_times = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = r.frame(u, stream=sptr)
+        lh._check(lh.lib().lh_download(r.ctx, host_hdr.data_ptr(), out.hdr, npx * 16), "lh_download", r.ctx)
+        t1 = time.perf_counter()
+        if i >= args.warmup:
+            e2e_times.append((t1 - t0) * 1e3)
+    e2e_ms = sum(e2e_times) / len(e2e_times)
+
+    # roofline: the dominant stage among the HBM-bound ones
+    vis_inst = st.visible_instances[0]
+    cand = st.candidate_meshlets[0]
+    vis_ml = st.visible_opaque[0] + st.visible_alpha_clip[0]
+    cand_sh = sum(st.candidate_meshlets[1:5])
+    vis_sh = sum(st.visible_opaque[1:5])
+    algo = {
+        "cull_meshlets": cand * (MESHLET_BYTES + PREFIX_ENTRY_BYTES) + vis_ml * DRAW_WRITE_BYTES,
+        "shadow_cull_meshlets": cand_sh * (MESHLET_BYTES + PREFIX_ENTRY_BYTES) + vis_sh * DRAW_WRITE_BYTES,
+        "resolve": npx * (VIS_PIXEL_BYTES + HDR_PIXEL_BYTES),
+        "depth_fit": npx * VIS_PIXEL_BYTES,
+        "clear": npx * 8 + 4 * d.shadow_size ** 2 * 4,
+    }
+    dom = max(algo, key=lambda k: stage_ms.get(k, 0.0))
+    peak, peak_kind = _measured_peak_hbm()
+    achieved = algo[dom] / (stage_ms[dom] * 1e-3) / 1e9 if stage_ms.get(dom) else 0.0
+    tri_total = d.total_triangles
+    line = {
+        "metric": METRIC, "value": ms, "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded procedural scene, seed %d)" % scene.seed,
+        "config": {"workload": _workload_name(args.config, d), "l2": "flushed between frames (256 MiB write)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "gtri_per_s": tri_total / (ms * 1e-3) / 1e9,
+        "visible_meshlets": vis_ml, "candidate_meshlets": cand, "visible_instances": vis_inst,
+        "stage_ms": {k: round(v, 4) for k, v in stage_ms.items()},
+        "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": 560 + 8, "d2h_bytes_per_step": npx * 16},
+        "gpu_launches": 13 * args.steps,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                     "algorithmic_bytes": algo[dom]},
+        "status_flags": int(st.flags),
+    }
+    if clk:
+        line["clocks"] = clk
+    if rank == 0 and args.cpu_frames > 0:
+        med, threads, stages = cpu_oracle_frames(scene, args.cpu_frames)
+        line["cpu_baseline"] = {"value": med, "unit": "ms", "cores": threads, "kind": "port",
+                                "sample": "median of %d full frames of the workload" % args.cpu_frames,
+                                "speedup_vs_gpu_frame": med / ms}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", type=int, default=2)
+    ap.add_argument("--seed", type=int, default=None)
+    ap.add_argument("--cpu-frames", type=int, default=3)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

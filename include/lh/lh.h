@@ -1,0 +1,191 @@
+/*
+ * C ABI of the GB300 visibility pipeline.
+ *
+ * This is the drop-in boundary that replaces the reference's per-frame
+ * `render()` call (src/rendering.h:4-16, src/rendering.cpp:28-548) and the
+ * Vulkan objects behind it.  The reference enters its GPU passes through one
+ * 8-byte push constant holding the address of the `Uniforms` buffer
+ * (src/shaders/common/bindings.glsl:23-30, src/rendering.cpp:56-61); every
+ * scene buffer is then reached through device addresses stored in
+ * `Instance` / `MeshInfo` (src/shared_cpu_gpu.h:18-34,86-99).  Here the
+ * caller hands over the same `Instance` array (device pointer, records
+ * linking to caller-owned MeshInfo / vertex / meshlet buffers by device
+ * address) and one `Uniforms` struct per frame from host memory.
+ *
+ * Conventions:
+ *  - Ownership: the caller owns the scene buffers (like the reference's VMA
+ *    buffers); the context owns all scratch and outputs (prefix sectors,
+ *    visible lists, draw commands, visibility buffer, shadow maps, HDR).
+ *  - Errors: every entry point returns an lh_status; nothing aborts.
+ *    Device-side problems (capacity overflow, an expired bounded wait, a
+ *    malformed meshlet) are recorded in a status word read by lh_read_status.
+ *  - Threading: one context per host thread; work is stream ordered.
+ *  - `stream` arguments are CUDA streams (cudaStream_t) passed as void*;
+ *    NULL is the legacy default stream.
+ */
+#ifndef LH_LH_H
+#define LH_LH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "shared.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t lh_status;
+#define LH_OK 0
+#define LH_ERR_INVALID_ARGUMENT 1
+#define LH_ERR_CUDA 2
+#define LH_ERR_OUT_OF_MEMORY 3
+#define LH_ERR_CAPACITY 4
+#define LH_ERR_TIMEOUT 5
+#define LH_ERR_NO_SCENE 6
+#define LH_ERR_UNSUPPORTED 7
+
+/* Device status flags (lh_device_status.flags). */
+#define LH_FLAG_INSTANCE_OVERFLOW 0x1u /* more visible instances than max_instances */
+#define LH_FLAG_DRAW_OVERFLOW 0x2u     /* more visible meshlets than max_draws */
+#define LH_FLAG_QUEUE_OVERFLOW 0x4u    /* raster big-triangle queue full: triangles dropped */
+#define LH_FLAG_TIMEOUT 0x8u           /* a bounded device-side wait expired */
+#define LH_FLAG_BAD_MESHLET 0x10u      /* micro index >= meshlet vertex count: triangle skipped */
+#define LH_FLAG_NO_DEPTH 0x20u         /* every main-view pixel is sky: cascades are NaN */
+#define LH_FLAG_SLOT_OVERFLOW 0x40u    /* a draw slot does not fit the 24-bit visibility ID */
+
+/* Rasterisation rules shared by every raster kernel (and restated by the
+ * CPU oracle).  Vertices are snapped to 1/256 pixel; a pixel is covered when
+ * its centre is inside the triangle under the top-left rule; triangles with
+ * a vertex outside |x|,|y| <= LH_GUARD_BAND * w or outside 0 <= z <= w are
+ * clipped in clip space first. */
+#define LH_SUBPIXEL_BITS 8
+#define LH_GUARD_BAND 256.0f
+
+/* Texture descriptor: RGBA8 texels, row major, repeat addressing, bilinear
+ * filtering of level 0.  `texels` is a device address for lh_set_scene. */
+typedef struct lh_texture {
+    uint64_t texels;
+    uint32_t width;
+    uint32_t height;
+    uint32_t srgb; /* 1: RGB channels are sRGB encoded (decoded before filtering) */
+    uint32_t reserved;
+} lh_texture;
+
+typedef struct lh_config {
+    uint32_t width;           /* main view, pixels */
+    uint32_t height;
+    uint32_t shadow_size;     /* edge of each of the 4 cascade maps (1024 in the reference) */
+    uint32_t max_instances;   /* prefix-sector capacity (MAX_INSTANCES = 1024 in the reference) */
+    uint32_t max_draws;       /* visible meshlets per class per view (MAX_OPAQUE_DRAWS) */
+    uint32_t max_big_triangles; /* raster overflow queue; 0 = default */
+    uint32_t max_probes;      /* probe views for lh_frame_batched; 0 = none */
+    uint32_t max_probe_pixels; /* total pixels over all probe views */
+    int32_t device;           /* CUDA device ordinal */
+    uint32_t flags;           /* reserved, 0 */
+} lh_config;
+
+/* Device pointers to the context-owned results of the last frame. */
+typedef struct lh_frame_out {
+    uint64_t visibility;   /* u64[height][width]: (float bits of depth << 32) | packed ID; 0 = clear */
+    uint64_t hdr;          /* float4[height][width]: linear HDR radiance, alpha = 1 */
+    uint64_t shadow_maps;  /* float[4][shadow_size][shadow_size]: cascade depth, clear 1.0 */
+    uint64_t misc_storage; /* MiscStorage */
+    uint64_t prefix_sums;  /* n_views prefix sectors of prefix_sector_bytes each */
+    uint64_t meshlet_references; /* n_views sections of 2*max_draws MeshletReference */
+    uint64_t draw_calls;   /* n_views sections: {u32 num_opaque, u32 num_alpha_clip, DrawIndirectCommand[2*max_draws]} */
+    uint64_t probe_visibility; /* u64 visibility of all probe views, packed back to back */
+    uint64_t prefix_sector_bytes;
+    uint64_t draw_call_section_bytes;
+    uint32_t width, height, shadow_size, max_instances, max_draws;
+    uint32_t n_views;      /* 5 for lh_frame: main, cascade 0..3 */
+    uint32_t n_probes;
+    uint32_t reserved;
+} lh_frame_out;
+
+typedef struct lh_device_status {
+    uint32_t flags;
+    uint32_t n_views;
+    uint32_t visible_instances[40];  /* per view: entries in the prefix sector */
+    uint32_t candidate_meshlets[40]; /* per view: inclusive total of the sector */
+    uint32_t visible_opaque[40];     /* per view: num_opaque */
+    uint32_t visible_alpha_clip[40]; /* per view: num_alpha_clip */
+    uint32_t big_triangles;          /* triangles sent to the tiled raster path */
+    uint32_t clipped_triangles;      /* triangles sent to the clipper */
+} lh_device_status;
+
+typedef struct lh_ctx lh_ctx;
+
+/* Library version, for load checks. */
+uint32_t lh_version(void);
+
+/* Create a context: allocates every scratch and output buffer from the
+ * capacities in `config` (replaces Resources / InstanceResources,
+ * src/frame_resources.h:7-93, src/main.cpp:442-532). */
+lh_status lh_create(const lh_config* config, lh_ctx** out_ctx);
+
+/* Bind the scene: `d_instances` is a device array of n Instance records whose
+ * mesh_info_address fields are device addresses (src/main.cpp:433-440);
+ * `textures` is a host array of descriptors with device texel addresses,
+ * indexed by MeshInfo texture indices (replaces the bindless texture array,
+ * src/shaders/common/bindings.glsl:7, src/descriptor_set.cpp:28-139). */
+lh_status lh_set_scene(lh_ctx* ctx, const Instance* d_instances, uint32_t n,
+                       const lh_texture* textures, uint32_t n_textures);
+
+/* One frame (src/rendering.cpp:79-474): instance cull + prefix sum, meshlet
+ * cull, visibility raster, depth reduction, cascade fit, shadow cull +
+ * raster, lighting resolve.  `host_uniforms` is read during the call;
+ * the address fields in it are ignored (the context supplies its own
+ * buffers).  Asynchronous with respect to the host. */
+lh_status lh_frame(lh_ctx* ctx, const Uniforms* host_uniforms, void* stream,
+                   lh_frame_out* out);
+
+/* Batched form: main view, 4 cascades and n_probes probe views (each probe
+ * described by its own Uniforms: matrices, camera and window_size).  Cull
+ * and raster of all views run in one persistent launch. */
+lh_status lh_frame_batched(lh_ctx* ctx, const Uniforms* host_uniforms,
+                           const Uniforms* probe_uniforms, uint32_t n_probes,
+                           void* stream, lh_frame_out* out);
+
+/* Pointers to the context's result buffers (valid until lh_destroy). */
+lh_status lh_get_outputs(lh_ctx* ctx, lh_frame_out* out);
+
+/* Synchronise the context's last stream and read the device status. */
+lh_status lh_read_status(lh_ctx* ctx, lh_device_status* out);
+
+/* Launch-shape knobs of the raster and cull kernels (set by the autotuner,
+ * lighthugger_gb300/autotune.py).  Results never depend on them. */
+typedef struct lh_tuning {
+    uint32_t small_px;        /* a lane rasterises triangles whose bbox has <= small_px pixels */
+    uint32_t medium_px;       /* the warp rasterises up to medium_px; larger go to 16-row bands */
+    float cull_blocks_per_sm; /* persistent meshlet-cull blocks per SM */
+    uint32_t reserved;
+} lh_tuning;
+
+lh_status lh_set_tuning(lh_ctx* ctx, const lh_tuning* tuning);
+lh_status lh_get_tuning(lh_ctx* ctx, lh_tuning* tuning);
+
+/* Per-stage timing with CUDA events recorded on the frame's stream (the
+ * replacement of the reference's Tracy GPU zones, src/rendering.cpp:41-42,
+ * 140-492).  Stages: 0 clear, 1 cull instances, 2 cull meshlets, 3 raster,
+ * 4 depth reduce + cascade fit, 5 shadow instance cull, 6 shadow meshlet
+ * cull, 7 shadow raster, 8 resolve. */
+#define LH_N_STAGES 9
+lh_status lh_set_profiling(lh_ctx* ctx, int enable);
+/* Milliseconds of each stage of the last profiled frame (synchronises). */
+lh_status lh_get_stage_times(lh_ctx* ctx, float* ms, uint32_t n);
+
+/* Synchronise the context's last stream and copy `bytes` from a device
+ * address (e.g. a field of lh_frame_out) to host memory. */
+lh_status lh_download(lh_ctx* ctx, void* host_dst, uint64_t device_src, size_t bytes);
+
+/* Human-readable text of the last host-side error of this context. */
+const char* lh_last_error(lh_ctx* ctx);
+
+void lh_destroy(lh_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LH_LH_H */

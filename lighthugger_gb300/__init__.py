@@ -1,0 +1,360 @@
+"""GB300 visibility pipeline: Python host mirror of the C ABI (include/lh/lh.h).
+
+The reference drives its GPU passes from C++ (`render()`, src/rendering.cpp:28)
+with a `Uniforms` struct per frame and device-address-linked scene buffers.
+This module exposes the same operator boundary to Python through ctypes:
+
+    scene = Scene(config_id=2, seed=20261205)    # seeded synthetic scene (host + device copy)
+    r = Renderer(Config(width=1920, height=1080, shadow_size=1024, max_instances=4096))
+    r.set_scene(scene)
+    r.frame(scene.uniforms)                       # cull -> raster -> depth -> cascades -> shadows -> resolve
+    vis = r.visibility()                          # numpy u64 [H, W]
+
+The native library must be present (built by lighthugger_gb300.build); there
+is no CPU fallback -- a missing library raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "liblh.so")
+
+LH_OK = 0
+STATUS_NAMES = {0: "OK", 1: "INVALID_ARGUMENT", 2: "CUDA", 3: "OUT_OF_MEMORY", 4: "CAPACITY", 5: "TIMEOUT",
+                6: "NO_SCENE", 7: "UNSUPPORTED"}
+
+FLAG_INSTANCE_OVERFLOW = 0x1
+FLAG_DRAW_OVERFLOW = 0x2
+FLAG_QUEUE_OVERFLOW = 0x4
+FLAG_TIMEOUT = 0x8
+FLAG_BAD_MESHLET = 0x10
+FLAG_NO_DEPTH = 0x20
+
+STAGES = ["clear", "cull_instances", "cull_meshlets", "raster", "depth_fit", "shadow_cull_instances",
+          "shadow_cull_meshlets", "shadow_raster", "resolve"]
+
+UNIFORMS_BYTES = 560
+MISC_BYTES = 792
+INSTANCE_BYTES = 112
+
+
+class LHError(RuntimeError):
+    def __init__(self, status, what, detail=""):
+        super().__init__("%s failed: %s%s" % (what, STATUS_NAMES.get(status, status), (" (%s)" % detail) if detail else ""))
+        self.status = status
+
+
+class Config(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("shadow_size", C.c_uint32),
+                ("max_instances", C.c_uint32), ("max_draws", C.c_uint32), ("max_big_triangles", C.c_uint32),
+                ("max_probes", C.c_uint32), ("max_probe_pixels", C.c_uint32), ("device", C.c_int32),
+                ("flags", C.c_uint32)]
+
+
+class Texture(C.Structure):
+    _fields_ = [("texels", C.c_uint64), ("width", C.c_uint32), ("height", C.c_uint32), ("srgb", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
+class FrameOut(C.Structure):
+    _fields_ = [("visibility", C.c_uint64), ("hdr", C.c_uint64), ("shadow_maps", C.c_uint64),
+                ("misc_storage", C.c_uint64), ("prefix_sums", C.c_uint64), ("meshlet_references", C.c_uint64),
+                ("draw_calls", C.c_uint64), ("probe_visibility", C.c_uint64), ("prefix_sector_bytes", C.c_uint64),
+                ("draw_call_section_bytes", C.c_uint64), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("shadow_size", C.c_uint32), ("max_instances", C.c_uint32), ("max_draws", C.c_uint32),
+                ("n_views", C.c_uint32), ("n_probes", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class DeviceStatus(C.Structure):
+    _fields_ = [("flags", C.c_uint32), ("n_views", C.c_uint32), ("visible_instances", C.c_uint32 * 40),
+                ("candidate_meshlets", C.c_uint32 * 40), ("visible_opaque", C.c_uint32 * 40),
+                ("visible_alpha_clip", C.c_uint32 * 40), ("big_triangles", C.c_uint32),
+                ("clipped_triangles", C.c_uint32)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("small_px", C.c_uint32), ("medium_px", C.c_uint32), ("cull_blocks_per_sm", C.c_float),
+                ("reserved", C.c_uint32)]
+
+
+class SceneParams(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("n_instances", C.c_uint32), ("n_probes", C.c_uint32),
+                ("detail", C.c_float), ("quantized", C.c_uint32), ("reference_normal_transform", C.c_uint32),
+                ("alpha_clip_materials", C.c_uint32), ("reserved", C.c_uint32 * 4)]
+
+
+Uniforms = C.c_uint8 * UNIFORMS_BYTES
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("config_id", C.c_uint32), ("n_instances", C.c_uint32), ("n_meshes", C.c_uint32),
+                ("n_textures", C.c_uint32), ("n_probes", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("shadow_size", C.c_uint32), ("total_meshlets", C.c_uint64), ("total_triangles", C.c_uint64),
+                ("seed", C.c_uint64), ("host_instances", C.c_void_p), ("host_textures", C.POINTER(Texture)),
+                ("device_instances", C.c_void_p), ("device_textures", C.POINTER(Texture)), ("uniforms", Uniforms),
+                ("probes", C.c_void_p), ("device_bytes", C.c_uint64)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("yaw", C.c_float), ("pitch", C.c_float), ("fov_degrees", C.c_float),
+                ("sun_latitude", C.c_float), ("sun_longitude", C.c_float), ("width", C.c_uint32),
+                ("height", C.c_uint32), ("shadow_cam_distance", C.c_float), ("cascade_split_pow", C.c_float),
+                ("num_instances", C.c_uint32)]
+
+
+_lib = None
+
+
+def lib():
+    """Load the native library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("native library %s is missing: run lighthugger_gb300.build.build()" % LIB_PATH)
+    L = C.CDLL(LIB_PATH)
+    P = C.c_void_p
+    L.lh_version.restype = C.c_uint32
+    L.lh_create.argtypes = [C.POINTER(Config), C.POINTER(P)]
+    L.lh_set_scene.argtypes = [P, P, C.c_uint32, C.POINTER(Texture), C.c_uint32]
+    L.lh_frame.argtypes = [P, P, P, C.POINTER(FrameOut)]
+    L.lh_frame_batched.argtypes = [P, P, P, C.c_uint32, P, C.POINTER(FrameOut)]
+    L.lh_get_outputs.argtypes = [P, C.POINTER(FrameOut)]
+    L.lh_read_status.argtypes = [P, C.POINTER(DeviceStatus)]
+    L.lh_download.argtypes = [P, P, C.c_uint64, C.c_size_t]
+    L.lh_last_error.argtypes = [P]
+    L.lh_last_error.restype = C.c_char_p
+    L.lh_destroy.argtypes = [P]
+    L.lh_destroy.restype = None
+    L.lh_set_profiling.argtypes = [P, C.c_int]
+    L.lh_get_stage_times.argtypes = [P, C.POINTER(C.c_float), C.c_uint32]
+    L.lh_set_tuning.argtypes = [P, C.POINTER(Tuning)]
+    L.lh_get_tuning.argtypes = [P, C.POINTER(Tuning)]
+    L.lh_scene_create.argtypes = [C.c_uint32, C.c_uint64, C.POINTER(SceneParams), C.POINTER(P)]
+    L.lh_scene_describe.argtypes = [P, C.POINTER(SceneDesc)]
+    L.lh_scene_upload.argtypes = [P, C.c_int]
+    L.lh_scene_destroy.argtypes = [P]
+    L.lh_scene_destroy.restype = None
+    L.lh_make_uniforms.argtypes = [C.POINTER(Camera), C.POINTER(Uniforms)]
+    for name in ("lh_create", "lh_set_scene", "lh_frame", "lh_frame_batched", "lh_get_outputs", "lh_read_status",
+                 "lh_download", "lh_set_profiling", "lh_get_stage_times", "lh_set_tuning", "lh_get_tuning", "lh_scene_create", "lh_scene_describe",
+                 "lh_scene_upload", "lh_make_uniforms"):
+        getattr(L, name).restype = C.c_int32
+    _lib = L
+    return L
+
+
+def _check(st, what, ctx=None):
+    if st != LH_OK:
+        detail = ""
+        if ctx:
+            detail = (lib().lh_last_error(ctx) or b"").decode(errors="replace")
+        raise LHError(st, what, detail)
+
+
+def default_seed(config_id):
+    return 20261203 + config_id
+
+
+class Scene:
+    """A seeded synthetic scene (lh_scene_create); `upload()` makes the device copy."""
+
+    def __init__(self, config_id, seed=None, **params):
+        self.config_id = config_id
+        self.seed = default_seed(config_id) if seed is None else seed
+        p = SceneParams()
+        for k, v in params.items():
+            if v is not None:
+                setattr(p, k, v)
+        h = C.c_void_p()
+        _check(lib().lh_scene_create(config_id, self.seed, C.byref(p), C.byref(h)), "lh_scene_create")
+        self.handle = h
+        self.params = params
+        self._describe()
+
+    def _describe(self):
+        d = SceneDesc()
+        _check(lib().lh_scene_describe(self.handle, C.byref(d)), "lh_scene_describe")
+        self.desc = d
+
+    def upload(self, device=0):
+        _check(lib().lh_scene_upload(self.handle, device), "lh_scene_upload")
+        self._describe()
+        return self
+
+    @property
+    def uniforms(self):
+        u = Uniforms()
+        C.memmove(u, self.desc.uniforms, UNIFORMS_BYTES)
+        return u
+
+    def probe_uniforms(self):
+        n = self.desc.n_probes
+        arr = (Uniforms * max(n, 1))()
+        if n:
+            C.memmove(arr, self.desc.probes, UNIFORMS_BYTES * n)
+        return arr, n
+
+    def host_instances_ptr(self):
+        return self.desc.host_instances
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().lh_scene_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def make_uniforms(position, yaw, pitch, fov_degrees, width, height, num_instances, sun_latitude=-5.6,
+                  sun_longitude=1.37, shadow_cam_distance=1024.0, cascade_split_pow=3.0):
+    """Host uniform math of src/main.cpp:734-760 (lookAt + infinite reverse-Z)."""
+    cam = Camera()
+    cam.position[:] = position
+    cam.yaw, cam.pitch, cam.fov_degrees = yaw, pitch, fov_degrees
+    cam.sun_latitude, cam.sun_longitude = sun_latitude, sun_longitude
+    cam.width, cam.height = width, height
+    cam.shadow_cam_distance, cam.cascade_split_pow = shadow_cam_distance, cascade_split_pow
+    cam.num_instances = num_instances
+    u = Uniforms()
+    _check(lib().lh_make_uniforms(C.byref(cam), C.byref(u)), "lh_make_uniforms")
+    return u
+
+
+def uniforms_fields(u):
+    """Numpy view of the matrix / vector fields of a Uniforms blob."""
+    b = np.frombuffer(bytes(u), dtype=np.uint8)
+    f = b[:448].view(np.float32).reshape(7, 4, 4)
+    names = ["combined_perspective_view", "inv_perspective_view", "view", "initial_view", "perspective",
+             "perspective_inverse", "view_inverse"]
+    out = {n: f[i] for i, n in enumerate(names)}
+    v = b[496:532].view(np.float32)
+    out["camera_pos"], out["sun_dir"], out["sun_intensity"] = v[0:3], v[3:6], v[6:9]
+    out["num_instances"] = int(b[532:536].view(np.uint32)[0])
+    out["window_size"] = tuple(int(x) for x in b[536:544].view(np.uint32))
+    out["shadow_cam_distance"], out["cascade_split_pow"] = (float(x) for x in b[544:552].view(np.float32))
+    return out
+
+
+class Renderer:
+    """One lh_ctx: owns scratch and outputs; `frame()` enqueues one frame."""
+
+    def __init__(self, config):
+        h = C.c_void_p()
+        _check(lib().lh_create(C.byref(config), C.byref(h)), "lh_create")
+        self.ctx = h
+        self.config = config
+        self.out = FrameOut()
+        self.stream = None
+
+    def set_scene(self, scene):
+        d = scene.desc
+        if not d.device_instances:
+            raise ValueError("scene is not uploaded")
+        _check(lib().lh_set_scene(self.ctx, d.device_instances, d.n_instances, d.device_textures, d.n_textures),
+               "lh_set_scene", self.ctx)
+        self.scene = scene
+
+    def set_tuning(self, small_px=None, medium_px=None, cull_blocks_per_sm=None):
+        t = self.tuning()
+        if small_px is not None:
+            t.small_px = small_px
+        if medium_px is not None:
+            t.medium_px = medium_px
+        if cull_blocks_per_sm is not None:
+            t.cull_blocks_per_sm = cull_blocks_per_sm
+        _check(lib().lh_set_tuning(self.ctx, C.byref(t)), "lh_set_tuning", self.ctx)
+
+    def set_profiling(self, enable=True):
+        _check(lib().lh_set_profiling(self.ctx, 1 if enable else 0), "lh_set_profiling", self.ctx)
+
+    def stage_times(self):
+        ms = (C.c_float * len(STAGES))()
+        _check(lib().lh_get_stage_times(self.ctx, ms, len(STAGES)), "lh_get_stage_times", self.ctx)
+        return dict(zip(STAGES, [float(x) for x in ms]))
+
+    def tuning(self):
+        t = Tuning()
+        _check(lib().lh_get_tuning(self.ctx, C.byref(t)), "lh_get_tuning", self.ctx)
+        return t
+
+    def frame(self, uniforms, stream=None):
+        s = stream if stream is not None else self.stream
+        _check(lib().lh_frame(self.ctx, C.byref(uniforms), s, C.byref(self.out)), "lh_frame", self.ctx)
+        return self.out
+
+    def frame_batched(self, uniforms, probes, n_probes, stream=None):
+        s = stream if stream is not None else self.stream
+        _check(lib().lh_frame_batched(self.ctx, C.byref(uniforms), probes if n_probes else None, n_probes, s,
+                                      C.byref(self.out)), "lh_frame_batched", self.ctx)
+        return self.out
+
+    def status(self):
+        st = DeviceStatus()
+        _check(lib().lh_read_status(self.ctx, C.byref(st)), "lh_read_status", self.ctx)
+        return st
+
+    def download(self, device_ptr, nbytes, dtype=np.uint8):
+        buf = np.empty(nbytes, dtype=np.uint8)
+        if nbytes:
+            _check(lib().lh_download(self.ctx, buf.ctypes.data, device_ptr, nbytes), "lh_download", self.ctx)
+        return buf.view(dtype)
+
+    # ---- typed result accessors (synchronising)
+    def visibility(self):
+        o = self.out
+        return self.download(o.visibility, o.width * o.height * 8, np.uint64).reshape(o.height, o.width)
+
+    def hdr(self):
+        o = self.out
+        return self.download(o.hdr, o.width * o.height * 16, np.float32).reshape(o.height, o.width, 4)
+
+    def shadow_maps(self):
+        o = self.out
+        S = o.shadow_size
+        return self.download(o.shadow_maps, 4 * S * S * 4, np.float32).reshape(4, S, S)
+
+    def misc(self):
+        return self.download(self.out.misc_storage, MISC_BYTES)
+
+    def prefix_sector(self, view):
+        o = self.out
+        raw = self.download(o.prefix_sums + view * o.prefix_sector_bytes, o.prefix_sector_bytes)
+        return raw
+
+    def draw_section(self, view):
+        o = self.out
+        return self.download(o.draw_calls + view * o.draw_call_section_bytes, o.draw_call_section_bytes)
+
+    def meshlet_references(self, view):
+        o = self.out
+        n = 2 * o.max_draws
+        return self.download(o.meshlet_references + view * n * 8, n * 8)
+
+    def probe_visibility(self, probes, n_probes):
+        """List of u64 [h, w] arrays, one per probe (packed back to back, 32-pixel aligned)."""
+        out, off = [], 0
+        for p in range(n_probes):
+            f = uniforms_fields(probes[p])
+            w, h = f["window_size"]
+            a = self.download(self.out.probe_visibility + off * 8, w * h * 8, np.uint64).reshape(h, w)
+            out.append(a)
+            off += (w * h + 31) // 32 * 32
+        return out
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            lib().lh_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

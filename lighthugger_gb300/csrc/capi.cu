@@ -1,0 +1,556 @@
+// C ABI of the visibility pipeline: context, buffers and the stream-ordered
+// frame that replaces src/rendering.cpp:28-474 (render()).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "lh/lh.h"
+#include "lh_internal.cuh"
+
+using namespace lh;
+
+namespace {
+
+constexpr uint32_t kVersion = 1;
+
+struct Alloc {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+}  // namespace
+
+struct lh_ctx {
+    lh_config cfg{};
+    int device = 0;
+    int sms = 0;
+    std::string err;
+    std::vector<Alloc> allocs;
+    // fixed buffers
+    Uniforms* d_uniforms = nullptr;  // [0] main, [1..max_probes] probes
+    float* d_consts = nullptr;       // frame constants
+    float* d_srgb = nullptr;
+    MiscStorage* d_misc = nullptr;
+    uint32_t* d_status = nullptr;
+    uint8_t* d_sectors = nullptr;
+    MeshletReference* d_refs = nullptr;
+    uint8_t* d_draws = nullptr;
+    uint64_t* d_vis = nullptr;
+    float* d_shadow = nullptr;
+    float4* d_hdr = nullptr;
+    uint64_t* d_probe_vis = nullptr;
+    BigTri* d_big = nullptr;
+    ClipItem* d_clip = nullptr;
+    ViewDev* d_views = nullptr;
+    lh_texture* d_textures = nullptr;
+    uint32_t n_textures = 0;
+    // per-frame zeroed scratch (look-back words and tile claims)
+    uint8_t* d_reset = nullptr;
+    size_t reset_bytes = 0;
+    size_t sector_bytes = 0, draw_bytes = 0;
+    uint32_t max_views = 0;
+    // scene
+    const Instance* instances = nullptr;
+    uint32_t n_instances = 0;
+    uint64_t scene_meshlets = 0;
+    // host staging for per-frame constants (pinned, double buffered)
+    uint8_t* h_staging[2] = {nullptr, nullptr};
+    cudaEvent_t staging_done[2] = {nullptr, nullptr};
+    size_t staging_bytes = 0;
+    uint32_t frame_index = 0;
+    uint32_t n_views_last = 5;
+    uint32_t n_probes_last = 0;
+    cudaStream_t last_stream = nullptr;
+    std::vector<ViewDev> h_views;
+    lh_tuning tuning{};
+    // stage timing
+    bool profiling = false;
+    cudaEvent_t stage_ev[LH_N_STAGES + 1] = {};
+    // graph
+    cudaGraphExec_t graph_exec = nullptr;
+    uint32_t graph_probes = 0;
+};
+
+namespace {
+
+lh_status fail(lh_ctx* c, lh_status st, const std::string& msg) {
+    if (c) c->err = msg;
+    return st;
+}
+
+lh_status cuda_fail(lh_ctx* c, cudaError_t e, const char* what) {
+    return fail(c, e == cudaErrorMemoryAllocation ? LH_ERR_OUT_OF_MEMORY : LH_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <class T>
+cudaError_t dalloc(lh_ctx* c, T** out, size_t bytes) {
+    void* p = nullptr;
+    size_t b = align_up(std::max<size_t>(bytes, 16), 256);
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e != cudaSuccess) return e;
+    c->allocs.push_back({p, b});
+    *out = reinterpret_cast<T*>(p);
+    return cudaSuccess;
+}
+
+void free_all(lh_ctx* c) {
+    for (auto& ev : c->stage_ev)
+        if (ev) { cudaEventDestroy(ev); ev = nullptr; }
+    if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+    c->graph_exec = nullptr;
+    for (auto& a : c->allocs) cudaFree(a.p);
+    c->allocs.clear();
+    for (int i = 0; i < 2; i++) {
+        if (c->h_staging[i]) cudaFreeHost(c->h_staging[i]);
+        if (c->staging_done[i]) cudaEventDestroy(c->staging_done[i]);
+        c->h_staging[i] = nullptr;
+        c->staging_done[i] = nullptr;
+    }
+}
+
+// View order: 0 main, 1..n_probes probes, then cascades 0..3.
+void build_views(lh_ctx* c, uint32_t n_probes, const Uniforms* probe_uniforms) {
+    const lh_config& cfg = c->cfg;
+    c->h_views.clear();
+    size_t probe_off = 0;
+    uint32_t n_views = 5 + n_probes;
+    uint32_t n_inst_tiles = (c->n_instances + kInstTile - 1) / kInstTile + 1;
+    uint32_t ml_tiles = (uint32_t)((c->scene_meshlets + kMlTile - 1) / kMlTile) + 1;
+    size_t per_view = align_up(16 + 8 * (size_t)n_inst_tiles + 8 * (size_t)ml_tiles, 256);
+    for (uint32_t v = 0; v < n_views; v++) {
+        ViewDev vw{};
+        bool cascade = v >= 1 + n_probes;
+        vw.kind = cascade ? kViewShadow : kViewVisibility;
+        vw.cascade = cascade ? v - 1 - n_probes : 0;
+        if (v == 0) {
+            vw.width = cfg.width;
+            vw.height = cfg.height;
+            vw.target = c->d_vis;
+            vw.uniforms = c->d_uniforms;
+        } else if (!cascade) {
+            const Uniforms& pu = probe_uniforms[v - 1];
+            vw.width = pu.window_size.x;
+            vw.height = pu.window_size.y;
+            vw.target = c->d_probe_vis + probe_off;
+            probe_off += align_up((size_t)vw.width * vw.height, 32);
+            vw.uniforms = c->d_uniforms + v;
+        } else {
+            vw.width = vw.height = cfg.shadow_size;
+            vw.target = c->d_shadow + (size_t)vw.cascade * cfg.shadow_size * cfg.shadow_size;
+            vw.uniforms = c->d_uniforms;
+        }
+        vw.sector = c->d_sectors + v * c->sector_bytes;
+        vw.refs = c->d_refs + (size_t)v * 2 * cfg.max_draws;
+        vw.draws = c->d_draws + v * c->draw_bytes;
+        vw.section_base = v * 2 * cfg.max_draws;
+        uint8_t* r = c->d_reset + kStWords * 4 + v * per_view;
+        vw.claim = reinterpret_cast<uint32_t*>(r);
+        vw.inst_status = reinterpret_cast<uint64_t*>(r + 16);
+        vw.ml_status = reinterpret_cast<uint64_t*>(r + 16 + 8 * (size_t)n_inst_tiles);
+        vw.ml_tile_cap = ml_tiles;
+        c->h_views.push_back(vw);
+    }
+}
+
+size_t reset_bytes_for(const lh_ctx* c) {
+    uint32_t n_inst_tiles = (c->n_instances + kInstTile - 1) / kInstTile + 1;
+    uint32_t ml_tiles = (uint32_t)((c->scene_meshlets + kMlTile - 1) / kMlTile) + 1;
+    size_t per_view = align_up(16 + 8 * (size_t)n_inst_tiles + 8 * (size_t)ml_tiles, 256);
+    return align_up(kStWords * 4, 256) + per_view * c->max_views;
+}
+
+FrameDev frame_dev(const lh_ctx* c, uint32_t n_views, uint32_t n_instances) {
+    FrameDev f{};
+    f.instances = c->instances;
+    f.n_instances = n_instances;
+    f.max_instances = c->cfg.max_instances;
+    f.max_draws = c->cfg.max_draws;
+    f.n_views = n_views;
+    f.misc = c->d_misc;
+    f.status = reinterpret_cast<uint32_t*>(c->d_reset);
+    f.views = c->d_views;
+    f.big = c->d_big;
+    f.big_cap = c->cfg.max_big_triangles;
+    f.clip = c->d_clip;
+    f.clip_cap = c->cfg.max_big_triangles;
+    f.textures = c->d_textures;
+    f.n_textures = c->n_textures;
+    f.shadow_maps = c->d_shadow;
+    f.shadow_size = c->cfg.shadow_size;
+    f.hdr = c->d_hdr;
+    f.visibility = c->d_vis;
+    f.uniforms = c->d_uniforms;
+    f.frame_consts = c->d_consts;
+    f.srgb_lut = c->d_srgb;
+    return f;
+}
+
+lh_status check_ctx(lh_ctx* c) {
+    if (!c) return LH_ERR_INVALID_ARGUMENT;
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaSetDevice");
+    return LH_OK;
+}
+
+// Stage per-frame constants (uniforms + host-evaluated pow terms) in pinned
+// memory and copy them to the device on `s`.
+lh_status upload_frame_constants(lh_ctx* c, const Uniforms* u, const Uniforms* probes, uint32_t n_probes,
+                                 cudaStream_t s) {
+    uint32_t slot = c->frame_index++ & 1u;
+    cudaError_t e = cudaEventSynchronize(c->staging_done[slot]);
+    if (e != cudaSuccess) return cuda_fail(c, e, "staging event");
+    uint8_t* h = c->h_staging[slot];
+    Uniforms* hu = reinterpret_cast<Uniforms*>(h);
+    hu[0] = *u;
+    for (uint32_t p = 0; p < n_probes; p++) hu[1 + p] = probes[p];
+    for (uint32_t v = 0; v <= n_probes; v++) {
+        // address fields are the context's own buffers
+        hu[v].meshlet_references = (uint64_t)(uintptr_t)c->h_views[v].refs;
+        hu[v].instances = (uint64_t)(uintptr_t)c->instances;
+        hu[v].draw_calls = (uint64_t)(uintptr_t)c->h_views[v].draws;
+        hu[v].misc_storage = (uint64_t)(uintptr_t)c->d_misc;
+        hu[v].num_meshlets_prefix_sum = (uint64_t)(uintptr_t)c->h_views[v].sector;
+        hu[v].dispatches = 0;
+    }
+    size_t ubytes = sizeof(Uniforms) * (1 + n_probes);
+    float* consts = reinterpret_cast<float*>(h + sizeof(Uniforms) * (1 + c->cfg.max_probes));
+    // generate_shadow_matrices.glsl:39-48: pow(0.5|0.75, cascade_split_pow),
+    // uniform-only terms, evaluated here in double and rounded to float.
+    consts[0] = (float)std::pow(0.5, (double)u->cascade_split_pow);
+    consts[1] = (float)std::pow(0.75, (double)u->cascade_split_pow);
+    e = cudaMemcpyAsync(c->d_uniforms, h, ubytes, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_consts, consts, 2 * sizeof(float), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaEventRecord(c->staging_done[slot], s);
+    if (e != cudaSuccess) return cuda_fail(c, e, "upload uniforms");
+    return LH_OK;
+}
+
+// The frame's kernels, all stream ordered (capturable).
+lh_status enqueue_frame(lh_ctx* c, uint32_t n_probes, uint32_t n_instances, cudaStream_t s) {
+    const uint32_t n_persp = 1 + n_probes, n_views = n_persp + 4;
+    FrameDev f = frame_dev(c, n_views, n_instances);
+    const lh_tuning& t = c->tuning;
+    uint32_t stage = 0;
+    auto mark = [&](cudaError_t e) {
+        if (e == cudaSuccess && c->profiling) e = cudaEventRecord(c->stage_ev[stage], s);
+        stage++;
+        return e;
+    };
+    cudaError_t e = mark(cudaSuccess);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_reset, 0, c->reset_bytes, s);
+    if (e == cudaSuccess) e = mark(launch_clear_targets(f, s, c->sms));
+    // visibility views: instance cull + prefix, meshlet cull, raster
+    if (e == cudaSuccess) e = mark(launch_cull_instances(f, 0, n_persp, s));
+    uint32_t bpv = std::max(2u, (uint32_t)(c->sms * t.cull_blocks_per_sm) / n_persp);
+    if (e == cudaSuccess) e = mark(launch_cull_meshlets(f, 0, n_persp, bpv, s));
+    if (e == cudaSuccess)
+        e = mark(launch_raster_kind(f, 0, n_persp, kViewVisibility, t.small_px, t.medium_px, s, c->sms));
+    // depth range + cascade fit (main view only)
+    if (e == cudaSuccess) e = mark(launch_depth_reduce_fit(f, s, c->sms));
+    // cascades
+    uint32_t bpc = std::max(2u, (uint32_t)(c->sms * t.cull_blocks_per_sm) / 4);
+    if (e == cudaSuccess) e = mark(launch_cull_instances(f, n_persp, 4, s));
+    if (e == cudaSuccess) e = mark(launch_cull_meshlets(f, n_persp, 4, bpc, s));
+    if (e == cudaSuccess)
+        e = mark(launch_raster_kind(f, n_persp, 4, kViewShadow, t.small_px, t.medium_px, s, c->sms));
+    // lighting resolve of the main view
+    if (e == cudaSuccess) e = mark(launch_resolve(f, c->cfg.width, c->cfg.height, s));
+    if (e != cudaSuccess) return cuda_fail(c, e, "frame launch");
+    return LH_OK;
+}
+
+lh_status prepare_views(lh_ctx* c, const Uniforms* probes, uint32_t n_probes) {
+    build_views(c, n_probes, probes);
+    cudaError_t e = cudaMemcpy(c->d_views, c->h_views.data(), sizeof(ViewDev) * c->h_views.size(),
+                               cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(c, e, "views upload");
+    c->n_views_last = (uint32_t)c->h_views.size();
+    c->n_probes_last = n_probes;
+    return LH_OK;
+}
+
+void fill_out(const lh_ctx* c, lh_frame_out* o) {
+    std::memset(o, 0, sizeof(*o));
+    o->visibility = (uint64_t)(uintptr_t)c->d_vis;
+    o->hdr = (uint64_t)(uintptr_t)c->d_hdr;
+    o->shadow_maps = (uint64_t)(uintptr_t)c->d_shadow;
+    o->misc_storage = (uint64_t)(uintptr_t)c->d_misc;
+    o->prefix_sums = (uint64_t)(uintptr_t)c->d_sectors;
+    o->meshlet_references = (uint64_t)(uintptr_t)c->d_refs;
+    o->draw_calls = (uint64_t)(uintptr_t)c->d_draws;
+    o->probe_visibility = (uint64_t)(uintptr_t)c->d_probe_vis;
+    o->prefix_sector_bytes = c->sector_bytes;
+    o->draw_call_section_bytes = c->draw_bytes;
+    o->width = c->cfg.width;
+    o->height = c->cfg.height;
+    o->shadow_size = c->cfg.shadow_size;
+    o->max_instances = c->cfg.max_instances;
+    o->max_draws = c->cfg.max_draws;
+    o->n_views = c->n_views_last;
+    o->n_probes = c->n_probes_last;
+}
+
+lh_status validate_probes(lh_ctx* c, const Uniforms* probes, uint32_t n_probes) {
+    if (n_probes > c->cfg.max_probes) return fail(c, LH_ERR_CAPACITY, "more probes than max_probes");
+    if (n_probes && !probes) return fail(c, LH_ERR_INVALID_ARGUMENT, "probe_uniforms is NULL");
+    uint64_t px = 0;
+    for (uint32_t p = 0; p < n_probes; p++) {
+        if (probes[p].window_size.x == 0 || probes[p].window_size.y == 0)
+            return fail(c, LH_ERR_INVALID_ARGUMENT, "probe with an empty window");
+        px += align_up((size_t)probes[p].window_size.x * probes[p].window_size.y, 32);
+    }
+    if (px > c->cfg.max_probe_pixels) return fail(c, LH_ERR_CAPACITY, "probe pixels exceed max_probe_pixels");
+    return LH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+uint32_t lh_version(void) { return kVersion; }
+
+lh_status lh_create(const lh_config* config, lh_ctx** out) {
+    if (!config || !out) return LH_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    lh_config cfg = *config;
+    if (cfg.width == 0 || cfg.height == 0 || cfg.width > 16384 || cfg.height > 16384) return LH_ERR_INVALID_ARGUMENT;
+    if (cfg.shadow_size == 0) cfg.shadow_size = 1024;
+    if (cfg.shadow_size > 16384) return LH_ERR_INVALID_ARGUMENT;
+    if (cfg.max_instances == 0) cfg.max_instances = MAX_INSTANCES;
+    if (cfg.max_draws == 0) cfg.max_draws = MAX_OPAQUE_DRAWS;
+    // draw slots (opaque + alpha) must fit the 24-bit visibility ID
+    if ((uint64_t)cfg.max_draws * 2 > (1ull << 24)) return LH_ERR_INVALID_ARGUMENT;
+    if (cfg.max_big_triangles == 0) cfg.max_big_triangles = 1u << 20;
+    if (cfg.max_probes > kMaxViews - 5) return LH_ERR_INVALID_ARGUMENT;
+    lh_ctx* c = new (std::nothrow) lh_ctx();
+    if (!c) return LH_ERR_OUT_OF_MEMORY;
+    c->cfg = cfg;
+    c->device = cfg.device;
+    c->tuning = lh_tuning{4u, 4096u, 4.0f, 0u};
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device);
+    c->max_views = 5 + cfg.max_probes;
+    c->sector_bytes = align_up(8 + 8 * (size_t)cfg.max_instances, 16);
+    c->draw_bytes = align_up(8 + 16 * 2 * (size_t)cfg.max_draws, 16);
+    const size_t W = cfg.width, H = cfg.height, S = cfg.shadow_size;
+    if (e == cudaSuccess) e = dalloc(c, &c->d_uniforms, sizeof(Uniforms) * (1 + cfg.max_probes));
+    if (e == cudaSuccess) e = dalloc(c, &c->d_consts, 64);
+    if (e == cudaSuccess) e = dalloc(c, &c->d_srgb, 256 * sizeof(float));
+    if (e == cudaSuccess) e = dalloc(c, &c->d_misc, sizeof(MiscStorage));
+    if (e == cudaSuccess) e = dalloc(c, &c->d_sectors, c->sector_bytes * c->max_views);
+    if (e == cudaSuccess) e = dalloc(c, &c->d_refs, sizeof(MeshletReference) * 2 * (size_t)cfg.max_draws * c->max_views);
+    if (e == cudaSuccess) e = dalloc(c, &c->d_draws, c->draw_bytes * c->max_views);
+    if (e == cudaSuccess) e = dalloc(c, &c->d_vis, W * H * 8);
+    if (e == cudaSuccess) e = dalloc(c, &c->d_shadow, 4 * S * S * 4);
+    if (e == cudaSuccess) e = dalloc(c, &c->d_hdr, W * H * 16);
+    if (e == cudaSuccess) e = dalloc(c, &c->d_probe_vis, (size_t)std::max(cfg.max_probe_pixels, 32u) * 8);
+    if (e == cudaSuccess) e = dalloc(c, &c->d_big, sizeof(BigTri) * (size_t)cfg.max_big_triangles);
+    if (e == cudaSuccess) e = dalloc(c, &c->d_clip, sizeof(ClipItem) * (size_t)cfg.max_big_triangles);
+    if (e == cudaSuccess) e = dalloc(c, &c->d_views, sizeof(ViewDev) * c->max_views);
+    if (e == cudaSuccess) {
+        float lut[256];
+        for (int i = 0; i < 256; i++) {
+            double v = i / 255.0;
+            lut[i] = (float)(v <= 0.04045 ? v / 12.92 : std::pow((v + 0.055) / 1.055, 2.4));
+        }
+        e = cudaMemcpy(c->d_srgb, lut, sizeof(lut), cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess) e = cudaMemset(c->d_misc, 0, sizeof(MiscStorage));
+    c->staging_bytes = sizeof(Uniforms) * (1 + cfg.max_probes) + 64;
+    for (int i = 0; i < 2 && e == cudaSuccess; i++) {
+        e = cudaMallocHost(reinterpret_cast<void**>(&c->h_staging[i]), c->staging_bytes);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->staging_done[i], cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) {
+        lh_status st = e == cudaErrorMemoryAllocation ? LH_ERR_OUT_OF_MEMORY : LH_ERR_CUDA;
+        free_all(c);
+        delete c;
+        return st;
+    }
+    *out = c;
+    return LH_OK;
+}
+
+lh_status lh_set_scene(lh_ctx* c, const Instance* d_instances, uint32_t n, const lh_texture* textures,
+                       uint32_t n_textures) {
+    lh_status st = check_ctx(c);
+    if (st != LH_OK) return st;
+    if (n && !d_instances) return fail(c, LH_ERR_INVALID_ARGUMENT, "d_instances is NULL");
+    if (((uintptr_t)d_instances & 15) != 0) return fail(c, LH_ERR_INVALID_ARGUMENT, "d_instances must be 16-byte aligned");
+    if (n_textures && !textures) return fail(c, LH_ERR_INVALID_ARGUMENT, "textures is NULL");
+    for (uint32_t i = 0; i < n_textures; i++)
+        if (!textures[i].texels || !textures[i].width || !textures[i].height || (textures[i].texels & 3))
+            return fail(c, LH_ERR_INVALID_ARGUMENT, "bad texture descriptor");
+    cudaError_t e = cudaSuccess;
+    if (c->graph_exec) {
+        cudaGraphExecDestroy(c->graph_exec);
+        c->graph_exec = nullptr;
+    }
+    c->instances = d_instances;
+    c->n_instances = n;
+    // total candidate meshlets bounds the look-back scratch
+    unsigned long long* d_sum = nullptr;
+    e = cudaMalloc(&d_sum, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = launch_sum_meshlets(d_instances, n, d_sum, 0);
+    unsigned long long total = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&total, d_sum, sizeof(total), cudaMemcpyDeviceToHost);
+    if (d_sum) cudaFree(d_sum);
+    if (e != cudaSuccess) return cuda_fail(c, e, "scene meshlet count");
+    c->scene_meshlets = total;
+    // textures
+    if (c->d_textures) {
+        for (auto it = c->allocs.begin(); it != c->allocs.end(); ++it)
+            if (it->p == c->d_textures) { cudaFree(it->p); c->allocs.erase(it); break; }
+        c->d_textures = nullptr;
+    }
+    e = dalloc(c, &c->d_textures, sizeof(lh_texture) * std::max(1u, n_textures));
+    if (e == cudaSuccess && n_textures)
+        e = cudaMemcpy(c->d_textures, textures, sizeof(lh_texture) * n_textures, cudaMemcpyHostToDevice);
+    c->n_textures = n_textures;
+    // per-frame scratch
+    if (c->d_reset) {
+        for (auto it = c->allocs.begin(); it != c->allocs.end(); ++it)
+            if (it->p == c->d_reset) { cudaFree(it->p); c->allocs.erase(it); break; }
+        c->d_reset = nullptr;
+    }
+    c->reset_bytes = reset_bytes_for(c);
+    if (e == cudaSuccess) e = dalloc(c, &c->d_reset, c->reset_bytes);
+    if (e != cudaSuccess) return cuda_fail(c, e, "scene buffers");
+    return prepare_views(c, nullptr, 0);
+}
+
+lh_status lh_frame(lh_ctx* c, const Uniforms* u, void* stream, lh_frame_out* out) {
+    return lh_frame_batched(c, u, nullptr, 0, stream, out);
+}
+
+lh_status lh_frame_batched(lh_ctx* c, const Uniforms* u, const Uniforms* probes, uint32_t n_probes, void* stream,
+                           lh_frame_out* out) {
+    lh_status st = check_ctx(c);
+    if (st != LH_OK) return st;
+    if (!u) return fail(c, LH_ERR_INVALID_ARGUMENT, "uniforms is NULL");
+    if (!c->d_reset) return fail(c, LH_ERR_NO_SCENE, "lh_set_scene was not called");
+    if (u->window_size.x != c->cfg.width || u->window_size.y != c->cfg.height)
+        return fail(c, LH_ERR_INVALID_ARGUMENT, "uniforms.window_size differs from the context's size");
+    if ((st = validate_probes(c, probes, n_probes)) != LH_OK) return st;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    bool same_views = n_probes == c->n_probes_last;
+    if (same_views && n_probes) {
+        for (uint32_t p = 0; p < n_probes && same_views; p++)
+            same_views = probes[p].window_size.x == c->h_views[1 + p].width &&
+                         probes[p].window_size.y == c->h_views[1 + p].height;
+    }
+    if (!same_views) {
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return cuda_fail(c, e, "stream sync");
+        if ((st = prepare_views(c, probes, n_probes)) != LH_OK) return st;
+    }
+    if ((st = upload_frame_constants(c, u, probes, n_probes, s)) != LH_OK) return st;
+    uint32_t n_inst = std::min(u->num_instances, c->n_instances);
+    if ((st = enqueue_frame(c, n_probes, n_inst, s)) != LH_OK) return st;
+    c->last_stream = s;
+    if (out) fill_out(c, out);
+    return LH_OK;
+}
+
+lh_status lh_get_outputs(lh_ctx* c, lh_frame_out* out) {
+    if (!c || !out) return LH_ERR_INVALID_ARGUMENT;
+    fill_out(c, out);
+    return LH_OK;
+}
+
+lh_status lh_read_status(lh_ctx* c, lh_device_status* out) {
+    lh_status st = check_ctx(c);
+    if (st != LH_OK) return st;
+    if (!out) return LH_ERR_INVALID_ARGUMENT;
+    std::memset(out, 0, sizeof(*out));
+    cudaError_t e = cudaStreamSynchronize(c->last_stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "stream sync");
+    if (!c->d_reset) return LH_OK;
+    uint32_t words[kStWords];
+    e = cudaMemcpy(words, c->d_reset, sizeof(words), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(c, e, "status read");
+    out->flags = words[kStFlags];
+    out->big_triangles = words[kStBigCount];
+    out->clipped_triangles = words[kStClipCount];
+    out->n_views = c->n_views_last;
+    for (uint32_t v = 0; v < c->n_views_last && v < 40; v++) {
+        unsigned long long counter = 0;
+        uint32_t draws[2] = {0, 0};
+        e = cudaMemcpy(&counter, c->h_views[v].sector, 8, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(draws, c->h_views[v].draws, 8, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_fail(c, e, "status read");
+        out->visible_instances[v] = (uint32_t)(counter >> 32);
+        out->candidate_meshlets[v] = (uint32_t)counter;
+        out->visible_opaque[v] = draws[0];
+        out->visible_alpha_clip[v] = draws[1];
+    }
+    return LH_OK;
+}
+
+lh_status lh_set_profiling(lh_ctx* c, int enable) {
+    lh_status st = check_ctx(c);
+    if (st != LH_OK) return st;
+    if (enable && !c->stage_ev[0]) {
+        for (auto& ev : c->stage_ev) {
+            cudaError_t e = cudaEventCreate(&ev);
+            if (e != cudaSuccess) return cuda_fail(c, e, "event create");
+        }
+    }
+    c->profiling = enable != 0;
+    return LH_OK;
+}
+
+lh_status lh_get_stage_times(lh_ctx* c, float* ms, uint32_t n) {
+    lh_status st = check_ctx(c);
+    if (st != LH_OK) return st;
+    if (!ms || !c->profiling) return fail(c, LH_ERR_INVALID_ARGUMENT, "profiling is off");
+    cudaError_t e = cudaEventSynchronize(c->stage_ev[LH_N_STAGES]);
+    for (uint32_t i = 0; i < n && i < LH_N_STAGES && e == cudaSuccess; i++)
+        e = cudaEventElapsedTime(&ms[i], c->stage_ev[i], c->stage_ev[i + 1]);
+    if (e != cudaSuccess) return cuda_fail(c, e, "stage times");
+    return LH_OK;
+}
+
+lh_status lh_download(lh_ctx* c, void* dst, uint64_t src, size_t bytes) {
+    lh_status st = check_ctx(c);
+    if (st != LH_OK) return st;
+    if (!dst || !src) return fail(c, LH_ERR_INVALID_ARGUMENT, "null pointer");
+    cudaError_t e = cudaStreamSynchronize(c->last_stream);
+    if (e == cudaSuccess) e = cudaMemcpy(dst, reinterpret_cast<const void*>(src), bytes, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(c, e, "download");
+    return LH_OK;
+}
+
+const char* lh_last_error(lh_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+void lh_destroy(lh_ctx* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->last_stream) cudaStreamSynchronize(c->last_stream);
+    free_all(c);
+    delete c;
+}
+
+lh_status lh_set_tuning(lh_ctx* c, const lh_tuning* t) {
+    if (!c || !t) return LH_ERR_INVALID_ARGUMENT;
+    if (t->small_px > 4096 || t->medium_px < t->small_px || t->cull_blocks_per_sm <= 0.0f) return LH_ERR_INVALID_ARGUMENT;
+    c->tuning = *t;
+    return LH_OK;
+}
+
+lh_status lh_get_tuning(lh_ctx* c, lh_tuning* t) {
+    if (!c || !t) return LH_ERR_INVALID_ARGUMENT;
+    *t = c->tuning;
+    return LH_OK;
+}
+
+}  // extern "C"

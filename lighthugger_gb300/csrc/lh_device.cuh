@@ -1,0 +1,252 @@
+// Device-side building blocks of the visibility pipeline: GLSL-ordered float
+// math, scene access through device addresses, the culling tests, the
+// rasterisation rules and the samplers.
+//
+// Every kernel including this file is compiled with --fmad=false and IEEE
+// division / square root, so each float operation below rounds on its own;
+// the evaluation orders are the ones the CPU oracle states (dot =
+// (x*x' + y*y') + z*z', mat4*vec4 = ((c0*x + c1*y) + c2*z) + c3*w, ...),
+// which makes culling, visibility IDs, depth and shadow maps bit exact.
+#pragma once
+
+#include <cstdint>
+
+#include "lh/lh.h"
+
+namespace lh {
+
+// ------------------------------------------------------------------ vectors
+struct f2 { float x, y; };
+struct f3 { float x, y, z; };
+struct f4 { float x, y, z, w; };
+
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a) { return {-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ f3 operator*(f3 a, f3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+__device__ __forceinline__ f3 operator/(f3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+__device__ __forceinline__ float dot(f3 a, f3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+__device__ __forceinline__ float length(f3 v) { return sqrtf(dot(v, v)); }
+__device__ __forceinline__ f3 normalize(f3 v) { float l = length(v); return {v.x / l, v.y / l, v.z / l}; }
+__device__ __forceinline__ f3 cross(f3 a, f3 b) {
+    return {a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y};
+}
+__device__ __forceinline__ f3 ld3(const lh_vec3& v) { return {v.x, v.y, v.z}; }
+
+// mat4 * vec4 with the column-major reference layout.
+__device__ __forceinline__ f4 mul(const lh_mat4& m, f4 v) {
+    const lh_vec4 &c0 = m.cols[0], &c1 = m.cols[1], &c2 = m.cols[2], &c3 = m.cols[3];
+    return {((c0.x * v.x + c1.x * v.y) + c2.x * v.z) + c3.x * v.w,
+            ((c0.y * v.x + c1.y * v.y) + c2.y * v.z) + c3.y * v.w,
+            ((c0.z * v.x + c1.z * v.y) + c2.z * v.z) + c3.z * v.w,
+            ((c0.w * v.x + c1.w * v.y) + c2.w * v.z) + c3.w * v.w};
+}
+__device__ __forceinline__ f3 mul3(const lh_mat3& m, f3 v) {
+    const lh_vec3 &c0 = m.cols[0], &c1 = m.cols[1], &c2 = m.cols[2];
+    return {(c0.x * v.x + c1.x * v.y) + c2.x * v.z, (c0.y * v.x + c1.y * v.y) + c2.y * v.z,
+            (c0.z * v.x + c1.z * v.y) + c2.z * v.z};
+}
+// max/min with the std::max / std::min conventions the oracle uses
+// (the first argument is kept when the comparison is false).
+__device__ __forceinline__ float gmax(float a, float b) { return (a < b) ? b : a; }
+__device__ __forceinline__ float gmin(float a, float b) { return (b < a) ? b : a; }
+__device__ __forceinline__ uint32_t f2u(float f) { return __float_as_uint(f); }
+__device__ __forceinline__ float u2f(uint32_t u) { return __uint_as_float(u); }
+
+// ------------------------------------------------------------------ scene access
+__device__ __forceinline__ const MeshInfo* mesh_info_of(const Instance* inst) {
+    return reinterpret_cast<const MeshInfo*>(inst->mesh_info_address);
+}
+__device__ __forceinline__ uint32_t load_index(const MeshInfo* mi, uint32_t flags, uint32_t vertex_id) {
+    if (flags & MESH_INFO_FLAGS_32_BIT_INDICES) return __ldg(reinterpret_cast<const uint32_t*>(mi->indices) + vertex_id);
+    return __ldg(reinterpret_cast<const uint16_t*>(mi->indices) + vertex_id);
+}
+__device__ __forceinline__ f3 load_position(uint64_t positions, uint32_t flags, uint32_t index) {
+    if (flags & MESH_INFO_FLAGS_FP32_VERTICES) {
+        const float* p = reinterpret_cast<const float*>(positions) + (size_t)index * 3;
+        return {__ldg(p), __ldg(p + 1), __ldg(p + 2)};
+    }
+    const uint16_t* p = reinterpret_cast<const uint16_t*>(positions) + (size_t)index * 3;
+    return {(float)__ldg(p), (float)__ldg(p + 1), (float)__ldg(p + 2)};
+}
+__device__ __forceinline__ f3 load_normal_raw(uint64_t normals, uint32_t flags, uint32_t index) {
+    if (flags & MESH_INFO_FLAGS_FP32_VERTICES) {
+        const float* p = reinterpret_cast<const float*>(normals) + (size_t)index * 3;
+        return {__ldg(p), __ldg(p + 1), __ldg(p + 2)};
+    }
+    const int8_t* p = reinterpret_cast<const int8_t*>(normals) + (size_t)index * 3;
+    return {(float)p[0], (float)p[1], (float)p[2]};
+}
+__device__ __forceinline__ f2 load_uv_raw(uint64_t uvs, uint32_t flags, uint32_t index) {
+    if (flags & MESH_INFO_FLAGS_FP32_VERTICES) {
+        const float* p = reinterpret_cast<const float*>(uvs) + (size_t)index * 2;
+        return {__ldg(p), __ldg(p + 1)};
+    }
+    const uint16_t* p = reinterpret_cast<const uint16_t*>(uvs) + (size_t)index * 2;
+    return {(float)__ldg(p), (float)__ldg(p + 1)};
+}
+__device__ __forceinline__ f3 world_pos(const lh_mat4& transform, f3 p) {
+    f4 w = mul(transform, f4{p.x, p.y, p.z, 1.0f});
+    return {w.x, w.y, w.z};
+}
+
+// ------------------------------------------------------------------ culling (culling.glsl)
+__device__ __forceinline__ float max_scale(const lh_mat4& t) {
+    float sx = length(f3{t.cols[0].x, t.cols[0].y, t.cols[0].z});
+    float sy = length(f3{t.cols[1].x, t.cols[1].y, t.cols[1].z});
+    float sz = length(f3{t.cols[2].x, t.cols[2].y, t.cols[2].z});
+    return gmax(gmax(sx, sy), sz);
+}
+
+// culling.glsl:1-46; true = culled.
+__device__ __forceinline__ bool cull_bounding_sphere(const Uniforms& u, const lh_mat4& transform, lh_vec4 bs) {
+    f4 w4 = mul(transform, f4{bs.x, bs.y, bs.z, 1.0f});
+    float radius = bs.w * max_scale(transform);
+    f4 vs = mul(u.initial_view, f4{w4.x, w4.y, w4.z, 1.0f});
+    vs.z = -vs.z;
+    bool visible = vs.z + radius > NEAR_PLANE;
+    const lh_mat4& P = u.perspective;
+    f3 fx = normalize(f3{P.cols[0].w + P.cols[0].x, P.cols[1].w + P.cols[1].x, P.cols[2].w + P.cols[2].x});
+    f3 fy = normalize(f3{P.cols[0].w + P.cols[0].y, P.cols[1].w + P.cols[1].y, P.cols[2].w + P.cols[2].y});
+    visible = visible && vs.z * fx.z + fabsf(vs.x) * fx.x < radius;
+    visible = visible && vs.z * fy.z - fabsf(vs.y) * fy.y < radius;
+    return !visible;
+}
+
+// culling.glsl:48-135; true = culled.
+__device__ __forceinline__ bool cull_bounding_sphere_shadows(const MiscStorage& m, const lh_mat4& transform,
+                                                             lh_vec4 bs, uint32_t c) {
+    f4 w4 = mul(transform, f4{bs.x, bs.y, bs.z, 1.0f});
+    float radius = bs.w * max_scale(transform);
+    f4 world{w4.x, w4.y, w4.z, 1.0f};
+    f4 v = mul(m.shadow_view_matrices[c], world);
+    float R = m.shadow_sphere_radii[c];
+    if (!((fabsf(v.x) - radius < R) && (fabsf(v.y) - radius < R))) return true;
+    for (uint32_t k = 0; k < c; k++) {
+        f4 vk = mul(m.shadow_view_matrices[k], world);
+        float Rk = m.shadow_sphere_radii[k];
+        if ((fabsf(vk.x) + radius < Rk) && (fabsf(vk.y) + radius < Rk)) return true;
+    }
+    return false;
+}
+
+// culling.glsl:137-145
+__device__ __forceinline__ bool cull_cone_perspective(const Uniforms& u, const Instance* inst, const lh_mat4& transform,
+                                                      const Meshlet& ml) {
+    f4 a4 = mul(transform, f4{ml.cone_apex.x, ml.cone_apex.y, ml.cone_apex.z, 1.0f});
+    f3 axis = normalize(mul3(inst->normal_transform, ld3(ml.cone_axis)));
+    return dot(normalize(f3{a4.x, a4.y, a4.z} - ld3(u.camera_pos)), normalize(axis)) >= ml.cone_cutoff;
+}
+// culling.glsl:147-151
+__device__ __forceinline__ bool cull_cone_orthographic(const Uniforms& u, const Instance* inst, const Meshlet& ml) {
+    f3 axis = normalize(mul3(inst->normal_transform, ld3(ml.cone_axis)));
+    return dot(ld3(u.sun_dir), axis) >= ml.cone_cutoff;
+}
+
+// ------------------------------------------------------------------ rasterisation rules
+// Outcode bits: 1 z > w, 2 z < 0, 4 x > g*w, 8 x < -g*w, 16 y > g*w,
+// 32 y < -g*w; 64 = a non-finite coordinate or w <= 0 (the triangle is dropped).
+__device__ __forceinline__ uint32_t outcode(f4 v) {
+    if (!(isfinite(v.x) && isfinite(v.y) && isfinite(v.z) && isfinite(v.w) && v.w > 0.0f)) return 64u;
+    uint32_t c = 0;
+    float g = LH_GUARD_BAND * v.w;
+    if (v.z > v.w) c |= 1u;
+    if (v.z < 0.0f) c |= 2u;
+    if (v.x > g) c |= 4u;
+    if (v.x < -g) c |= 8u;
+    if (v.y > g) c |= 16u;
+    if (v.y < -g) c |= 32u;
+    return c;
+}
+
+struct SnapV { int32_t X, Y; float z; };
+
+// Viewport transform + snap to 1/256 pixel (round to nearest even).
+__device__ __forceinline__ SnapV snap(f4 v, float hw, float hh) {
+    float ndx = v.x / v.w, ndy = v.y / v.w;
+    SnapV s;
+    s.z = v.z / v.w;
+    float xf = ndx * hw + hw, yf = ndy * hh + hh;
+    s.X = __float2int_rn(xf * 256.0f);
+    s.Y = __float2int_rn(yf * 256.0f);
+    return s;
+}
+
+__device__ __forceinline__ int64_t cross3(const SnapV& a, const SnapV& b, const SnapV& c) {
+    return ((int64_t)a.X * b.Y - (int64_t)b.X * a.Y) + ((int64_t)b.X * c.Y - (int64_t)c.X * b.Y) +
+           ((int64_t)c.X * a.Y - (int64_t)a.X * c.Y);
+}
+
+// Triangle ready for coverage: orientation normalised (interior has every
+// edge function >= 0), bias 1 for edges that are not top-left.
+struct TriSetup {
+    int32_t X0, Y0, X1, Y1, X2, Y2;
+    float z0, s1, s2;
+    uint32_t id;
+    int32_t px0, py0, px1, py1;
+    uint32_t bias;  // bit0 edge12, bit1 edge20, bit2 edge01 not top-left
+};
+
+__device__ __forceinline__ bool top_left(int32_t ax, int32_t ay, int32_t bx, int32_t by) {
+    int32_t dy = by - ay, dx = bx - ax;
+    return dy > 0 || (dy == 0 && dx < 0);
+}
+
+// Build the setup of a normalised triangle; returns false when no pixel
+// centre of the (W x H) target can be covered.
+__device__ __forceinline__ bool make_setup(SnapV v0, SnapV v1, SnapV v2, uint32_t id, uint32_t W, uint32_t H,
+                                           TriSetup& t) {
+    int64_t A = (int64_t)(v2.Y - v1.Y) * (v0.X - v1.X) - (int64_t)(v2.X - v1.X) * (v0.Y - v1.Y);
+    if (A <= 0) return false;
+    int32_t minX = min(v0.X, min(v1.X, v2.X)), maxX = max(v0.X, max(v1.X, v2.X));
+    int32_t minY = min(v0.Y, min(v1.Y, v2.Y)), maxY = max(v0.Y, max(v1.Y, v2.Y));
+    t.px0 = max((minX + 127) >> 8, 0);
+    t.px1 = min((maxX - 128) >> 8, (int32_t)W - 1);
+    t.py0 = max((minY + 127) >> 8, 0);
+    t.py1 = min((maxY - 128) >> 8, (int32_t)H - 1);
+    if (t.px0 > t.px1 || t.py0 > t.py1) return false;
+    t.X0 = v0.X; t.Y0 = v0.Y; t.X1 = v1.X; t.Y1 = v1.Y; t.X2 = v2.X; t.Y2 = v2.Y;
+    float fA = __ll2float_rn(A);
+    t.z0 = v0.z;
+    t.s1 = (v1.z - v0.z) / fA;
+    t.s2 = (v2.z - v0.z) / fA;
+    t.id = id;
+    t.bias = (top_left(v1.X, v1.Y, v2.X, v2.Y) ? 0u : 1u) | (top_left(v2.X, v2.Y, v0.X, v0.Y) ? 0u : 2u) |
+             (top_left(v0.X, v0.Y, v1.X, v1.Y) ? 0u : 4u);
+    return true;
+}
+
+// Coverage + depth of pixel (px, py); returns false when not covered.
+__device__ __forceinline__ bool cover(const TriSetup& t, int32_t px, int32_t py, float& depth) {
+    int64_t Px = (int64_t)px * 256 + 128, Py = (int64_t)py * 256 + 128;
+    int64_t e12 = (int64_t)(t.Y2 - t.Y1) * (Px - t.X1) - (int64_t)(t.X2 - t.X1) * (Py - t.Y1);
+    int64_t e20 = (int64_t)(t.Y0 - t.Y2) * (Px - t.X2) - (int64_t)(t.X0 - t.X2) * (Py - t.Y2);
+    int64_t e01 = (int64_t)(t.Y1 - t.Y0) * (Px - t.X0) - (int64_t)(t.X1 - t.X0) * (Py - t.Y0);
+    if (e12 < (int64_t)(t.bias & 1u) || e20 < (int64_t)((t.bias >> 1) & 1u) || e01 < (int64_t)((t.bias >> 2) & 1u))
+        return false;
+    float d = (t.z0 + __ll2float_rn(e20) * t.s1) + __ll2float_rn(e01) * t.s2;
+    d = d > 0.0f ? d : 0.0f;
+    depth = d < 1.0f ? d : 1.0f;
+    return true;
+}
+
+// Depth test + write: kind 0 keeps the max of (depth bits << 32 | id) in a
+// u64 visibility target (reverse-Z GREATER), kind 1 keeps the min of depth
+// bits in a u32 shadow target (LESS).
+template <int KIND>
+__device__ __forceinline__ void write_fragment(void* target, uint32_t W, int32_t px, int32_t py, float depth,
+                                               uint32_t id) {
+    size_t pix = (size_t)py * W + px;
+    if (KIND == 0) {
+        unsigned long long key = ((unsigned long long)f2u(depth) << 32) | id;
+        unsigned long long* p = reinterpret_cast<unsigned long long*>(target) + pix;
+        if (key > *reinterpret_cast<volatile unsigned long long*>(p)) atomicMax(p, key);
+    } else {
+        uint32_t bits = f2u(depth);
+        uint32_t* p = reinterpret_cast<uint32_t*>(target) + pix;
+        if (bits < *reinterpret_cast<volatile uint32_t*>(p)) atomicMin(p, bits);
+    }
+}
+
+}  // namespace lh

@@ -1,0 +1,106 @@
+// Device-visible frame description shared by the kernels and the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "lh/lh.h"
+
+namespace lh {
+
+constexpr uint32_t kMaxViews = 40;           // main + 4 cascades + up to 35 probes
+constexpr uint32_t kInstTile = 256;          // instances per instance-cull tile
+constexpr uint32_t kMlThreads = 256;         // threads per meshlet-cull block
+constexpr uint32_t kMlItems = 8;             // candidates per thread (striped)
+constexpr uint32_t kMlTile = kMlThreads * kMlItems;
+constexpr uint32_t kSpinLimit = 1u << 22;    // bounded waits (with __nanosleep back-off)
+
+// Look-back status word: [63:62] 0 = not ready, 1 = tile aggregate,
+// 2 = inclusive prefix; [61:0] payload (field-wise additive counts).
+constexpr uint64_t kStatAgg = 1ull << 62;
+constexpr uint64_t kStatIncl = 2ull << 62;
+constexpr uint64_t kPayloadMask = (1ull << 62) - 1;
+
+enum ViewKind : uint32_t { kViewVisibility = 0, kViewShadow = 1 };
+
+struct ViewDev {
+    uint32_t kind;
+    uint32_t cascade;
+    uint32_t width, height;
+    const Uniforms* uniforms;   // perspective views: their own; cascades: the main view's
+    uint8_t* sector;            // prefix sector: u64 counter + PrefixSumValue[max_instances]
+    MeshletReference* refs;     // 2*max_draws
+    uint8_t* draws;             // u32 num_opaque, u32 num_alpha_clip, DrawIndirectCommand[2*max_draws]
+    void* target;               // u64 visibility or u32 depth
+    uint64_t* inst_status;      // per-frame zeroed look-back words, instance cull
+    uint64_t* ml_status;        // per-frame zeroed look-back words, meshlet cull
+    uint32_t* claim;            // per-frame zeroed: [0] instance tiles, [1] meshlet tiles
+    uint32_t section_base;      // firstInstance offset of this view's reference section
+    uint32_t ml_tile_cap;       // capacity of ml_status
+};
+
+// Triangle handed to the tiled raster path (one entry per 16-row band).
+struct BigTri {
+    int32_t X0, Y0, X1, Y1, X2, Y2;
+    float z0, s1, s2;
+    uint32_t id;
+    uint32_t view;
+    uint32_t bias;
+    int32_t px0, px1, py0, py1;  // band-restricted pixel bounds
+};
+
+struct ClipItem {
+    uint32_t view, slot, tri, pad;
+};
+
+// Per-frame scratch words (zeroed at frame start).
+enum StatusWord : uint32_t {
+    kStFlags = 0,
+    kStBigCount = 1,
+    kStClipCount = 2,
+    kStRasterClaim = 3,
+    kStBigClaim = 4,
+    kStReduceDone = 5,
+    kStClipClaim = 6,
+    kStWords = 16
+};
+
+struct FrameDev {
+    const Instance* instances;
+    uint32_t n_instances;
+    uint32_t max_instances;
+    uint32_t max_draws;
+    uint32_t n_views;
+    MiscStorage* misc;
+    uint32_t* status;           // kStWords words
+    const ViewDev* views;       // n_views
+    BigTri* big;
+    uint32_t big_cap;
+    ClipItem* clip;
+    uint32_t clip_cap;
+    const lh_texture* textures;
+    uint32_t n_textures;
+    float* shadow_maps;
+    uint32_t shadow_size;
+    float4* hdr;
+    uint64_t* visibility;       // main view
+    const Uniforms* uniforms;   // main view
+    const float* frame_consts;  // [0] pow(0.5, split), [1] pow(0.75, split)
+    const float* srgb_lut;      // 256 entries
+};
+
+// Launchers (stream ordered).  Each returns the CUDA error of its launch.
+cudaError_t launch_clear_targets(const FrameDev& f, cudaStream_t s, int sms);
+cudaError_t launch_cull_instances(const FrameDev& f, uint32_t view_begin, uint32_t n_views, cudaStream_t s);
+cudaError_t launch_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint32_t n_views, uint32_t blocks_per_view,
+                                 cudaStream_t s);
+// Raster all views [view_begin, view_begin + n_views) of one kind (kViewVisibility
+// or kViewShadow): main kernel, clipper, band kernel.
+cudaError_t launch_raster_kind(const FrameDev& f, uint32_t view_begin, uint32_t n_views, int kind, uint32_t small_px,
+                               uint32_t medium_px, cudaStream_t s, int sms);
+cudaError_t launch_depth_reduce_fit(const FrameDev& f, cudaStream_t s, int sms);
+cudaError_t launch_resolve(const FrameDev& f, uint32_t width, uint32_t height, cudaStream_t s);
+cudaError_t launch_sum_meshlets(const Instance* instances, uint32_t n, unsigned long long* out, cudaStream_t s);
+
+}  // namespace lh

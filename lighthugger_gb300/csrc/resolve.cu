@@ -1,0 +1,450 @@
+// Frame set-up, min/max depth reduction fused with the cascade fit, and the
+// full-screen lighting resolve.
+//
+// Reference passes: reset_buffers_a/b/c (src/shaders/compute/
+// reset_buffers.glsl:9-57), read_depth (compute/read_depth.glsl:22-83),
+// generate_shadow_matrices (compute/generate_shadow_matrices.glsl:15-110) and
+// render_geometry (src/shaders/render_geometry.comp:70-266).
+#include "lh_device.cuh"
+#include "lh_internal.cuh"
+
+namespace lh {
+namespace {
+
+// ---------------------------------------------------------------- frame set-up
+// grid = (blocks, n_views): clears each view's target (visibility 0, shadow
+// depth 1.0) with 16-byte stores; block (0, 0) also resets the per-view
+// counters and the depth range (reset_buffers.glsl:9-29, util.glsl:61-70).
+__global__ void __launch_bounds__(256) k_clear_targets(FrameDev f) {
+    const ViewDev* vw = f.views + blockIdx.y;
+    const uint64_t npx = (uint64_t)vw->width * vw->height;
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (uint64_t)gridDim.x * blockDim.x;
+    if (vw->kind == kViewVisibility) {
+        uint4* p = reinterpret_cast<uint4*>(vw->target);
+        const uint64_t n = npx / 2;
+        for (uint64_t i = tid; i < n; i += stride) p[i] = make_uint4(0, 0, 0, 0);
+        if ((npx & 1) && tid == 0) reinterpret_cast<unsigned long long*>(vw->target)[npx - 1] = 0ull;
+    } else {
+        const uint32_t one = 0x3F800000u;
+        uint4* p = reinterpret_cast<uint4*>(vw->target);
+        const uint64_t n = npx / 4;
+        for (uint64_t i = tid; i < n; i += stride) p[i] = make_uint4(one, one, one, one);
+        for (uint64_t i = n * 4 + tid; i < npx; i += stride) reinterpret_cast<uint32_t*>(vw->target)[i] = one;
+    }
+    if (blockIdx.x == 0 && blockIdx.y == 0) {
+        for (uint32_t v = threadIdx.x; v < f.n_views; v += blockDim.x) {
+            *reinterpret_cast<unsigned long long*>(f.views[v].sector) = 0ull;
+            *reinterpret_cast<unsigned long long*>(f.views[v].draws) = 0ull;
+        }
+        if (threadIdx.x == 0) {
+            f.misc->min_depth = 0xFFFFFFFFu;
+            f.misc->max_depth = 0u;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- cascade fit
+// matrices.glsl:9-19
+__device__ lh_mat4 look_at(f3 eye, f3 at, f3 up) {
+    f3 fw = normalize(at - eye);
+    f3 r = normalize(cross(fw, up));
+    f3 u = cross(r, fw);
+    lh_mat4 m;
+    m.cols[0] = {r.x, u.x, -fw.x, 0.0f};
+    m.cols[1] = {r.y, u.y, -fw.y, 0.0f};
+    m.cols[2] = {r.z, u.z, -fw.z, 0.0f};
+    m.cols[3] = {-dot(r, eye), -dot(u, eye), dot(fw, eye), 1.0f};
+    return m;
+}
+// matrices.glsl:21-40
+__device__ lh_mat4 orthographic(float left, float right, float bottom, float top, float n, float fr) {
+    float rml = right - left, rpl = right + left, tmb = top - bottom, tpb = top + bottom, fmn = fr - n;
+    lh_mat4 m;
+    m.cols[0] = {2.0f / rml, 0.0f, 0.0f, 0.0f};
+    m.cols[1] = {0.0f, -2.0f / tmb, 0.0f, 0.0f};
+    m.cols[2] = {0.0f, 0.0f, -1.0f / fmn, 0.0f};
+    m.cols[3] = {-(rpl / rml), -(tpb / tmb), -(n / fmn), 1.0f};
+    return m;
+}
+__device__ lh_mat4 matmul(const lh_mat4& a, const lh_mat4& b) {
+    lh_mat4 r;
+    for (int c = 0; c < 4; c++) {
+        f4 v = mul(a, f4{b.cols[c].x, b.cols[c].y, b.cols[c].z, b.cols[c].w});
+        r.cols[c] = {v.x, v.y, v.z, v.w};
+    }
+    return r;
+}
+
+// generate_shadow_matrices.glsl:15-110 for cascade c.  pow(0.5, split) and
+// pow(0.75, split) arrive precomputed (host, double, rounded to float).
+__device__ void fit_cascade(const FrameDev& f, uint32_t c, uint32_t min_bits, uint32_t max_bits) {
+    const Uniforms& u = *f.uniforms;
+    MiscStorage& m = *f.misc;
+    float min_depth = u2f(min_bits), max_depth = u2f(max_bits);
+    float min_distance = NEAR_PLANE / max_depth;
+    float max_distance = NEAR_PLANE / min_depth;
+    float p05 = f.frame_consts[0], p075 = f.frame_consts[1];
+    float splits[4] = {max_depth, NEAR_PLANE / (min_distance * (1.0f - p05) + max_distance * p05),
+                       NEAR_PLANE / (min_distance * (1.0f - p075) + max_distance * p075), min_depth};
+    float last = c > 0 ? splits[c - 1] : max_depth;
+    float split = splits[c];
+    f3 corners[8] = {{-1.0f, 1.0f, last},  {1.0f, 1.0f, last},  {1.0f, -1.0f, last},  {-1.0f, -1.0f, last},
+                     {-1.0f, 1.0f, split}, {1.0f, 1.0f, split}, {1.0f, -1.0f, split}, {-1.0f, -1.0f, split}};
+    for (int i = 0; i < 8; i++) {
+        f4 ic = mul(u.inv_perspective_view, f4{corners[i].x, corners[i].y, corners[i].z, 1.0f});
+        corners[i] = f3{ic.x / ic.w, ic.y / ic.w, ic.z / ic.w};
+    }
+    f3 center{0.0f, 0.0f, 0.0f};
+    for (int i = 0; i < 8; i++) center = center + corners[i];
+    center = center / 8.0f;
+    float radius = 0.0f;
+    for (int i = 0; i < 8; i++) radius = gmax(radius, length(corners[i] - center));
+    radius = ceilf(radius * 16.0f) / 16.0f;
+    f3 eye = ld3(u.sun_dir) * u.shadow_cam_distance + center;
+    lh_mat4 view = look_at(eye, center, f3{0.0f, 1.0f, 0.0f});
+    lh_mat4 proj = orthographic(-radius, radius, -radius, radius, 0.0f, u.shadow_cam_distance * 2.0f);
+    lh_mat4 mat = matmul(proj, view);
+    lh_mat4 bias;
+    bias.cols[0] = {0.5f, 0.0f, 0.0f, 0.0f};
+    bias.cols[1] = {0.0f, 0.5f, 0.0f, 0.0f};
+    bias.cols[2] = {0.0f, 0.0f, 1.0f, 0.0f};
+    bias.cols[3] = {0.5f, 0.5f, 0.0f, 1.0f};
+    m.shadow_matrices[c] = mat;
+    m.uv_space_shadow_matrices[c] = matmul(bias, mat);
+    m.shadow_view_matrices[c] = view;
+    m.shadow_sphere_radii[c] = radius;
+}
+
+// Min over non-zero depth bits and max over all depth bits of the main view
+// (read_depth.glsl:3-18,57-82: the 4x4 gathers with clamp-to-edge visit
+// every texel), reduced per warp and merged with one atomic per warp; the
+// last block to finish fits the 4 cascades.
+__global__ void __launch_bounds__(256) k_depth_reduce_fit(FrameDev f) {
+    const uint64_t npx = (uint64_t)f.uniforms->window_size.x * f.uniforms->window_size.y;
+    uint32_t mn = 0xFFFFFFFFu, mx = 0u;
+    const uint4* p = reinterpret_cast<const uint4*>(f.visibility);
+    const uint64_t n2 = npx / 2;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint4 v = __ldcs(p + i);  // streaming: each pixel is read once
+        uint32_t d0 = v.y, d1 = v.w;
+        mx = max(mx, max(d0, d1));
+        if (d0) mn = min(mn, d0);
+        if (d1) mn = min(mn, d1);
+    }
+    if ((npx & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+        uint32_t d = (uint32_t)(reinterpret_cast<const unsigned long long*>(f.visibility)[npx - 1] >> 32);
+        mx = max(mx, d);
+        if (d) mn = min(mn, d);
+    }
+    mn = __reduce_min_sync(0xFFFFFFFFu, mn);
+    mx = __reduce_max_sync(0xFFFFFFFFu, mx);
+    if ((threadIdx.x & 31) == 0) {
+        if (mn != 0xFFFFFFFFu) atomicMin(&f.misc->min_depth, mn);
+        atomicMax(&f.misc->max_depth, mx);
+    }
+    __shared__ bool s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(&f.status[kStReduceDone], 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    const uint32_t min_bits = atomicOr(&f.misc->min_depth, 0u), max_bits = atomicOr(&f.misc->max_depth, 0u);
+    if (threadIdx.x == 0 && min_bits == 0xFFFFFFFFu) atomicOr(&f.status[kStFlags], LH_FLAG_NO_DEPTH);
+    if (threadIdx.x < 4) fit_cascade(f, threadIdx.x, min_bits, max_bits);
+}
+
+// ---------------------------------------------------------------- resolve
+struct Tex4 { float r, g, b, a; };
+
+// Bilinear filtering of level 0 with repeat addressing.
+__device__ Tex4 sample_repeat(const FrameDev& f, uint32_t index, f2 uv) {
+    if (index >= f.n_textures) return {0.0f, 0.0f, 0.0f, 0.0f};
+    const lh_texture t = f.textures[index];
+    const uint8_t* tex = reinterpret_cast<const uint8_t*>(t.texels);
+    float u = uv.x * (float)t.width - 0.5f, v = uv.y * (float)t.height - 0.5f;
+    if (!(fabsf(u) < 1e9f)) u = 0.0f;
+    if (!(fabsf(v) < 1e9f)) v = 0.0f;
+    float fu = floorf(u), fv = floorf(v);
+    float a = u - fu, b = v - fv;
+    long long i0 = (long long)fu, j0 = (long long)fv;
+    long long W = t.width, H = t.height;
+    long long ia = ((i0 % W) + W) % W, ib = (((i0 + 1) % W) + W) % W;
+    long long ja = ((j0 % H) + H) % H, jb = (((j0 + 1) % H) + H) % H;
+    auto texel = [&](long long i, long long j) {
+        uchar4 p = __ldg(reinterpret_cast<const uchar4*>(tex) + ((size_t)j * W + i));
+        Tex4 r;
+        if (t.srgb) { r.r = f.srgb_lut[p.x]; r.g = f.srgb_lut[p.y]; r.b = f.srgb_lut[p.z]; }
+        else { r.r = (float)p.x / 255.0f; r.g = (float)p.y / 255.0f; r.b = (float)p.z / 255.0f; }
+        r.a = (float)p.w / 255.0f;
+        return r;
+    };
+    Tex4 t00 = texel(ia, ja), t10 = texel(ib, ja), t01 = texel(ia, jb), t11 = texel(ib, jb);
+    float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+    Tex4 r;
+    r.r = ((t00.r * w00 + t10.r * w10) + t01.r * w01) + t11.r * w11;
+    r.g = ((t00.g * w00 + t10.g * w10) + t01.g * w01) + t11.g * w11;
+    r.b = ((t00.b * w00 + t10.b * w10) + t01.b * w01) + t11.b * w11;
+    r.a = ((t00.a * w00 + t10.a * w10) + t01.a * w01) + t11.a * w11;
+    return r;
+}
+
+// Comparison sampling (compare op LESS, linear, clamp to edge) of layer
+// clamp(round(layer), 0, 3).
+__device__ float sample_shadow(const FrameDev& f, f2 uv, float layer_f, float ref) {
+    int layer = __float2int_rn(layer_f);
+    layer = min(max(layer, 0), 3);
+    const uint32_t S = f.shadow_size;
+    const float* map = f.shadow_maps + (size_t)layer * S * S;
+    float u = uv.x * (float)S - 0.5f, v = uv.y * (float)S - 0.5f;
+    if (!(fabsf(u) < 1e9f)) u = 0.0f;
+    if (!(fabsf(v) < 1e9f)) v = 0.0f;
+    float fu = floorf(u), fv = floorf(v);
+    float a = u - fu, b = v - fv;
+    long long i0 = (long long)fu, j0 = (long long)fv;
+    auto cl = [&](long long i) { return i < 0 ? 0ll : (i > (long long)S - 1 ? (long long)S - 1 : i); };
+    auto cmp = [&](long long i, long long j) { return ref < __ldg(map + (size_t)cl(j) * S + cl(i)) ? 1.0f : 0.0f; };
+    float c00 = cmp(i0, j0), c10 = cmp(i0 + 1, j0), c01 = cmp(i0, j0 + 1), c11 = cmp(i0 + 1, j0 + 1);
+    float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+    return ((c00 * w00 + c10 * w10) + c01 * w01) + c11 * w11;
+}
+
+constexpr float kPi = 3.14159265358979323846f;
+
+// pbr.glsl:3-96
+__device__ __forceinline__ float F_Schlick1(float u, float f0, float f90) { return f0 + (f90 - f0) * powf(1.0f - u, 5.0f); }
+__device__ __forceinline__ float Fd_Burley(float NoV, float NoL, float LoH, float rough) {
+    float f90 = 0.5f + 2.0f * rough * LoH * LoH;
+    float light = F_Schlick1(NoL, 1.0f, f90);
+    float view = F_Schlick1(NoV, 1.0f, f90);
+    return light * view * (1.0f / kPi);
+}
+__device__ __forceinline__ float D_GGX(float NoH, float a) {
+    float a2 = a * a;
+    float fq = (NoH * a2 - NoH) * NoH + 1.0f;
+    return a2 / (kPi * fq * fq);
+}
+__device__ __forceinline__ float V_SmithGGXCorrelated(float NoV, float NoL, float a) {
+    float a2 = a * a;
+    float GGXL = NoV * sqrtf((-NoL * a2 + NoL) * NoL + a2);
+    float GGXV = NoL * sqrtf((-NoV * a2 + NoV) * NoV + a2);
+    return 0.5f / (GGXV + GGXL);
+}
+__device__ __forceinline__ float clampf(float x, float lo, float hi) { return gmin(gmax(x, lo), hi); }
+__device__ f3 BRDF(f3 v, f3 l, f3 n, float pr, float metallic, f3 base, bool thin) {
+    f3 h = normalize(v + l);
+    f3 diffuse = base * (1.0f - metallic);
+    float refl = (1.5f - 1.0f) / (1.5f + 1.0f);
+    refl = refl * refl;
+    f3 f0 = f3{refl, refl, refl} * (1.0f - metallic) + base * metallic;
+    float NoV = clampf(dot(n, v), 1e-5f, 1.0f);
+    float NoL = clampf(dot(n, l), 0.0f, 1.0f);
+    float NoH = clampf(dot(n, h), 0.0f, 1.0f);
+    float LoH = clampf(dot(l, h), 0.0f, 1.0f);
+    float rough = pr * pr;
+    float D = D_GGX(NoH, rough);
+    float p = powf(1.0f - LoH, 5.0f);
+    f3 F{f0.x + (1.0f - f0.x) * p, f0.y + (1.0f - f0.y) * p, f0.z + (1.0f - f0.z) * p};
+    float V = V_SmithGGXCorrelated(NoV, NoL, rough);
+    f3 Fr = F * (D * V);
+    f3 Fd = diffuse * Fd_Burley(NoV, NoL, LoH, rough);
+    f3 irr = (Fd + Fr) * NoL;
+    irr = f3{gmax(irr.x, 0.0f), gmax(irr.y, 0.0f), gmax(irr.z, 0.0f)};
+    if (thin) {
+        float rNoV = clampf(dot(-n, v), 1e-5f, 1.0f);
+        float rNoL = clampf(dot(-n, l), 0.0f, 1.0f);
+        irr = irr + diffuse * Fd_Burley(rNoV, rNoL, LoH, rough) * rNoL;
+    }
+    return {isnan(irr.x) ? 0.0f : irr.x, isnan(irr.y) ? 0.0f : irr.y, isnan(irr.z) ? 0.0f : irr.z};
+}
+
+struct Bary { f3 lambda, ddx, ddy; };
+
+// vbuffer.glsl:11-63
+__device__ Bary calc_full_bary(f4 p0, f4 p1, f4 p2, f2 ndc, f2 win) {
+    Bary r;
+    f3 invW{1.0f / p0.w, 1.0f / p1.w, 1.0f / p2.w};
+    f2 n0{p0.x * invW.x, p0.y * invW.x}, n1{p1.x * invW.y, p1.y * invW.y}, n2{p2.x * invW.z, p2.y * invW.z};
+    f2 ca{n2.x - n1.x, n2.y - n1.y}, cb{n0.x - n1.x, n0.y - n1.y};
+    float invDet = 1.0f / (ca.x * cb.y - cb.x * ca.y);
+    r.ddx = f3{n1.y - n2.y, n2.y - n0.y, n0.y - n1.y} * invDet * invW;
+    r.ddy = f3{n2.x - n1.x, n0.x - n2.x, n1.x - n0.x} * invDet * invW;
+    float ddxSum = dot(r.ddx, f3{1.0f, 1.0f, 1.0f});
+    float ddySum = dot(r.ddy, f3{1.0f, 1.0f, 1.0f});
+    f2 dv{ndc.x - n0.x, ndc.y - n0.y};
+    float interpInvW = (invW.x + dv.x * ddxSum) + dv.y * ddySum;
+    float interpW = 1.0f / interpInvW;
+    r.lambda.x = interpW * ((invW.x + dv.x * r.ddx.x) + dv.y * r.ddy.x);
+    r.lambda.y = interpW * ((0.0f + dv.x * r.ddx.y) + dv.y * r.ddy.y);
+    r.lambda.z = interpW * ((0.0f + dv.x * r.ddx.z) + dv.y * r.ddy.z);
+    r.ddx = r.ddx * (2.0f / win.x);
+    r.ddy = r.ddy * (2.0f / win.y);
+    ddxSum *= 2.0f / win.x;
+    ddySum *= 2.0f / win.y;
+    r.ddy = r.ddy * -1.0f;
+    ddySum *= -1.0f;
+    float interpW_ddx = 1.0f / (interpInvW + ddxSum);
+    float interpW_ddy = 1.0f / (interpInvW + ddySum);
+    r.ddx = (r.lambda * interpInvW + r.ddx) * interpW_ddx - r.lambda;
+    r.ddy = (r.lambda * interpInvW + r.ddy) * interpW_ddy - r.lambda;
+    return r;
+}
+__device__ __forceinline__ f3 interp_deriv(const Bary& b, float v0, float v1, float v2) {
+    f3 m{v0, v1, v2};
+    return {dot(m, b.lambda), dot(m, b.ddx), dot(m, b.ddy)};
+}
+
+struct MeshInfoResolve {
+    uint64_t positions, indices, normals, uvs, micro_indices, meshlets;
+    uint32_t flags;
+    lh_vec2 texture_scale, texture_offset;
+    uint32_t base_tex, mr_tex, normal_tex;
+    lh_vec3 base_color_factor;
+};
+__device__ __forceinline__ MeshInfoResolve load_mesh_info_resolve(const MeshInfo* mi) {
+    const unsigned long long* w = reinterpret_cast<const unsigned long long*>(mi);
+    const uint32_t* d = reinterpret_cast<const uint32_t*>(mi);
+    MeshInfoResolve r;
+    r.positions = __ldg(w + 0);
+    r.indices = __ldg(w + 1);
+    r.normals = __ldg(w + 2);
+    r.uvs = __ldg(w + 3);
+    r.micro_indices = __ldg(w + 4);
+    r.meshlets = __ldg(w + 5);
+    r.flags = (uint32_t)((__ldg(w + 6) >> 16) & 0xFFu);
+    r.texture_scale = {__uint_as_float(__ldg(d + 17)), __uint_as_float(__ldg(d + 18))};
+    r.texture_offset = {__uint_as_float(__ldg(d + 19)), __uint_as_float(__ldg(d + 20))};
+    uint32_t t01 = __ldg(d + 21), t2 = __ldg(d + 22);
+    r.base_tex = t01 & 0xFFFFu;
+    r.mr_tex = t01 >> 16;
+    r.normal_tex = t2 & 0xFFFFu;
+    r.base_color_factor = {__uint_as_float(__ldg(d + 23)), __uint_as_float(__ldg(d + 24)), __uint_as_float(__ldg(d + 25))};
+    return r;
+}
+
+// render_geometry.comp:70-266, one thread per pixel (blocks of 32 x 8).
+__global__ void __launch_bounds__(256) k_resolve(FrameDev f) {
+    const Uniforms& u = *f.uniforms;
+    const uint32_t W = u.window_size.x, H = u.window_size.y;
+    const uint32_t x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const f2 ndc{(float)x / (float)W * 2.0f - 1.0f, (float)y / (float)H * 2.0f - 1.0f};
+    const unsigned long long vis = __ldcs(reinterpret_cast<const unsigned long long*>(f.visibility) + (size_t)y * W + x);
+    float4* out = f.hdr + (size_t)y * W + x;
+    if (u2f((uint32_t)(vis >> 32)) == 0.0f) {
+        f4 un = mul(u.perspective_inverse, f4{ndc.x, ndc.y, 0.0f, 1.0f});
+        f3 lr = normalize(f3{un.x, un.y, un.z});
+        f4 r4 = mul(u.view_inverse, f4{lr.x, lr.y, lr.z, 0.0f});
+        // procedural sky in place of the missing cubemap asset
+        f3 s = f3{0.25f + 0.10f * r4.y, 0.35f + 0.15f * r4.y, 0.55f + 0.25f * r4.y} * powf(2.0f, 3.0f);
+        __stcs(out, make_float4(s.x, s.y, s.z, 1.0f));
+        return;
+    }
+    const uint32_t packed = (uint32_t)vis;
+    const uint32_t slot = packed & ((1u << 24) - 1u), tri = packed >> 24;
+    const MeshletReference ref = f.views[0].refs[slot];
+    const Instance* inst = f.instances + ref.instance_index;
+    const MeshInfoResolve mi = load_mesh_info_resolve(mesh_info_of(inst));
+    const Meshlet* ml = reinterpret_cast<const Meshlet*>(mi.meshlets) + ref.meshlet_index;
+    const uint32_t tri_off = __ldg(&ml->triangle_offset), idx_off = __ldg(&ml->index_offset);
+    const uint8_t* micro = reinterpret_cast<const uint8_t*>(mi.micro_indices) + tri_off + tri * 3;
+    const uint32_t flags = mi.flags;
+    uint32_t idx[3];
+    for (int k = 0; k < 3; k++) {
+        uint32_t vi = idx_off + __ldg(micro + k);
+        idx[k] = (flags & MESH_INFO_FLAGS_32_BIT_INDICES) ? __ldg(reinterpret_cast<const uint32_t*>(mi.indices) + vi)
+                                                          : __ldg(reinterpret_cast<const uint16_t*>(mi.indices) + vi);
+    }
+    const lh_mat4& T = inst->transform;
+    f3 pa = world_pos(T, load_position(mi.positions, flags, idx[0]));
+    f3 pb = world_pos(T, load_position(mi.positions, flags, idx[1]));
+    f3 pc = world_pos(T, load_position(mi.positions, flags, idx[2]));
+    const lh_mat4& PV = u.combined_perspective_view;
+    Bary bary = calc_full_bary(mul(PV, f4{pa.x, pa.y, pa.z, 1.0f}), mul(PV, f4{pb.x, pb.y, pb.z, 1.0f}),
+                               mul(PV, f4{pc.x, pc.y, pc.z, 1.0f}), ndc, f2{(float)W, (float)H});
+    f3 wx = interp_deriv(bary, pa.x, pb.x, pc.x), wy = interp_deriv(bary, pa.y, pb.y, pc.y),
+       wz = interp_deriv(bary, pa.z, pb.z, pc.z);
+    f3 world{wx.x, wy.x, wz.x}, wdx{wx.y, wy.y, wz.y}, wdy{wx.z, wy.z, wz.z};
+    f2 ua = load_uv_raw(mi.uvs, flags, idx[0]), ub = load_uv_raw(mi.uvs, flags, idx[1]),
+       uc = load_uv_raw(mi.uvs, flags, idx[2]);
+    f2 ts{mi.texture_scale.x, mi.texture_scale.y};
+    f3 uvx = interp_deriv(bary, ua.x * ts.x, ub.x * ts.x, uc.x * ts.x);
+    f3 uvy = interp_deriv(bary, ua.y * ts.y, ub.y * ts.y, uc.y * ts.y);
+    f2 uv{uvx.x + mi.texture_offset.x, uvy.x + mi.texture_offset.y};
+    f2 uvdx{uvx.y, uvy.y}, uvdy{uvx.z, uvy.z};
+    f3 view_vector = normalize(ld3(u.camera_pos) - world);
+    f3 na = normalize(load_normal_raw(mi.normals, flags, idx[0]));
+    f3 nb = normalize(load_normal_raw(mi.normals, flags, idx[1]));
+    f3 nc = normalize(load_normal_raw(mi.normals, flags, idx[2]));
+    f3 normal{interp_deriv(bary, na.x, nb.x, nc.x).x, interp_deriv(bary, na.y, nb.y, nc.y).x,
+              interp_deriv(bary, na.z, nb.z, nc.z).x};
+    normal = normalize(mul3(inst->normal_transform, normal));
+    f3 gn = cross(pb - pa, pc - pa);
+    if (dot(gn, view_vector) < 0.0f) normal = -normal;
+    uint32_t ci;
+    f4 sc{0.0f, 0.0f, 0.0f, 0.0f};
+    for (ci = 0; ci < 4; ci++) {
+        sc = mul(f.misc->uv_space_shadow_matrices[ci], f4{world.x, world.y, world.z, 1.0f});
+        float ox = sc.x - 0.5f, oy = sc.y - 0.5f;
+        if (fabsf(ox) < 0.5f && fabsf(oy) < 0.5f) break;
+    }
+    const bool alpha = (flags & MESH_INFO_FLAGS_ALPHA_CLIP) != 0;
+    const float bias = alpha ? 0.000002f : 0.0f;
+    sc = f4{sc.x / sc.w, sc.y / sc.w, sc.z / sc.w, sc.w / sc.w};
+    float shadow_sum = 0.0f;
+    for (int ox = -1; ox <= 1; ox++)
+        for (int oy = -1; oy <= 1; oy++) {
+            f2 off{(float)ox / 1024.0f, (float)oy / 1024.0f};
+            shadow_sum += sample_shadow(f, f2{sc.x + off.x, sc.y + off.y}, (float)ci, sc.z - bias);
+        }
+    shadow_sum /= 9.0f;
+    if (sc.z > 1.0f) shadow_sum = 1.0f;
+    Tex4 bc = sample_repeat(f, mi.base_tex, uv);
+    f3 base{bc.r * mi.base_color_factor.x, bc.g * mi.base_color_factor.y, bc.b * mi.base_color_factor.z};
+    Tex4 mr = sample_repeat(f, mi.mr_tex, uv);
+    float roughness = mr.g, metallic = mr.b;
+    if (mi.normal_tex != UNUSED_TEXTURE_INDEX) {
+        Tex4 nt = sample_repeat(f, mi.normal_tex, uv);
+        f3 mn{nt.r * 255.0f / 127.0f - 128.0f / 127.0f, nt.g * 255.0f / 127.0f - 128.0f / 127.0f,
+              nt.b * 255.0f / 127.0f - 128.0f / 127.0f};
+        f3 dpy = cross(wdy, normal), dpx = cross(normal, wdx);
+        f3 t = dpy * uvdx.x + dpx * uvdy.x;
+        f3 b = dpy * uvdx.y + dpx * uvdy.y;
+        float invmax = 1.0f / sqrtf(gmax(dot(t, t), dot(b, b)));
+        f3 tt = t * invmax, bb = b * invmax;
+        normal = normalize(f3{(tt.x * mn.x + bb.x * mn.y) + normal.x * mn.z, (tt.y * mn.x + bb.y * mn.y) + normal.y * mn.z,
+                              (tt.z * mn.x + bb.z * mn.y) + normal.z * mn.z});
+    }
+    // AMBIENT_SH (render_geometry.comp:40-57): only sh[0] = sh[2] = 0.025.
+    const float amb_level = 0.025f;
+    const f3 zero{0.0f, 0.0f, 0.0f}, sh0{amb_level, amb_level, amb_level};
+    f3 amb = ((((((((sh0 + zero * normal.x) + sh0 * normal.y) + zero * normal.z) + zero * (normal.x * normal.z)) +
+                  zero * (normal.z * normal.y)) + zero * (normal.y * normal.x)) +
+               zero * (3.0f * normal.z * normal.z - 1.0f)) + zero * (normal.x * normal.x - normal.y * normal.y));
+    f3 ambient = amb * (base * (1.0f - metallic));
+    float sun_intensity = kPi * shadow_sum;
+    f3 sun = BRDF(view_vector, ld3(u.sun_dir), normal, roughness, metallic, base, alpha) * sun_intensity;
+    f3 o = sun + ambient;
+    __stcs(out, make_float4(o.x, o.y, o.z, 1.0f));
+}
+
+}  // namespace
+
+cudaError_t launch_clear_targets(const FrameDev& f, cudaStream_t s, int sms) {
+    dim3 grid((unsigned)sms, f.n_views);
+    k_clear_targets<<<grid, 256, 0, s>>>(f);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_depth_reduce_fit(const FrameDev& f, cudaStream_t s, int sms) {
+    k_depth_reduce_fit<<<(unsigned)sms * 2, 256, 0, s>>>(f);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_resolve(const FrameDev& f, uint32_t width, uint32_t height, cudaStream_t s) {
+    dim3 grid((width + 31) / 32, (height + 7) / 8);
+    k_resolve<<<grid, dim3(32, 8), 0, s>>>(f);
+    return cudaGetLastError();
+}
+
+}  // namespace lh

@@ -1,0 +1,120 @@
+"""CUDA path (through the C ABI) against the CPU oracle on seeded scenes.
+
+Bit exact: prefix-sum sectors, visible-meshlet lists, draw commands,
+visibility IDs and depth, MiscStorage (cascade fit), shadow maps.
+Within 2^-10 max abs: linear HDR radiance.
+"""
+import numpy as np
+import pytest
+
+from tests.parity import compare_frame
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(native, oracle, config_id, seed=None, max_draws=200000, max_instances=None, frames=1, **params):
+    lh = native
+    scene = lh.Scene(config_id, seed=seed, **params).upload(0)
+    d = scene.desc
+    cap = max_instances or max(1024, d.n_instances)
+    cfg = lh.Config(width=d.width, height=d.height, shadow_size=d.shadow_size, max_instances=cap,
+                    max_draws=max_draws, device=0)
+    r = lh.Renderer(cfg)
+    r.set_scene(scene)
+    for _ in range(frames):
+        r.frame(scene.uniforms)
+    st = r.status()
+    fr = oracle.run_scene(scene, shadow_size=d.shadow_size, max_instances=cap, max_draws=max_draws)
+    return scene, r, fr, st, cap
+
+
+def _assert_parity(r, fr, md, cap, st, fr_flags=None):
+    errors, stats = compare_frame(r, fr, md, cap)
+    assert not errors, "\n".join(errors) + "\nstats %s" % stats
+    if fr_flags is not None:
+        assert st.flags == fr_flags, "device flags %#x oracle %#x" % (st.flags, fr_flags)
+    return stats
+
+
+def test_config1_frame_parity(native, oracle):
+    scene, r, fr, st, cap = _run(native, oracle, 1)
+    stats = _assert_parity(r, fr, 200000, cap, st, fr.flags)
+    assert stats["covered"] > 1000
+    assert st.visible_opaque[0] > 0
+
+
+def test_config1_repeat_frames_identical(native, oracle):
+    """Two frames in a row give identical results (counters reset, canonical order)."""
+    scene, r, fr, st, cap = _run(native, oracle, 1, frames=2)
+    _assert_parity(r, fr, 200000, cap, st)
+
+
+def test_config1_quantized_formats(native, oracle):
+    """Reference vertex formats: u16 positions, i8 normals, u16 uvs, 16-bit indices."""
+    scene, r, fr, st, cap = _run(native, oracle, 1, quantized=1)
+    _assert_parity(r, fr, 200000, cap, st)
+
+
+def test_config1_reference_normal_transform(native, oracle):
+    """normal_transform = mat3(inverse(M)) exactly as the reference's Instance constructor."""
+    scene, r, fr, st, cap = _run(native, oracle, 1, reference_normal_transform=1)
+    _assert_parity(r, fr, 200000, cap, st)
+
+
+def test_config2_reduced_parity(native, oracle):
+    """Config 2 layout (clustered scene, textured materials) at reduced mesh detail."""
+    scene, r, fr, st, cap = _run(native, oracle, 2, detail=0.25, n_instances=1024, width=960, height=540)
+    stats = _assert_parity(r, fr, 200000, cap, st)
+    assert stats["covered"] > 10000
+
+
+def test_config2_full_parity(native, oracle):
+    """Config 2 at full size: 4,096 instances, ~50M triangles, 1920x1080."""
+    scene, r, fr, st, cap = _run(native, oracle, 2)
+    stats = _assert_parity(r, fr, 200000, cap, st)
+    assert stats["covered"] > 100000
+
+
+def test_overflow_capacities_flagged(native, oracle):
+    """Capacities below need: work is dropped and flagged, never written out of bounds."""
+    scene, r, fr, st, cap = _run(native, oracle, 1, max_draws=500, max_instances=16)
+    assert st.flags & native.FLAG_INSTANCE_OVERFLOW
+    assert st.flags & native.FLAG_DRAW_OVERFLOW
+    assert fr.flags & native.FLAG_INSTANCE_OVERFLOW
+    _assert_parity(r, fr, 500, 16, st)
+
+
+def test_empty_view(native, oracle):
+    """Camera looking away from everything: no visible instances, all-sky frame."""
+    lh = native
+    scene = lh.Scene(1).upload(0)
+    d = scene.desc
+    u = lh.make_uniforms((0.0, 0.0, -150.0), -1.5707963, 0.0, 60.0, d.width, d.height, d.n_instances)
+    cfg = lh.Config(width=d.width, height=d.height, shadow_size=1024, max_instances=1024, max_draws=200000)
+    r = lh.Renderer(cfg)
+    r.set_scene(scene)
+    r.frame(u)
+    st = r.status()
+    fr = oracle.run_scene(scene, shadow_size=1024, max_instances=1024, max_draws=200000, uniforms=u)
+    assert st.visible_instances[0] == 0
+    assert st.flags & lh.FLAG_NO_DEPTH
+    errors, _ = compare_frame(r, fr, 200000, 1024)
+    assert not errors, errors
+
+
+def test_zero_instances(native):
+    lh = native
+    scene = lh.Scene(1, n_instances=1).upload(0)
+    d = scene.desc
+    u = scene.uniforms
+    cfg = lh.Config(width=d.width, height=d.height, shadow_size=256, max_instances=1024, max_draws=1000)
+    r = lh.Renderer(cfg)
+    r.set_scene(scene)
+    # uniforms.num_instances = 0: nothing is culled or drawn
+    b = bytearray(bytes(u))
+    b[532:536] = (0).to_bytes(4, "little")
+    u0 = lh.Uniforms.from_buffer_copy(bytes(b))
+    r.frame(u0)
+    st = r.status()
+    assert st.visible_instances[0] == 0 and st.visible_opaque[0] == 0
+    assert (r.visibility() == 0).all()
