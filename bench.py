@@ -244,6 +244,8 @@ def run_gpu(args):
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "gtri_per_s": tri_total / (ms * 1e-3) / 1e9,
         "visible_meshlets": vis_ml, "candidate_meshlets": cand, "visible_instances": vis_inst,
+        "shadow_visible_meshlets": [int(st.visible_opaque[k]) for k in range(1, 5)],
+        "big_triangles_last_pass": int(st.big_triangles), "clipped_triangles_last_pass": int(st.clipped_triangles),
         "stage_ms": {k: round(v, 4) for k, v in stage_ms.items()},
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": 560 + 8, "d2h_bytes_per_step": npx * 16},
         "gpu_launches": 13 * args.steps,

@@ -48,6 +48,7 @@ struct lh_ctx {
     float4* d_hdr = nullptr;
     uint64_t* d_probe_vis = nullptr;
     BigTri* d_big = nullptr;
+    uint32_t* d_big_base = nullptr;
     ClipItem* d_clip = nullptr;
     ViewDev* d_views = nullptr;
     lh_texture* d_textures = nullptr;
@@ -179,6 +180,7 @@ FrameDev frame_dev(const lh_ctx* c, uint32_t n_views, uint32_t n_instances) {
     f.status = reinterpret_cast<uint32_t*>(c->d_reset);
     f.views = c->d_views;
     f.big = c->d_big;
+    f.big_base = c->d_big_base;
     f.big_cap = c->cfg.max_big_triangles;
     f.clip = c->d_clip;
     f.clip_cap = c->cfg.max_big_triangles;
@@ -335,7 +337,7 @@ lh_status lh_create(const lh_config* config, lh_ctx** out) {
     if (!c) return LH_ERR_OUT_OF_MEMORY;
     c->cfg = cfg;
     c->device = cfg.device;
-    c->tuning = lh_tuning{4u, 4096u, 4.0f, 0u};
+    c->tuning = lh_tuning{8u, 256u, 4.0f, 0u};
     cudaError_t e = cudaSetDevice(c->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device);
     c->max_views = 5 + cfg.max_probes;
@@ -354,6 +356,7 @@ lh_status lh_create(const lh_config* config, lh_ctx** out) {
     if (e == cudaSuccess) e = dalloc(c, &c->d_hdr, W * H * 16);
     if (e == cudaSuccess) e = dalloc(c, &c->d_probe_vis, (size_t)std::max(cfg.max_probe_pixels, 32u) * 8);
     if (e == cudaSuccess) e = dalloc(c, &c->d_big, sizeof(BigTri) * (size_t)cfg.max_big_triangles);
+    if (e == cudaSuccess) e = dalloc(c, &c->d_big_base, sizeof(uint32_t) * (size_t)cfg.max_big_triangles);
     if (e == cudaSuccess) e = dalloc(c, &c->d_clip, sizeof(ClipItem) * (size_t)cfg.max_big_triangles);
     if (e == cudaSuccess) e = dalloc(c, &c->d_views, sizeof(ViewDev) * c->max_views);
     if (e == cudaSuccess) {
@@ -479,7 +482,7 @@ lh_status lh_read_status(lh_ctx* c, lh_device_status* out) {
     e = cudaMemcpy(words, c->d_reset, sizeof(words), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(c, e, "status read");
     out->flags = words[kStFlags];
-    out->big_triangles = words[kStBigCount];
+    out->big_triangles = words[kStBigPacked + 1] >> 8;  // high word of the packed u64: count << 8
     out->clipped_triangles = words[kStClipCount];
     out->n_views = c->n_views_last;
     for (uint32_t v = 0; v < c->n_views_last && v < 40; v++) {

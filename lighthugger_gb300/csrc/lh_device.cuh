@@ -233,19 +233,17 @@ __device__ __forceinline__ bool cover(const TriSetup& t, int32_t px, int32_t py,
 
 // Depth test + write: kind 0 keeps the max of (depth bits << 32 | id) in a
 // u64 visibility target (reverse-Z GREATER), kind 1 keeps the min of depth
-// bits in a u32 shadow target (LESS).
+// bits in a u32 shadow target (LESS).  The atomics return nothing (RED), so
+// a warp never waits on the L2 round trip of a fragment.
 template <int KIND>
 __device__ __forceinline__ void write_fragment(void* target, uint32_t W, int32_t px, int32_t py, float depth,
                                                uint32_t id) {
     size_t pix = (size_t)py * W + px;
     if (KIND == 0) {
         unsigned long long key = ((unsigned long long)f2u(depth) << 32) | id;
-        unsigned long long* p = reinterpret_cast<unsigned long long*>(target) + pix;
-        if (key > *reinterpret_cast<volatile unsigned long long*>(p)) atomicMax(p, key);
+        atomicMax(reinterpret_cast<unsigned long long*>(target) + pix, key);
     } else {
-        uint32_t bits = f2u(depth);
-        uint32_t* p = reinterpret_cast<uint32_t*>(target) + pix;
-        if (bits < *reinterpret_cast<volatile uint32_t*>(p)) atomicMin(p, bits);
+        atomicMin(reinterpret_cast<uint32_t*>(target) + pix, f2u(depth));
     }
 }
 

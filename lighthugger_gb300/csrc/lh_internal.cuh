@@ -40,29 +40,33 @@ struct ViewDev {
     uint32_t ml_tile_cap;       // capacity of ml_status
 };
 
-// Triangle handed to the tiled raster path (one entry per 16-row band).
+// Triangle handed to the chunked raster path: its set-up (orientation
+// normalised, pixel bounds) and the first of its 16 x 64-pixel chunks.
 struct BigTri {
     int32_t X0, Y0, X1, Y1, X2, Y2;
     float z0, s1, s2;
     uint32_t id;
     uint32_t view;
     uint32_t bias;
-    int32_t px0, px1, py0, py1;  // band-restricted pixel bounds
+    int32_t px0, px1, py0, py1;
 };
+constexpr int32_t kChunkRows = 16;
+constexpr int32_t kChunkCols = 64;
 
 struct ClipItem {
     uint32_t view, slot, tri, pad;
 };
 
-// Per-frame scratch words (zeroed at frame start).
+// Per-frame scratch words (zeroed at frame start; the raster words again
+// before each raster pass).
 enum StatusWord : uint32_t {
     kStFlags = 0,
-    kStBigCount = 1,
-    kStClipCount = 2,
-    kStRasterClaim = 3,
-    kStBigClaim = 4,
-    kStReduceDone = 5,
-    kStClipClaim = 6,
+    kStClipCount = 1,
+    kStRasterClaim = 2,
+    kStBigClaim = 3,
+    kStReduceDone = 4,
+    kStClipClaim = 5,
+    kStBigPacked = 8,  // u64 (words 8-9): big-triangle count << 40 | chunk count
     kStWords = 16
 };
 
@@ -76,6 +80,7 @@ struct FrameDev {
     uint32_t* status;           // kStWords words
     const ViewDev* views;       // n_views
     BigTri* big;
+    uint32_t* big_base;         // first chunk of each big triangle (ascending)
     uint32_t big_cap;
     ClipItem* clip;
     uint32_t clip_cap;

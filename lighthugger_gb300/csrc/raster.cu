@@ -78,26 +78,33 @@ __device__ __forceinline__ void load_transform(const Instance* inst, lh_mat4& m)
     for (int i = 0; i < 4; i++) d[i] = __ldg(s + i);
 }
 
+// Append a big triangle with one 64-bit atomic of {triangles:hi24, chunks:lo40}
+// (the packed single-pass append of prefix_sum.glsl:17-30): the triangle's
+// index and its first chunk come from the same word, so chunk bases ascend
+// with the index and the band kernel finds a chunk's triangle by binary search.
 __device__ void push_big(const FrameDev& f, const TriSetup& t, uint32_t view) {
-    uint32_t nb = (uint32_t)(t.py1 - t.py0) / kBandRows + 1;
-    uint32_t pos = atomicAdd(&f.status[kStBigCount], nb);
-    if ((uint64_t)pos + nb > f.big_cap) {
+    const uint32_t nbx = (uint32_t)(t.px1 - t.px0) / kChunkCols + 1;
+    const uint32_t nby = (uint32_t)(t.py1 - t.py0) / kChunkRows + 1;
+    const unsigned long long n = (unsigned long long)nbx * nby;
+    const unsigned long long old =
+        atomicAdd(reinterpret_cast<unsigned long long*>(f.status + kStBigPacked), (1ull << 40) | n);
+    const uint64_t idx = old >> 40, base = old & ((1ull << 40) - 1);
+    if (idx >= f.big_cap || base + n > 0xFFFFFFFFull) {
         atomicOr(&f.status[kStFlags], LH_FLAG_QUEUE_OVERFLOW);
         return;
     }
-    for (uint32_t b = 0; b < nb; b++) {
-        BigTri e;
-        e.X0 = t.X0; e.Y0 = t.Y0; e.X1 = t.X1; e.Y1 = t.Y1; e.X2 = t.X2; e.Y2 = t.Y2;
-        e.z0 = t.z0; e.s1 = t.s1; e.s2 = t.s2;
-        e.id = t.id;
-        e.view = view;
-        e.bias = t.bias;
-        e.px0 = t.px0;
-        e.px1 = t.px1;
-        e.py0 = t.py0 + (int32_t)(b * kBandRows);
-        e.py1 = min(t.py1, e.py0 + (int32_t)kBandRows - 1);
-        f.big[pos + b] = e;
-    }
+    BigTri e;
+    e.X0 = t.X0; e.Y0 = t.Y0; e.X1 = t.X1; e.Y1 = t.Y1; e.X2 = t.X2; e.Y2 = t.Y2;
+    e.z0 = t.z0; e.s1 = t.s1; e.s2 = t.s2;
+    e.id = t.id;
+    e.view = view;
+    e.bias = t.bias;
+    e.px0 = t.px0;
+    e.px1 = t.px1;
+    e.py0 = t.py0;
+    e.py1 = t.py1;
+    f.big[idx] = e;
+    f.big_base[idx] = (uint32_t)base;
 }
 
 template <int KIND>
@@ -136,8 +143,8 @@ __device__ __forceinline__ TriSetup shfl_setup(const TriSetup& s, int src) {
 }
 
 template <int KIND>
-__global__ void __launch_bounds__(kRasterWarps * 32) k_raster(FrameDev f, uint32_t view_begin, uint32_t n_views,
-                                                              RasterTune tune) {
+__global__ void __launch_bounds__(kRasterWarps * 32, 3) k_raster(FrameDev f, uint32_t view_begin, uint32_t n_views,
+                                                                 RasterTune tune) {
     __shared__ uint32_t s_prefix[kMaxViews + 1];
     __shared__ uint32_t s_nop[kMaxViews];
     __shared__ __align__(16) lh_mat4 s_vp[kMaxViews];
@@ -333,24 +340,68 @@ __global__ void __launch_bounds__(128) k_raster_clip(FrameDev f) {
     }
 }
 
+// Edge function of edge a->b at pixel centre (px, py).
+__device__ __forceinline__ int64_t edge_at(int32_t ax, int32_t ay, int32_t bx, int32_t by, int32_t px, int32_t py) {
+    return (int64_t)(by - ay) * ((int64_t)px * 256 + 128 - ax) - (int64_t)(bx - ax) * ((int64_t)py * 256 + 128 - ay);
+}
+
+// True when the edge's test fails at all four corners of the pixel
+// rectangle (the edge function is affine, so it fails everywhere inside).
+__device__ __forceinline__ bool edge_rejects(int32_t ax, int32_t ay, int32_t bx, int32_t by, int32_t x0, int32_t x1,
+                                             int32_t y0, int32_t y1, int64_t bias) {
+    return edge_at(ax, ay, bx, by, x0, y0) < bias && edge_at(ax, ay, bx, by, x1, y0) < bias &&
+           edge_at(ax, ay, bx, by, x0, y1) < bias && edge_at(ax, ay, bx, by, x1, y1) < bias;
+}
+
+// One warp per 16 x 64-pixel chunk of a big triangle; chunks whose
+// rectangle lies outside one edge are skipped whole.
 template <int KIND>
 __global__ void __launch_bounds__(256) k_raster_big(FrameDev f) {
-    const uint32_t n = min(*reinterpret_cast<volatile uint32_t*>(&f.status[kStBigCount]), f.big_cap);
+    const unsigned long long packed = *reinterpret_cast<volatile unsigned long long*>(f.status + kStBigPacked);
+    const uint32_t ntri = (uint32_t)min((unsigned long long)f.big_cap, packed >> 40);
+    const unsigned long long total = packed & ((1ull << 40) - 1);
     const uint32_t lane = threadIdx.x & 31;
+    if (ntri == 0) return;
     for (;;) {
-        uint32_t item = 0;
-        if (lane == 0) item = atomicAdd(&f.status[kStBigClaim], 1u);
-        item = __shfl_sync(0xFFFFFFFFu, item, 0);
-        if (item >= n) break;
-        const BigTri b = f.big[item];
+        unsigned long long c = 0;
+        if (lane == 0) c = atomicAdd(&f.status[kStBigClaim], 1u);
+        c = __shfl_sync(0xFFFFFFFFu, c, 0);
+        if (c >= total) break;
+        // upper_bound over the ascending chunk bases, minus one
+        uint32_t first = 0, count = ntri;
+        while (count > 0) {
+            uint32_t step = count / 2, cur = first + step;
+            bool greater = c >= f.big_base[cur];
+            first = greater ? cur + 1 : first;
+            count = greater ? count - (step + 1) : step;
+        }
+        if (first == 0) continue;
+        const uint32_t i = first - 1;
+        const BigTri b = f.big[i];
+        const uint32_t nbx = (uint32_t)(b.px1 - b.px0) / kChunkCols + 1;
+        const uint32_t nby = (uint32_t)(b.py1 - b.py0) / kChunkRows + 1;
+        const unsigned long long local = c - f.big_base[i];
+        if (local >= (unsigned long long)nbx * nby) continue;  // chunk of a dropped triangle
+        const int32_t cx = (int32_t)(local % nbx), cy = (int32_t)(local / nbx);
+        const int32_t x0 = b.px0 + cx * kChunkCols, x1 = min(b.px1, x0 + kChunkCols - 1);
+        const int32_t y0 = b.py0 + cy * kChunkRows, y1 = min(b.py1, y0 + kChunkRows - 1);
+        if (edge_rejects(b.X1, b.Y1, b.X2, b.Y2, x0, x1, y0, y1, b.bias & 1u) ||
+            edge_rejects(b.X2, b.Y2, b.X0, b.Y0, x0, x1, y0, y1, (b.bias >> 1) & 1u) ||
+            edge_rejects(b.X0, b.Y0, b.X1, b.Y1, x0, x1, y0, y1, (b.bias >> 2) & 1u))
+            continue;
         TriSetup t;
         t.X0 = b.X0; t.Y0 = b.Y0; t.X1 = b.X1; t.Y1 = b.Y1; t.X2 = b.X2; t.Y2 = b.Y2;
         t.z0 = b.z0; t.s1 = b.s1; t.s2 = b.s2;
         t.id = b.id;
         t.bias = b.bias;
-        t.px0 = b.px0; t.px1 = b.px1; t.py0 = b.py0; t.py1 = b.py1;
         const ViewDev* vw = f.views + b.view;
-        raster_warp<KIND>(t, vw->target, vw->width, lane);
+        void* target = vw->target;
+        const uint32_t W = vw->width;
+        for (int32_t py = y0; py <= y1; py++)
+            for (int32_t px = x0 + (int32_t)lane; px <= x1; px += 32) {
+                float d;
+                if (cover(t, px, py, d)) write_fragment<KIND>(target, W, px, py, d, t.id);
+            }
     }
 }
 
@@ -361,7 +412,8 @@ cudaError_t launch_raster_kind(const FrameDev& f, uint32_t view_begin, uint32_t 
     if (n_views == 0) return cudaSuccess;
     if (n_views > kMaxViews) return cudaErrorInvalidValue;
     RasterTune tune{small_px, medium_px};
-    cudaError_t e = cudaMemsetAsync(f.status + kStBigCount, 0, sizeof(uint32_t) * 6, s);
+    // raster words: clip count, claims, reduce counter, packed big-triangle word
+    cudaError_t e = cudaMemsetAsync(f.status + kStClipCount, 0, sizeof(uint32_t) * (kStBigPacked + 2 - kStClipCount), s);
     if (e != cudaSuccess) return e;
     if (kind == kViewVisibility) {
         k_raster<0><<<sms * 4, kRasterWarps * 32, 0, s>>>(f, view_begin, n_views, tune);

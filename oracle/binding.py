@@ -25,7 +25,8 @@ class FrameDesc(C.Structure):
 class FrameOut(C.Structure):
     _fields_ = [("prefix_sums", C.c_void_p), ("meshlet_references", C.c_void_p), ("draw_calls", C.c_void_p),
                 ("visibility", C.c_void_p), ("shadow_maps", C.c_void_p), ("misc", C.c_void_p), ("hdr", C.c_void_p),
-                ("stage_ms", C.c_double * 8), ("flags", C.c_uint32), ("reserved", C.c_uint32)]
+                ("stage_ms", C.c_double * 8), ("flags", C.c_uint32), ("reserved", C.c_uint32),
+                ("stats", C.c_uint64 * 16)]
 
 
 _lib = None
@@ -90,6 +91,13 @@ class OracleFrame:
     @property
     def stage_ms(self):
         return dict(zip(STAGE_NAMES, list(self.out.stage_ms)))
+
+    @property
+    def raster_stats(self):
+        names = ["triangles", "fragments", "bbox_le4", "bbox_le64", "bbox_le4096", "bbox_gt4096", "clipped",
+                 "max_meshlet_fragments"]
+        s = list(self.out.stats)
+        return {"visibility": dict(zip(names, s[:8])), "shadow": dict(zip(names, s[8:]))}
 
     @property
     def flags(self):

@@ -376,6 +376,7 @@ struct Target {
     uint64_t* vis;
     uint32_t* depth;
     uint32_t id;
+    uint64_t* stats;  // per-thread counters (may be null)
 };
 
 // Rasterise one snapped triangle whose orientation is already normalised
@@ -390,6 +391,11 @@ static void raster_tri(const Target& t, SnapV v0, SnapV v1, SnapV v2) {
     px0 = std::max(px0, 0); py0 = std::max(py0, 0);
     px1 = std::min(px1, (int32_t)t.W - 1); py1 = std::min(py1, (int32_t)t.H - 1);
     if (px0 > px1 || py0 > py1) return;
+    if (t.stats) {
+        uint64_t npx = (uint64_t)(px1 - px0 + 1) * (uint64_t)(py1 - py0 + 1);
+        t.stats[0]++;
+        t.stats[npx <= 4 ? 2 : npx <= 64 ? 3 : npx <= 4096 ? 4 : 5]++;
+    }
     int64_t b12 = top_left(v1, v2) ? 0 : 1, b20 = top_left(v2, v0) ? 0 : 1, b01 = top_left(v0, v1) ? 0 : 1;
     float fA = (float)A;
     float s1 = (v1.z - v0.z) / fA, s2 = (v2.z - v0.z) / fA;
@@ -402,6 +408,7 @@ static void raster_tri(const Target& t, SnapV v0, SnapV v1, SnapV v2) {
             float dpt = (v0.z + (float)e20 * s1) + (float)e01 * s2;
             dpt = dpt > 0.0f ? dpt : 0.0f;
             dpt = dpt < 1.0f ? dpt : 1.0f;
+            if (t.stats) t.stats[1]++;
             size_t pix = (size_t)py * t.W + px;
             if (t.kind == 0)
                 atomic_max_u64(&t.vis[pix], ((uint64_t)f2u(dpt) << 32) | t.id);
@@ -463,6 +470,7 @@ static void raster_primitive(const Target& t, const ClipV c[3]) {
             for (int i = 0; i < n; i++) poly[i] = out[i];
         }
         if (n < 3) return;
+        if (t.stats) t.stats[6]++;
     }
     SnapV s[9];
     for (int i = 0; i < n; i++) s[i] = snap(poly[i], hw, hh);
@@ -510,8 +518,11 @@ static void raster_view(Frame& F, uint32_t view, const Target& tgt_proto, const 
     for (uint32_t i = 0; i < nop; i++) slots.push_back(i);
     for (uint32_t i = 0; i < nal; i++) slots.push_back(md + i);
     std::atomic<uint32_t> flags{0};
+    std::vector<std::atomic<uint64_t>> acc(8);
+    uint64_t* out_stats = F.o->stats + (tgt_proto.kind ? 8 : 0);
     F.pool.run(slots.size(), 16, [&](size_t b, size_t e) {
         uint32_t fl = 0;
+        uint64_t st[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         for (size_t k = b; k < e; k++) {
             uint32_t slot = slots[k];
             const MeshletReference& ref = L.refs[slot];
@@ -527,12 +538,19 @@ static void raster_view(Frame& F, uint32_t view, const Target& tgt_proto, const 
                 if (!triangle_clip(F.d, vp, ref, tri, c, &fl)) continue;
                 Target t = tgt_proto;
                 t.id = LH_PACK_ID(tri, slot);
+                t.stats = st;
                 raster_primitive(t, c);
             }
+            uint64_t frags = st[1] - st[7];
+            st[7] = st[1];
+            uint64_t cur = acc[7].load();
+            while (frags > cur && !acc[7].compare_exchange_weak(cur, frags)) {}
         }
+        for (int i = 0; i < 7; i++) acc[i] += st[i];
         flags.fetch_or(fl);
     });
     F.o->flags |= flags.load();
+    for (int i = 0; i < 8; i++) out_stats[i] += acc[i].load();
 }
 
 // ------------------------------------------------------------ read_depth.glsl
@@ -951,6 +969,7 @@ int lho_frame(const lho_frame_desc* d, lho_frame_out* o) {
     uint32_t st = d->stages ? d->stages : LHO_STAGE_ALL;
     double t0 = now_ms(), t = t0;
     std::memset(o->stage_ms, 0, sizeof(o->stage_ms));
+    std::memset(o->stats, 0, sizeof(o->stats));
     o->flags = 0;
     // reset_buffers.glsl:9-29 and reset_counters (util.glsl:61-70)
     for (uint32_t v = 0; v < 5; v++) {
@@ -969,7 +988,7 @@ int lho_frame(const lho_frame_desc* d, lho_frame_out* o) {
     }
     lap(0);
     if (st & LHO_STAGE_RASTER) {
-        Target tg{0, F.W, F.H, o->visibility, nullptr, 0};
+        Target tg{0, F.W, F.H, o->visibility, nullptr, 0, nullptr};
         raster_view(F, 0, tg, d->uniforms->combined_perspective_view);
     }
     lap(1);
@@ -984,7 +1003,8 @@ int lho_frame(const lho_frame_desc* d, lho_frame_out* o) {
         for (uint32_t c = 0; c < 4; c++) write_draw_calls(F, 1 + c);
         lap(3);
         for (uint32_t c = 0; c < 4; c++) {
-            Target tg{1, F.S, F.S, nullptr, reinterpret_cast<uint32_t*>(o->shadow_maps + (size_t)c * F.S * F.S), 0};
+            Target tg{1, F.S, F.S, nullptr, reinterpret_cast<uint32_t*>(o->shadow_maps + (size_t)c * F.S * F.S), 0,
+                      nullptr};
             raster_view(F, 1 + c, tg, o->misc->shadow_matrices[c]);
         }
         lap(4);
@@ -1001,7 +1021,7 @@ int lho_raster_triangle(const float clip[12], uint32_t id, uint32_t kind, uint32
     if (!clip || !target || width == 0 || height == 0 || kind > 1) return LH_ERR_INVALID_ARGUMENT;
     ClipV c[3];
     for (int k = 0; k < 3; k++) c[k] = ClipV{clip[k * 4], clip[k * 4 + 1], clip[k * 4 + 2], clip[k * 4 + 3]};
-    Target t{kind, width, height, nullptr, nullptr, id};
+    Target t{kind, width, height, nullptr, nullptr, id, nullptr};
     std::vector<uint32_t> depth;
     if (kind == 0) {
         t.vis = target;

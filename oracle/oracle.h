@@ -75,6 +75,10 @@ typedef struct lho_frame_out {
     double stage_ms[8]; /* cull, raster, depth+fit, shadow cull, shadow raster, resolve, total, threads */
     uint32_t flags;     /* LH_FLAG_* */
     uint32_t reserved;
+    /* raster statistics, [0..7] visibility views, [8..15] shadow views:
+     * triangles set up, fragments covered, bbox <= 4 px, <= 64, <= 4096,
+     * > 4096, clipped, max fragments of one meshlet */
+    uint64_t stats[16];
 } lho_frame_out;
 
 int lho_frame(const lho_frame_desc* desc, lho_frame_out* out);
