@@ -175,6 +175,24 @@ lh_status lh_set_profiling(lh_ctx* ctx, int enable);
 /* Milliseconds of each stage of the last profiled frame (synchronises). */
 lh_status lh_get_stage_times(lh_ctx* ctx, float* ms, uint32_t n);
 
+/* Instance cull + single-pass prefix sum of one view that allocates
+ * nothing.  No counterpart in the reference: it exists for callers that
+ * cannot call cudaMalloc -- an engine that owns all device memory under a
+ * fixed budget, a frame loop that must not stall on an allocation (cudaMalloc
+ * can synchronise the device), code recording into a stream capture.
+ * Inputs: the device Instance array (16-byte aligned) and host Uniforms
+ * (passed to the kernel by value).  Output: a caller-owned prefix sector
+ * {u64 counter; PrefixSumValue[capacity]} in device memory, identical to
+ * lh_frame's main-view sector.  `d_flags` (optional, device) receives
+ * LH_FLAG_* bits.  The kernel's scratch is a fixed array inside the library
+ * of about 33 KB per GPU, so n_instances is limited to 1,048,576
+ * (LH_ERR_CAPACITY beyond).  The first call on a device looks up that
+ * array's address and should come before any stream capture; all calls share
+ * the array, so calls that overlap on the GPU race -- serialise them. */
+lh_status lh_cull_instances_noalloc(const Instance* d_instances, uint32_t n_instances,
+                                    const Uniforms* host_uniforms, uint8_t* d_sector, uint32_t capacity,
+                                    uint32_t* d_flags, void* stream);
+
 /* Synchronise the context's last stream and copy `bytes` from a device
  * address (e.g. a field of lh_frame_out) to host memory. */
 lh_status lh_download(lh_ctx* ctx, void* host_dst, uint64_t device_src, size_t bytes);
