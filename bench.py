@@ -96,6 +96,17 @@ def _measured_peak_hbm():
         return 6800.0, "fallback"
 
 
+def reduce_max_over_ranks(value, device=None):
+    """Max of a per-rank float over the process group (identity with one rank)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def cpu_oracle_frames(scene, frames, threads=0):
     from oracle import binding as ob
     d = scene.desc
@@ -200,10 +211,7 @@ def run_gpu(args):
     ms = sum(ms_steps) / len(ms_steps)
     stage_ms = {k: v / args.steps for k, v in stage_acc.items()}
     r.set_profiling(False)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = reduce_max_over_ranks(ms, device="cuda")
 
     # e2e through the C ABI with host buffers
     npx = d.width * d.height

@@ -145,13 +145,14 @@ __device__ __forceinline__ bool cull_cone_orthographic(const Uniforms& u, const 
 }
 
 // ------------------------------------------------------------------ rasterisation rules
-// Outcode bits: 1 z > w, 2 z < 0, 4 x > g*w, 8 x < -g*w, 16 y > g*w,
-// 32 y < -g*w; 64 = a non-finite coordinate or w <= 0 (the triangle is dropped).
+// Outcode bits: 1 z > w (or w <= 0), 2 z < 0, 4 x > g*w, 8 x < -g*w,
+// 16 y > g*w, 32 y < -g*w; 64 = a non-finite coordinate (the triangle is
+// dropped).  Any other bit sends the triangle to the clipper.
 __device__ __forceinline__ uint32_t outcode(f4 v) {
-    if (!(isfinite(v.x) && isfinite(v.y) && isfinite(v.z) && isfinite(v.w) && v.w > 0.0f)) return 64u;
+    if (!(isfinite(v.x) && isfinite(v.y) && isfinite(v.z) && isfinite(v.w))) return 64u;
     uint32_t c = 0;
     float g = LH_GUARD_BAND * v.w;
-    if (v.z > v.w) c |= 1u;
+    if (v.z > v.w || !(v.w > 0.0f)) c |= 1u;
     if (v.z < 0.0f) c |= 2u;
     if (v.x > g) c |= 4u;
     if (v.x < -g) c |= 8u;

@@ -316,6 +316,9 @@ __global__ void __launch_bounds__(128) k_raster_clip(FrameDev f) {
         }
         int np = clip_polygon(poly, 3);
         if (np < 3) continue;
+        bool projectable = true;  // false only for a triangle through the eye point
+        for (int k = 0; k < np; k++) projectable = projectable && poly[k].w > 0.0f;
+        if (!projectable) continue;
         const uint32_t W = vw->width, H = vw->height;
         const float hw = (float)W * 0.5f, hh = (float)H * 0.5f;
         SnapV s[9];

@@ -336,14 +336,16 @@ static void write_draw_calls(Frame& F, uint32_t view) {
 struct ClipV { float x, y, z, w; };
 struct SnapV { int32_t X, Y; float z; };
 
-// A vertex with a non-finite coordinate or w <= 0 drops the whole triangle.
+// A vertex with a non-finite coordinate drops the whole triangle.
 static bool finite4(const ClipV& v) {
-    return std::isfinite(v.x) && std::isfinite(v.y) && std::isfinite(v.z) && std::isfinite(v.w) && v.w > 0.0f;
+    return std::isfinite(v.x) && std::isfinite(v.y) && std::isfinite(v.z) && std::isfinite(v.w);
 }
+// Outcode bits: 1 z > w (or w <= 0), 2 z < 0, 4 x > g*w, 8 x < -g*w,
+// 16 y > g*w, 32 y < -g*w.
 static uint32_t outcode(const ClipV& v) {
     uint32_t c = 0;
     float g = LH_GUARD_BAND * v.w;
-    if (v.z > v.w) c |= 1;
+    if (v.z > v.w || !(v.w > 0.0f)) c |= 1;
     if (v.z < 0.0f) c |= 2;
     if (v.x > g) c |= 4;
     if (v.x < -g) c |= 8;
@@ -470,6 +472,9 @@ static void raster_primitive(const Target& t, const ClipV c[3]) {
             for (int i = 0; i < n; i++) poly[i] = out[i];
         }
         if (n < 3) return;
+        // a vertex left at w <= 0 (only a triangle through the eye point) cannot be projected
+        for (int i = 0; i < n; i++)
+            if (!(poly[i].w > 0.0f)) return;
         if (t.stats) t.stats[6]++;
     }
     SnapV s[9];

@@ -118,3 +118,45 @@ def test_zero_instances(native):
     st = r.status()
     assert st.visible_instances[0] == 0 and st.visible_opaque[0] == 0
     assert (r.visibility() == 0).all()
+
+
+def _camera_at_surface(lh, scene, inst_index, gap):
+    """Uniforms for a camera `gap` metres outside instance `inst_index`'s
+    bounding sphere, looking at its centre (gap < near plane: triangles
+    cross the near plane and must be clipped)."""
+    from tests import scene_view as sv
+    inst = sv.instances(scene)[inst_index]
+    T = inst["transform"]  # [col][row]
+    centre = T[3][:3].astype(np.float64)
+    mi = sv.mesh_info(int(inst["mesh_info_address"]))
+    bs = mi["bounding_sphere"].astype(np.float64)
+    scale = max(np.linalg.norm(T[c][:3]) for c in range(3))
+    centre = centre + sum(T[c][:3] * bs[c] for c in range(3))
+    radius = bs[3] * scale
+    direction = np.array([0.3, 0.2, -1.0])
+    direction /= np.linalg.norm(direction)
+    eye = centre + direction * (radius * 0.999 + gap)
+    f = -direction
+    yaw, pitch = float(np.arctan2(f[2], f[0])), float(np.arcsin(f[1]))
+    d = scene.desc
+    return lh.make_uniforms(tuple(float(x) for x in eye), yaw, pitch, 60.0, d.width, d.height, d.n_instances)
+
+
+@pytest.mark.parametrize("gap", [0.004, 0.5])
+def test_near_plane_clipping_parity(native, oracle, gap):
+    """Camera against an object's surface: near-plane and guard-band clipping."""
+    lh = native
+    scene = lh.Scene(1, width=640, height=360).upload(0)
+    d = scene.desc
+    u = _camera_at_surface(lh, scene, 3, gap)
+    cfg = lh.Config(width=d.width, height=d.height, shadow_size=512, max_instances=1024, max_draws=200000)
+    r = lh.Renderer(cfg)
+    r.set_scene(scene)
+    r.frame(u)
+    st = r.status()
+    fr = oracle.run_scene(scene, shadow_size=512, max_instances=1024, max_draws=200000, uniforms=u)
+    errors, stats = compare_frame(r, fr, 200000, 1024)
+    assert not errors, "\n".join(errors) + " %s" % stats
+    assert stats["covered"] > 0.5 * d.width * d.height  # the object fills the view
+    if gap < 0.01:
+        assert fr.raster_stats["visibility"]["clipped"] > 0
