@@ -121,9 +121,10 @@ def test_zero_instances(native):
 
 
 def _camera_at_surface(lh, scene, inst_index, gap):
-    """Uniforms for a camera `gap` metres outside instance `inst_index`'s
-    bounding sphere, looking at its centre (gap < near plane: triangles
-    cross the near plane and must be clipped)."""
+    """Uniforms for a camera `gap` metres above instance `inst_index`'s
+    surface, looking along the surface: triangles under the eye reach from
+    behind it to far in front, so they cross the near plane (gap < 0.01)
+    and leave the guard band, and must be clipped."""
     from tests import scene_view as sv
     inst = sv.instances(scene)[inst_index]
     T = inst["transform"]  # [col][row]
@@ -133,10 +134,13 @@ def _camera_at_surface(lh, scene, inst_index, gap):
     scale = max(np.linalg.norm(T[c][:3]) for c in range(3))
     centre = centre + sum(T[c][:3] * bs[c] for c in range(3))
     radius = bs[3] * scale
-    direction = np.array([0.3, 0.2, -1.0])
-    direction /= np.linalg.norm(direction)
-    eye = centre + direction * (radius * 0.999 + gap)
-    f = -direction
+    n = np.array([0.3, 0.2, -1.0])
+    n /= np.linalg.norm(n)
+    eye = centre + n * (radius * 0.999 + gap)
+    f = np.cross(n, [0.0, 1.0, 0.0])
+    f /= np.linalg.norm(f)
+    f = f - n * 0.05  # dip slightly towards the surface
+    f /= np.linalg.norm(f)
     yaw, pitch = float(np.arctan2(f[2], f[0])), float(np.arcsin(f[1]))
     d = scene.desc
     return lh.make_uniforms(tuple(float(x) for x in eye), yaw, pitch, 60.0, d.width, d.height, d.n_instances)
@@ -157,6 +161,6 @@ def test_near_plane_clipping_parity(native, oracle, gap):
     fr = oracle.run_scene(scene, shadow_size=512, max_instances=1024, max_draws=200000, uniforms=u)
     errors, stats = compare_frame(r, fr, 200000, 1024)
     assert not errors, "\n".join(errors) + " %s" % stats
-    assert stats["covered"] > 0.5 * d.width * d.height  # the object fills the view
+    assert stats["covered"] > 0.05 * d.width * d.height  # the surface fills part of the view
     if gap < 0.01:
         assert fr.raster_stats["visibility"]["clipped"] > 0
