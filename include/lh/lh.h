@@ -147,6 +147,14 @@ lh_status lh_frame_batched(lh_ctx* ctx, const Uniforms* host_uniforms,
                            const Uniforms* probe_uniforms, uint32_t n_probes,
                            void* stream, lh_frame_out* out);
 
+/* Same frame as lh_frame_batched, replayed from a CUDA graph: the first call
+ * (or a call with different probe sizes, tuning or scene) captures the
+ * frame's launches into a graph on a private stream; every call copies the
+ * per-frame uniforms on `stream` and launches the graph there. */
+lh_status lh_frame_graph(lh_ctx* ctx, const Uniforms* host_uniforms,
+                         const Uniforms* probe_uniforms, uint32_t n_probes,
+                         void* stream, lh_frame_out* out);
+
 /* Pointers to the context's result buffers (valid until lh_destroy). */
 lh_status lh_get_outputs(lh_ctx* ctx, lh_frame_out* out);
 
@@ -154,12 +162,17 @@ lh_status lh_get_outputs(lh_ctx* ctx, lh_frame_out* out);
 lh_status lh_read_status(lh_ctx* ctx, lh_device_status* out);
 
 /* Launch-shape knobs of the raster and cull kernels (set by the autotuner,
- * lighthugger_gb300/autotune.py).  Results never depend on them. */
+ * lighthugger_gb300/autotune.py) and the launch schedule.  Results never
+ * depend on them. */
+#define LH_SCHEDULE_DEFAULT 0    /* lh_frame: per stage; lh_frame_batched: persistent */
+#define LH_SCHEDULE_PER_STAGE 1  /* one launch per stage, each over all views of a kind */
+#define LH_SCHEDULE_PERSISTENT 2 /* cull + raster of all views in one cooperative launch */
+#define LH_SCHEDULE_PER_VIEW 3   /* each view's cull and raster launched on its own (the reference's per-cascade loop) */
 typedef struct lh_tuning {
     uint32_t small_px;        /* a lane rasterises triangles whose bbox has <= small_px pixels */
-    uint32_t medium_px;       /* the warp rasterises up to medium_px; larger go to 16-row bands */
-    float cull_blocks_per_sm; /* persistent meshlet-cull blocks per SM */
-    uint32_t reserved;
+    uint32_t medium_px;       /* the warp rasterises up to medium_px; larger go to 16 x 64-pixel chunks */
+    float cull_blocks_per_sm; /* meshlet-cull blocks per SM (per-stage schedule); blocks per SM (persistent) */
+    uint32_t schedule;        /* LH_SCHEDULE_* */
 } lh_tuning;
 
 lh_status lh_set_tuning(lh_ctx* ctx, const lh_tuning* tuning);

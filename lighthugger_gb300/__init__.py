@@ -74,9 +74,12 @@ class DeviceStatus(C.Structure):
                 ("clipped_triangles", C.c_uint32)]
 
 
+SCHEDULE_DEFAULT, SCHEDULE_PER_STAGE, SCHEDULE_PERSISTENT, SCHEDULE_PER_VIEW = 0, 1, 2, 3
+
+
 class Tuning(C.Structure):
     _fields_ = [("small_px", C.c_uint32), ("medium_px", C.c_uint32), ("cull_blocks_per_sm", C.c_float),
-                ("reserved", C.c_uint32)]
+                ("schedule", C.c_uint32)]
 
 
 class SceneParams(C.Structure):
@@ -121,6 +124,7 @@ def lib():
     L.lh_set_scene.argtypes = [P, P, C.c_uint32, C.POINTER(Texture), C.c_uint32]
     L.lh_frame.argtypes = [P, P, P, C.POINTER(FrameOut)]
     L.lh_frame_batched.argtypes = [P, P, P, C.c_uint32, P, C.POINTER(FrameOut)]
+    L.lh_frame_graph.argtypes = [P, P, P, C.c_uint32, P, C.POINTER(FrameOut)]
     L.lh_get_outputs.argtypes = [P, C.POINTER(FrameOut)]
     L.lh_read_status.argtypes = [P, C.POINTER(DeviceStatus)]
     L.lh_download.argtypes = [P, P, C.c_uint64, C.c_size_t]
@@ -138,7 +142,8 @@ def lib():
     L.lh_scene_destroy.argtypes = [P]
     L.lh_scene_destroy.restype = None
     L.lh_make_uniforms.argtypes = [C.POINTER(Camera), C.POINTER(Uniforms)]
-    for name in ("lh_create", "lh_set_scene", "lh_frame", "lh_frame_batched", "lh_get_outputs", "lh_read_status",
+    for name in ("lh_create", "lh_set_scene", "lh_frame", "lh_frame_batched", "lh_frame_graph", "lh_get_outputs",
+                 "lh_read_status",
                  "lh_download", "lh_set_profiling", "lh_get_stage_times", "lh_set_tuning", "lh_get_tuning", "lh_scene_create", "lh_scene_describe",
                  "lh_scene_upload", "lh_make_uniforms"):
         getattr(L, name).restype = C.c_int32
@@ -261,8 +266,10 @@ class Renderer:
                "lh_set_scene", self.ctx)
         self.scene = scene
 
-    def set_tuning(self, small_px=None, medium_px=None, cull_blocks_per_sm=None):
+    def set_tuning(self, small_px=None, medium_px=None, cull_blocks_per_sm=None, schedule=None):
         t = self.tuning()
+        if schedule is not None:
+            t.schedule = schedule
         if small_px is not None:
             t.small_px = small_px
         if medium_px is not None:
@@ -293,6 +300,12 @@ class Renderer:
         s = stream if stream is not None else self.stream
         _check(lib().lh_frame_batched(self.ctx, C.byref(uniforms), probes if n_probes else None, n_probes, s,
                                       C.byref(self.out)), "lh_frame_batched", self.ctx)
+        return self.out
+
+    def frame_graph(self, uniforms, probes=None, n_probes=0, stream=None):
+        s = stream if stream is not None else self.stream
+        _check(lib().lh_frame_graph(self.ctx, C.byref(uniforms), probes if n_probes else None, n_probes, s,
+                                    C.byref(self.out)), "lh_frame_graph", self.ctx)
         return self.out
 
     def status(self):

@@ -78,6 +78,10 @@ struct lh_ctx {
     // graph
     cudaGraphExec_t graph_exec = nullptr;
     uint32_t graph_probes = 0;
+    uint32_t graph_instances = 0;
+    lh_tuning graph_tuning{};
+    cudaStream_t capture_stream = nullptr;
+    bool capturing = false;
 };
 
 namespace {
@@ -108,6 +112,8 @@ void free_all(lh_ctx* c) {
         if (ev) { cudaEventDestroy(ev); ev = nullptr; }
     if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
     c->graph_exec = nullptr;
+    if (c->capture_stream) cudaStreamDestroy(c->capture_stream);
+    c->capture_stream = nullptr;
     for (auto& a : c->allocs) cudaFree(a.p);
     c->allocs.clear();
     for (int i = 0; i < 2; i++) {
@@ -236,34 +242,67 @@ lh_status upload_frame_constants(lh_ctx* c, const Uniforms* u, const Uniforms* p
     return LH_OK;
 }
 
-// The frame's kernels, all stream ordered (capturable).
-lh_status enqueue_frame(lh_ctx* c, uint32_t n_probes, uint32_t n_instances, cudaStream_t s) {
+// The frame's kernels, all stream ordered (capturable).  `batched` selects
+// the default schedule of lh_frame_batched.
+lh_status enqueue_frame(lh_ctx* c, uint32_t n_probes, uint32_t n_instances, bool batched, cudaStream_t s) {
     const uint32_t n_persp = 1 + n_probes, n_views = n_persp + 4;
     FrameDev f = frame_dev(c, n_views, n_instances);
     const lh_tuning& t = c->tuning;
+    uint32_t schedule = t.schedule;
+    if (schedule == LH_SCHEDULE_DEFAULT) schedule = batched ? LH_SCHEDULE_PERSISTENT : LH_SCHEDULE_PER_STAGE;
+    if (schedule == LH_SCHEDULE_PERSISTENT && persistent_blocks_per_sm() <= 0) schedule = LH_SCHEDULE_PER_STAGE;
+    const bool prof = c->profiling && !c->capturing;
     uint32_t stage = 0;
     auto mark = [&](cudaError_t e) {
-        if (e == cudaSuccess && c->profiling) e = cudaEventRecord(c->stage_ev[stage], s);
+        if (e == cudaSuccess && prof) e = cudaEventRecord(c->stage_ev[stage], s);
         stage++;
+        return e;
+    };
+    auto skip_to = [&](uint32_t k, cudaError_t e) {  // stages fused into one launch share a mark
+        while (e == cudaSuccess && stage < k) e = mark(e);
         return e;
     };
     cudaError_t e = mark(cudaSuccess);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->d_reset, 0, c->reset_bytes, s);
-    if (e == cudaSuccess) e = mark(launch_clear_targets(f, s, c->sms));
-    // visibility views: instance cull + prefix, meshlet cull, raster
-    if (e == cudaSuccess) e = mark(launch_cull_instances(f, 0, n_persp, s));
-    uint32_t bpv = std::max(2u, (uint32_t)(c->sms * t.cull_blocks_per_sm) / n_persp);
-    if (e == cudaSuccess) e = mark(launch_cull_meshlets(f, 0, n_persp, bpv, s));
-    if (e == cudaSuccess)
-        e = mark(launch_raster_kind(f, 0, n_persp, kViewVisibility, t.small_px, t.medium_px, s, c->sms));
-    // depth range + cascade fit (main view only)
-    if (e == cudaSuccess) e = mark(launch_depth_reduce_fit(f, s, c->sms));
-    // cascades
-    uint32_t bpc = std::max(2u, (uint32_t)(c->sms * t.cull_blocks_per_sm) / 4);
-    if (e == cudaSuccess) e = mark(launch_cull_instances(f, n_persp, 4, s));
-    if (e == cudaSuccess) e = mark(launch_cull_meshlets(f, n_persp, 4, bpc, s));
-    if (e == cudaSuccess)
-        e = mark(launch_raster_kind(f, n_persp, 4, kViewShadow, t.small_px, t.medium_px, s, c->sms));
+    const uint32_t cull_blocks = std::max(1u, (uint32_t)(c->sms * t.cull_blocks_per_sm));
+    if (schedule == LH_SCHEDULE_PERSISTENT) {
+        // stages 0..7 in one launch: the time lands in stage 0 ("clear")
+        if (e == cudaSuccess)
+            e = launch_frame_persistent(f, n_persp, t.small_px, t.medium_px, t.cull_blocks_per_sm, s, c->sms);
+        e = mark(e);
+        e = skip_to(8, e);
+    } else if (schedule == LH_SCHEDULE_PER_VIEW) {
+        if (e == cudaSuccess) e = mark(launch_clear_targets(f, s, c->sms));
+        for (uint32_t v = 0; v < n_persp && e == cudaSuccess; v++) {
+            e = launch_cull_instances(f, v, 1, s);
+            if (e == cudaSuccess) e = launch_cull_meshlets(f, v, 1, cull_blocks, s);
+            if (e == cudaSuccess)
+                e = launch_raster_kind(f, v, 1, kViewVisibility, t.small_px, t.medium_px, s, c->sms);
+        }
+        e = skip_to(4, e);
+        if (e == cudaSuccess) e = mark(launch_depth_reduce_fit(f, s, c->sms));
+        for (uint32_t k = 0; k < 4 && e == cudaSuccess; k++) {
+            e = launch_cull_instances(f, n_persp + k, 1, s);
+            if (e == cudaSuccess) e = launch_cull_meshlets(f, n_persp + k, 1, cull_blocks, s);
+            if (e == cudaSuccess)
+                e = launch_raster_kind(f, n_persp + k, 1, kViewShadow, t.small_px, t.medium_px, s, c->sms);
+        }
+        e = skip_to(8, e);
+    } else {
+        if (e == cudaSuccess) e = mark(launch_clear_targets(f, s, c->sms));
+        // visibility views: instance cull + prefix, meshlet cull, raster
+        if (e == cudaSuccess) e = mark(launch_cull_instances(f, 0, n_persp, s));
+        if (e == cudaSuccess) e = mark(launch_cull_meshlets(f, 0, n_persp, cull_blocks, s));
+        if (e == cudaSuccess)
+            e = mark(launch_raster_kind(f, 0, n_persp, kViewVisibility, t.small_px, t.medium_px, s, c->sms));
+        // depth range + cascade fit (main view only)
+        if (e == cudaSuccess) e = mark(launch_depth_reduce_fit(f, s, c->sms));
+        // cascades
+        if (e == cudaSuccess) e = mark(launch_cull_instances(f, n_persp, 4, s));
+        if (e == cudaSuccess) e = mark(launch_cull_meshlets(f, n_persp, 4, cull_blocks, s));
+        if (e == cudaSuccess)
+            e = mark(launch_raster_kind(f, n_persp, 4, kViewShadow, t.small_px, t.medium_px, s, c->sms));
+    }
     // lighting resolve of the main view
     if (e == cudaSuccess) e = mark(launch_resolve(f, c->cfg.width, c->cfg.height, s));
     if (e != cudaSuccess) return cuda_fail(c, e, "frame launch");
@@ -337,7 +376,7 @@ lh_status lh_create(const lh_config* config, lh_ctx** out) {
     if (!c) return LH_ERR_OUT_OF_MEMORY;
     c->cfg = cfg;
     c->device = cfg.device;
-    c->tuning = lh_tuning{8u, 256u, 4.0f, 0u};
+    c->tuning = lh_tuning{8u, 256u, 2.0f, LH_SCHEDULE_DEFAULT};
     cudaError_t e = cudaSetDevice(c->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device);
     c->max_views = 5 + cfg.max_probes;
@@ -431,12 +470,20 @@ lh_status lh_set_scene(lh_ctx* c, const Instance* d_instances, uint32_t n, const
     return prepare_views(c, nullptr, 0);
 }
 
+static lh_status frame_impl(lh_ctx* c, const Uniforms* u, const Uniforms* probes, uint32_t n_probes, void* stream,
+                            lh_frame_out* out, bool batched);
+
 lh_status lh_frame(lh_ctx* c, const Uniforms* u, void* stream, lh_frame_out* out) {
-    return lh_frame_batched(c, u, nullptr, 0, stream, out);
+    return frame_impl(c, u, nullptr, 0, stream, out, false);
 }
 
 lh_status lh_frame_batched(lh_ctx* c, const Uniforms* u, const Uniforms* probes, uint32_t n_probes, void* stream,
                            lh_frame_out* out) {
+    return frame_impl(c, u, probes, n_probes, stream, out, true);
+}
+
+static lh_status frame_impl(lh_ctx* c, const Uniforms* u, const Uniforms* probes, uint32_t n_probes, void* stream,
+                            lh_frame_out* out, bool batched) {
     lh_status st = check_ctx(c);
     if (st != LH_OK) return st;
     if (!u) return fail(c, LH_ERR_INVALID_ARGUMENT, "uniforms is NULL");
@@ -458,7 +505,69 @@ lh_status lh_frame_batched(lh_ctx* c, const Uniforms* u, const Uniforms* probes,
     }
     if ((st = upload_frame_constants(c, u, probes, n_probes, s)) != LH_OK) return st;
     uint32_t n_inst = std::min(u->num_instances, c->n_instances);
-    if ((st = enqueue_frame(c, n_probes, n_inst, s)) != LH_OK) return st;
+    if ((st = enqueue_frame(c, n_probes, n_inst, batched, s)) != LH_OK) return st;
+    c->last_stream = s;
+    if (out) fill_out(c, out);
+    return LH_OK;
+}
+
+lh_status lh_frame_graph(lh_ctx* c, const Uniforms* u, const Uniforms* probes, uint32_t n_probes, void* stream,
+                         lh_frame_out* out) {
+    lh_status st = check_ctx(c);
+    if (st != LH_OK) return st;
+    if (!u) return fail(c, LH_ERR_INVALID_ARGUMENT, "uniforms is NULL");
+    if (!c->d_reset) return fail(c, LH_ERR_NO_SCENE, "lh_set_scene was not called");
+    if (u->window_size.x != c->cfg.width || u->window_size.y != c->cfg.height)
+        return fail(c, LH_ERR_INVALID_ARGUMENT, "uniforms.window_size differs from the context's size");
+    if ((st = validate_probes(c, probes, n_probes)) != LH_OK) return st;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const uint32_t n_inst = std::min(u->num_instances, c->n_instances);
+    bool same_views = n_probes == c->n_probes_last;
+    for (uint32_t p = 0; p < n_probes && same_views; p++)
+        same_views = probes[p].window_size.x == c->h_views[1 + p].width &&
+                     probes[p].window_size.y == c->h_views[1 + p].height;
+    cudaError_t e;
+    if (!same_views) {
+        e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return cuda_fail(c, e, "stream sync");
+        if ((st = prepare_views(c, probes, n_probes)) != LH_OK) return st;
+        if (c->graph_exec) {
+            cudaGraphExecDestroy(c->graph_exec);
+            c->graph_exec = nullptr;
+        }
+    }
+    const bool tuning_changed = std::memcmp(&c->graph_tuning, &c->tuning, sizeof(lh_tuning)) != 0;
+    if (!c->graph_exec || c->graph_probes != n_probes || c->graph_instances != n_inst || tuning_changed) {
+        if (c->graph_exec) {
+            cudaGraphExecDestroy(c->graph_exec);
+            c->graph_exec = nullptr;
+        }
+        if (!c->capture_stream) {
+            e = cudaStreamCreateWithFlags(&c->capture_stream, cudaStreamNonBlocking);
+            if (e != cudaSuccess) return cuda_fail(c, e, "capture stream");
+        }
+        e = cudaStreamBeginCapture(c->capture_stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return cuda_fail(c, e, "begin capture");
+        c->capturing = true;
+        st = enqueue_frame(c, n_probes, n_inst, true, c->capture_stream);
+        c->capturing = false;
+        cudaGraph_t g = nullptr;
+        e = cudaStreamEndCapture(c->capture_stream, &g);
+        if (st != LH_OK) {
+            if (g) cudaGraphDestroy(g);
+            return st;
+        }
+        if (e != cudaSuccess) return cuda_fail(c, e, "end capture");
+        e = cudaGraphInstantiate(&c->graph_exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_fail(c, e, "graph instantiate");
+        c->graph_probes = n_probes;
+        c->graph_instances = n_inst;
+        c->graph_tuning = c->tuning;
+    }
+    if ((st = upload_frame_constants(c, u, probes, n_probes, s)) != LH_OK) return st;
+    e = cudaGraphLaunch(c->graph_exec, s);
+    if (e != cudaSuccess) return cuda_fail(c, e, "graph launch");
     c->last_stream = s;
     if (out) fill_out(c, out);
     return LH_OK;
@@ -545,7 +654,9 @@ void lh_destroy(lh_ctx* c) {
 
 lh_status lh_set_tuning(lh_ctx* c, const lh_tuning* t) {
     if (!c || !t) return LH_ERR_INVALID_ARGUMENT;
-    if (t->small_px > 4096 || t->medium_px < t->small_px || t->cull_blocks_per_sm <= 0.0f) return LH_ERR_INVALID_ARGUMENT;
+    if (t->small_px > 4096 || t->medium_px < t->small_px || !(t->cull_blocks_per_sm > 0.0f) ||
+        t->cull_blocks_per_sm > 64.0f || t->schedule > LH_SCHEDULE_PER_VIEW)
+        return LH_ERR_INVALID_ARGUMENT;
     c->tuning = *t;
     return LH_OK;
 }

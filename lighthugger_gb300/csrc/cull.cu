@@ -1,366 +1,19 @@
-// Instance cull + single-pass prefix sum, and the per-meshlet cull that
-// writes the draw lists ("mesh shaders in compute").
-//
-// Reference passes: cull_instances / cull_instances_shadows
-// (src/shaders/cull_instances.comp:7-56) appending into a prefix-sum sector
-// with one 64-bit atomicAdd of {count:hi32, sum:lo32}
-// (src/shaders/common/prefix_sum.glsl:17-30), and write_draw_calls /
-// write_draw_calls_shadows (src/shaders/write_draw_calls.comp:7-117), which
-// look up each candidate meshlet with an upper_bound over the inclusive sums
-// (prefix_sum.glsl:33-46, util.glsl:42-59) and append visible meshlets with
-// a 32-bit atomicAdd.
-//
-// GB300 design: the appends are order-preserving.  Each block owns one tile
-// (claimed in order from a per-view counter), reduces its tile with warp
-// scans, publishes the tile aggregate in one 64-bit status word and looks
-// back over its predecessors' words (decoupled look-back) for its exclusive
-// prefix.  The output order is therefore the canonical one -- instances
-// ascending, then meshlets ascending -- and visible lists / visibility IDs are
-// deterministic.  The sector keeps the reference layout and its final packed
-// {count:hi32, sum:lo32} counter.
-#include "lh_device.cuh"
-#include "lh_internal.cuh"
+// Kernels of the instance cull + single-pass prefix sum and of the meshlet
+// cull; the work itself is in cull_phases.cuh (shared with the persistent
+// multi-view kernel).
+#include "cull_phases.cuh"
 
 namespace lh {
 namespace {
 
-__device__ __forceinline__ void st_status(uint64_t* p, uint64_t v) {
-    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-__device__ __forceinline__ uint64_t ld_status(const uint64_t* p) {
-    uint64_t v;
-    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
-
-// Decoupled look-back by one thread: publish the tile aggregate, walk back
-// until an inclusive prefix is found, publish the tile's inclusive prefix.
-// Every wait is bounded; on expiry the status flag LH_FLAG_TIMEOUT is set and
-// the missing predecessors count as zero (no hang, results flagged).
-__device__ uint64_t lookback(uint64_t* status, uint32_t tile, uint64_t agg, uint32_t* flags) {
-    if (tile == 0) {
-        st_status(&status[0], kStatIncl | agg);
-        return 0;
-    }
-    st_status(&status[tile], kStatAgg | agg);
-    uint64_t excl = 0;
-    int64_t t = (int64_t)tile - 1;
-    uint32_t spins = 0;
-    bool timed_out = false;
-    while (t >= 0) {
-        uint64_t s = ld_status(&status[t]);
-        uint64_t fl = s >> 62;
-        if (fl == 0) {
-            if (++spins >= kSpinLimit) { timed_out = true; break; }
-            if (spins > 32) __nanosleep(spins > 1024 ? 256 : 32);
-            continue;
-        }
-        excl += s & kPayloadMask;
-        if (fl == 2) break;
-        --t;
-    }
-    if (timed_out) atomicOr(&flags[kStFlags], LH_FLAG_TIMEOUT);
-    st_status(&status[tile], kStatIncl | (excl + agg));
-    return excl;
-}
-
-union InstanceBits {
-    Instance inst;
-    float4 v[7];
-};
-union MeshletBits {
-    Meshlet m;
-    uint2 v[7];
-};
-
-__device__ __forceinline__ void load_instance(const Instance* p, InstanceBits& out) {
-    const float4* s = reinterpret_cast<const float4*>(p);
-#pragma unroll
-    for (int i = 0; i < 7; i++) out.v[i] = __ldg(s + i);
-}
-__device__ __forceinline__ void load_meshlet(const Meshlet* p, MeshletBits& out) {
-    const uint2* s = reinterpret_cast<const uint2*>(p);
-#pragma unroll
-    for (int i = 0; i < 7; i++) out.v[i] = __ldg(s + i);
-}
-
-// Fields of a MeshInfo the cull needs (loaded as aligned 8-byte words).
-struct MeshInfoCull {
-    uint64_t meshlets;
-    uint32_t num_meshlets;
-    uint32_t flags;
-    lh_vec4 bounding_sphere;
-};
-__device__ __forceinline__ MeshInfoCull load_mesh_info(const MeshInfo* mi) {
-    const unsigned long long* w = reinterpret_cast<const unsigned long long*>(mi);
-    unsigned long long w5 = __ldg(w + 5), w6 = __ldg(w + 6), w7 = __ldg(w + 7);
-    uint32_t w8 = __ldg(reinterpret_cast<const uint32_t*>(mi) + 16);
-    MeshInfoCull r;
-    r.meshlets = w5;
-    r.num_meshlets = (uint32_t)(w6 & 0xFFFFu);
-    r.flags = (uint32_t)((w6 >> 16) & 0xFFu);
-    r.bounding_sphere.x = __uint_as_float((uint32_t)(w6 >> 32));
-    r.bounding_sphere.y = __uint_as_float((uint32_t)w7);
-    r.bounding_sphere.z = __uint_as_float((uint32_t)(w7 >> 32));
-    r.bounding_sphere.w = __uint_as_float(w8);
-    return r;
-}
-
-// Copy a struct of `bytes` (multiple of 8) into shared memory.
-__device__ __forceinline__ void copy_to_smem(void* dst, const void* src, uint32_t bytes) {
-    const unsigned long long* s = reinterpret_cast<const unsigned long long*>(src);
-    unsigned long long* d = reinterpret_cast<unsigned long long*>(dst);
-    for (uint32_t i = threadIdx.x; i < bytes / 8; i += blockDim.x) d[i] = s[i];
-}
-
-// Inclusive warp scan of a 64-bit additive payload.
-__device__ __forceinline__ uint64_t warp_incl_scan(uint64_t v) {
-    const uint32_t lane = threadIdx.x & 31;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        uint64_t n = __shfl_up_sync(0xFFFFFFFFu, v, o);
-        if (lane >= (uint32_t)o) v += n;
-    }
-    return v;
-}
-
-constexpr uint64_t kSum40 = (1ull << 40) - 1;
-
-// ---------------------------------------------------------------- instance cull
-// grid = (ceil(n / kInstTile), n_views); one instance per thread.
+// grid = (tiles per view, n_views)
 __global__ void __launch_bounds__(kInstTile) k_cull_instances(FrameDev f, uint32_t view_begin) {
-    __shared__ __align__(16) Uniforms s_u;
-    __shared__ __align__(16) MiscStorage s_m;
-    __shared__ uint64_t s_warp[kInstTile / 32];
-    __shared__ uint64_t s_excl;
-    __shared__ uint32_t s_tile;
-    const ViewDev* vw = f.views + view_begin + blockIdx.y;
-    const uint32_t kind = vw->kind, cascade = vw->cascade;
-    if (threadIdx.x == 0) s_tile = atomicAdd(&vw->claim[0], 1u);
-    if (kind == kViewVisibility)
-        copy_to_smem(&s_u, vw->uniforms, sizeof(Uniforms));
-    else
-        copy_to_smem(&s_m, f.misc, sizeof(MiscStorage));
-    __syncthreads();
-    const uint32_t tile = s_tile;
-    const uint32_t i = tile * kInstTile + threadIdx.x;
-    bool keep = false;
-    uint32_t nm = 0;
-    if (i < f.n_instances) {
-        InstanceBits ib;
-        load_instance(f.instances + i, ib);
-        MeshInfoCull mi = load_mesh_info(mesh_info_of(&ib.inst));
-        nm = mi.num_meshlets;
-        keep = kind == kViewVisibility ? !cull_bounding_sphere(s_u, ib.inst.transform, mi.bounding_sphere)
-                                       : !cull_bounding_sphere_shadows(s_m, ib.inst.transform, mi.bounding_sphere, cascade);
-    }
-    const uint64_t pay = keep ? ((1ull << 40) | nm) : 0ull;
-    uint64_t incl = warp_incl_scan(pay);
-    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 31) s_warp[warp] = incl;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint64_t run = 0;
-        for (uint32_t w = 0; w < kInstTile / 32; w++) {
-            uint64_t t = s_warp[w];
-            s_warp[w] = run;
-            run += t;
-        }
-        uint64_t excl = lookback(vw->inst_status, tile, run, f.status);
-        s_excl = excl;
-        if (tile == gridDim.x - 1) {
-            uint64_t total = excl + run;
-            uint64_t count = total >> 40;
-            *reinterpret_cast<unsigned long long*>(vw->sector) = (count << 32) | (uint32_t)(total & kSum40);
-            if (count > f.max_instances) atomicOr(&f.status[kStFlags], LH_FLAG_INSTANCE_OVERFLOW);
-        }
-    }
-    __syncthreads();
-    if (keep) {
-        uint64_t before = s_excl + s_warp[warp] + incl - pay;
-        uint32_t pos = (uint32_t)(before >> 40);
-        if (pos < f.max_instances) {
-            PrefixSumValue v;
-            v.index = i;
-            v.sum = (uint32_t)(before & kSum40) + nm;
-            reinterpret_cast<PrefixSumValue*>(vw->sector + 8)[pos] = v;
-        }
-    }
+    phase_cull_instances_tile(f, view_begin + blockIdx.y, gridDim.x);
 }
 
-// ---------------------------------------------------------------- meshlet cull
-__device__ __forceinline__ uint32_t upper_bound(const PrefixSumValue* v, uint32_t count, uint32_t target) {
-    uint32_t first = 0;
-    while (count > 0) {
-        uint32_t step = count / 2, cur = first + step;
-        bool greater = target >= v[cur].sum;
-        first = greater ? cur + 1 : first;
-        count = greater ? count - (step + 1) : step;
-    }
-    return first;
-}
-
-// Persistent: grid = (blocks_per_view, n_views); each block claims tiles of
-// kMlTile candidate meshlets of its view in order.
-__global__ void __launch_bounds__(kMlThreads) k_cull_meshlets(FrameDev f, uint32_t view_begin) {
-    __shared__ __align__(16) Uniforms s_u;
-    __shared__ __align__(16) MiscStorage s_m;
-    __shared__ PrefixSumValue s_entries[kMlTile];
-    __shared__ uint32_t s_cnt[2][kMlItems * (kMlThreads / 32)];
-    __shared__ uint32_t s_tile, s_ea, s_ne, s_tot[2];
-    __shared__ uint64_t s_excl;
-    const ViewDev* vw = f.views + view_begin + blockIdx.y;
-    const uint32_t kind = vw->kind, cascade = vw->cascade;
-    const uint32_t md = f.max_draws;
-    copy_to_smem(&s_u, vw->uniforms, sizeof(Uniforms));
-    if (kind == kViewShadow) copy_to_smem(&s_m, f.misc, sizeof(MiscStorage));
-    const PrefixSumValue* values = reinterpret_cast<const PrefixSumValue*>(vw->sector + 8);
-    const unsigned long long counter = *reinterpret_cast<volatile unsigned long long*>(vw->sector);
-    uint32_t count = (uint32_t)(counter >> 32), total = (uint32_t)counter;
-    if (count > f.max_instances) {
-        count = f.max_instances;
-        total = count ? values[count - 1].sum : 0;
-    }
-    uint32_t n_tiles = (uint32_t)(((uint64_t)total + kMlTile - 1) / kMlTile);
-    if (n_tiles > vw->ml_tile_cap) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&f.status[kStFlags], LH_FLAG_DRAW_OVERFLOW);
-        n_tiles = vw->ml_tile_cap;
-    }
-    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    MeshletReference* out_refs = vw->refs;
-    uint32_t* draw_counts = reinterpret_cast<uint32_t*>(vw->draws);
-    DrawIndirectCommand* draws = reinterpret_cast<DrawIndirectCommand*>(vw->draws + 8);
-    __syncthreads();
-    for (;;) {
-        if (threadIdx.x == 0) {
-            uint32_t tile = atomicAdd(&vw->claim[1], 1u);
-            s_tile = tile;
-            if (tile < n_tiles) {
-                uint32_t t0 = tile * kMlTile, t1 = min(total, t0 + kMlTile);
-                uint32_t ea = upper_bound(values, count, t0), eb = upper_bound(values, count, t1 - 1);
-                s_ea = ea;
-                s_ne = eb - ea + 1;
-            }
-        }
-        __syncthreads();
-        const uint32_t tile = s_tile;
-        if (tile >= n_tiles) break;
-        const uint32_t t0 = tile * kMlTile, t1 = min(total, t0 + kMlTile);
-        const uint32_t ea = s_ea, ne = s_ne;
-        const bool smem_entries = ne <= kMlTile;
-        if (smem_entries)
-            for (uint32_t j = threadIdx.x; j < ne; j += kMlThreads) s_entries[j] = values[ea + j];
-        __syncthreads();
-
-        uint32_t cls_bits = 0;  // 2 bits per item: 1 opaque, 2 alpha clip
-        MeshletReference refs[kMlItems];
-#pragma unroll
-        for (uint32_t k = 0; k < kMlItems; k++) {
-            const uint32_t c = t0 + k * kMlThreads + threadIdx.x;
-            refs[k].instance_index = 0;
-            refs[k].meshlet_index = 0;
-            if (c < t1) {
-                PrefixSumValue r;
-                if (smem_entries) {
-                    uint32_t j = upper_bound(s_entries, ne, c);
-                    r = s_entries[min(j, ne - 1)];
-                } else {
-                    r = values[min(upper_bound(values, count, c), count - 1)];
-                }
-                InstanceBits ib;
-                load_instance(f.instances + r.index, ib);
-                const MeshInfo* mip = mesh_info_of(&ib.inst);
-                MeshInfoCull mi = load_mesh_info(mip);
-                uint32_t local = c - (r.sum - mi.num_meshlets);
-                refs[k].instance_index = r.index;
-                refs[k].meshlet_index = (uint16_t)local;
-                MeshletBits mb;
-                load_meshlet(reinterpret_cast<const Meshlet*>(mi.meshlets) + (uint16_t)local, mb);
-                const bool alpha = (mi.flags & MESH_INFO_FLAGS_ALPHA_CLIP) != 0;
-                bool vis;
-                if (kind == kViewVisibility)
-                    vis = !cull_bounding_sphere(s_u, ib.inst.transform, mb.m.bounding_sphere) &&
-                          (alpha || !cull_cone_perspective(s_u, &ib.inst, ib.inst.transform, mb.m));
-                else
-                    vis = !cull_bounding_sphere_shadows(s_m, ib.inst.transform, mb.m.bounding_sphere, cascade) &&
-                          (alpha || !cull_cone_orthographic(s_u, &ib.inst, mb.m));
-                if (vis) cls_bits |= (alpha ? 2u : 1u) << (2 * k);
-            }
-        }
-        // Ordered compaction: counts per (item k, warp), k-major.
-        uint32_t bal_op[kMlItems], bal_al[kMlItems];
-#pragma unroll
-        for (uint32_t k = 0; k < kMlItems; k++) {
-            uint32_t cl = (cls_bits >> (2 * k)) & 3u;
-            bal_op[k] = __ballot_sync(0xFFFFFFFFu, cl == 1u);
-            bal_al[k] = __ballot_sync(0xFFFFFFFFu, cl == 2u);
-            if (lane == 0) {
-                s_cnt[0][k * (kMlThreads / 32) + warp] = __popc(bal_op[k]);
-                s_cnt[1][k * (kMlThreads / 32) + warp] = __popc(bal_al[k]);
-            }
-        }
-        __syncthreads();
-        if (warp == 0) {
-            // exclusive scan of 64 counts per class: 2 per lane
-            constexpr uint32_t N = kMlItems * (kMlThreads / 32);
-            static_assert(N == 64, "scan layout");
-#pragma unroll
-            for (int cl = 0; cl < 2; cl++) {
-                uint32_t a = s_cnt[cl][2 * lane], b = s_cnt[cl][2 * lane + 1];
-                uint32_t s = a + b, incl = s;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    uint32_t n = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-                    if (lane >= (uint32_t)o) incl += n;
-                }
-                uint32_t ex = incl - s;
-                s_cnt[cl][2 * lane] = ex;
-                s_cnt[cl][2 * lane + 1] = ex + a;
-                if (lane == 31) s_tot[cl] = incl;
-            }
-            __syncwarp();
-            if (lane == 0) {
-                uint64_t agg = ((uint64_t)s_tot[0] << 31) | (uint64_t)s_tot[1];
-                uint64_t excl = lookback(vw->ml_status, tile, agg, f.status);
-                s_excl = excl;
-                if (tile == n_tiles - 1) {
-                    uint64_t tot = excl + agg;
-                    uint32_t nop = (uint32_t)(tot >> 31), nal = (uint32_t)(tot & 0x7FFFFFFFu);
-                    draw_counts[0] = nop;
-                    draw_counts[1] = nal;
-                    if (nop > md || nal > md) atomicOr(&f.status[kStFlags], LH_FLAG_DRAW_OVERFLOW);
-                }
-            }
-        }
-        __syncthreads();
-        const uint32_t ex_op = (uint32_t)(s_excl >> 31), ex_al = (uint32_t)(s_excl & 0x7FFFFFFFu);
-        const uint32_t lt = (1u << lane) - 1u;
-#pragma unroll
-        for (uint32_t k = 0; k < kMlItems; k++) {
-            uint32_t cl = (cls_bits >> (2 * k)) & 3u;
-            if (!cl) continue;
-            uint32_t pos, slot;
-            if (cl == 1u) {
-                pos = ex_op + s_cnt[0][k * (kMlThreads / 32) + warp] + __popc(bal_op[k] & lt);
-                slot = pos;
-            } else {
-                pos = ex_al + s_cnt[1][k * (kMlThreads / 32) + warp] + __popc(bal_al[k] & lt);
-                slot = md + pos;
-            }
-            if (pos >= md) continue;
-            const Instance* inst = f.instances + refs[k].instance_index;
-            const Meshlet* ml = reinterpret_cast<const Meshlet*>(load_mesh_info(mesh_info_of(inst)).meshlets) +
-                                refs[k].meshlet_index;
-            DrawIndirectCommand dc;
-            dc.vertexCount = (uint32_t)__ldg(&ml->triangle_count) * 3u;
-            dc.instanceCount = 1;
-            dc.firstVertex = 0;
-            dc.firstInstance = vw->section_base + slot;
-            draws[slot] = dc;
-            out_refs[slot] = refs[k];
-        }
-        __syncthreads();
-    }
+// persistent over (view, tile) claims of views [view_begin, view_begin + n_views)
+__global__ void __launch_bounds__(kMlThreads) k_cull_meshlets(FrameDev f, uint32_t view_begin, uint32_t n_views) {
+    phase_cull_meshlets(f, view_begin, n_views, &f.status[kStMlClaim]);
 }
 
 __global__ void k_sum_meshlets(const Instance* inst, uint32_t n, unsigned long long* out) {
@@ -380,11 +33,12 @@ cudaError_t launch_cull_instances(const FrameDev& f, uint32_t view_begin, uint32
     return cudaGetLastError();
 }
 
-cudaError_t launch_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint32_t n_views, uint32_t blocks_per_view,
+cudaError_t launch_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint32_t n_views, uint32_t blocks,
                                  cudaStream_t s) {
     if (n_views == 0) return cudaSuccess;
-    dim3 grid(blocks_per_view, n_views);
-    k_cull_meshlets<<<grid, kMlThreads, 0, s>>>(f, view_begin);
+    cudaError_t e = cudaMemsetAsync(&f.status[kStMlClaim], 0, sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    k_cull_meshlets<<<blocks, kMlThreads, 0, s>>>(f, view_begin, n_views);
     return cudaGetLastError();
 }
 

@@ -86,6 +86,27 @@ __device__ __forceinline__ f2 load_uv_raw(uint64_t uvs, uint32_t flags, uint32_t
     const uint16_t* p = reinterpret_cast<const uint16_t*>(uvs) + (size_t)index * 2;
     return {(float)__ldg(p), (float)__ldg(p + 1)};
 }
+// Whole records with vector loads: Instance (112 B, 16-byte aligned array)
+// and Meshlet (56 B, 8-byte aligned).
+union InstanceBits {
+    Instance inst;
+    float4 v[7];
+};
+union MeshletBits {
+    Meshlet m;
+    uint2 v[7];
+};
+__device__ __forceinline__ void load_instance(const Instance* p, InstanceBits& out) {
+    const float4* s = reinterpret_cast<const float4*>(p);
+#pragma unroll
+    for (int i = 0; i < 7; i++) out.v[i] = __ldg(s + i);
+}
+__device__ __forceinline__ void load_meshlet(const Meshlet* p, MeshletBits& out) {
+    const uint2* s = reinterpret_cast<const uint2*>(p);
+#pragma unroll
+    for (int i = 0; i < 7; i++) out.v[i] = __ldg(s + i);
+}
+
 __device__ __forceinline__ f3 world_pos(const lh_mat4& transform, f3 p) {
     f4 w = mul(transform, f4{p.x, p.y, p.z, 1.0f});
     return {w.x, w.y, w.z};

@@ -66,6 +66,8 @@ enum StatusWord : uint32_t {
     kStBigClaim = 3,
     kStReduceDone = 4,
     kStClipClaim = 5,
+    kStMlClaim = 6,    // meshlet-cull (view, tile) claims
+    kStBarrier = 7,    // grid barrier of the persistent kernel
     kStBigPacked = 8,  // u64 (words 8-9): big-triangle count << 40 | chunk count
     kStWords = 16
 };
@@ -98,13 +100,17 @@ struct FrameDev {
 // Launchers (stream ordered).  Each returns the CUDA error of its launch.
 cudaError_t launch_clear_targets(const FrameDev& f, cudaStream_t s, int sms);
 cudaError_t launch_cull_instances(const FrameDev& f, uint32_t view_begin, uint32_t n_views, cudaStream_t s);
-cudaError_t launch_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint32_t n_views, uint32_t blocks_per_view,
+cudaError_t launch_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint32_t n_views, uint32_t blocks,
                                  cudaStream_t s);
 // Raster all views [view_begin, view_begin + n_views) of one kind (kViewVisibility
 // or kViewShadow): main kernel, clipper, band kernel.
 cudaError_t launch_raster_kind(const FrameDev& f, uint32_t view_begin, uint32_t n_views, int kind, uint32_t small_px,
                                uint32_t medium_px, cudaStream_t s, int sms);
 cudaError_t launch_depth_reduce_fit(const FrameDev& f, cudaStream_t s, int sms);
+// Clear + cull + raster of every view in one cooperative persistent launch.
+cudaError_t launch_frame_persistent(const FrameDev& f, uint32_t n_persp, uint32_t small_px, uint32_t medium_px,
+                                    float blocks_per_sm, cudaStream_t s, int sms);
+int persistent_blocks_per_sm();
 cudaError_t launch_resolve(const FrameDev& f, uint32_t width, uint32_t height, cudaStream_t s);
 cudaError_t launch_sum_meshlets(const Instance* instances, uint32_t n, unsigned long long* out, cudaStream_t s);
 

@@ -1,0 +1,137 @@
+// One persistent launch for the cull and raster of every view of a frame:
+// the main view, the probe views and the 4 shadow cascades.
+//
+// The stages are the same device phases the per-stage kernels run
+// (cull_phases.cuh, raster_phases.cuh, frame_phases.cuh); here one
+// cooperative grid (every block resident) runs them back to back with grid
+// barriers in between, so the frame's cull + raster costs one launch instead
+// of ~15, and small views (probes) share the machine with the large ones in
+// every phase.  The order of phases is the reference's pass order
+// (src/rendering.cpp:79-438): clear, instance cull, meshlet cull, raster of
+// the visibility views; depth reduction; cascade fit; instance cull, meshlet
+// cull, raster of the cascades.
+#include "cull_phases.cuh"
+#include "frame_phases.cuh"
+#include "raster_phases.cuh"
+
+namespace lh {
+namespace {
+
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Grid barrier on a counter that only grows within the launch: barrier k
+// completes when the counter reaches k * gridDim.x.  All blocks are
+// resident (cooperative launch), and the wait is bounded: on expiry
+// LH_FLAG_TIMEOUT is recorded and the block goes on (results flagged, no
+// hang).
+__device__ void grid_barrier(const FrameDev& f, uint32_t& epoch) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        epoch++;
+        const uint32_t target = epoch * gridDim.x;
+        __threadfence();
+        atomicAdd(&f.status[kStBarrier], 1u);
+        uint32_t spins = 0;
+        while (ld_acquire_u32(&f.status[kStBarrier]) < target) {
+            if (++spins >= kSpinLimit) {
+                atomicOr(&f.status[kStFlags], LH_FLAG_TIMEOUT);
+                break;
+            }
+            if (spins > 16) __nanosleep(spins > 1024 ? 256 : 32);
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+// Resets the raster words between the visibility and the shadow passes.
+__device__ void reset_raster_words(const FrameDev& f) {
+    for (uint32_t w = kStClipCount + threadIdx.x; w < kStBigPacked + 2; w += blockDim.x)
+        if (w != kStBarrier && w != kStReduceDone) f.status[w] = 0u;
+}
+
+constexpr int kPersistentThreads = 256;
+
+__global__ void __launch_bounds__(kPersistentThreads, 2) k_frame_persistent(FrameDev f, uint32_t n_persp,
+                                                                           RasterTune tune) {
+    uint32_t epoch = 0;
+    const uint64_t gtid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, gstride = (uint64_t)gridDim.x * blockDim.x;
+    const uint32_t n_views = n_persp + 4;
+    // clear every target; block 0 resets the per-view counters and the depth range
+    for (uint32_t v = 0; v < n_views; v++) phase_clear_view(f, v, gtid, gstride, blockIdx.x == 0 && v == 0);
+    grid_barrier(f, epoch);
+    const uint32_t inst_tiles = (f.n_instances + kInstTile - 1) / kInstTile;
+    // visibility views: instance cull + prefix sum
+    for (uint32_t vb = blockIdx.x; vb < inst_tiles * n_persp; vb += gridDim.x)
+        phase_cull_instances_tile(f, vb / inst_tiles, inst_tiles);
+    grid_barrier(f, epoch);
+    phase_cull_meshlets(f, 0, n_persp, &f.status[kStMlClaim]);
+    grid_barrier(f, epoch);
+    phase_raster<0>(f, 0, n_persp, tune, &f.status[kStRasterClaim]);
+    grid_barrier(f, epoch);
+    phase_raster_clip<0>(f, (uint32_t)gtid, (uint32_t)gstride);
+    grid_barrier(f, epoch);
+    phase_raster_big<0>(f);
+    grid_barrier(f, epoch);
+    // depth range of the main view, then the cascade fit
+    phase_depth_reduce(f, gtid, gstride);
+    grid_barrier(f, epoch);
+    if (blockIdx.x == 0) {
+        phase_fit(f);
+        reset_raster_words(f);
+    }
+    grid_barrier(f, epoch);
+    // cascades
+    for (uint32_t vb = blockIdx.x; vb < inst_tiles * 4; vb += gridDim.x)
+        phase_cull_instances_tile(f, n_persp + vb / inst_tiles, inst_tiles);
+    grid_barrier(f, epoch);
+    phase_cull_meshlets(f, n_persp, 4, &f.status[kStMlClaim]);
+    grid_barrier(f, epoch);
+    phase_raster<1>(f, n_persp, 4, tune, &f.status[kStRasterClaim]);
+    grid_barrier(f, epoch);
+    phase_raster_clip<1>(f, (uint32_t)gtid, (uint32_t)gstride);
+    grid_barrier(f, epoch);
+    phase_raster_big<1>(f);
+}
+
+int g_persistent_blocks_per_sm = -1;
+
+}  // namespace
+
+// Blocks per SM at which the persistent kernel is resident (0 if it cannot be).
+int persistent_blocks_per_sm() {
+    if (g_persistent_blocks_per_sm < 0) {
+        int n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_frame_persistent, kPersistentThreads, 0) != cudaSuccess)
+            n = 0;
+        g_persistent_blocks_per_sm = n;
+    }
+    return g_persistent_blocks_per_sm;
+}
+
+cudaError_t launch_frame_persistent(const FrameDev& f, uint32_t n_persp, uint32_t small_px, uint32_t medium_px,
+                                    float blocks_per_sm, cudaStream_t s, int sms) {
+    const int resident = persistent_blocks_per_sm();
+    if (resident <= 0) return cudaErrorCooperativeLaunchTooLarge;
+    int per_sm = (int)blocks_per_sm;
+    if (per_sm < 1) per_sm = 1;
+    if (per_sm > resident) per_sm = resident;
+    RasterTune tune{small_px, medium_px};
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(sms * per_sm));
+    cfg.blockDim = dim3(kPersistentThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_frame_persistent, f, n_persp, tune);
+}
+
+}  // namespace lh

@@ -1,0 +1,408 @@
+// Compute rasteriser for the visibility buffer and the cascade shadow maps.
+//
+// Replaces the reference's hardware draws: visbuffer_opaque_vertex/pixel
+// (src/shaders/rasterization.glsl:12-58) with depth GREATER / clear 0 /
+// back-face culling (src/pipelines.cpp:10-13,67-71,287-300), and
+// shadowmap_opaque_vertex (rasterization.glsl:101-111) with depth LESS /
+// clear 1 / front-face culling (pipelines.cpp:15-19,73-77,257-270), driven
+// by drawIndirectCount over the draw lists (src/rendering.cpp:197-266,
+// 325-438).  Alpha-clip draws are rasterised as opaque (no alpha test).
+//
+// Layout of the work:
+//  k_raster       one warp per visible meshlet (claimed dynamically across
+//                 all views of the launch): the meshlet's <= 64 vertices are
+//                 transformed once, snapped to 1/256 px and kept in shared
+//                 memory; then one lane per triangle does set-up and face
+//                 culling.  Triangles covering <= `small` pixel centres are
+//                 rasterised by their lane, up to `medium` by the whole warp,
+//                 larger ones go to a queue of 16-row bands; triangles that
+//                 need clipping go to the clip queue.
+//  k_raster_clip  one thread per clipped triangle: Sutherland-Hodgman in
+//                 clip space against 0 <= z <= w and the guard band, fan
+//                 triangulation, band queue.
+//  k_raster_big   one warp per band.
+// The depth test is an atomicMax of (depth bits << 32 | packed ID) for the
+// visibility buffer and an atomicMin of depth bits for shadow maps, so the
+// result does not depend on the order of the work.
+#pragma once
+
+#include "lh_device.cuh"
+#include "lh_internal.cuh"
+
+namespace lh {
+namespace {
+
+constexpr int kRasterWarps = 8;
+
+struct RasterTune {
+    uint32_t small_px;   // lane path up to this many bbox pixels
+    uint32_t medium_px;  // warp path up to this many; larger: band queue
+};
+
+__device__ __forceinline__ const lh_mat4& view_matrix(const FrameDev& f, const ViewDev* vw) {
+    return vw->kind == kViewVisibility ? vw->uniforms->combined_perspective_view : f.misc->shadow_matrices[vw->cascade];
+}
+
+// Fields of a MeshInfo the raster needs.
+struct MeshInfoRaster {
+    uint64_t positions, indices, micro_indices, meshlets;
+    uint32_t flags;
+};
+__device__ __forceinline__ MeshInfoRaster load_mesh_info_raster(const MeshInfo* mi) {
+    const unsigned long long* w = reinterpret_cast<const unsigned long long*>(mi);
+    MeshInfoRaster r;
+    r.positions = __ldg(w + 0);
+    r.indices = __ldg(w + 1);
+    r.micro_indices = __ldg(w + 4);
+    r.meshlets = __ldg(w + 5);
+    r.flags = (uint32_t)((__ldg(w + 6) >> 16) & 0xFFu);
+    return r;
+}
+__device__ __forceinline__ uint32_t load_index_raw(uint64_t indices, uint32_t flags, uint32_t i) {
+    if (flags & MESH_INFO_FLAGS_32_BIT_INDICES) return __ldg(reinterpret_cast<const uint32_t*>(indices) + i);
+    return __ldg(reinterpret_cast<const uint16_t*>(indices) + i);
+}
+
+__device__ __forceinline__ void load_transform(const Instance* inst, lh_mat4& m) {
+    const float4* s = reinterpret_cast<const float4*>(inst);
+    float4* d = reinterpret_cast<float4*>(&m);
+#pragma unroll
+    for (int i = 0; i < 4; i++) d[i] = __ldg(s + i);
+}
+
+// Append a big triangle with one 64-bit atomic of {triangles:hi24, chunks:lo40}
+// (the packed single-pass append of prefix_sum.glsl:17-30): the triangle's
+// index and its first chunk come from the same word, so chunk bases ascend
+// with the index and the band kernel finds a chunk's triangle by binary search.
+__device__ void push_big(const FrameDev& f, const TriSetup& t, uint32_t view) {
+    const uint32_t nbx = (uint32_t)(t.px1 - t.px0) / kChunkCols + 1;
+    const uint32_t nby = (uint32_t)(t.py1 - t.py0) / kChunkRows + 1;
+    const unsigned long long n = (unsigned long long)nbx * nby;
+    const unsigned long long old =
+        atomicAdd(reinterpret_cast<unsigned long long*>(f.status + kStBigPacked), (1ull << 40) | n);
+    const uint64_t idx = old >> 40, base = old & ((1ull << 40) - 1);
+    if (idx >= f.big_cap || base + n > 0xFFFFFFFFull) {
+        atomicOr(&f.status[kStFlags], LH_FLAG_QUEUE_OVERFLOW);
+        return;
+    }
+    BigTri e;
+    e.X0 = t.X0; e.Y0 = t.Y0; e.X1 = t.X1; e.Y1 = t.Y1; e.X2 = t.X2; e.Y2 = t.Y2;
+    e.z0 = t.z0; e.s1 = t.s1; e.s2 = t.s2;
+    e.id = t.id;
+    e.view = view;
+    e.bias = t.bias;
+    e.px0 = t.px0;
+    e.px1 = t.px1;
+    e.py0 = t.py0;
+    e.py1 = t.py1;
+    f.big[idx] = e;
+    f.big_base[idx] = (uint32_t)base;
+}
+
+template <int KIND>
+__device__ __forceinline__ void raster_lane(const TriSetup& t, void* target, uint32_t W) {
+    for (int32_t py = t.py0; py <= t.py1; py++)
+        for (int32_t px = t.px0; px <= t.px1; px++) {
+            float d;
+            if (cover(t, px, py, d)) write_fragment<KIND>(target, W, px, py, d, t.id);
+        }
+}
+
+// All lanes of a warp cover the pixels of one triangle's bbox.
+template <int KIND>
+__device__ __forceinline__ void raster_warp(const TriSetup& t, void* target, uint32_t W, uint32_t lane) {
+    const uint32_t w = (uint32_t)(t.px1 - t.px0 + 1);
+    const uint32_t npx = w * (uint32_t)(t.py1 - t.py0 + 1);
+    const float inv_w = 1.0f / (float)w;
+    for (uint32_t p = lane; p < npx; p += 32) {
+        int32_t ry = (int32_t)(((float)p + 0.5f) * inv_w);
+        int32_t rx = (int32_t)p - ry * (int32_t)w;
+        if (rx < 0) { ry--; rx += (int32_t)w; }
+        else if (rx >= (int32_t)w) { ry++; rx -= (int32_t)w; }
+        int32_t px = t.px0 + rx, py = t.py0 + ry;
+        float d;
+        if (cover(t, px, py, d)) write_fragment<KIND>(target, W, px, py, d, t.id);
+    }
+}
+
+__device__ __forceinline__ TriSetup shfl_setup(const TriSetup& s, int src) {
+    TriSetup r;
+    const uint32_t* a = reinterpret_cast<const uint32_t*>(&s);
+    uint32_t* b = reinterpret_cast<uint32_t*>(&r);
+#pragma unroll
+    for (int i = 0; i < (int)(sizeof(TriSetup) / 4); i++) b[i] = __shfl_sync(0xFFFFFFFFu, a[i], src);
+    return r;
+}
+
+// One warp per visible meshlet of views [view_begin, view_begin + n_views),
+// claimed from `claim_word`.  Persistent: returns when the claims run out.
+template <int KIND>
+__device__ void phase_raster(const FrameDev& f, uint32_t view_begin, uint32_t n_views, RasterTune tune,
+                             uint32_t* claim_word) {
+    __shared__ uint32_t s_prefix[kMaxViews + 1];
+    __shared__ uint32_t s_nop[kMaxViews];
+    __shared__ __align__(16) lh_mat4 s_vp[kMaxViews];
+    __shared__ SnapV s_v[kRasterWarps][MAX_MESHLET_UNIQUE_VERTICES];
+    __shared__ uint8_t s_oc[kRasterWarps][MAX_MESHLET_UNIQUE_VERTICES];
+    __shared__ uint32_t s_micro[kRasterWarps][(MAX_MESHLET_TRIANGLES * 3 + 3) / 4];
+    const uint32_t md = f.max_draws;
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (uint32_t v = 0; v < n_views; v++) {
+            const uint32_t* cnt = reinterpret_cast<const uint32_t*>(f.views[view_begin + v].draws);
+            uint32_t nop = min(cnt[0], md), nal = min(cnt[1], md);
+            s_prefix[v] = run;
+            s_nop[v] = nop;
+            run += nop + nal;
+        }
+        s_prefix[n_views] = run;
+    }
+    for (uint32_t i = threadIdx.x; i < n_views * 16; i += blockDim.x) {
+        const lh_mat4& m = view_matrix(f, f.views + view_begin + i / 16);
+        reinterpret_cast<float*>(&s_vp[i / 16])[i % 16] = reinterpret_cast<const float*>(&m)[i % 16];
+    }
+    __syncthreads();
+    const uint32_t total = s_prefix[n_views];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    SnapV* sv = s_v[warp];
+    uint8_t* so = s_oc[warp];
+    const uint8_t* mic = reinterpret_cast<const uint8_t*>(s_micro[warp]);
+    for (;;) {
+        uint32_t item = 0;
+        if (lane == 0) item = atomicAdd(claim_word, 1u);
+        item = __shfl_sync(0xFFFFFFFFu, item, 0);
+        if (item >= total) break;
+        uint32_t v = 0;
+        while (item >= s_prefix[v + 1]) v++;
+        const uint32_t view = view_begin + v;
+        const ViewDev* vw = f.views + view;
+        const uint32_t local = item - s_prefix[v];
+        const uint32_t slot = local < s_nop[v] ? local : md + (local - s_nop[v]);
+        const MeshletReference ref = vw->refs[slot];
+        const Instance* inst = f.instances + ref.instance_index;
+        lh_mat4 transform;
+        load_transform(inst, transform);
+        const MeshInfoRaster mi = load_mesh_info_raster(mesh_info_of(inst));
+        MeshletBits mb;
+        load_meshlet(reinterpret_cast<const Meshlet*>(mi.meshlets) + ref.meshlet_index, mb);
+        const uint32_t W = vw->width, H = vw->height;
+        void* target = vw->target;
+        const float hw = (float)W * 0.5f, hh = (float)H * 0.5f;
+        const uint32_t nv = mb.m.index_count, nt = mb.m.triangle_count;
+        if (nv > MAX_MESHLET_UNIQUE_VERTICES || nt > MAX_MESHLET_TRIANGLES) {
+            // beyond the meshletiser limits: malformed, skipped and flagged
+            if (lane == 0) atomicOr(&f.status[kStFlags], LH_FLAG_BAD_MESHLET);
+            continue;
+        }
+        for (uint32_t j = lane; j < nv; j += 32) {
+            uint32_t idx = load_index_raw(mi.indices, mi.flags, mb.m.index_offset + j);
+            f3 w = world_pos(transform, load_position(mi.positions, mi.flags, idx));
+            f4 c = mul(s_vp[v], f4{w.x, w.y, w.z, 1.0f});
+            uint32_t oc = outcode(c);
+            SnapV s{0, 0, 0.0f};
+            if (!oc) s = snap(c, hw, hh);
+            sv[j] = s;
+            so[j] = (uint8_t)oc;
+        }
+        const uint64_t mbase = mi.micro_indices + mb.m.triangle_offset;
+        const uint32_t nbytes = nt * 3;
+        if ((mbase & 3) == 0) {
+            for (uint32_t j = lane; j < (nbytes + 3) / 4; j += 32)
+                s_micro[warp][j] = __ldg(reinterpret_cast<const uint32_t*>(mbase) + j);
+        } else {
+            uint8_t* d = reinterpret_cast<uint8_t*>(s_micro[warp]);
+            for (uint32_t j = lane; j < nbytes; j += 32) d[j] = __ldg(reinterpret_cast<const uint8_t*>(mbase) + j);
+        }
+        __syncwarp();
+        for (uint32_t base = 0; base < nt; base += 32) {
+            const uint32_t t = base + lane;
+            bool medium = false;
+            TriSetup st;
+            if (t < nt) {
+                const uint32_t m0 = mic[3 * t], m1 = mic[3 * t + 1], m2 = mic[3 * t + 2];
+                if (m0 >= nv || m1 >= nv || m2 >= nv) {
+                    atomicOr(&f.status[kStFlags], LH_FLAG_BAD_MESHLET);
+                } else {
+                    const uint32_t o0 = so[m0], o1 = so[m1], o2 = so[m2];
+                    if (((o0 | o1 | o2) & 64u) || (o0 & o1 & o2)) {
+                        // non-finite / w <= 0, or entirely outside one plane
+                    } else if (o0 | o1 | o2) {
+                        uint32_t pos = atomicAdd(&f.status[kStClipCount], 1u);
+                        if (pos < f.clip_cap) f.clip[pos] = ClipItem{view, slot, t, 0u};
+                        else atomicOr(&f.status[kStFlags], LH_FLAG_QUEUE_OVERFLOW);
+                    } else {
+                        SnapV a = sv[m0], b = sv[m1], c = sv[m2];
+                        int64_t cr = cross3(a, b, c);
+                        bool keep = KIND == 0 ? cr < 0 : cr > 0;
+                        if (keep) {
+                            if (cr > 0) { SnapV tmp = b; b = c; c = tmp; }
+                            if (make_setup(a, b, c, LH_PACK_ID(t, slot), W, H, st)) {
+                                uint32_t npx = (uint32_t)(st.px1 - st.px0 + 1) * (uint32_t)(st.py1 - st.py0 + 1);
+                                if (npx <= tune.small_px) raster_lane<KIND>(st, target, W);
+                                else if (npx <= tune.medium_px) medium = true;
+                                else push_big(f, st, view);
+                            }
+                        }
+                    }
+                }
+            }
+            uint32_t mask = __ballot_sync(0xFFFFFFFFu, medium);
+            while (mask) {
+                int src = __ffs(mask) - 1;
+                mask &= mask - 1;
+                TriSetup b = shfl_setup(st, src);
+                raster_warp<KIND>(b, target, W, lane);
+            }
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+}
+
+// Sutherland-Hodgman against w-z, z, g*w-x, g*w+x, g*w-y, g*w+y >= 0.
+__device__ int clip_polygon(f4* poly, int n) {
+    f4 out[9];
+    for (int plane = 0; plane < 6 && n >= 3; plane++) {
+        int m = 0;
+        for (int i = 0; i < n; i++) {
+            f4 a = poly[i], b = poly[i + 1 < n ? i + 1 : 0];
+            float ga = LH_GUARD_BAND * a.w, gb = LH_GUARD_BAND * b.w;
+            float da, db;
+            switch (plane) {
+                case 0: da = a.w - a.z; db = b.w - b.z; break;
+                case 1: da = a.z; db = b.z; break;
+                case 2: da = ga - a.x; db = gb - b.x; break;
+                case 3: da = ga + a.x; db = gb + b.x; break;
+                case 4: da = ga - a.y; db = gb - b.y; break;
+                default: da = ga + a.y; db = gb + b.y; break;
+            }
+            if (da >= 0.0f) out[m++] = a;
+            if ((da >= 0.0f) != (db >= 0.0f)) {
+                float tt = da / (da - db);
+                out[m++] = f4{a.x + tt * (b.x - a.x), a.y + tt * (b.y - a.y), a.z + tt * (b.z - a.z), a.w + tt * (b.w - a.w)};
+            }
+        }
+        n = m;
+        for (int i = 0; i < n; i++) poly[i] = out[i];
+    }
+    return n;
+}
+
+// One thread per clipped triangle; thread `gtid` of `gstride`.
+template <int KIND>
+__device__ void phase_raster_clip(const FrameDev& f, uint32_t gtid, uint32_t gstride) {
+    const uint32_t n = min(*reinterpret_cast<volatile uint32_t*>(&f.status[kStClipCount]), f.clip_cap);
+    for (uint32_t i = gtid; i < n; i += gstride) {
+        const ClipItem it = f.clip[i];
+        const ViewDev* vw = f.views + it.view;
+        const MeshletReference ref = vw->refs[it.slot];
+        const Instance* inst = f.instances + ref.instance_index;
+        lh_mat4 transform;
+        load_transform(inst, transform);
+        const MeshInfoRaster mi = load_mesh_info_raster(mesh_info_of(inst));
+        MeshletBits mb;
+        load_meshlet(reinterpret_cast<const Meshlet*>(mi.meshlets) + ref.meshlet_index, mb);
+        const lh_mat4& vp = view_matrix(f, vw);
+        const uint8_t* micro = reinterpret_cast<const uint8_t*>(mi.micro_indices) + mb.m.triangle_offset + it.tri * 3;
+        f4 poly[9];
+        for (int k = 0; k < 3; k++) {
+            uint32_t idx = load_index_raw(mi.indices, mi.flags, mb.m.index_offset + micro[k]);
+            f3 w = world_pos(transform, load_position(mi.positions, mi.flags, idx));
+            poly[k] = mul(vp, f4{w.x, w.y, w.z, 1.0f});
+        }
+        int np = clip_polygon(poly, 3);
+        if (np < 3) continue;
+        bool projectable = true;  // false only for a triangle through the eye point
+        for (int k = 0; k < np; k++) projectable = projectable && poly[k].w > 0.0f;
+        if (!projectable) continue;
+        const uint32_t W = vw->width, H = vw->height;
+        const float hw = (float)W * 0.5f, hh = (float)H * 0.5f;
+        SnapV s[9];
+        for (int k = 0; k < np; k++) s[k] = snap(poly[k], hw, hh);
+        int64_t pc = 0;
+        for (int k = 0; k < np; k++) {
+            const SnapV &a = s[k], &b = s[k + 1 < np ? k + 1 : 0];
+            pc += (int64_t)a.X * b.Y - (int64_t)b.X * a.Y;
+        }
+        if (pc == 0) continue;
+        if (KIND == 0 && pc > 0) continue;
+        if (KIND == 1 && pc < 0) continue;
+        const uint32_t id = LH_PACK_ID(it.tri, it.slot);
+        for (int k = 1; k + 1 < np; k++) {
+            SnapV a = s[0], b = s[k], c = s[k + 1];
+            int64_t tc = cross3(a, b, c);
+            if (tc == 0 || ((tc < 0) != (pc < 0))) continue;
+            if (tc > 0) { SnapV tmp = b; b = c; c = tmp; }
+            TriSetup st;
+            if (make_setup(a, b, c, id, W, H, st)) push_big(f, st, it.view);
+        }
+    }
+}
+
+// Edge function of edge a->b at pixel centre (px, py).
+__device__ __forceinline__ int64_t edge_at(int32_t ax, int32_t ay, int32_t bx, int32_t by, int32_t px, int32_t py) {
+    return (int64_t)(by - ay) * ((int64_t)px * 256 + 128 - ax) - (int64_t)(bx - ax) * ((int64_t)py * 256 + 128 - ay);
+}
+
+// True when the edge's test fails at all four corners of the pixel
+// rectangle (the edge function is affine, so it fails everywhere inside).
+__device__ __forceinline__ bool edge_rejects(int32_t ax, int32_t ay, int32_t bx, int32_t by, int32_t x0, int32_t x1,
+                                             int32_t y0, int32_t y1, int64_t bias) {
+    return edge_at(ax, ay, bx, by, x0, y0) < bias && edge_at(ax, ay, bx, by, x1, y0) < bias &&
+           edge_at(ax, ay, bx, by, x0, y1) < bias && edge_at(ax, ay, bx, by, x1, y1) < bias;
+}
+
+// One warp per 16 x 64-pixel chunk of a big triangle; chunks whose
+// rectangle lies outside one edge are skipped whole.
+template <int KIND>
+__device__ void phase_raster_big(const FrameDev& f) {
+    const unsigned long long packed = *reinterpret_cast<volatile unsigned long long*>(f.status + kStBigPacked);
+    const uint32_t ntri = (uint32_t)min((unsigned long long)f.big_cap, packed >> 40);
+    const unsigned long long total = packed & ((1ull << 40) - 1);
+    const uint32_t lane = threadIdx.x & 31;
+    if (ntri == 0) return;
+    for (;;) {
+        unsigned long long c = 0;
+        if (lane == 0) c = atomicAdd(&f.status[kStBigClaim], 1u);
+        c = __shfl_sync(0xFFFFFFFFu, c, 0);
+        if (c >= total) break;
+        // upper_bound over the ascending chunk bases, minus one
+        uint32_t first = 0, count = ntri;
+        while (count > 0) {
+            uint32_t step = count / 2, cur = first + step;
+            bool greater = c >= f.big_base[cur];
+            first = greater ? cur + 1 : first;
+            count = greater ? count - (step + 1) : step;
+        }
+        if (first == 0) continue;
+        const uint32_t i = first - 1;
+        const BigTri b = f.big[i];
+        const uint32_t nbx = (uint32_t)(b.px1 - b.px0) / kChunkCols + 1;
+        const uint32_t nby = (uint32_t)(b.py1 - b.py0) / kChunkRows + 1;
+        const unsigned long long local = c - f.big_base[i];
+        if (local >= (unsigned long long)nbx * nby) continue;  // chunk of a dropped triangle
+        const int32_t cx = (int32_t)(local % nbx), cy = (int32_t)(local / nbx);
+        const int32_t x0 = b.px0 + cx * kChunkCols, x1 = min(b.px1, x0 + kChunkCols - 1);
+        const int32_t y0 = b.py0 + cy * kChunkRows, y1 = min(b.py1, y0 + kChunkRows - 1);
+        if (edge_rejects(b.X1, b.Y1, b.X2, b.Y2, x0, x1, y0, y1, b.bias & 1u) ||
+            edge_rejects(b.X2, b.Y2, b.X0, b.Y0, x0, x1, y0, y1, (b.bias >> 1) & 1u) ||
+            edge_rejects(b.X0, b.Y0, b.X1, b.Y1, x0, x1, y0, y1, (b.bias >> 2) & 1u))
+            continue;
+        TriSetup t;
+        t.X0 = b.X0; t.Y0 = b.Y0; t.X1 = b.X1; t.Y1 = b.Y1; t.X2 = b.X2; t.Y2 = b.Y2;
+        t.z0 = b.z0; t.s1 = b.s1; t.s2 = b.s2;
+        t.id = b.id;
+        t.bias = b.bias;
+        const ViewDev* vw = f.views + b.view;
+        void* target = vw->target;
+        const uint32_t W = vw->width;
+        for (int32_t py = y0; py <= y1; py++)
+            for (int32_t px = x0 + (int32_t)lane; px <= x1; px += 32) {
+                float d;
+                if (cover(t, px, py, d)) write_fragment<KIND>(target, W, px, py, d, t.id);
+            }
+    }
+}
+
+}  // namespace
+}  // namespace lh
