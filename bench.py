@@ -264,6 +264,8 @@ def run_gpu(args):
     }
     if clk:
         line["clocks"] = clk
+    if args.batched:
+        line["batched"] = bench_batched(lh, torch, args, local_rank)
     if rank == 0 and args.cpu_frames > 0:
         med, threads, stages = cpu_oracle_frames(scene, args.cpu_frames)
         line["cpu_baseline"] = {"value": med, "unit": "ms", "cores": threads, "kind": "port",
@@ -276,6 +278,54 @@ def run_gpu(args):
     return 0
 
 
+def bench_batched(lh, torch, args, device):
+    """Batched views (main 1920x1080 + 32 probes 64^2-512^2 + 4 cascades at
+    2048^2, scene of the large configuration): device time per frame of the
+    cull + raster + resolve under each launch schedule, CUDA-graph replayed."""
+    scene = lh.Scene(3, seed=args.seed).upload(device)
+    d = scene.desc
+    probes, n = scene.probe_uniforms()
+    px = 0
+    for p in range(n):
+        w, h = lh.uniforms_fields(probes[p])["window_size"]
+        px += (w * h + 31) // 32 * 32
+    cfg = lh.Config(width=d.width, height=d.height, shadow_size=d.shadow_size, max_instances=max(1024, d.n_instances),
+                    max_draws=2000000, max_probes=n, max_probe_pixels=px, device=device)
+    r = lh.Renderer(cfg)
+    r.set_scene(scene)
+    stream = torch.cuda.Stream()
+    sptr = stream.cuda_stream
+    u = scene.uniforms
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    out = {"workload": "main %dx%d + %d probes (%d px) + 4 cascades %d^2" % (d.width, d.height, n, px, d.shadow_size)}
+    for name, sched, graph in (("persistent_graph", lh.SCHEDULE_PERSISTENT, True),
+                               ("per_stage_graph", lh.SCHEDULE_PER_STAGE, True),
+                               ("per_view_graph", lh.SCHEDULE_PER_VIEW, True),
+                               ("per_view_launches", lh.SCHEDULE_PER_VIEW, False)):
+        r.set_tuning(schedule=sched)
+        run = (lambda: r.frame_graph(u, probes, n, stream=sptr)) if graph else \
+            (lambda: r.frame_batched(u, probes, n, stream=sptr))
+        for _ in range(max(3, args.warmup)):
+            run()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        for i in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(i))
+                ev[i][0].record(stream)
+            run()
+            with torch.cuda.stream(stream):
+                ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        out[name + "_ms"] = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+    st = r.status()
+    out["status_flags"] = int(st.flags)
+    out["visible_meshlets_all_views"] = int(sum(st.visible_opaque[v] for v in range(5 + n)))
+    out["speedup_persistent_vs_per_view_launches"] = out["per_view_launches_ms"] / out["persistent_graph_ms"]
+    out["speedup_persistent_vs_per_view_graph"] = out["per_view_graph_ms"] / out["persistent_graph_ms"]
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -285,6 +335,7 @@ def main():
     ap.add_argument("--config", type=int, default=2)
     ap.add_argument("--seed", type=int, default=None)
     ap.add_argument("--cpu-frames", type=int, default=3)
+    ap.add_argument("--batched", type=int, default=1, help="also time the batched multi-view frame (config 3)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

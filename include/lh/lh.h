@@ -155,6 +155,31 @@ lh_status lh_frame_graph(lh_ctx* ctx, const Uniforms* host_uniforms,
                          const Uniforms* probe_uniforms, uint32_t n_probes,
                          void* stream, lh_frame_out* out);
 
+/* Gradient buffers of one mesh for lh_resolve_backward (device addresses;
+ * any may be 0 to skip it).  Gradients are added to what is there. */
+typedef struct lh_mesh_grads {
+    uint64_t positions;         /* float[3] per vertex: d/d(position as the shader reads it) */
+    uint64_t normals;           /* float[3] per vertex: d/d(raw normal) */
+    uint64_t uvs;               /* float[2] per vertex: d/d(raw uv) */
+    uint64_t base_color_factor; /* float[3]: d/d(MeshInfo.base_color_factor) */
+} lh_mesh_grads;
+
+typedef struct lh_grad_targets {
+    uint64_t instance_grads; /* device array [n_instances] of device addresses of lh_mesh_grads (0 = skip) */
+    uint64_t texture_grads;  /* device array [n_textures] of device addresses of float4[h][w]: d/d(linear texel) (0 = skip) */
+    uint64_t light_dir;      /* float[3]: d/d(Uniforms.sun_dir) */
+    uint64_t light_color;    /* float[3]: d/d(Uniforms.sun_intensity), the light colour */
+} lh_grad_targets;
+
+/* Adjoint of the lighting resolve of the last frame with visibility held
+ * fixed (triangle IDs, face flip, cascade choice and shadow-map compare
+ * results are the forward's; everything continuous is differentiated).
+ * `d_grad_hdr` is the upstream gradient, float4[height][width] (alpha
+ * ignored).  The forward quantities are recomputed per pixel from the
+ * visibility buffer, not stored.  Normal-mapped materials are not
+ * differentiated.  No counterpart in the reference. */
+lh_status lh_resolve_backward(lh_ctx* ctx, uint64_t d_grad_hdr, const lh_grad_targets* targets, void* stream);
+
 /* Pointers to the context's result buffers (valid until lh_destroy). */
 lh_status lh_get_outputs(lh_ctx* ctx, lh_frame_out* out);
 

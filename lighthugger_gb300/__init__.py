@@ -82,6 +82,16 @@ class Tuning(C.Structure):
                 ("schedule", C.c_uint32)]
 
 
+class MeshGrads(C.Structure):
+    _fields_ = [("positions", C.c_uint64), ("normals", C.c_uint64), ("uvs", C.c_uint64),
+                ("base_color_factor", C.c_uint64)]
+
+
+class GradTargets(C.Structure):
+    _fields_ = [("instance_grads", C.c_uint64), ("texture_grads", C.c_uint64), ("light_dir", C.c_uint64),
+                ("light_color", C.c_uint64)]
+
+
 class SceneParams(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("n_instances", C.c_uint32), ("n_probes", C.c_uint32),
                 ("detail", C.c_float), ("quantized", C.c_uint32), ("reference_normal_transform", C.c_uint32),
@@ -132,6 +142,7 @@ def lib():
     L.lh_last_error.restype = C.c_char_p
     L.lh_destroy.argtypes = [P]
     L.lh_destroy.restype = None
+    L.lh_resolve_backward.argtypes = [P, C.c_uint64, C.POINTER(GradTargets), P]
     L.lh_set_profiling.argtypes = [P, C.c_int]
     L.lh_get_stage_times.argtypes = [P, C.POINTER(C.c_float), C.c_uint32]
     L.lh_set_tuning.argtypes = [P, C.POINTER(Tuning)]
@@ -144,7 +155,7 @@ def lib():
     L.lh_make_uniforms.argtypes = [C.POINTER(Camera), C.POINTER(Uniforms)]
     for name in ("lh_create", "lh_set_scene", "lh_frame", "lh_frame_batched", "lh_frame_graph", "lh_get_outputs",
                  "lh_read_status",
-                 "lh_download", "lh_set_profiling", "lh_get_stage_times", "lh_set_tuning", "lh_get_tuning", "lh_scene_create", "lh_scene_describe",
+                 "lh_download", "lh_resolve_backward", "lh_set_profiling", "lh_get_stage_times", "lh_set_tuning", "lh_get_tuning", "lh_scene_create", "lh_scene_describe",
                  "lh_scene_upload", "lh_make_uniforms"):
         getattr(L, name).restype = C.c_int32
     _lib = L

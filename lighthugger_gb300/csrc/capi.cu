@@ -608,6 +608,23 @@ lh_status lh_read_status(lh_ctx* c, lh_device_status* out) {
     return LH_OK;
 }
 
+lh_status lh_resolve_backward(lh_ctx* c, uint64_t d_grad_hdr, const lh_grad_targets* targets, void* stream) {
+    lh_status st = check_ctx(c);
+    if (st != LH_OK) return st;
+    if (!d_grad_hdr || !targets) return fail(c, LH_ERR_INVALID_ARGUMENT, "null gradient or targets");
+    if (!c->d_reset) return fail(c, LH_ERR_NO_SCENE, "lh_set_scene was not called");
+    if ((d_grad_hdr & 15) || (targets->instance_grads & 7) || (targets->texture_grads & 7) ||
+        (targets->light_dir & 3) || (targets->light_color & 3))
+        return fail(c, LH_ERR_INVALID_ARGUMENT, "misaligned gradient buffer");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    FrameDev f = frame_dev(c, c->n_views_last, c->n_instances);
+    cudaError_t e = launch_resolve_backward(f, c->cfg.width, c->cfg.height, reinterpret_cast<const float4*>(d_grad_hdr),
+                                            *targets, s);
+    if (e != cudaSuccess) return cuda_fail(c, e, "resolve backward");
+    c->last_stream = s;
+    return LH_OK;
+}
+
 lh_status lh_set_profiling(lh_ctx* c, int enable) {
     lh_status st = check_ctx(c);
     if (st != LH_OK) return st;

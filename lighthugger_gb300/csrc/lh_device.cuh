@@ -112,6 +112,36 @@ __device__ __forceinline__ f3 world_pos(const lh_mat4& transform, f3 p) {
     return {w.x, w.y, w.z};
 }
 
+// Fields of a MeshInfo the resolve needs (loaded as aligned words).
+struct MeshInfoResolve {
+    uint64_t positions, indices, normals, uvs, micro_indices, meshlets;
+    uint32_t flags;
+    lh_vec2 texture_scale, texture_offset;
+    uint32_t base_tex, mr_tex, normal_tex;
+    lh_vec3 base_color_factor;
+};
+__device__ __forceinline__ MeshInfoResolve load_mesh_info_resolve(const MeshInfo* mi) {
+    const unsigned long long* w = reinterpret_cast<const unsigned long long*>(mi);
+    const uint32_t* d = reinterpret_cast<const uint32_t*>(mi);
+    MeshInfoResolve r;
+    r.positions = __ldg(w + 0);
+    r.indices = __ldg(w + 1);
+    r.normals = __ldg(w + 2);
+    r.uvs = __ldg(w + 3);
+    r.micro_indices = __ldg(w + 4);
+    r.meshlets = __ldg(w + 5);
+    r.flags = (uint32_t)((__ldg(w + 6) >> 16) & 0xFFu);
+    r.texture_scale = {__uint_as_float(__ldg(d + 17)), __uint_as_float(__ldg(d + 18))};
+    r.texture_offset = {__uint_as_float(__ldg(d + 19)), __uint_as_float(__ldg(d + 20))};
+    uint32_t t01 = __ldg(d + 21), t2 = __ldg(d + 22);
+    r.base_tex = t01 & 0xFFFFu;
+    r.mr_tex = t01 >> 16;
+    r.normal_tex = t2 & 0xFFFFu;
+    r.base_color_factor = {__uint_as_float(__ldg(d + 23)), __uint_as_float(__ldg(d + 24)), __uint_as_float(__ldg(d + 25))};
+    return r;
+}
+
+
 // ------------------------------------------------------------------ culling (culling.glsl)
 __device__ __forceinline__ float max_scale(const lh_mat4& t) {
     float sx = length(f3{t.cols[0].x, t.cols[0].y, t.cols[0].z});

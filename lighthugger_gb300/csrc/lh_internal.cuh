@@ -112,6 +112,8 @@ cudaError_t launch_frame_persistent(const FrameDev& f, uint32_t n_persp, uint32_
                                     float blocks_per_sm, cudaStream_t s, int sms);
 int persistent_blocks_per_sm();
 cudaError_t launch_resolve(const FrameDev& f, uint32_t width, uint32_t height, cudaStream_t s);
+cudaError_t launch_resolve_backward(const FrameDev& f, uint32_t width, uint32_t height, const float4* grad,
+                                    const lh_grad_targets& t, cudaStream_t s);
 cudaError_t launch_sum_meshlets(const Instance* instances, uint32_t n, unsigned long long* out, cudaStream_t s);
 
 }  // namespace lh

@@ -150,34 +150,6 @@ __device__ __forceinline__ f3 interp_deriv(const Bary& b, float v0, float v1, fl
     return {dot(m, b.lambda), dot(m, b.ddx), dot(m, b.ddy)};
 }
 
-struct MeshInfoResolve {
-    uint64_t positions, indices, normals, uvs, micro_indices, meshlets;
-    uint32_t flags;
-    lh_vec2 texture_scale, texture_offset;
-    uint32_t base_tex, mr_tex, normal_tex;
-    lh_vec3 base_color_factor;
-};
-__device__ __forceinline__ MeshInfoResolve load_mesh_info_resolve(const MeshInfo* mi) {
-    const unsigned long long* w = reinterpret_cast<const unsigned long long*>(mi);
-    const uint32_t* d = reinterpret_cast<const uint32_t*>(mi);
-    MeshInfoResolve r;
-    r.positions = __ldg(w + 0);
-    r.indices = __ldg(w + 1);
-    r.normals = __ldg(w + 2);
-    r.uvs = __ldg(w + 3);
-    r.micro_indices = __ldg(w + 4);
-    r.meshlets = __ldg(w + 5);
-    r.flags = (uint32_t)((__ldg(w + 6) >> 16) & 0xFFu);
-    r.texture_scale = {__uint_as_float(__ldg(d + 17)), __uint_as_float(__ldg(d + 18))};
-    r.texture_offset = {__uint_as_float(__ldg(d + 19)), __uint_as_float(__ldg(d + 20))};
-    uint32_t t01 = __ldg(d + 21), t2 = __ldg(d + 22);
-    r.base_tex = t01 & 0xFFFFu;
-    r.mr_tex = t01 >> 16;
-    r.normal_tex = t2 & 0xFFFFu;
-    r.base_color_factor = {__uint_as_float(__ldg(d + 23)), __uint_as_float(__ldg(d + 24)), __uint_as_float(__ldg(d + 25))};
-    return r;
-}
-
 // render_geometry.comp:70-266, one thread per pixel (blocks of 32 x 8).
 __global__ void __launch_bounds__(256) k_resolve(FrameDev f) {
     const Uniforms& u = *f.uniforms;
@@ -279,7 +251,10 @@ __global__ void __launch_bounds__(256) k_resolve(FrameDev f) {
                zero * (3.0f * normal.z * normal.z - 1.0f)) + zero * (normal.x * normal.x - normal.y * normal.y));
     f3 ambient = amb * (base * (1.0f - metallic));
     float sun_intensity = kPi * shadow_sum;
-    f3 sun = BRDF(view_vector, ld3(u.sun_dir), normal, roughness, metallic, base, alpha) * sun_intensity;
+    // Uniforms.sun_intensity is the light colour (1,1,1 in the reference, whose
+    // shaders never read it; main.cpp:649): a multiply by 1 leaves every bit.
+    f3 sun = (BRDF(view_vector, ld3(u.sun_dir), normal, roughness, metallic, base, alpha) * sun_intensity) *
+             ld3(u.sun_intensity);
     f3 o = sun + ambient;
     __stcs(out, make_float4(o.x, o.y, o.z, 1.0f));
 }

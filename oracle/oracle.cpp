@@ -940,7 +940,10 @@ template <class T> static V4<T> resolve_pixel(const lho_frame_desc* d, const lho
                   zero * ((T)3 * normal.z * normal.z - (T)1)) + zero * (normal.x * normal.x - normal.y * normal.y));
     V3<T> ambient = amb * (base * ((T)1 - metallic));
     T sun_intensity = (T)PI_F * shadow_sum;
-    V3<T> sun = BRDF<T>(view_vector, v3<T>(u.sun_dir), normal, roughness, metallic, base, alpha) * sun_intensity;
+    // Uniforms.sun_intensity as the light colour: (1,1,1) reproduces the
+    // reference, whose shaders do not read the field (main.cpp:649).
+    V3<T> sun = (BRDF<T>(view_vector, v3<T>(u.sun_dir), normal, roughness, metallic, base, alpha) * sun_intensity) *
+                v3<T>(u.sun_intensity);
     V3<T> out = sun + ambient;
     return {out.x, out.y, out.z, (T)1};
 }

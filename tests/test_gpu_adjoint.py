@@ -1,0 +1,195 @@
+"""Resolve adjoint on the GPU (lh_resolve_backward) against the oracle's FP64
+reference gradient: central differences (h = 1e-4) of the FP64 forward
+resolve over the same float buffers, visibility held fixed, upstream
+gradient N(0,1) on interior pixels (>= 2 px inside their triangle) and zero
+elsewhere.  Parameters: vertex positions, normals and uvs of triangles under
+those pixels, per-material base-colour factors, light direction and colour.
+Relative error bound 1e-3."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from tests import scene_view as sv
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-3
+
+
+def _interior_pixels(vis, margin=2):
+    ids = (vis & np.uint64(0xFFFFFFFF)).astype(np.int64)
+    cov = (vis >> np.uint64(32)) != 0
+    ok = cov.copy()
+    H, W = vis.shape
+    for dy in range(-margin, margin + 1):
+        for dx in range(-margin, margin + 1):
+            sh = np.full_like(ids, -1)
+            ys = slice(max(dy, 0), H + min(dy, 0))
+            yd = slice(max(-dy, 0), H + min(-dy, 0))
+            xs = slice(max(dx, 0), W + min(dx, 0))
+            xd = slice(max(-dx, 0), W + min(-dx, 0))
+            sh[yd, xd] = ids[ys, xs]
+            ok &= sh == ids
+    return ok
+
+
+class HostScene:
+    """Writable views of the host scene's float buffers (what the oracle reads)."""
+
+    def __init__(self, scene):
+        self.scene = scene
+        self.inst = sv.instances(scene)
+        self.infos = {}
+        for a in self.inst["mesh_info_address"]:
+            a = int(a)
+            if a not in self.infos:
+                self.infos[a] = sv.Mesh(sv.mesh_info(a))
+
+    def float_view(self, addr, n):
+        return np.ctypeslib.as_array((C.c_float * n).from_address(addr))
+
+    def vertex_arrays(self, info_addr):
+        m = self.infos[info_addr]
+        nv = len(m.positions)
+        mi = m.mi
+        return (self.float_view(int(mi["positions"]), nv * 3).reshape(nv, 3),
+                self.float_view(int(mi["normals"]), nv * 3).reshape(nv, 3),
+                self.float_view(int(mi["uvs"]), nv * 2).reshape(nv, 2))
+
+    def bcf_view(self, info_addr):
+        return self.float_view(info_addr + 92, 3)
+
+
+def test_adjoint_matches_fp64_central_differences(native, oracle):
+    import torch
+    lh = native
+    scene = lh.Scene(4, width=256, height=256, n_instances=512).upload(0)
+    d = scene.desc
+    cfg = lh.Config(width=d.width, height=d.height, shadow_size=1024, max_instances=1024, max_draws=200000)
+    r = lh.Renderer(cfg)
+    r.set_scene(scene)
+    u = scene.uniforms
+    r.frame(u)
+    fr = oracle.run_scene(scene, shadow_size=1024, max_instances=1024, max_draws=200000, uniforms=u)
+    vis = fr.vis
+    assert np.array_equal(r.visibility(), vis)
+    interior = _interior_pixels(vis)
+    rng = np.random.default_rng(11)
+    ys, xs = np.nonzero(interior)
+    assert len(ys) > 200, "too few interior pixels: %d" % len(ys)
+    pick = rng.choice(len(ys), size=min(600, len(ys)), replace=False)
+    G = np.zeros((d.height, d.width, 4), np.float32)
+    G[ys[pick], xs[pick], :3] = rng.normal(size=(len(pick), 3)).astype(np.float32)
+    hs = HostScene(scene)
+
+    # ---- GPU adjoint into per-mesh buffers
+    info_addrs = sorted(hs.infos)
+    dev = torch.device("cuda")
+    bufs = {}
+    rec = np.zeros((len(info_addrs), 4), np.uint64)
+    for k, a in enumerate(info_addrs):
+        nv = len(hs.infos[a].positions)
+        b = {"pos": torch.zeros(nv * 3, device=dev), "nrm": torch.zeros(nv * 3, device=dev),
+             "uv": torch.zeros(nv * 2, device=dev), "bcf": torch.zeros(4, device=dev)}
+        bufs[a] = b
+        rec[k] = [b["pos"].data_ptr(), b["nrm"].data_ptr(), b["uv"].data_ptr(), b["bcf"].data_ptr()]
+    rec_dev = torch.from_numpy(rec.view(np.int64)).to(dev)
+    inst_rec = np.array([rec_dev.data_ptr() + 32 * info_addrs.index(int(a)) for a in hs.inst["mesh_info_address"]],
+                        np.uint64)
+    inst_rec_dev = torch.from_numpy(inst_rec.view(np.int64)).to(dev)
+    light = torch.zeros(8, device=dev)
+    g_dev = torch.from_numpy(G).to(dev)
+    t = lh.GradTargets(instance_grads=inst_rec_dev.data_ptr(), texture_grads=0, light_dir=light.data_ptr(),
+                       light_color=light.data_ptr() + 16)
+    torch.cuda.synchronize()
+    st = lh.lib().lh_resolve_backward(r.ctx, g_dev.data_ptr(), C.byref(t), None)
+    assert st == 0
+    torch.cuda.synchronize()
+    gpu = {a: {k: v.cpu().numpy().astype(np.float64) for k, v in b.items()} for a, b in bufs.items()}
+    gl = light.cpu().numpy().astype(np.float64)
+
+    # ---- FP64 reference: L(theta) = sum G . hdr64
+    Gd = G.astype(np.float64)
+
+    def loss():
+        h = oracle.resolve_f64(fr)
+        return float((h[..., :3] * Gd[..., :3]).sum())
+
+    def fd(arr, i, h):
+        """Central difference of L in arr[i] (a float32 view) with exact steps."""
+        x0 = arr[i]
+
+        def at(step):
+            arr[i] = np.float32(x0 + step)
+            dx = float(arr[i]) - float(x0)
+            v = loss()
+            arr[i] = x0
+            return v, dx
+
+        (lp, dp), (lm, dm) = at(h), at(-h)
+        (lp2, dp2), (lm2, dm2) = at(h / 2), at(-h / 2)
+        g1 = (lp - lm) / (dp - dm)
+        g2 = (lp2 - lm2) / (dp2 - dm2)
+        return g1, abs(g1 - g2) <= 1e-3 * (abs(g1) + abs(g2)) + 1e-9
+
+    checks, skipped, worst = [], 0, 0.0
+
+    def record(kind, got, ref, ok):
+        nonlocal skipped
+        if not ok:
+            skipped += 1
+            return
+        checks.append((kind, got, ref))
+
+    # vertices of triangles under picked pixels
+    uf = lh.uniforms_fields(u)
+    vis_p = vis[ys[pick], xs[pick]]
+    slots = (vis_p & np.uint64(0xFFFFFF)).astype(np.int64)
+    tris = (vis_p >> np.uint64(24) & np.uint64(0xFF)).astype(np.int64)
+    refs = fr.meshlet_references(0).view(np.uint32).reshape(-1, 2)
+    verts = []
+    for s_, t_ in list(zip(slots, tris))[:12]:
+        inst_i = int(refs[s_, 0])
+        ml_i = int(refs[s_, 1] & 0xFFFF)
+        a = int(hs.inst["mesh_info_address"][inst_i])
+        micro, idx = hs.infos[a].meshlet_triangles(ml_i)
+        verts.append((a, int(idx[t_][0])))
+    verts = list(dict.fromkeys(verts))[:8]
+    for a, vi in verts:
+        P, N, UV = hs.vertex_arrays(a)
+        for c in range(3):
+            g, ok = fd(P[vi], c, 1e-4 * max(1.0, abs(float(P[vi][c]))))
+            record("position", gpu[a]["pos"][vi * 3 + c], g, ok)
+            g, ok = fd(N[vi], c, 1e-4)
+            record("normal", gpu[a]["nrm"][vi * 3 + c], g, ok)
+        for c in range(2):
+            g, ok = fd(UV[vi], c, 1e-4)
+            record("uv", gpu[a]["uv"][vi * 2 + c], g, ok)
+    for a in info_addrs[:3]:
+        bv = hs.bcf_view(a)
+        for c in range(3):
+            g, ok = fd(bv, c, 1e-4)
+            record("base_color_factor", gpu[a]["bcf"][c], g, ok)
+    ub = np.ctypeslib.as_array((C.c_float * 140).from_address(C.addressof(fr._ubuf)))
+    for c in range(3):
+        g, ok = fd(ub, 127 + c, 1e-4)  # sun_dir at byte 508
+        record("light_dir", gl[c], g, ok)
+        g, ok = fd(ub, 130 + c, 1e-4)  # sun_intensity at byte 520
+        record("light_color", gl[4 + c], g, ok)
+
+    assert len(checks) >= 40, "only %d checks (%d skipped)" % (len(checks), skipped)
+    by_kind = {}
+    for kind, got, ref in checks:
+        by_kind.setdefault(kind, []).append((got, ref))
+    report = []
+    for kind, lst in by_kind.items():
+        refs_ = np.array([b for a, b in lst])
+        scale = max(np.abs(refs_).max(), 1e-6)
+        for got, ref in lst:
+            err = abs(got - ref) / max(abs(ref), 1e-2 * scale)
+            worst = max(worst, err)
+            if err > REL_TOL:
+                report.append("%s: gpu %.8g fp64 %.8g rel %.2e" % (kind, got, ref, err))
+    assert not report, "\n".join(report[:20]) + "\n(%d checks, %d skipped)" % (len(checks), skipped)
+    print("adjoint: %d checks, %d skipped, worst relative error %.2e" % (len(checks), skipped, worst))
