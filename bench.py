@@ -266,6 +266,8 @@ def run_gpu(args):
         line["clocks"] = clk
     if args.batched:
         line["batched"] = bench_batched(lh, torch, args, local_rank)
+    if args.differentiable:
+        line["differentiable"] = bench_differentiable(lh, torch, args, local_rank)
     if rank == 0 and args.cpu_frames > 0:
         med, threads, stages = cpu_oracle_frames(scene, args.cpu_frames)
         line["cpu_baseline"] = {"value": med, "unit": "ms", "cores": threads, "kind": "port",
@@ -318,12 +320,77 @@ def bench_batched(lh, torch, args, device):
                 ev[i][1].record(stream)
         torch.cuda.synchronize()
         out[name + "_ms"] = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+    # where a batched frame's time goes (per-stage schedule, CUDA events)
+    r.set_tuning(schedule=lh.SCHEDULE_PER_STAGE)
+    r.set_profiling(True)
+    r.frame_batched(u, probes, n, stream=sptr)
+    out["per_stage_stage_ms"] = {k: round(v, 4) for k, v in r.stage_times().items()}
+    r.set_profiling(False)
     st = r.status()
     out["status_flags"] = int(st.flags)
     out["visible_meshlets_all_views"] = int(sum(st.visible_opaque[v] for v in range(5 + n)))
     out["speedup_persistent_vs_per_view_launches"] = out["per_view_launches_ms"] / out["persistent_graph_ms"]
     out["speedup_persistent_vs_per_view_graph"] = out["per_view_graph_ms"] / out["persistent_graph_ms"]
     return out
+
+
+def bench_differentiable(lh, torch, args, device):
+    """Differentiable resolve (2,048 instances of 4 meshes at 512x512): the
+    forward resolve kernel and the adjoint (lh_resolve_backward with every
+    gradient target) timed with CUDA events on one stream."""
+    import ctypes as C
+    import numpy as np
+    from lighthugger_gb300.diff import _scene_records
+    scene = lh.Scene(4, seed=args.seed).upload(device)
+    d = scene.desc
+    r = lh.Renderer(lh.Config(width=d.width, height=d.height, shadow_size=d.shadow_size,
+                              max_instances=max(1024, d.n_instances), max_draws=2000000, device=device))
+    r.set_scene(scene)
+    stream = torch.cuda.Stream()
+    sptr = stream.cuda_stream
+    u = scene.uniforms
+    recs, inst = _scene_records(scene)
+    dev = torch.device("cuda", device)
+    total_v = sum(m.vertices for m in recs)
+    g_pos = torch.zeros(total_v * 3, device=dev)
+    g_nrm = torch.zeros(total_v * 3, device=dev)
+    g_uv = torch.zeros(total_v * 2, device=dev)
+    g_bcf = torch.zeros(len(recs) * 4, device=dev)
+    first, rows = 0, []
+    for k, m in enumerate(recs):
+        rows.append([g_pos.data_ptr() + 12 * first, g_nrm.data_ptr() + 12 * first, g_uv.data_ptr() + 8 * first,
+                     g_bcf.data_ptr() + 16 * k])
+        first += m.vertices
+    rec_dev = torch.tensor(np.array(rows, np.uint64).view(np.int64), device=dev)
+    inst_rec = torch.tensor((rec_dev.data_ptr() + 32 * inst.astype(np.int64)), device=dev)
+    tex_grads = [torch.zeros(t.width * t.height * 4, device=dev) for t in
+                 (scene.desc.host_textures[i] for i in range(d.n_textures))]
+    tex_tab = torch.tensor([t.data_ptr() for t in tex_grads], dtype=torch.int64, device=dev)
+    light = torch.zeros(8, device=dev)
+    grad = torch.randn(d.height, d.width, 4, device=dev)
+    t = lh.GradTargets(instance_grads=inst_rec.data_ptr(), texture_grads=tex_tab.data_ptr(),
+                       light_dir=light.data_ptr(), light_color=light.data_ptr() + 16)
+    r.set_profiling(True)
+    fwd, bwd = [], []
+    for i in range(max(3, args.warmup) + args.steps):
+        r.frame(u, stream=sptr)
+        st_ms = r.stage_times()["resolve"]
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            a.record(stream)
+        lh._check(lh.lib().lh_resolve_backward(r.ctx, grad.data_ptr(), C.byref(t), C.c_void_p(sptr)),
+                  "lh_resolve_backward", r.ctx)
+        with torch.cuda.stream(stream):
+            b.record(stream)
+        torch.cuda.synchronize()
+        if i >= max(3, args.warmup):
+            fwd.append(st_ms)
+            bwd.append(a.elapsed_time(b))
+    r.set_profiling(False)
+    f_ms, b_ms = sum(fwd) / len(fwd), sum(bwd) / len(bwd)
+    return {"workload": "%d instances of %d meshes, %dx%d, visibility fixed" % (d.n_instances, d.n_meshes, d.width,
+                                                                                 d.height),
+            "resolve_forward_ms": f_ms, "resolve_backward_ms": b_ms, "bwd_over_fwd": b_ms / f_ms}
 
 
 def main():
@@ -336,6 +403,7 @@ def main():
     ap.add_argument("--seed", type=int, default=None)
     ap.add_argument("--cpu-frames", type=int, default=3)
     ap.add_argument("--batched", type=int, default=1, help="also time the batched multi-view frame (config 3)")
+    ap.add_argument("--differentiable", type=int, default=1, help="also time the resolve adjoint (config 4)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -66,6 +66,22 @@ lh_status lh_scene_describe(const lh_scene* scene, lh_scene_desc* out);
 lh_status lh_scene_upload(lh_scene* scene, int device);
 void lh_scene_destroy(lh_scene* scene);
 
+/* One MeshInfo record of a scene (one per mesh x material pair). */
+typedef struct lh_scene_mesh {
+    const MeshInfo* host_info; /* host record (host addresses inside) */
+    uint64_t device_info;      /* device address of the record; 0 before lh_scene_upload */
+    uint64_t device_positions, device_normals, device_uvs; /* the record's device buffers */
+    uint32_t mesh;             /* index of the vertex buffers (records of one mesh share them) */
+    uint32_t vertices;
+    uint32_t triangles;
+    uint32_t flags;
+} lh_scene_mesh;
+
+uint32_t lh_scene_mesh_count(const lh_scene* scene);
+lh_status lh_scene_mesh_get(const lh_scene* scene, uint32_t index, lh_scene_mesh* out);
+/* MeshInfo record index of every instance (out: n_instances entries). */
+lh_status lh_scene_instance_records(const lh_scene* scene, uint32_t* out);
+
 /* Camera as the reference's CameraParams (src/input.h:18-49) plus the
  * window; fov in degrees. */
 typedef struct lh_camera {

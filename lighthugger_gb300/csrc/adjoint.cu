@@ -163,10 +163,9 @@ __global__ void __launch_bounds__(256, 2) k_resolve_backward(FrameDev f, const f
         fx.base_tex = mi.base_tex;
         fx.mr_tex = mi.mr_tex;
         fx.has_normal_map = mi.normal_tex != UNUSED_TEXTURE_INDEX;
-        // interpolated world position through the forward's own barycentrics
-        // (re-derived inside shade(); here only to pick the cascade)
+        // the cascade the forward chose: its own barycentrics and world
+        // position, in its absolute float arithmetic (render_geometry.comp:183-196)
         {
-            // compute lambda as the forward kernel does
             f4 c0 = mul(u.combined_perspective_view, f4{p.W[0].x, p.W[0].y, p.W[0].z, 1.0f});
             f4 c1 = mul(u.combined_perspective_view, f4{p.W[1].x, p.W[1].y, p.W[1].z, 1.0f});
             f4 c2 = mul(u.combined_perspective_view, f4{p.W[2].x, p.W[2].y, p.W[2].z, 1.0f});
@@ -202,6 +201,19 @@ __global__ void __launch_bounds__(256, 2) k_resolve_backward(FrameDev f, const f
             }
         }
         DeviceSampler smp{&f};
+        // face flip, far-plane test and compare results exactly as the forward
+        shade::decide<float>(fx, p, smp);
+        // the continuous part in camera-relative coordinates: W - cam is
+        // (nearly) exact, and PV T(cam), UVS T(cam) are formed in double
+        const double cx = u.camera_pos.x, cy = u.camera_pos.y, cz = u.camera_pos.z;
+        for (int r = 0; r < 4; r++) {
+            fx.pv[3][r] = (float)((double)fx.pv[3][r] + (((double)fx.pv[0][r] * cx + (double)fx.pv[1][r] * cy) +
+                                                         (double)fx.pv[2][r] * cz));
+            fx.uvs[3][r] = (float)((double)fx.uvs[3][r] + (((double)fx.uvs[0][r] * cx + (double)fx.uvs[1][r] * cy) +
+                                                           (double)fx.uvs[2][r] * cz));
+        }
+        for (int k = 0; k < 3; k++) p.W[k] = {p.W[k].x - u.camera_pos.x, p.W[k].y - u.camera_pos.y, p.W[k].z - u.camera_pos.z};
+        fx.cam[0] = fx.cam[1] = fx.cam[2] = 0.0f;
         v3<float> out;
         PixelGrad<float> g;
         shade::shade<float>(fx, p, smp, &out, v3<float>{gp.x, gp.y, gp.z}, &g);

@@ -56,7 +56,7 @@ __device__ void reset_raster_words(const FrameDev& f) {
 
 constexpr int kPersistentThreads = 256;
 
-__global__ void __launch_bounds__(kPersistentThreads, 2) k_frame_persistent(FrameDev f, uint32_t n_persp,
+__global__ void __launch_bounds__(kPersistentThreads, 3) k_frame_persistent(FrameDev f, uint32_t n_persp,
                                                                            RasterTune tune) {
     uint32_t epoch = 0;
     const uint64_t gtid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, gstride = (uint64_t)gridDim.x * blockDim.x;
@@ -117,9 +117,8 @@ cudaError_t launch_frame_persistent(const FrameDev& f, uint32_t n_persp, uint32_
                                     float blocks_per_sm, cudaStream_t s, int sms) {
     const int resident = persistent_blocks_per_sm();
     if (resident <= 0) return cudaErrorCooperativeLaunchTooLarge;
-    int per_sm = (int)blocks_per_sm;
-    if (per_sm < 1) per_sm = 1;
-    if (per_sm > resident) per_sm = resident;
+    (void)blocks_per_sm;
+    const int per_sm = resident;  // every resident slot: the raster phases need the occupancy
     RasterTune tune{small_px, medium_px};
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(sms * per_sm));

@@ -564,6 +564,8 @@ struct lh_scene {
     std::vector<std::unique_ptr<DeviceAlloc>> allocs;
     Instance* device_instances = nullptr;
     std::vector<lh_texture> device_textures;
+    std::vector<MeshInfo> device_infos;
+    uint64_t device_info_base = 0;
     uint64_t device_bytes = 0;
     Uniforms uniforms;
     std::vector<Uniforms> probes;
@@ -986,6 +988,8 @@ lh_status lh_scene_upload(lh_scene* s, int device) {
     uint64_t dinfo_base;
     lh_status st;
     if ((st = upload(s, dinfos.data(), dinfos.size() * sizeof(MeshInfo), &dinfo_base)) != LH_OK) return st;
+    s->device_infos = dinfos;
+    s->device_info_base = dinfo_base;
     std::vector<Instance> dinst = s->host_instances;
     for (size_t i = 0; i < dinst.size(); i++) dinst[i].mesh_info_address = dinfo_base + s->instance_info[i] * sizeof(MeshInfo);
     uint64_t dinst_ptr;
@@ -1003,6 +1007,32 @@ lh_status lh_scene_upload(lh_scene* s, int device) {
         s->device_textures.push_back(d);
     }
     s->device_instances = (Instance*)(uintptr_t)dinst_ptr;
+    return LH_OK;
+}
+
+uint32_t lh_scene_mesh_count(const lh_scene* s) { return s ? (uint32_t)s->host_infos.size() : 0; }
+
+lh_status lh_scene_mesh_get(const lh_scene* s, uint32_t i, lh_scene_mesh* out) {
+    if (!s || !out || i >= s->host_infos.size()) return LH_ERR_INVALID_ARGUMENT;
+    std::memset(out, 0, sizeof(*out));
+    out->host_info = &s->host_infos[i];
+    const BuiltMesh& m = s->meshes[s->info_mesh[i]];
+    out->mesh = s->info_mesh[i];
+    out->vertices = m.n_vertices;
+    out->triangles = m.n_triangles;
+    out->flags = s->host_infos[i].flags;
+    if (!s->device_infos.empty()) {
+        out->device_info = s->device_info_base + (uint64_t)i * sizeof(MeshInfo);
+        out->device_positions = s->device_infos[i].positions;
+        out->device_normals = s->device_infos[i].normals;
+        out->device_uvs = s->device_infos[i].uvs;
+    }
+    return LH_OK;
+}
+
+lh_status lh_scene_instance_records(const lh_scene* s, uint32_t* out) {
+    if (!s || !out) return LH_ERR_INVALID_ARGUMENT;
+    for (size_t i = 0; i < s->instance_info.size(); i++) out[i] = s->instance_info[i];
     return LH_OK;
 }
 

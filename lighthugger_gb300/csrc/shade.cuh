@@ -105,6 +105,10 @@ struct PixelFixed {
     uint32_t thin;         // alpha clip: thin-walled lobe
     uint32_t base_tex, mr_tex;
     uint32_t has_normal_map;
+    // discrete decisions of the forward, held fixed (see decide())
+    float flip;              // +1, or -1 when the triangle is seen from behind
+    uint32_t shadow_const;   // shadow coordinate beyond the cascade's far plane
+    uint64_t cmp;            // 36 shadow-map compare results: bit 4*tap + texel
 };
 
 // Differentiated inputs.
@@ -130,16 +134,30 @@ template <class T> struct PixelGrad {
 
 // Shadow-map access for the PCF: compare result of texel (i, j) of the layer
 // against `ref` (1 when ref < stored).
+// Compare results of one PCF tap (4 bits: texels 00, 10, 01, 11).
 template <class T, class Sampler>
-LH_HD T pcf_tap(const Sampler& smp, uint32_t layer, T u, T v, T ref, T S, T& da, T& db) {
+LH_HD uint32_t pcf_bits(const Sampler& smp, uint32_t layer, T u, T v, T ref, T S) {
+    T uu = u * S - T(0.5), vv = v * S - T(0.5);
+    if (!(tabs(uu) < T(1e9))) uu = T(0);
+    if (!(tabs(vv) < T(1e9))) vv = T(0);
+    int64_t i0 = (int64_t)tfloor(uu), j0 = (int64_t)tfloor(vv);
+    return (smp.shadow_cmp(layer, i0, j0, ref) != T(0) ? 1u : 0u) |
+           (smp.shadow_cmp(layer, i0 + 1, j0, ref) != T(0) ? 2u : 0u) |
+           (smp.shadow_cmp(layer, i0, j0 + 1, ref) != T(0) ? 4u : 0u) |
+           (smp.shadow_cmp(layer, i0 + 1, j0 + 1, ref) != T(0) ? 8u : 0u);
+}
+
+// One PCF tap with fixed compare results `bits`: the bilinear weights and
+// their derivatives in the tap's fractional position.
+template <class T>
+LH_HD T pcf_tap(uint32_t bits, T u, T v, T S, T& da, T& db) {
     T uu = u * S - T(0.5), vv = v * S - T(0.5);
     if (!(tabs(uu) < T(1e9))) uu = T(0);
     if (!(tabs(vv) < T(1e9))) vv = T(0);
     T fu = tfloor(uu), fv = tfloor(vv);
     T a = uu - fu, b = vv - fv;
-    int64_t i0 = (int64_t)fu, j0 = (int64_t)fv;
-    T c00 = smp.shadow_cmp(layer, i0, j0, ref), c10 = smp.shadow_cmp(layer, i0 + 1, j0, ref);
-    T c01 = smp.shadow_cmp(layer, i0, j0 + 1, ref), c11 = smp.shadow_cmp(layer, i0 + 1, j0 + 1, ref);
+    T c00 = (bits & 1u) ? T(1) : T(0), c10 = (bits & 2u) ? T(1) : T(0);
+    T c01 = (bits & 4u) ? T(1) : T(0), c11 = (bits & 8u) ? T(1) : T(0);
     T w00 = (T(1) - a) * (T(1) - b), w10 = a * (T(1) - b), w01 = (T(1) - a) * b, w11 = a * b;
     da = (T(1) - b) * (c10 - c00) + b * (c11 - c01);
     db = (T(1) - a) * (c01 - c00) + a * (c11 - c10);
@@ -166,9 +184,61 @@ template <class T> LH_HD BurleyOut<T> burley(T NoV, T NoL, T LoH, T a) {
     return r;
 }
 
+// The forward's discrete decisions for `p` (face flip, far-plane test,
+// the 36 compare results), in the arithmetic of the inputs given.
+template <class T, class Sampler>
+LH_HD void decide(PixelFixed& fx, const PixelParams<T>& p, const Sampler& smp) {
+    v3<T> C[3];
+    T iw[3];
+    v2<T> n[3];
+    for (int k = 0; k < 3; k++) {
+        C[k] = xform3(fx.pv, p.W[k], T(1));
+        iw[k] = T(1) / xform_w(fx.pv, p.W[k], T(1));
+        n[k] = {C[k].x * iw[k], C[k].y * iw[k]};
+    }
+    v2<T> ca{n[2].x - n[1].x, n[2].y - n[1].y}, cb{n[0].x - n[1].x, n[0].y - n[1].y};
+    T invDet = T(1) / (ca.x * cb.y - cb.x * ca.y);
+    T dxr[3] = {n[1].y - n[2].y, n[2].y - n[0].y, n[0].y - n[1].y};
+    T dyr[3] = {n[2].x - n[1].x, n[0].x - n[2].x, n[1].x - n[0].x};
+    T ddx0[3], ddy0[3];
+    for (int k = 0; k < 3; k++) {
+        ddx0[k] = dxr[k] * invDet * iw[k];
+        ddy0[k] = dyr[k] * invDet * iw[k];
+    }
+    T sx = (ddx0[0] * T(1) + ddx0[1] * T(1)) + ddx0[2] * T(1);
+    T sy = (ddy0[0] * T(1) + ddy0[1] * T(1)) + ddy0[2] * T(1);
+    v2<T> dv{T(fx.ndc[0]) - n[0].x, T(fx.ndc[1]) - n[0].y};
+    T wi = T(1) / ((iw[0] + dv.x * sx) + dv.y * sy);
+    T lam[3] = {wi * ((iw[0] + dv.x * ddx0[0]) + dv.y * ddy0[0]), wi * ((T(0) + dv.x * ddx0[1]) + dv.y * ddy0[1]),
+                wi * ((T(0) + dv.x * ddx0[2]) + dv.y * ddy0[2])};
+    v3<T> world = {(p.W[0].x * lam[0] + p.W[1].x * lam[1]) + p.W[2].x * lam[2],
+                   (p.W[0].y * lam[0] + p.W[1].y * lam[1]) + p.W[2].y * lam[2],
+                   (p.W[0].z * lam[0] + p.W[1].z * lam[1]) + p.W[2].z * lam[2]};
+    v3<T> V = normalize(sub(v3<T>{T(fx.cam[0]), T(fx.cam[1]), T(fx.cam[2])}, world));
+    v3<T> gn = cross(sub(p.W[1], p.W[0]), sub(p.W[2], p.W[0]));
+    fx.flip = dot(gn, V) < T(0) ? -1.0f : 1.0f;
+    v3<T> sc = xform3(fx.uvs, world, T(1));
+    T scw = xform_w(fx.uvs, world, T(1));
+    sc = {sc.x / scw, sc.y / scw, sc.z / scw};
+    fx.shadow_const = sc.z > T(1) ? 1u : 0u;
+    const uint32_t layer = fx.cascade > 3 ? 3u : fx.cascade;
+    uint64_t bits = 0;
+    for (int ox = -1; ox <= 1; ox++)
+        for (int oy = -1; oy <= 1; oy++) {
+            const uint32_t tap = (uint32_t)((ox + 1) * 3 + (oy + 1));
+            bits |= (uint64_t)pcf_bits(smp, layer, sc.x + T(ox) / T(1024), sc.y + T(oy) / T(1024), sc.z - T(fx.bias),
+                                       T(fx.shadow_size))
+                    << (4 * tap);
+        }
+    fx.cmp = bits;
+}
+
 // Forward (into *out) and, when `g` is non-null, the reverse pass for the
-// upstream gradient `gout` of the pixel's RGB.  `smp` provides
-// sample(tex, uv) -> Bilinear and shadow_cmp(layer, i, j, ref).
+// upstream gradient `gout` of the pixel's RGB, with the discrete decisions
+// in `fx` (decide()) held fixed.  The geometry may be given relative to any
+// origin (fx.pv, fx.uvs and fx.cam expressed for the same origin): the
+// backward kernel uses the camera, which keeps float32 from cancelling
+// world-scale coordinates.  `smp` provides sample(tex, uv) -> Bilinear.
 template <class T, class Sampler>
 LH_HD void shade(const PixelFixed& fx, const PixelParams<T>& p, const Sampler& smp, v3<T>* out, v3<T> gout,
                  PixelGrad<T>* g) {
@@ -223,8 +293,7 @@ LH_HD void shade(const PixelFixed& fx, const PixelParams<T>& p, const Sampler& s
                 (T(fx.nt[0][1]) * ni.x + T(fx.nt[1][1]) * ni.y) + T(fx.nt[2][1]) * ni.z,
                 (T(fx.nt[0][2]) * ni.x + T(fx.nt[1][2]) * ni.y) + T(fx.nt[2][2]) * ni.z};
     v3<T> n0 = normalize(nt);
-    v3<T> gn = cross(sub(p.W[1], p.W[0]), sub(p.W[2], p.W[0]));
-    const T flip = dot(gn, V) < T(0) ? T(-1) : T(1);
+    const T flip = T(fx.flip);
     v3<T> normal = mul(n0, flip);
     // shadow: cascade fixed by the forward; PCF weights differentiable
     v3<T> sc = xform3(fx.uvs, world, T(1));
@@ -232,12 +301,13 @@ LH_HD void shade(const PixelFixed& fx, const PixelParams<T>& p, const Sampler& s
     sc = {sc.x / scw, sc.y / scw, sc.z / scw};
     T shadow = T(0), dsh_dx = T(0), dsh_dy = T(0);
     const T S = T(fx.shadow_size);
-    const uint32_t layer = fx.cascade > 3 ? 3u : fx.cascade;
-    const bool shadow_const = sc.z > T(1);
+    const bool shadow_const = fx.shadow_const != 0;
     for (int ox = -1; ox <= 1; ox++)
         for (int oy = -1; oy <= 1; oy++) {
             T da, db;
-            shadow += pcf_tap(smp, layer, sc.x + T(ox) / T(1024), sc.y + T(oy) / T(1024), sc.z - T(fx.bias), S, da, db);
+            const uint32_t tap = (uint32_t)((ox + 1) * 3 + (oy + 1));
+            shadow += pcf_tap((uint32_t)(fx.cmp >> (4 * tap)) & 15u, sc.x + T(ox) / T(1024), sc.y + T(oy) / T(1024), S,
+                              da, db);
             dsh_dx += da * S;
             dsh_dy += db * S;
         }
@@ -442,10 +512,12 @@ LH_HD void shade(const PixelFixed& fx, const PixelParams<T>& p, const Sampler& s
         g->UV[k] = {g_uv.x * lam[k] * T(fx.ts[0]), g_uv.y * lam[k] * T(fx.ts[1])};
         g_lam[k] += g_uv.x * uvs[k].x + g_uv.y * uvs[k].y;
     }
-    // world = sum lam_k W_k
+    // world = sum lam_k W_k.  The lambdas sum to 1 for every input, so
+    // their gradients may be shifted by a common term: W_k - W_0 instead of
+    // W_k keeps float32 from cancelling world-scale coordinates.
     for (int k = 0; k < 3; k++) {
         g->W[k] = mul(g_world, lam[k]);
-        g_lam[k] += dot(p.W[k], g_world);
+        g_lam[k] += dot(sub(p.W[k], p.W[0]), g_world);
     }
     // ---- barycentrics: lam_k = wi * av_k
     T g_wi = (g_lam[0] * av[0] + g_lam[1] * av[1]) + g_lam[2] * av[2];
