@@ -850,7 +850,15 @@ static void build_config(lh_scene* s, uint32_t cfg, const lh_scene_params& p) {
     V3 cc = clusters[0].c;
     double cam_yaw = rng.uniform(0, 6.283185307179586);
     V3 cam{cc.x - std::cos(cam_yaw) * clusters[0].sigma * 0.5, 6.0, cc.z - std::sin(cam_yaw) * clusters[0].sigma * 0.5};
-    camera_uniforms(s, cam, cam_yaw, -0.05, 60.0, s->width, s->height, &s->uniforms);
+    double cam_pitch = -0.05;
+    if (cfg == 5) {
+        // The stress view looks down into the densest cluster from 60 m: the
+        // visible meshlets must fit the 24-bit draw slot of the visibility ID
+        // (util.glsl:18-20), and the view stays deep (depth complexity ~10).
+        cam.y = 60.0;
+        cam_pitch = -0.8;
+    }
+    camera_uniforms(s, cam, cam_yaw, cam_pitch, 60.0, s->width, s->height, &s->uniforms);
 
     uint32_t n_probes = p.n_probes ? p.n_probes : (cfg == 3 ? 32 : 0);
     for (uint32_t i = 0; i < n_probes; i++) {
