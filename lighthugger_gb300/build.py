@@ -4,7 +4,9 @@ CUDA sources are compiled for sm_103a only, with --fmad=false (every float
 operation rounds on its own, which is what makes culling, visibility and
 depth bit exact) and IEEE division / square root.  Host C++ (scene
 generator) is compiled with g++ without FMA contraction either.  Objects are
-built in parallel; no cmake.
+built in parallel; no cmake.  LH_NVCC_EXTRA adds nvcc flags, e.g.
+"-DLH_BWD_MIN_BLOCKS=1" for another launch shape of the resolve adjoint
+(objects are not rebuilt when only the flags change: pass force=True).
 """
 import concurrent.futures as cf
 import os
@@ -25,7 +27,7 @@ CPP_SOURCES = ["scene.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"),
-              "-I", CSRC]
+              "-I", CSRC] + os.environ.get("LH_NVCC_EXTRA", "").split()
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-I", os.path.join(ROOT, "include"),
              "-I", os.path.join(CUDA_HOME, "include")]
 

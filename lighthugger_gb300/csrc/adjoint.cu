@@ -5,6 +5,8 @@
 // gradients into the caller's buffers.  Targets every lane of a warp shares
 // (light direction / colour, a material's base-colour factor) are summed
 // across the warp first, so they take one atomic per warp.
+#include <algorithm>
+
 #include "frame_phases.cuh"
 #include "shade.cuh"
 
@@ -38,15 +40,15 @@ struct DeviceSampler {
         float fu = floorf(u), fv = floorf(v);
         s.a = u - fu;
         s.b = v - fv;
-        long long i0 = (long long)fu, j0 = (long long)fv;
-        long long W = t.width, H = t.height;
-        s.i0 = ((i0 % W) + W) % W;
-        s.i1 = (((i0 + 1) % W) + W) % W;
-        s.j0 = ((j0 % H) + H) % H;
-        s.j1 = (((j0 + 1) % H) + H) % H;
+        const int32_t i0 = (int32_t)fu, j0 = (int32_t)fv;
+        const int32_t W = (int32_t)t.width, H = (int32_t)t.height;
+        s.i0 = wrap_texel(i0, W);
+        s.i1 = wrap_texel(i0 + 1, W);
+        s.j0 = wrap_texel(j0, H);
+        s.j1 = wrap_texel(j0 + 1, H);
         s.size_u = (float)t.width;
         s.size_v = (float)t.height;
-        auto texel = [&](long long i, long long j, float* o) {
+        auto texel = [&](int32_t i, int32_t j, float* o) {
             uchar4 p = __ldg(tex + ((size_t)j * W + i));
             if (t.srgb) { o[0] = f->srgb_lut[p.x]; o[1] = f->srgb_lut[p.y]; o[2] = f->srgb_lut[p.z]; }
             else { o[0] = (float)p.x / 255.0f; o[1] = (float)p.y / 255.0f; o[2] = (float)p.z / 255.0f; }
@@ -58,234 +60,434 @@ struct DeviceSampler {
         texel(s.i1, s.j1, s.t11);
         return s;
     }
-    __device__ float shadow_cmp(uint32_t layer, int64_t i, int64_t j, float ref) const {
-        const int64_t S = f->shadow_size;
+    __device__ float shadow_cmp(uint32_t layer, int32_t i, int32_t j, float ref) const {
+        const int32_t S = (int32_t)f->shadow_size;
         i = i < 0 ? 0 : (i > S - 1 ? S - 1 : i);
         j = j < 0 ? 0 : (j > S - 1 ? S - 1 : j);
         return ref < __ldg(f->shadow_maps + ((size_t)layer * S + j) * S + i) ? 1.0f : 0.0f;
     }
 };
 
+constexpr uint32_t kFull = 0xFFFFFFFFu;
+// Launch shape: tiles of 32 x kBwdRows pixels, one warp per row, and the
+// blocks per SM the register budget is cut for (2: 128 registers a thread).
+#ifndef LH_BWD_ROWS
+#define LH_BWD_ROWS 8
+#endif
+#ifndef LH_BWD_MIN_BLOCKS
+#define LH_BWD_MIN_BLOCKS 2
+#endif
+constexpr int kBwdRows = LH_BWD_ROWS;
+constexpr int kBwdThreads = 32 * kBwdRows;
+constexpr uint32_t kCacheSlots = 256;     // shared-memory accumulators of hot gradient addresses
+constexpr uint32_t kSmallTexture = 64;    // textures of at most this many texels go through them
+
 __device__ __forceinline__ float warp_sum(float v) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
     return v;
 }
 
-// Add a 3-vector to `dst` (may be null per lane): one atomic per warp when
-// every lane targets the same address, else one per lane.
-__device__ __forceinline__ void add3(float* dst, float x, float y, float z) {
-    const unsigned long long key = (unsigned long long)dst;
-    const unsigned long long k0 = __shfl_sync(0xFFFFFFFFu, key, 0);
-    if (__all_sync(0xFFFFFFFFu, key == k0)) {
-        x = warp_sum(x);
-        y = warp_sum(y);
-        z = warp_sum(z);
-        if ((threadIdx.x & 31) == 0 && dst) {
-            atomicAdd(dst, x);
-            atomicAdd(dst + 1, y);
-            atomicAdd(dst + 2, z);
+// Per-block accumulators for addresses that many pixels of a block add to
+// (a material's base-colour factor, the texels of 1 x 1 constant textures):
+// open addressing over 256 slots keyed by the destination address, four
+// probes, then a plain global atomic.  Slots are flushed once at block end.
+struct HotCache {
+    unsigned long long key[kCacheSlots];
+    float sum[kCacheSlots];
+};
+
+__device__ __forceinline__ void cache_add(HotCache& c, float* addr, float v) {
+    const unsigned long long k = (unsigned long long)addr;
+    const uint32_t h = ((uint32_t)(k >> 2) * 2654435761u) >> 24;
+    for (uint32_t probe = 0; probe < 4; probe++) {
+        const uint32_t s = (h + probe) & (kCacheSlots - 1u);
+        unsigned long long cur = *reinterpret_cast<volatile unsigned long long*>(&c.key[s]);
+        if (cur == 0ull) cur = atomicCAS(&c.key[s], 0ull, k);
+        if (cur == 0ull || cur == k) {
+            atomicAdd(&c.sum[s], v);
+            return;
         }
-    } else if (dst) {
-        atomicAdd(dst, x);
-        atomicAdd(dst + 1, y);
-        atomicAdd(dst + 2, z);
     }
+    atomicAdd(addr, v);
 }
 
-__global__ void __launch_bounds__(256, 2) k_resolve_backward(FrameDev f, const float4* grad, lh_grad_targets t) {
+// Runs of equal keys along the warp (a warp is one row of 32 pixels, so a
+// triangle or a texel covers contiguous lanes): `end` is one past the last
+// lane of this lane's run, `head` marks its first lane.
+struct Run {
+    uint32_t end;
+    bool head;
+};
+
+__device__ __forceinline__ Run run_of(unsigned long long key) {
+    const uint32_t lane = threadIdx.x;
+    const unsigned long long prev = __shfl_up_sync(kFull, key, 1);
+    const bool head = lane == 0 || prev != key;
+    const uint32_t heads = __ballot_sync(kFull, head);
+    const uint32_t later = heads & ~((2u << lane) - 1u);
+    return {later ? (uint32_t)__ffs(later) - 1u : 32u, head};
+}
+
+// Sum of v over the lanes [lane, end) of the run: the full run sum at its head.
+__device__ __forceinline__ float run_sum(float v, const Run& r) {
+    const uint32_t lane = threadIdx.x;
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        const float w = __shfl_down_sync(kFull, v, o);
+        if (lane + o < r.end) v += w;
+    }
+    return v;
+}
+
+// What the scatter needs of a differentiated pixel besides its gradients.
+struct PixelOut {
+    bool ok;                // differentiated (covered, no normal map)
+    uint32_t packed;        // visibility ID: triangle within the view
+    const Instance* inst;
+    const lh_mesh_grads* rec;  // may be null
+    uint32_t idx[3];
+};
+
+// Recompute the forward of pixel (x, y) from the visibility buffer and run
+// the reverse pass of shade.cuh for the upstream gradient at that pixel.
+// `rel` holds column 3 of the camera-relative PV and of the 4 cascades'
+// UVS matrices (see rel_columns).
+__device__ __forceinline__ void pixel_backward(const FrameDev& f, const float4* grad, const lh_grad_targets& t,
+                                               const float* rel, uint32_t x, uint32_t y, PixelGrad<float>& g,
+                                               PixelOut& o) {
     const Uniforms& u = *f.uniforms;
     const uint32_t W = u.window_size.x, H = u.window_size.y;
-    const uint32_t x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+    o.ok = false;
     bool active = x < W && y < H;
     unsigned long long vis = 0;
     if (active) vis = __ldcs(reinterpret_cast<const unsigned long long*>(f.visibility) + (size_t)y * W + x);
     active = active && u2f((uint32_t)(vis >> 32)) != 0.0f;
-    float* bcf_dst = nullptr;
-    v3<float> g_sun{0.0f, 0.0f, 0.0f}, g_light{0.0f, 0.0f, 0.0f}, g_bcf{0.0f, 0.0f, 0.0f};
-    if (active) {
-        const float4 gp = grad[(size_t)y * W + x];
-        const uint32_t packed = (uint32_t)vis;
-        const uint32_t slot = packed & ((1u << 24) - 1u), tri = packed >> 24;
-        const MeshletReference ref = f.views[0].refs[slot];
-        const Instance* inst = f.instances + ref.instance_index;
-        const MeshInfoResolve mi = load_mesh_info_resolve(mesh_info_of(inst));
-        const Meshlet* ml = reinterpret_cast<const Meshlet*>(mi.meshlets) + ref.meshlet_index;
-        const uint32_t tri_off = __ldg(&ml->triangle_offset), idx_off = __ldg(&ml->index_offset);
-        const uint8_t* micro = reinterpret_cast<const uint8_t*>(mi.micro_indices) + tri_off + tri * 3;
-        const uint32_t flags = mi.flags;
-        uint32_t idx[3];
-        for (int k = 0; k < 3; k++) {
-            uint32_t vi = idx_off + __ldg(micro + k);
-            idx[k] = (flags & MESH_INFO_FLAGS_32_BIT_INDICES) ? __ldg(reinterpret_cast<const uint32_t*>(mi.indices) + vi)
-                                                              : __ldg(reinterpret_cast<const uint16_t*>(mi.indices) + vi);
+    if (!active) return;
+    const float4 gp = __ldcs(grad + (size_t)y * W + x);
+    const uint32_t packed = (uint32_t)vis;
+    const uint32_t slot = packed & ((1u << 24) - 1u), tri = packed >> 24;
+    const MeshletReference ref = f.views[0].refs[slot];
+    const Instance* inst = f.instances + ref.instance_index;
+    const MeshInfoResolve mi = load_mesh_info_resolve(mesh_info_of(inst));
+    const Meshlet* ml = reinterpret_cast<const Meshlet*>(mi.meshlets) + ref.meshlet_index;
+    const uint32_t tri_off = __ldg(&ml->triangle_offset), idx_off = __ldg(&ml->index_offset);
+    const uint8_t* micro = reinterpret_cast<const uint8_t*>(mi.micro_indices) + tri_off + tri * 3;
+    const uint32_t flags = mi.flags;
+    for (int k = 0; k < 3; k++) {
+        uint32_t vi = idx_off + __ldg(micro + k);
+        o.idx[k] = (flags & MESH_INFO_FLAGS_32_BIT_INDICES) ? __ldg(reinterpret_cast<const uint32_t*>(mi.indices) + vi)
+                                                            : __ldg(reinterpret_cast<const uint16_t*>(mi.indices) + vi);
+    }
+    const lh_mat4& T = inst->transform;
+    PixelParams<float> p;
+    for (int k = 0; k < 3; k++) {
+        f3 w = world_pos(T, load_position(mi.positions, flags, o.idx[k]));
+        p.W[k] = {w.x, w.y, w.z};
+        f3 nr = load_normal_raw(mi.normals, flags, o.idx[k]);
+        p.N[k] = {nr.x, nr.y, nr.z};
+        f2 uvr = load_uv_raw(mi.uvs, flags, o.idx[k]);
+        p.UV[k] = {uvr.x, uvr.y};
+    }
+    p.bcf = {mi.base_color_factor.x, mi.base_color_factor.y, mi.base_color_factor.z};
+    p.sun = {u.sun_dir.x, u.sun_dir.y, u.sun_dir.z};
+    p.light = {u.sun_intensity.x, u.sun_intensity.y, u.sun_intensity.z};
+    PixelFixed fx;
+    for (int c = 0; c < 4; c++) {
+        fx.pv[c][0] = u.combined_perspective_view.cols[c].x;
+        fx.pv[c][1] = u.combined_perspective_view.cols[c].y;
+        fx.pv[c][2] = u.combined_perspective_view.cols[c].z;
+        fx.pv[c][3] = u.combined_perspective_view.cols[c].w;
+    }
+    for (int c = 0; c < 3; c++) {
+        fx.nt[c][0] = inst->normal_transform.cols[c].x;
+        fx.nt[c][1] = inst->normal_transform.cols[c].y;
+        fx.nt[c][2] = inst->normal_transform.cols[c].z;
+    }
+    // the world position the forward interpolated decides the cascade
+    const f2 ndc{(float)x / (float)W * 2.0f - 1.0f, (float)y / (float)H * 2.0f - 1.0f};
+    fx.ndc[0] = ndc.x;
+    fx.ndc[1] = ndc.y;
+    fx.win[0] = (float)W;
+    fx.win[1] = (float)H;
+    fx.cam[0] = u.camera_pos.x;
+    fx.cam[1] = u.camera_pos.y;
+    fx.cam[2] = u.camera_pos.z;
+    fx.ts[0] = mi.texture_scale.x;
+    fx.ts[1] = mi.texture_scale.y;
+    fx.toff[0] = mi.texture_offset.x;
+    fx.toff[1] = mi.texture_offset.y;
+    fx.thin = (flags & MESH_INFO_FLAGS_ALPHA_CLIP) ? 1u : 0u;
+    fx.bias = fx.thin ? 0.000002f : 0.0f;
+    fx.shadow_size = (float)f.shadow_size;
+    fx.base_tex = mi.base_tex;
+    fx.mr_tex = mi.mr_tex;
+    fx.has_normal_map = mi.normal_tex != UNUSED_TEXTURE_INDEX;
+    // the cascade the forward chose: its own barycentrics and world
+    // position, in its absolute float arithmetic (render_geometry.comp:183-196)
+    {
+        f4 c0 = mul(u.combined_perspective_view, f4{p.W[0].x, p.W[0].y, p.W[0].z, 1.0f});
+        f4 c1 = mul(u.combined_perspective_view, f4{p.W[1].x, p.W[1].y, p.W[1].z, 1.0f});
+        f4 c2 = mul(u.combined_perspective_view, f4{p.W[2].x, p.W[2].y, p.W[2].z, 1.0f});
+        f3 invW{1.0f / c0.w, 1.0f / c1.w, 1.0f / c2.w};
+        f2 n0{c0.x * invW.x, c0.y * invW.x}, n1{c1.x * invW.y, c1.y * invW.y}, n2{c2.x * invW.z, c2.y * invW.z};
+        f2 ca{n2.x - n1.x, n2.y - n1.y}, cb{n0.x - n1.x, n0.y - n1.y};
+        float invDet = 1.0f / (ca.x * cb.y - cb.x * ca.y);
+        f3 ddx = f3{n1.y - n2.y, n2.y - n0.y, n0.y - n1.y} * invDet * invW;
+        f3 ddy = f3{n2.x - n1.x, n0.x - n2.x, n1.x - n0.x} * invDet * invW;
+        float ddxSum = dot(ddx, f3{1.0f, 1.0f, 1.0f});
+        float ddySum = dot(ddy, f3{1.0f, 1.0f, 1.0f});
+        f2 dv{ndc.x - n0.x, ndc.y - n0.y};
+        float interpInvW = (invW.x + dv.x * ddxSum) + dv.y * ddySum;
+        float interpW = 1.0f / interpInvW;
+        float l0 = interpW * ((invW.x + dv.x * ddx.x) + dv.y * ddy.x);
+        float l1 = interpW * ((0.0f + dv.x * ddx.y) + dv.y * ddy.y);
+        float l2 = interpW * ((0.0f + dv.x * ddx.z) + dv.y * ddy.z);
+        f3 world{(p.W[0].x * l0 + p.W[1].x * l1) + p.W[2].x * l2, (p.W[0].y * l0 + p.W[1].y * l1) + p.W[2].y * l2,
+                 (p.W[0].z * l0 + p.W[1].z * l1) + p.W[2].z * l2};
+        uint32_t ci;
+        for (ci = 0; ci < 4; ci++) {
+            f4 sc = mul(f.misc->uv_space_shadow_matrices[ci], f4{world.x, world.y, world.z, 1.0f});
+            float ox = sc.x - 0.5f, oy = sc.y - 0.5f;
+            if (fabsf(ox) < 0.5f && fabsf(oy) < 0.5f) break;
         }
-        const lh_mat4& T = inst->transform;
-        PixelParams<float> p;
-        for (int k = 0; k < 3; k++) {
-            f3 w = world_pos(T, load_position(mi.positions, flags, idx[k]));
-            p.W[k] = {w.x, w.y, w.z};
-            f3 nr = load_normal_raw(mi.normals, flags, idx[k]);
-            p.N[k] = {nr.x, nr.y, nr.z};
-            f2 uvr = load_uv_raw(mi.uvs, flags, idx[k]);
-            p.UV[k] = {uvr.x, uvr.y};
-        }
-        p.bcf = {mi.base_color_factor.x, mi.base_color_factor.y, mi.base_color_factor.z};
-        p.sun = {u.sun_dir.x, u.sun_dir.y, u.sun_dir.z};
-        p.light = {u.sun_intensity.x, u.sun_intensity.y, u.sun_intensity.z};
-        PixelFixed fx;
+        fx.cascade = ci;
+        const lh_mat4& m = f.misc->uv_space_shadow_matrices[ci > 3 ? 3 : ci];
         for (int c = 0; c < 4; c++) {
-            fx.pv[c][0] = u.combined_perspective_view.cols[c].x;
-            fx.pv[c][1] = u.combined_perspective_view.cols[c].y;
-            fx.pv[c][2] = u.combined_perspective_view.cols[c].z;
-            fx.pv[c][3] = u.combined_perspective_view.cols[c].w;
+            fx.uvs[c][0] = m.cols[c].x;
+            fx.uvs[c][1] = m.cols[c].y;
+            fx.uvs[c][2] = m.cols[c].z;
+            fx.uvs[c][3] = m.cols[c].w;
         }
-        for (int c = 0; c < 3; c++) {
-            fx.nt[c][0] = inst->normal_transform.cols[c].x;
-            fx.nt[c][1] = inst->normal_transform.cols[c].y;
-            fx.nt[c][2] = inst->normal_transform.cols[c].z;
-        }
-        // the world position the forward interpolated decides the cascade
-        const f2 ndc{(float)x / (float)W * 2.0f - 1.0f, (float)y / (float)H * 2.0f - 1.0f};
-        fx.ndc[0] = ndc.x;
-        fx.ndc[1] = ndc.y;
-        fx.win[0] = (float)W;
-        fx.win[1] = (float)H;
-        fx.cam[0] = u.camera_pos.x;
-        fx.cam[1] = u.camera_pos.y;
-        fx.cam[2] = u.camera_pos.z;
-        fx.ts[0] = mi.texture_scale.x;
-        fx.ts[1] = mi.texture_scale.y;
-        fx.toff[0] = mi.texture_offset.x;
-        fx.toff[1] = mi.texture_offset.y;
-        fx.thin = (flags & MESH_INFO_FLAGS_ALPHA_CLIP) ? 1u : 0u;
-        fx.bias = fx.thin ? 0.000002f : 0.0f;
-        fx.shadow_size = (float)f.shadow_size;
-        fx.base_tex = mi.base_tex;
-        fx.mr_tex = mi.mr_tex;
-        fx.has_normal_map = mi.normal_tex != UNUSED_TEXTURE_INDEX;
-        // the cascade the forward chose: its own barycentrics and world
-        // position, in its absolute float arithmetic (render_geometry.comp:183-196)
-        {
-            f4 c0 = mul(u.combined_perspective_view, f4{p.W[0].x, p.W[0].y, p.W[0].z, 1.0f});
-            f4 c1 = mul(u.combined_perspective_view, f4{p.W[1].x, p.W[1].y, p.W[1].z, 1.0f});
-            f4 c2 = mul(u.combined_perspective_view, f4{p.W[2].x, p.W[2].y, p.W[2].z, 1.0f});
-            f3 invW{1.0f / c0.w, 1.0f / c1.w, 1.0f / c2.w};
-            f2 n0{c0.x * invW.x, c0.y * invW.x}, n1{c1.x * invW.y, c1.y * invW.y}, n2{c2.x * invW.z, c2.y * invW.z};
-            f2 ca{n2.x - n1.x, n2.y - n1.y}, cb{n0.x - n1.x, n0.y - n1.y};
-            float invDet = 1.0f / (ca.x * cb.y - cb.x * ca.y);
-            f3 ddx = f3{n1.y - n2.y, n2.y - n0.y, n0.y - n1.y} * invDet * invW;
-            f3 ddy = f3{n2.x - n1.x, n0.x - n2.x, n1.x - n0.x} * invDet * invW;
-            float ddxSum = dot(ddx, f3{1.0f, 1.0f, 1.0f});
-            float ddySum = dot(ddy, f3{1.0f, 1.0f, 1.0f});
-            f2 dv{ndc.x - n0.x, ndc.y - n0.y};
-            float interpInvW = (invW.x + dv.x * ddxSum) + dv.y * ddySum;
-            float interpW = 1.0f / interpInvW;
-            float l0 = interpW * ((invW.x + dv.x * ddx.x) + dv.y * ddy.x);
-            float l1 = interpW * ((0.0f + dv.x * ddx.y) + dv.y * ddy.y);
-            float l2 = interpW * ((0.0f + dv.x * ddx.z) + dv.y * ddy.z);
-            f3 world{(p.W[0].x * l0 + p.W[1].x * l1) + p.W[2].x * l2, (p.W[0].y * l0 + p.W[1].y * l1) + p.W[2].y * l2,
-                     (p.W[0].z * l0 + p.W[1].z * l1) + p.W[2].z * l2};
-            uint32_t ci;
-            for (ci = 0; ci < 4; ci++) {
-                f4 sc = mul(f.misc->uv_space_shadow_matrices[ci], f4{world.x, world.y, world.z, 1.0f});
-                float ox = sc.x - 0.5f, oy = sc.y - 0.5f;
-                if (fabsf(ox) < 0.5f && fabsf(oy) < 0.5f) break;
-            }
-            fx.cascade = ci;
-            const lh_mat4& m = f.misc->uv_space_shadow_matrices[ci > 3 ? 3 : ci];
-            for (int c = 0; c < 4; c++) {
-                fx.uvs[c][0] = m.cols[c].x;
-                fx.uvs[c][1] = m.cols[c].y;
-                fx.uvs[c][2] = m.cols[c].z;
-                fx.uvs[c][3] = m.cols[c].w;
-            }
-        }
-        DeviceSampler smp{&f};
-        // face flip, far-plane test and compare results exactly as the forward
-        shade::decide<float>(fx, p, smp);
-        // the continuous part in camera-relative coordinates: W - cam is
-        // (nearly) exact, and PV T(cam), UVS T(cam) are formed in double
-        const double cx = u.camera_pos.x, cy = u.camera_pos.y, cz = u.camera_pos.z;
-        for (int r = 0; r < 4; r++) {
-            fx.pv[3][r] = (float)((double)fx.pv[3][r] + (((double)fx.pv[0][r] * cx + (double)fx.pv[1][r] * cy) +
-                                                         (double)fx.pv[2][r] * cz));
-            fx.uvs[3][r] = (float)((double)fx.uvs[3][r] + (((double)fx.uvs[0][r] * cx + (double)fx.uvs[1][r] * cy) +
-                                                           (double)fx.uvs[2][r] * cz));
-        }
-        for (int k = 0; k < 3; k++) p.W[k] = {p.W[k].x - u.camera_pos.x, p.W[k].y - u.camera_pos.y, p.W[k].z - u.camera_pos.z};
-        fx.cam[0] = fx.cam[1] = fx.cam[2] = 0.0f;
-        v3<float> out;
-        PixelGrad<float> g;
-        shade::shade<float>(fx, p, smp, &out, v3<float>{gp.x, gp.y, gp.z}, &g);
-        if (g.differentiated) {
-            g_sun = g.sun;
-            g_light = g.light;
-            g_bcf = g.bcf;
-            const uint64_t rec = t.instance_grads ? reinterpret_cast<const uint64_t*>(t.instance_grads)[ref.instance_index]
-                                                  : 0ull;
-            if (rec) {
-                const lh_mesh_grads mg = *reinterpret_cast<const lh_mesh_grads*>(rec);
-                for (int k = 0; k < 3; k++) {
-                    if (mg.positions) {
-                        // W = M3 P + t: dP = M3^T dW
-                        float* d = reinterpret_cast<float*>(mg.positions) + (size_t)idx[k] * 3;
-                        f3 gw{g.W[k].x, g.W[k].y, g.W[k].z};
-                        atomicAdd(d, dot(f3{T.cols[0].x, T.cols[0].y, T.cols[0].z}, gw));
-                        atomicAdd(d + 1, dot(f3{T.cols[1].x, T.cols[1].y, T.cols[1].z}, gw));
-                        atomicAdd(d + 2, dot(f3{T.cols[2].x, T.cols[2].y, T.cols[2].z}, gw));
-                    }
-                    if (mg.normals) {
-                        float* d = reinterpret_cast<float*>(mg.normals) + (size_t)idx[k] * 3;
-                        atomicAdd(d, g.N[k].x);
-                        atomicAdd(d + 1, g.N[k].y);
-                        atomicAdd(d + 2, g.N[k].z);
-                    }
-                    if (mg.uvs) {
-                        float* d = reinterpret_cast<float*>(mg.uvs) + (size_t)idx[k] * 2;
-                        atomicAdd(d, g.UV[k].x);
-                        atomicAdd(d + 1, g.UV[k].y);
-                    }
+    }
+    DeviceSampler smp{&f};
+    // face flip, far-plane test and compare results exactly as the forward
+    shade::decide<float>(fx, p, smp);
+    // the continuous part in camera-relative coordinates: W - cam is
+    // (nearly) exact, and PV T(cam), UVS T(cam) were formed in double
+    const uint32_t layer = fx.cascade > 3 ? 3u : fx.cascade;
+    for (int r = 0; r < 4; r++) {
+        fx.pv[3][r] = rel[r];
+        fx.uvs[3][r] = rel[4 + 4 * layer + r];
+    }
+    for (int k = 0; k < 3; k++) p.W[k] = {p.W[k].x - u.camera_pos.x, p.W[k].y - u.camera_pos.y, p.W[k].z - u.camera_pos.z};
+    fx.cam[0] = fx.cam[1] = fx.cam[2] = 0.0f;
+    v3<float> out;
+    shade::shade<float>(fx, p, smp, &out, v3<float>{gp.x, gp.y, gp.z}, &g);
+    if (!g.differentiated) return;
+    o.ok = true;
+    o.packed = packed;
+    o.inst = inst;
+    o.rec = t.instance_grads ? reinterpret_cast<const lh_mesh_grads*>(
+                                   reinterpret_cast<const uint64_t*>(t.instance_grads)[ref.instance_index])
+                             : nullptr;
+}
+
+// The four texels of one bilinear sample (00, 10, 01, 11): run-summed along
+// the warp and added to the texture's gradient image, channels [c0, c0 + nc).
+// Taps that land on the same texel (1-texel-wide textures, edges) are merged
+// into the first.
+template <int NC>
+__device__ __forceinline__ void scatter_texels(HotCache& cache, float* const base_addr[4], float v[4][NC], int c0,
+                                               bool small) {
+    float* a[4] = {base_addr[0], base_addr[1], base_addr[2], base_addr[3]};
+#pragma unroll
+    for (int q = 1; q < 4; q++)
+#pragma unroll
+        for (int p = 0; p < q; p++)
+            if (a[q] && a[q] == a[p]) {
+#pragma unroll
+                for (int c = 0; c < NC; c++) {
+                    v[p][c] += v[q][c];
+                    v[q][c] = 0.0f;
                 }
-                bcf_dst = reinterpret_cast<float*>(mg.base_color_factor);
+                a[q] = nullptr;
             }
-            if (t.texture_grads) {
-                // the 4 texels of each bilinear sample: 00, 10, 01, 11
-                const uint64_t* tg = reinterpret_cast<const uint64_t*>(t.texture_grads);
-                if (g.base_index < f.n_textures && tg[g.base_index]) {
-                    const uint32_t tw = f.textures[g.base_index].width;
-                    float4* dst = reinterpret_cast<float4*>(tg[g.base_index]);
-                    for (int q = 0; q < 4; q++) {
-                        int64_t i = g.base_ij[q & 1], j = g.base_ij[2 + (q >> 1)];
-                        float* d = reinterpret_cast<float*>(dst + (size_t)j * tw + i);
-                        atomicAdd(d, g.base_texel[q][0]);
-                        atomicAdd(d + 1, g.base_texel[q][1]);
-                        atomicAdd(d + 2, g.base_texel[q][2]);
-                    }
-                }
-                if (g.mr_index < f.n_textures && tg[g.mr_index]) {
-                    const uint32_t tw = f.textures[g.mr_index].width;
-                    float4* dst = reinterpret_cast<float4*>(tg[g.mr_index]);
-                    for (int q = 0; q < 4; q++) {
-                        int64_t i = g.mr_ij[q & 1], j = g.mr_ij[2 + (q >> 1)];
-                        float* d = reinterpret_cast<float*>(dst + (size_t)j * tw + i);
-                        atomicAdd(d + 1, g.mr_texel[q][0]);  // roughness (g)
-                        atomicAdd(d + 2, g.mr_texel[q][1]);  // metallic (b)
-                    }
-                }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        if (!__any_sync(kFull, a[q] != nullptr)) continue;
+        const Run r = run_of((unsigned long long)a[q]);
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            const float s = run_sum(v[q][c], r);
+            if (r.head && a[q]) {
+                if (small) cache_add(cache, a[q] + c0 + c, s);
+                else atomicAdd(a[q] + c0 + c, s);
             }
         }
     }
-    add3(reinterpret_cast<float*>(t.light_dir), g_sun.x, g_sun.y, g_sun.z);
-    add3(reinterpret_cast<float*>(t.light_color), g_light.x, g_light.y, g_light.z);
-    add3(bcf_dst, g_bcf.x, g_bcf.y, g_bcf.z);
 }
+
+// Column 3 of PV T(cam) and of UVS_c T(cam) for the 4 cascades, in double
+// and rounded once: rel[r] for PV, rel[4 + 4c + r] for cascade c.  Threads
+// 0..19 of the block each form one entry.
+__device__ __forceinline__ void rel_columns(const FrameDev& f, uint32_t tid, float* rel) {
+    if (tid >= 20) return;
+    const Uniforms& u = *f.uniforms;
+    const lh_mat4& m = tid < 4 ? u.combined_perspective_view : f.misc->uv_space_shadow_matrices[(tid - 4) / 4];
+    const uint32_t r = tid & 3u;
+    const float* c0 = &m.cols[0].x;
+    const float* c1 = &m.cols[1].x;
+    const float* c2 = &m.cols[2].x;
+    const float* c3 = &m.cols[3].x;
+    const double cx = u.camera_pos.x, cy = u.camera_pos.y, cz = u.camera_pos.z;
+    rel[tid] = (float)((double)c3[r] + (((double)c0[r] * cx + (double)c1[r] * cy) + (double)c2[r] * cz));
+}
+
+// One thread per pixel over 32 x kBwdRows tiles; a grid of resident blocks strides
+// over the tiles.  Gradients of the three vertices of a triangle are summed
+// over the triangle's run of pixels in the warp's row before the atomics;
+// the light gradients stay in registers until block end; base-colour
+// factors and small textures accumulate in the block's HotCache.
+__global__ void __launch_bounds__(kBwdThreads, LH_BWD_MIN_BLOCKS)
+    k_resolve_backward(FrameDev f, const float4* grad, lh_grad_targets t, uint32_t tiles_x, uint32_t n_tiles) {
+    __shared__ HotCache cache;
+    __shared__ float s_light[kBwdThreads / 32][6];
+    __shared__ float s_rel[20];
+    const uint32_t tid = threadIdx.y * 32 + threadIdx.x;
+    for (uint32_t s = tid; s < kCacheSlots; s += kBwdThreads) {
+        cache.key[s] = 0ull;
+        cache.sum[s] = 0.0f;
+    }
+    rel_columns(f, tid, s_rel);
+    __syncthreads();
+    float acc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    const uint64_t* tex_targets = reinterpret_cast<const uint64_t*>(t.texture_grads);
+    for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+        const uint32_t x = (tile % tiles_x) * 32 + threadIdx.x, y = (tile / tiles_x) * kBwdRows + threadIdx.y;
+        PixelGrad<float> g;
+        PixelOut o;
+        pixel_backward(f, grad, t, s_rel, x, y, g, o);
+        if (o.ok) {
+            acc[0] += g.sun.x;
+            acc[1] += g.sun.y;
+            acc[2] += g.sun.z;
+            acc[3] += g.light.x;
+            acc[4] += g.light.y;
+            acc[5] += g.light.z;
+        }
+        const lh_mesh_grads* mg = o.ok ? o.rec : nullptr;
+        // vertex attributes: one run per triangle
+        if (__any_sync(kFull, mg != nullptr)) {
+            const Run r = run_of(mg ? (unsigned long long)o.packed : ~0ull);
+            float v[24];
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                v[k * 8 + 0] = g.W[k].x;
+                v[k * 8 + 1] = g.W[k].y;
+                v[k * 8 + 2] = g.W[k].z;
+                v[k * 8 + 3] = g.N[k].x;
+                v[k * 8 + 4] = g.N[k].y;
+                v[k * 8 + 5] = g.N[k].z;
+                v[k * 8 + 6] = g.UV[k].x;
+                v[k * 8 + 7] = g.UV[k].y;
+            }
+#pragma unroll
+            for (int i = 0; i < 24; i++) v[i] = run_sum(v[i], r);
+            if (r.head && mg) {
+                const lh_mesh_grads d = *mg;
+                const lh_mat4& T = o.inst->transform;
+                const f3 c0{T.cols[0].x, T.cols[0].y, T.cols[0].z}, c1{T.cols[1].x, T.cols[1].y, T.cols[1].z},
+                    c2{T.cols[2].x, T.cols[2].y, T.cols[2].z};
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    const float* vk = v + k * 8;
+                    if (d.positions) {
+                        // W = M3 P + t: dP = M3^T dW
+                        float* p = reinterpret_cast<float*>(d.positions) + (size_t)o.idx[k] * 3;
+                        const f3 gw{vk[0], vk[1], vk[2]};
+                        atomicAdd(p, dot(c0, gw));
+                        atomicAdd(p + 1, dot(c1, gw));
+                        atomicAdd(p + 2, dot(c2, gw));
+                    }
+                    if (d.normals) {
+                        float* p = reinterpret_cast<float*>(d.normals) + (size_t)o.idx[k] * 3;
+                        atomicAdd(p, vk[3]);
+                        atomicAdd(p + 1, vk[4]);
+                        atomicAdd(p + 2, vk[5]);
+                    }
+                    if (d.uvs) {
+                        float* p = reinterpret_cast<float*>(d.uvs) + (size_t)o.idx[k] * 2;
+                        atomicAdd(p, vk[6]);
+                        atomicAdd(p + 1, vk[7]);
+                    }
+                }
+            }
+        }
+        // base-colour factor of the pixel's MeshInfo record
+        float* bcf_dst = mg ? reinterpret_cast<float*>(mg->base_color_factor) : nullptr;
+        if (__any_sync(kFull, bcf_dst != nullptr)) {
+            const Run r = run_of((unsigned long long)bcf_dst);
+            const float bx = run_sum(bcf_dst ? g.bcf.x : 0.0f, r);
+            const float by = run_sum(bcf_dst ? g.bcf.y : 0.0f, r);
+            const float bz = run_sum(bcf_dst ? g.bcf.z : 0.0f, r);
+            if (r.head && bcf_dst) {
+                cache_add(cache, bcf_dst, bx);
+                cache_add(cache, bcf_dst + 1, by);
+                cache_add(cache, bcf_dst + 2, bz);
+            }
+        }
+        if (tex_targets) {
+            // base colour (rgb of the texel) and metallic-roughness (g, b)
+            float* ba[4] = {nullptr, nullptr, nullptr, nullptr};
+            float* ma[4] = {nullptr, nullptr, nullptr, nullptr};
+            bool base_small = false, mr_small = false;
+            if (o.ok && g.base_index < f.n_textures && tex_targets[g.base_index]) {
+                const lh_texture& tx = f.textures[g.base_index];
+                float4* dst = reinterpret_cast<float4*>(tex_targets[g.base_index]);
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    ba[q] = reinterpret_cast<float*>(dst + (size_t)g.base_ij[2 + (q >> 1)] * tx.width + g.base_ij[q & 1]);
+                base_small = tx.width * tx.height <= kSmallTexture;
+            }
+            if (o.ok && g.mr_index < f.n_textures && tex_targets[g.mr_index]) {
+                const lh_texture& tx = f.textures[g.mr_index];
+                float4* dst = reinterpret_cast<float4*>(tex_targets[g.mr_index]);
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    ma[q] = reinterpret_cast<float*>(dst + (size_t)g.mr_ij[2 + (q >> 1)] * tx.width + g.mr_ij[q & 1]);
+                mr_small = tx.width * tx.height <= kSmallTexture;
+            }
+            scatter_texels<3>(cache, ba, g.base_texel, 0, base_small);
+            scatter_texels<2>(cache, ma, g.mr_texel, 1, mr_small);  // roughness (g), metallic (b)
+        }
+    }
+    // light direction / colour: one atomic per value per block
+#pragma unroll
+    for (int i = 0; i < 6; i++) {
+        const float s = warp_sum(acc[i]);
+        if (threadIdx.x == 0) s_light[threadIdx.y][i] = s;
+    }
+    __syncthreads();
+    if (tid < 6) {
+        float s = 0.0f;
+        for (int w = 0; w < kBwdThreads / 32; w++) s += s_light[w][tid];
+        float* dst = tid < 3 ? reinterpret_cast<float*>(t.light_dir) : reinterpret_cast<float*>(t.light_color);
+        if (dst) atomicAdd(dst + (tid % 3), s);
+    }
+    for (uint32_t s = tid; s < kCacheSlots; s += kBwdThreads)
+        if (cache.key[s]) atomicAdd(reinterpret_cast<float*>(cache.key[s]), cache.sum[s]);
+}
+
+int g_backward_blocks_per_sm = -1;
 
 }  // namespace
 
 cudaError_t launch_resolve_backward(const FrameDev& f, uint32_t width, uint32_t height, const float4* grad,
                                     const lh_grad_targets& t, cudaStream_t s) {
-    dim3 grid((width + 31) / 32, (height + 7) / 8);
-    k_resolve_backward<<<grid, dim3(32, 8), 0, s>>>(f, grad, t);
+    if (g_backward_blocks_per_sm < 0) {
+        int n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_resolve_backward, kBwdThreads, 0) != cudaSuccess) n = 1;
+        g_backward_blocks_per_sm = n > 0 ? n : 1;
+    }
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    const uint32_t tiles_x = (width + 31) / 32, tiles_y = (height + kBwdRows - 1) / kBwdRows;
+    const uint32_t n_tiles = tiles_x * tiles_y;
+    if (n_tiles == 0) return cudaSuccess;
+    const uint32_t grid = std::min<uint32_t>(n_tiles, (uint32_t)(sms * g_backward_blocks_per_sm));
+    k_resolve_backward<<<grid, dim3(32, kBwdRows), 0, s>>>(f, grad, t, tiles_x, n_tiles);
     return cudaGetLastError();
 }
 

@@ -11,6 +11,7 @@
 
 #include <cstdint>
 
+#include "int_float.cuh"
 #include "lh/lh.h"
 
 namespace lh {
@@ -53,6 +54,14 @@ __device__ __forceinline__ float gmax(float a, float b) { return (a < b) ? b : a
 __device__ __forceinline__ float gmin(float a, float b) { return (b < a) ? b : a; }
 __device__ __forceinline__ uint32_t f2u(float f) { return __float_as_uint(f); }
 __device__ __forceinline__ float u2f(uint32_t u) { return __uint_as_float(u); }
+
+// Repeat addressing of texel coordinate i into [0, n): the floor of a
+// sample coordinate below 1e9 in magnitude, so 32 bits hold it.
+__device__ __forceinline__ int32_t wrap_texel(int32_t i, int32_t n) {
+    if ((n & (n - 1)) == 0) return i & (n - 1);
+    const int32_t r = i % n;
+    return r < 0 ? r + n : r;
+}
 
 // ------------------------------------------------------------------ scene access
 __device__ __forceinline__ const MeshInfo* mesh_info_of(const Instance* inst) {
@@ -237,7 +246,8 @@ struct TriSetup {
     float z0, s1, s2;
     uint32_t id;
     int32_t px0, py0, px1, py1;
-    uint32_t bias;  // bit0 edge12, bit1 edge20, bit2 edge01 not top-left
+    uint32_t bias;  // bit0 edge12, bit1 edge20, bit2 edge01 not top-left;
+                    // bit3: every edge product in the bbox fits 32 bits
 };
 
 __device__ __forceinline__ bool top_left(int32_t ax, int32_t ay, int32_t bx, int32_t by) {
@@ -259,25 +269,44 @@ __device__ __forceinline__ bool make_setup(SnapV v0, SnapV v1, SnapV v2, uint32_
     t.py1 = min((maxY - 128) >> 8, (int32_t)H - 1);
     if (t.px0 > t.px1 || t.py0 > t.py1) return false;
     t.X0 = v0.X; t.Y0 = v0.Y; t.X1 = v1.X; t.Y1 = v1.Y; t.X2 = v2.X; t.Y2 = v2.Y;
-    float fA = __ll2float_rn(A);
+    float fA = i64_to_f32_rn(A);
     t.z0 = v0.z;
     t.s1 = (v1.z - v0.z) / fA;
     t.s2 = (v2.z - v0.z) / fA;
     t.id = id;
     t.bias = (top_left(v1.X, v1.Y, v2.X, v2.Y) ? 0u : 1u) | (top_left(v2.X, v2.Y, v0.X, v0.Y) ? 0u : 2u) |
              (top_left(v0.X, v0.Y, v1.X, v1.Y) ? 0u : 4u);
+    // pixel centres of the bbox lie inside the vertex extents, so each
+    // product of an edge function is at most ext_x * ext_y in magnitude
+    if ((int64_t)(maxX - minX) * (int64_t)(maxY - minY) < (1ll << 30)) t.bias |= 8u;
     return true;
 }
 
 // Coverage + depth of pixel (px, py); returns false when not covered.
 __device__ __forceinline__ bool cover(const TriSetup& t, int32_t px, int32_t py, float& depth) {
-    int64_t Px = (int64_t)px * 256 + 128, Py = (int64_t)py * 256 + 128;
-    int64_t e12 = (int64_t)(t.Y2 - t.Y1) * (Px - t.X1) - (int64_t)(t.X2 - t.X1) * (Py - t.Y1);
-    int64_t e20 = (int64_t)(t.Y0 - t.Y2) * (Px - t.X2) - (int64_t)(t.X0 - t.X2) * (Py - t.Y2);
-    int64_t e01 = (int64_t)(t.Y1 - t.Y0) * (Px - t.X0) - (int64_t)(t.X1 - t.X0) * (Py - t.Y0);
-    if (e12 < (int64_t)(t.bias & 1u) || e20 < (int64_t)((t.bias >> 1) & 1u) || e01 < (int64_t)((t.bias >> 2) & 1u))
-        return false;
-    float d = (t.z0 + __ll2float_rn(e20) * t.s1) + __ll2float_rn(e01) * t.s2;
+    float f20, f01;
+    if (t.bias & 8u) {
+        const int32_t Px = px * 256 + 128, Py = py * 256 + 128;
+        const int32_t e12 = (t.Y2 - t.Y1) * (Px - t.X1) - (t.X2 - t.X1) * (Py - t.Y1);
+        const int32_t e20 = (t.Y0 - t.Y2) * (Px - t.X2) - (t.X0 - t.X2) * (Py - t.Y2);
+        const int32_t e01 = (t.Y1 - t.Y0) * (Px - t.X0) - (t.X1 - t.X0) * (Py - t.Y0);
+        if (e12 < (int32_t)(t.bias & 1u) || e20 < (int32_t)((t.bias >> 1) & 1u) ||
+            e01 < (int32_t)((t.bias >> 2) & 1u))
+            return false;
+        f20 = i32_to_f32_rn(e20);
+        f01 = i32_to_f32_rn(e01);
+    } else {
+        const int64_t Px = (int64_t)px * 256 + 128, Py = (int64_t)py * 256 + 128;
+        const int64_t e12 = (int64_t)(t.Y2 - t.Y1) * (Px - t.X1) - (int64_t)(t.X2 - t.X1) * (Py - t.Y1);
+        const int64_t e20 = (int64_t)(t.Y0 - t.Y2) * (Px - t.X2) - (int64_t)(t.X0 - t.X2) * (Py - t.Y2);
+        const int64_t e01 = (int64_t)(t.Y1 - t.Y0) * (Px - t.X0) - (int64_t)(t.X1 - t.X0) * (Py - t.Y0);
+        if (e12 < (int64_t)(t.bias & 1u) || e20 < (int64_t)((t.bias >> 1) & 1u) ||
+            e01 < (int64_t)((t.bias >> 2) & 1u))
+            return false;
+        f20 = i64_to_f32_rn(e20);
+        f01 = i64_to_f32_rn(e01);
+    }
+    float d = (t.z0 + f20 * t.s1) + f01 * t.s2;
     d = d > 0.0f ? d : 0.0f;
     depth = d < 1.0f ? d : 1.0f;
     return true;

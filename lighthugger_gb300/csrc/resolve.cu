@@ -23,11 +23,11 @@ __device__ Tex4 sample_repeat(const FrameDev& f, uint32_t index, f2 uv) {
     if (!(fabsf(v) < 1e9f)) v = 0.0f;
     float fu = floorf(u), fv = floorf(v);
     float a = u - fu, b = v - fv;
-    long long i0 = (long long)fu, j0 = (long long)fv;
-    long long W = t.width, H = t.height;
-    long long ia = ((i0 % W) + W) % W, ib = (((i0 + 1) % W) + W) % W;
-    long long ja = ((j0 % H) + H) % H, jb = (((j0 + 1) % H) + H) % H;
-    auto texel = [&](long long i, long long j) {
+    const int32_t i0 = (int32_t)fu, j0 = (int32_t)fv;
+    const int32_t W = (int32_t)t.width, H = (int32_t)t.height;
+    const int32_t ia = wrap_texel(i0, W), ib = wrap_texel(i0 + 1, W);
+    const int32_t ja = wrap_texel(j0, H), jb = wrap_texel(j0 + 1, H);
+    auto texel = [&](int32_t i, int32_t j) {
         uchar4 p = __ldg(reinterpret_cast<const uchar4*>(tex) + ((size_t)j * W + i));
         Tex4 r;
         if (t.srgb) { r.r = f.srgb_lut[p.x]; r.g = f.srgb_lut[p.y]; r.b = f.srgb_lut[p.z]; }
@@ -57,9 +57,9 @@ __device__ float sample_shadow(const FrameDev& f, f2 uv, float layer_f, float re
     if (!(fabsf(v) < 1e9f)) v = 0.0f;
     float fu = floorf(u), fv = floorf(v);
     float a = u - fu, b = v - fv;
-    long long i0 = (long long)fu, j0 = (long long)fv;
-    auto cl = [&](long long i) { return i < 0 ? 0ll : (i > (long long)S - 1 ? (long long)S - 1 : i); };
-    auto cmp = [&](long long i, long long j) { return ref < __ldg(map + (size_t)cl(j) * S + cl(i)) ? 1.0f : 0.0f; };
+    const int32_t i0 = (int32_t)fu, j0 = (int32_t)fv;
+    auto cl = [&](int32_t i) { return i < 0 ? 0 : (i > (int32_t)S - 1 ? (int32_t)S - 1 : i); };
+    auto cmp = [&](int32_t i, int32_t j) { return ref < __ldg(map + (size_t)cl(j) * S + cl(i)) ? 1.0f : 0.0f; };
     float c00 = cmp(i0, j0), c10 = cmp(i0 + 1, j0), c01 = cmp(i0, j0 + 1), c11 = cmp(i0 + 1, j0 + 1);
     float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
     return ((c00 * w00 + c10 * w10) + c01 * w01) + c11 * w11;

@@ -82,7 +82,7 @@ template <class T> struct Bilinear {
     T t00[4], t10[4], t01[4], t11[4];
     T a, b;          // fractional position
     T size_u, size_v;  // texture size (d(frac)/d(uv))
-    int64_t i0, i1, j0, j1;  // texel coordinates (wrapped)
+    int32_t i0, i1, j0, j1;  // texel coordinates (wrapped)
     uint32_t index;
 };
 template <class T> LH_HD T bilerp(const Bilinear<T>& s, int c) {
@@ -127,7 +127,7 @@ template <class T> struct PixelGrad {
     v3<T> bcf, sun, light;
     T base_texel[4][3];  // d/d(linear rgb) of texels 00, 10, 01, 11
     T mr_texel[4][2];    // d/d(roughness = g, metallic = b) of the 4 texels
-    int64_t base_ij[4], mr_ij[4];  // texel columns (i0, i1) and rows (j0, j1) of the two samples
+    int32_t base_ij[4], mr_ij[4];  // texel columns (i0, i1) and rows (j0, j1) of the two samples
     uint32_t base_index, mr_index;
     bool differentiated;
 };
@@ -140,7 +140,8 @@ LH_HD uint32_t pcf_bits(const Sampler& smp, uint32_t layer, T u, T v, T ref, T S
     T uu = u * S - T(0.5), vv = v * S - T(0.5);
     if (!(tabs(uu) < T(1e9))) uu = T(0);
     if (!(tabs(vv) < T(1e9))) vv = T(0);
-    int64_t i0 = (int64_t)tfloor(uu), j0 = (int64_t)tfloor(vv);
+    // |uu|, |vv| < 1e9: 32-bit texel coordinates suffice
+    int32_t i0 = (int32_t)tfloor(uu), j0 = (int32_t)tfloor(vv);
     return (smp.shadow_cmp(layer, i0, j0, ref) != T(0) ? 1u : 0u) |
            (smp.shadow_cmp(layer, i0 + 1, j0, ref) != T(0) ? 2u : 0u) |
            (smp.shadow_cmp(layer, i0, j0 + 1, ref) != T(0) ? 4u : 0u) |

@@ -27,8 +27,8 @@ struct HostSampler {
         double fu = std::floor(u), fv = std::floor(v);
         s.a = u - fu;
         s.b = v - fv;
-        int64_t i0 = (int64_t)fu, j0 = (int64_t)fv;
-        auto wrap = [](int64_t i, int64_t n) { return ((i % n) + n) % n; };
+        int32_t i0 = (int32_t)fu, j0 = (int32_t)fv;
+        auto wrap = [](int32_t i, int32_t n) { return ((i % n) + n) % n; };
         s.i0 = wrap(i0, tw); s.i1 = wrap(i0 + 1, tw); s.j0 = wrap(j0, th); s.j1 = wrap(j0 + 1, th);
         for (int c = 0; c < 4; c++) {
             s.t00[c] = t[(s.j0 * tw + s.i0) * 4 + c];
@@ -41,7 +41,7 @@ struct HostSampler {
         s.index = index;
         return s;
     }
-    double shadow_cmp(uint32_t layer, int64_t i, int64_t j, double ref) const {
+    double shadow_cmp(uint32_t layer, int32_t i, int32_t j, double ref) const {
         i = i < 0 ? 0 : (i > S - 1 ? S - 1 : i);
         j = j < 0 ? 0 : (j > S - 1 ? S - 1 : j);
         return ref < shadow[(layer * S + j) * S + i] ? 1.0 : 0.0;
@@ -182,8 +182,10 @@ int main(int argc, char** argv) {
             shade<double>(fq, p, probe, &o, gout, nullptr);
             sb = smp.sample(0, probe.last[0]);
             Bilinear<double> sm = smp.sample(1, probe.last[1]);
-            int64_t ti[4] = {sb.j0 * smp.tw + sb.i0, sb.j0 * smp.tw + sb.i1, sb.j1 * smp.tw + sb.i0, sb.j1 * smp.tw + sb.i1};
-            int64_t tm[4] = {sm.j0 * smp.tw + sm.i0, sm.j0 * smp.tw + sm.i1, sm.j1 * smp.tw + sm.i0, sm.j1 * smp.tw + sm.i1};
+            int64_t ti[4] = {(int64_t)sb.j0 * smp.tw + sb.i0, (int64_t)sb.j0 * smp.tw + sb.i1,
+                             (int64_t)sb.j1 * smp.tw + sb.i0, (int64_t)sb.j1 * smp.tw + sb.i1};
+            int64_t tm[4] = {(int64_t)sm.j0 * smp.tw + sm.i0, (int64_t)sm.j0 * smp.tw + sm.i1,
+                             (int64_t)sm.j1 * smp.tw + sm.i0, (int64_t)sm.j1 * smp.tw + sm.i1};
             bool dup_b = false, dup_m = false;
             for (int a = 0; a < 4; a++)
                 for (int b = a + 1; b < 4; b++) { dup_b |= ti[a] == ti[b]; dup_m |= tm[a] == tm[b]; }
@@ -220,7 +222,7 @@ int main(int argc, char** argv) {
             f.i0 = d.i0; f.i1 = d.i1; f.j0 = d.j0; f.j1 = d.j1; f.index = d.index;
             return f;
         }
-        float shadow_cmp(uint32_t layer, int64_t i, int64_t j, float ref) const {
+        float shadow_cmp(uint32_t layer, int32_t i, int32_t j, float ref) const {
             return (float)h->shadow_cmp(layer, i, j, ref);
         }
     };

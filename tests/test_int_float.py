@@ -1,0 +1,20 @@
+"""The rasteriser's integer -> float conversions (lighthugger_gb300/csrc/
+int_float.cuh), which keep the per-fragment edge-to-depth conversion off the
+FP64 unit, compiled for the host and compared bit for bit with the
+round-to-nearest-even conversion."""
+import os
+import subprocess
+import tempfile
+
+from tests.conftest import ROOT
+
+
+def test_conversions_round_like_the_conversion_instructions():
+    src = os.path.join(ROOT, "tests", "native", "int_float_check.cpp")
+    with tempfile.TemporaryDirectory() as d:
+        exe = os.path.join(d, "int_float_check")
+        subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I",
+                        os.path.join(ROOT, "lighthugger_gb300", "csrc"), src, "-o", exe], check=True)
+        r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "bad 0" in r.stdout
