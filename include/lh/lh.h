@@ -180,6 +180,13 @@ typedef struct lh_grad_targets {
  * differentiated.  No counterpart in the reference. */
 lh_status lh_resolve_backward(lh_ctx* ctx, uint64_t d_grad_hdr, const lh_grad_targets* targets, void* stream);
 
+/* lh_frame_graph followed by lh_resolve_backward of that frame, both in one
+ * captured CUDA graph (re-captured when the views, instance count, tuning,
+ * gradient buffer or targets change).  No counterpart in the reference. */
+lh_status lh_frame_graph_backward(lh_ctx* ctx, const Uniforms* uniforms, const Uniforms* probes, uint32_t n_probes,
+                                  uint64_t d_grad_hdr, const lh_grad_targets* targets, void* stream,
+                                  lh_frame_out* out);
+
 /* Pointers to the context's result buffers (valid until lh_destroy). */
 lh_status lh_get_outputs(lh_ctx* ctx, lh_frame_out* out);
 
@@ -198,6 +205,8 @@ typedef struct lh_tuning {
     uint32_t medium_px;       /* the warp rasterises up to medium_px; larger go to 16 x 64-pixel chunks */
     float cull_blocks_per_sm; /* meshlet-cull blocks per SM (per-stage schedule); blocks per SM (persistent) */
     uint32_t schedule;        /* LH_SCHEDULE_* */
+    uint32_t raster_batch;    /* meshlets a raster warp claims per atomic (0: 4 when the views hold more than
+                                 256 meshlets per warp of the grid, else 1) */
 } lh_tuning;
 
 lh_status lh_set_tuning(lh_ctx* ctx, const lh_tuning* tuning);

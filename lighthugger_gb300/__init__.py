@@ -79,7 +79,7 @@ SCHEDULE_DEFAULT, SCHEDULE_PER_STAGE, SCHEDULE_PERSISTENT, SCHEDULE_PER_VIEW = 0
 
 class Tuning(C.Structure):
     _fields_ = [("small_px", C.c_uint32), ("medium_px", C.c_uint32), ("cull_blocks_per_sm", C.c_float),
-                ("schedule", C.c_uint32)]
+                ("schedule", C.c_uint32), ("raster_batch", C.c_uint32)]
 
 
 class MeshGrads(C.Structure):
@@ -143,6 +143,8 @@ def lib():
     L.lh_destroy.argtypes = [P]
     L.lh_destroy.restype = None
     L.lh_resolve_backward.argtypes = [P, C.c_uint64, C.POINTER(GradTargets), P]
+    L.lh_frame_graph_backward.argtypes = [P, P, P, C.c_uint32, C.c_uint64, C.POINTER(GradTargets), P,
+                                          C.POINTER(FrameOut)]
     L.lh_set_profiling.argtypes = [P, C.c_int]
     L.lh_get_stage_times.argtypes = [P, C.POINTER(C.c_float), C.c_uint32]
     L.lh_set_tuning.argtypes = [P, C.POINTER(Tuning)]
@@ -155,7 +157,7 @@ def lib():
     L.lh_make_uniforms.argtypes = [C.POINTER(Camera), C.POINTER(Uniforms)]
     for name in ("lh_create", "lh_set_scene", "lh_frame", "lh_frame_batched", "lh_frame_graph", "lh_get_outputs",
                  "lh_read_status",
-                 "lh_download", "lh_resolve_backward", "lh_set_profiling", "lh_get_stage_times", "lh_set_tuning", "lh_get_tuning", "lh_scene_create", "lh_scene_describe",
+                 "lh_download", "lh_resolve_backward", "lh_frame_graph_backward", "lh_set_profiling", "lh_get_stage_times", "lh_set_tuning", "lh_get_tuning", "lh_scene_create", "lh_scene_describe",
                  "lh_scene_upload", "lh_make_uniforms"):
         getattr(L, name).restype = C.c_int32
     _lib = L
@@ -277,10 +279,12 @@ class Renderer:
                "lh_set_scene", self.ctx)
         self.scene = scene
 
-    def set_tuning(self, small_px=None, medium_px=None, cull_blocks_per_sm=None, schedule=None):
+    def set_tuning(self, small_px=None, medium_px=None, cull_blocks_per_sm=None, schedule=None, raster_batch=None):
         t = self.tuning()
         if schedule is not None:
             t.schedule = schedule
+        if raster_batch is not None:
+            t.raster_batch = raster_batch
         if small_px is not None:
             t.small_px = small_px
         if medium_px is not None:
@@ -317,6 +321,15 @@ class Renderer:
         s = stream if stream is not None else self.stream
         _check(lib().lh_frame_graph(self.ctx, C.byref(uniforms), probes if n_probes else None, n_probes, s,
                                     C.byref(self.out)), "lh_frame_graph", self.ctx)
+        return self.out
+
+    def frame_graph_backward(self, uniforms, probes, n_probes, grad_ptr, targets, stream=None):
+        """The batched frame and the resolve adjoint of its main view, replayed
+        from one captured CUDA graph."""
+        s = stream if stream is not None else self.stream
+        _check(lib().lh_frame_graph_backward(self.ctx, C.byref(uniforms), probes if n_probes else None, n_probes,
+                                             grad_ptr, C.byref(targets), s, C.byref(self.out)),
+               "lh_frame_graph_backward", self.ctx)
         return self.out
 
     def status(self):

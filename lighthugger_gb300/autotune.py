@@ -2,8 +2,9 @@
 
 The raster kernels split triangles into three bins by the pixel count of
 their bounding box -- rasterised by one lane (<= small_px), by one warp
-(<= medium_px), or cut into 16 x 64-pixel chunks spread over all warps -- and
-a batched frame can run per stage or as one persistent launch.  None of this
+(<= medium_px), or cut into 16 x 64-pixel chunks spread over all warps --,
+claim `raster_batch` meshlets per atomic, and a batched frame can run per
+stage or as one persistent launch.  None of this
 changes a single output bit; it only moves time.  `tune()` times frames of
 the given workload with CUDA events for every candidate and keeps the
 fastest; results are cached per GPU name and workload signature in
@@ -18,6 +19,7 @@ CACHE = os.path.join(_HERE, "_build", "tuning.json")
 
 SMALL = (4, 8, 16, 32)
 MEDIUM = (64, 128, 256, 512, 1024)
+BATCH = (1, 2, 4, 8)
 
 
 def _signature(renderer, n_probes, batched):
@@ -69,7 +71,8 @@ def tune(renderer, uniforms, probes=None, n_probes=0, batched=False, frames=4, u
     cache = _load() if use_cache else {}
     if key in cache:
         best = cache[key]
-        renderer.set_tuning(small_px=best["small_px"], medium_px=best["medium_px"], schedule=best["schedule"])
+        renderer.set_tuning(small_px=best["small_px"], medium_px=best["medium_px"], schedule=best["schedule"],
+                            raster_batch=best.get("raster_batch", 0))
         return best, {}
     stream = stream or torch.cuda.Stream()
     sptr = stream.cuda_stream
@@ -81,15 +84,25 @@ def tune(renderer, uniforms, probes=None, n_probes=0, batched=False, frames=4, u
         schedules = (SCHEDULE_PER_STAGE,)
     results = {}
     best, best_ms = None, float("inf")
+    # bins and schedule first (automatic claim batch), then the claim batch
     for sched, small, medium in itertools.product(schedules, SMALL, MEDIUM):
         if medium < small:
             continue
-        renderer.set_tuning(small_px=small, medium_px=medium, schedule=sched)
+        renderer.set_tuning(small_px=small, medium_px=medium, schedule=sched, raster_batch=0)
         ms = time_frames(renderer, run, frames, stream)
-        results["%d/%d/%d" % (sched, small, medium)] = ms
+        results["%d/%d/%d/0" % (sched, small, medium)] = ms
         if ms < best_ms:
-            best_ms, best = ms, {"small_px": small, "medium_px": medium, "schedule": sched, "ms": ms}
-    renderer.set_tuning(small_px=best["small_px"], medium_px=best["medium_px"], schedule=best["schedule"])
+            best_ms, best = ms, {"small_px": small, "medium_px": medium, "schedule": sched, "raster_batch": 0, "ms": ms}
+    for batch in BATCH:
+        renderer.set_tuning(small_px=best["small_px"], medium_px=best["medium_px"], schedule=best["schedule"],
+                            raster_batch=batch)
+        ms = time_frames(renderer, run, frames, stream)
+        results["%d/%d/%d/%d" % (best["schedule"], best["small_px"], best["medium_px"], batch)] = ms
+        if ms < best_ms:
+            best_ms = ms
+            best = dict(best, raster_batch=batch, ms=ms)
+    renderer.set_tuning(small_px=best["small_px"], medium_px=best["medium_px"], schedule=best["schedule"],
+                        raster_batch=best["raster_batch"])
     if use_cache:
         cache[key] = best
         _save(cache)

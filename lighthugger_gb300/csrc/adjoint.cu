@@ -9,12 +9,12 @@
 
 #include "frame_phases.cuh"
 #include "shade.cuh"
+#include "tma.cuh"
 
 namespace lh {
 namespace {
 
 using shade::Bilinear;
-using shade::PixelFixed;
 using shade::PixelGrad;
 using shade::PixelParams;
 using shade::v2;
@@ -81,6 +81,40 @@ constexpr int kBwdRows = LH_BWD_ROWS;
 constexpr int kBwdThreads = 32 * kBwdRows;
 constexpr uint32_t kCacheSlots = 256;     // shared-memory accumulators of hot gradient addresses
 constexpr uint32_t kSmallTexture = 64;    // textures of at most this many texels go through them
+
+// Fixed inputs of a pixel for shade.cuh whose matrices are read from
+// memory at each use -- PV and the cascades' UVS from the block's shared
+// copies, the instance's normal transform from global memory -- rather
+// than held in registers through the whole pixel.  `pv3` / `uvs3` point at
+// the column 3 in use (absolute for the decisions, camera-relative after).
+__device__ __forceinline__ float lds_f32(const float* p) {
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(smem_u32(p)));
+    return v;
+}
+__device__ __forceinline__ float ldg_f32(const float* p) {
+    float v;
+    asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+}
+
+struct DeviceFixed : shade::PixelScalars {
+    const float* pv;    // shared: 16 floats, column-major
+    const float* pv3;   // shared: 4 floats
+    const float* uvs;   // shared: 16 floats of the pixel's cascade
+    const float* uvs3;  // shared: 4 floats
+    const float* nt;    // global: Instance::normal_transform, 3 columns of 3
+    __device__ float PV(int c, int r) const { return c == 3 ? lds_f32(pv3 + r) : lds_f32(pv + 4 * c + r); }
+    __device__ float UVS(int c, int r) const { return c == 3 ? lds_f32(uvs3 + r) : lds_f32(uvs + 4 * c + r); }
+    __device__ float NT(int c, int r) const { return ldg_f32(nt + 3 * c + r); }
+};
+
+// Block-shared copies of the frame's matrices for DeviceFixed.
+struct FrameMats {
+    float pv[16];        // combined_perspective_view
+    float uvs[4][16];    // uv_space_shadow_matrices
+    float rel[20];       // column 3 of PV T(cam) and of UVS_c T(cam) (rel_columns)
+};
 
 __device__ __forceinline__ float warp_sum(float v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
@@ -149,12 +183,13 @@ struct PixelOut {
 };
 
 // Recompute the forward of pixel (x, y) from the visibility buffer and run
-// the reverse pass of shade.cuh for the upstream gradient at that pixel.
-// `rel` holds column 3 of the camera-relative PV and of the 4 cascades'
-// UVS matrices (see rel_columns).
+// the surface half of the reverse pass of shade.cuh for the upstream
+// gradient at that pixel; fx, p and st carry what the geometry half needs.
+// `M` holds the block's copies of the frame matrices.
 __device__ __forceinline__ void pixel_backward(const FrameDev& f, const float4* grad, const lh_grad_targets& t,
-                                               const float* rel, uint32_t x, uint32_t y, PixelGrad<float>& g,
-                                               PixelOut& o) {
+                                               const FrameMats& M, uint32_t x, uint32_t y, PixelGrad<float>& g,
+                                               PixelOut& o, DeviceFixed& fx, PixelParams<float>& p,
+                                               shade::SurfaceState<float>& st) {
     const Uniforms& u = *f.uniforms;
     const uint32_t W = u.window_size.x, H = u.window_size.y;
     o.ok = false;
@@ -179,7 +214,6 @@ __device__ __forceinline__ void pixel_backward(const FrameDev& f, const float4* 
                                                             : __ldg(reinterpret_cast<const uint16_t*>(mi.indices) + vi);
     }
     const lh_mat4& T = inst->transform;
-    PixelParams<float> p;
     for (int k = 0; k < 3; k++) {
         f3 w = world_pos(T, load_position(mi.positions, flags, o.idx[k]));
         p.W[k] = {w.x, w.y, w.z};
@@ -191,19 +225,9 @@ __device__ __forceinline__ void pixel_backward(const FrameDev& f, const float4* 
     p.bcf = {mi.base_color_factor.x, mi.base_color_factor.y, mi.base_color_factor.z};
     p.sun = {u.sun_dir.x, u.sun_dir.y, u.sun_dir.z};
     p.light = {u.sun_intensity.x, u.sun_intensity.y, u.sun_intensity.z};
-    PixelFixed fx;
-    for (int c = 0; c < 4; c++) {
-        fx.pv[c][0] = u.combined_perspective_view.cols[c].x;
-        fx.pv[c][1] = u.combined_perspective_view.cols[c].y;
-        fx.pv[c][2] = u.combined_perspective_view.cols[c].z;
-        fx.pv[c][3] = u.combined_perspective_view.cols[c].w;
-    }
-    for (int c = 0; c < 3; c++) {
-        fx.nt[c][0] = inst->normal_transform.cols[c].x;
-        fx.nt[c][1] = inst->normal_transform.cols[c].y;
-        fx.nt[c][2] = inst->normal_transform.cols[c].z;
-    }
-    // the world position the forward interpolated decides the cascade
+    fx.pv = M.pv;
+    fx.pv3 = M.pv + 12;
+    fx.nt = &inst->normal_transform.cols[0].x;
     const f2 ndc{(float)x / (float)W * 2.0f - 1.0f, (float)y / (float)H * 2.0f - 1.0f};
     fx.ndc[0] = ndc.x;
     fx.ndc[1] = ndc.y;
@@ -222,57 +246,34 @@ __device__ __forceinline__ void pixel_backward(const FrameDev& f, const float4* 
     fx.base_tex = mi.base_tex;
     fx.mr_tex = mi.mr_tex;
     fx.has_normal_map = mi.normal_tex != UNUSED_TEXTURE_INDEX;
-    // the cascade the forward chose: its own barycentrics and world
-    // position, in its absolute float arithmetic (render_geometry.comp:183-196)
+    DeviceSampler smp{&f};
     {
-        f4 c0 = mul(u.combined_perspective_view, f4{p.W[0].x, p.W[0].y, p.W[0].z, 1.0f});
-        f4 c1 = mul(u.combined_perspective_view, f4{p.W[1].x, p.W[1].y, p.W[1].z, 1.0f});
-        f4 c2 = mul(u.combined_perspective_view, f4{p.W[2].x, p.W[2].y, p.W[2].z, 1.0f});
-        f3 invW{1.0f / c0.w, 1.0f / c1.w, 1.0f / c2.w};
-        f2 n0{c0.x * invW.x, c0.y * invW.x}, n1{c1.x * invW.y, c1.y * invW.y}, n2{c2.x * invW.z, c2.y * invW.z};
-        f2 ca{n2.x - n1.x, n2.y - n1.y}, cb{n0.x - n1.x, n0.y - n1.y};
-        float invDet = 1.0f / (ca.x * cb.y - cb.x * ca.y);
-        f3 ddx = f3{n1.y - n2.y, n2.y - n0.y, n0.y - n1.y} * invDet * invW;
-        f3 ddy = f3{n2.x - n1.x, n0.x - n2.x, n1.x - n0.x} * invDet * invW;
-        float ddxSum = dot(ddx, f3{1.0f, 1.0f, 1.0f});
-        float ddySum = dot(ddy, f3{1.0f, 1.0f, 1.0f});
-        f2 dv{ndc.x - n0.x, ndc.y - n0.y};
-        float interpInvW = (invW.x + dv.x * ddxSum) + dv.y * ddySum;
-        float interpW = 1.0f / interpInvW;
-        float l0 = interpW * ((invW.x + dv.x * ddx.x) + dv.y * ddy.x);
-        float l1 = interpW * ((0.0f + dv.x * ddx.y) + dv.y * ddy.y);
-        float l2 = interpW * ((0.0f + dv.x * ddx.z) + dv.y * ddy.z);
-        f3 world{(p.W[0].x * l0 + p.W[1].x * l1) + p.W[2].x * l2, (p.W[0].y * l0 + p.W[1].y * l1) + p.W[2].y * l2,
-                 (p.W[0].z * l0 + p.W[1].z * l1) + p.W[2].z * l2};
+        // the world position the forward interpolated, in its absolute float
+        // arithmetic, picks the cascade (render_geometry.comp:183-196) and
+        // places the PCF taps
+        const v3<float> world = shade::forward_world(fx, p);
         uint32_t ci;
         for (ci = 0; ci < 4; ci++) {
-            f4 sc = mul(f.misc->uv_space_shadow_matrices[ci], f4{world.x, world.y, world.z, 1.0f});
+            const lh_mat4& m = *reinterpret_cast<const lh_mat4*>(M.uvs[ci]);
+            f4 sc = mul(m, f4{world.x, world.y, world.z, 1.0f});
             float ox = sc.x - 0.5f, oy = sc.y - 0.5f;
             if (fabsf(ox) < 0.5f && fabsf(oy) < 0.5f) break;
         }
         fx.cascade = ci;
-        const lh_mat4& m = f.misc->uv_space_shadow_matrices[ci > 3 ? 3 : ci];
-        for (int c = 0; c < 4; c++) {
-            fx.uvs[c][0] = m.cols[c].x;
-            fx.uvs[c][1] = m.cols[c].y;
-            fx.uvs[c][2] = m.cols[c].z;
-            fx.uvs[c][3] = m.cols[c].w;
-        }
+        fx.uvs = M.uvs[ci > 3 ? 3 : ci];
+        fx.uvs3 = fx.uvs + 12;
+        // face flip, far-plane test and compare results exactly as the forward
+        shade::decide_at(fx, p, world, smp);
     }
-    DeviceSampler smp{&f};
-    // face flip, far-plane test and compare results exactly as the forward
-    shade::decide<float>(fx, p, smp);
     // the continuous part in camera-relative coordinates: W - cam is
     // (nearly) exact, and PV T(cam), UVS T(cam) were formed in double
     const uint32_t layer = fx.cascade > 3 ? 3u : fx.cascade;
-    for (int r = 0; r < 4; r++) {
-        fx.pv[3][r] = rel[r];
-        fx.uvs[3][r] = rel[4 + 4 * layer + r];
-    }
+    fx.pv3 = M.rel;
+    fx.uvs3 = M.rel + 4 + 4 * layer;
     for (int k = 0; k < 3; k++) p.W[k] = {p.W[k].x - u.camera_pos.x, p.W[k].y - u.camera_pos.y, p.W[k].z - u.camera_pos.z};
     fx.cam[0] = fx.cam[1] = fx.cam[2] = 0.0f;
     v3<float> out;
-    shade::shade<float>(fx, p, smp, &out, v3<float>{gp.x, gp.y, gp.z}, &g);
+    shade::shade_surface<float>(fx, p, smp, &out, v3<float>{gp.x, gp.y, gp.z}, &g, &st);
     if (!g.differentiated) return;
     o.ok = true;
     o.packed = packed;
@@ -342,13 +343,15 @@ __global__ void __launch_bounds__(kBwdThreads, LH_BWD_MIN_BLOCKS)
     k_resolve_backward(FrameDev f, const float4* grad, lh_grad_targets t, uint32_t tiles_x, uint32_t n_tiles) {
     __shared__ HotCache cache;
     __shared__ float s_light[kBwdThreads / 32][6];
-    __shared__ float s_rel[20];
+    __shared__ __align__(16) FrameMats s_mats;
     const uint32_t tid = threadIdx.y * 32 + threadIdx.x;
     for (uint32_t s = tid; s < kCacheSlots; s += kBwdThreads) {
         cache.key[s] = 0ull;
         cache.sum[s] = 0.0f;
     }
-    rel_columns(f, tid, s_rel);
+    if (tid < 16) s_mats.pv[tid] = (&f.uniforms->combined_perspective_view.cols[0].x)[tid];
+    if (tid < 64) s_mats.uvs[tid / 16][tid % 16] = (&f.misc->uv_space_shadow_matrices[tid / 16].cols[0].x)[tid % 16];
+    rel_columns(f, tid, s_mats.rel);
     __syncthreads();
     float acc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     const uint64_t* tex_targets = reinterpret_cast<const uint64_t*>(t.texture_grads);
@@ -356,7 +359,10 @@ __global__ void __launch_bounds__(kBwdThreads, LH_BWD_MIN_BLOCKS)
         const uint32_t x = (tile % tiles_x) * 32 + threadIdx.x, y = (tile / tiles_x) * kBwdRows + threadIdx.y;
         PixelGrad<float> g;
         PixelOut o;
-        pixel_backward(f, grad, t, s_rel, x, y, g, o);
+        DeviceFixed fx;
+        PixelParams<float> p;
+        shade::SurfaceState<float> st;
+        pixel_backward(f, grad, t, s_mats, x, y, g, o, fx, p, st);
         if (o.ok) {
             acc[0] += g.sun.x;
             acc[1] += g.sun.y;
@@ -366,7 +372,46 @@ __global__ void __launch_bounds__(kBwdThreads, LH_BWD_MIN_BLOCKS)
             acc[5] += g.light.z;
         }
         const lh_mesh_grads* mg = o.ok ? o.rec : nullptr;
-        // vertex attributes: one run per triangle
+        // base-colour factor of the pixel's MeshInfo record
+        float* bcf_dst = mg ? reinterpret_cast<float*>(mg->base_color_factor) : nullptr;
+        if (__any_sync(kFull, bcf_dst != nullptr)) {
+            const Run r = run_of((unsigned long long)bcf_dst);
+            const float bx = run_sum(bcf_dst ? g.bcf.x : 0.0f, r);
+            const float by = run_sum(bcf_dst ? g.bcf.y : 0.0f, r);
+            const float bz = run_sum(bcf_dst ? g.bcf.z : 0.0f, r);
+            if (r.head && bcf_dst) {
+                cache_add(cache, bcf_dst, bx);
+                cache_add(cache, bcf_dst + 1, by);
+                cache_add(cache, bcf_dst + 2, bz);
+            }
+        }
+        if (tex_targets) {
+            // base colour (rgb of the texel) and metallic-roughness (g, b)
+            float* ba[4] = {nullptr, nullptr, nullptr, nullptr};
+            float* ma[4] = {nullptr, nullptr, nullptr, nullptr};
+            bool base_small = false, mr_small = false;
+            if (o.ok && g.base_index < f.n_textures && tex_targets[g.base_index]) {
+                const lh_texture& tx = f.textures[g.base_index];
+                float4* dst = reinterpret_cast<float4*>(tex_targets[g.base_index]);
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    ba[q] = reinterpret_cast<float*>(dst + (size_t)g.base_ij[2 + (q >> 1)] * tx.width + g.base_ij[q & 1]);
+                base_small = tx.width * tx.height <= kSmallTexture;
+            }
+            if (o.ok && g.mr_index < f.n_textures && tex_targets[g.mr_index]) {
+                const lh_texture& tx = f.textures[g.mr_index];
+                float4* dst = reinterpret_cast<float4*>(tex_targets[g.mr_index]);
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    ma[q] = reinterpret_cast<float*>(dst + (size_t)g.mr_ij[2 + (q >> 1)] * tx.width + g.mr_ij[q & 1]);
+                mr_small = tx.width * tx.height <= kSmallTexture;
+            }
+            scatter_texels<3>(cache, ba, g.base_texel, 0, base_small);
+            scatter_texels<2>(cache, ma, g.mr_texel, 1, mr_small);  // roughness (g), metallic (b)
+        }
+        // the geometry half of the reverse, then the vertex attributes: one
+        // run per triangle
+        if (o.ok) shade::shade_geometry<float>(fx, p, st, &g);
         if (__any_sync(kFull, mg != nullptr)) {
             const Run r = run_of(mg ? (unsigned long long)o.packed : ~0ull);
             float v[24];
@@ -412,43 +457,6 @@ __global__ void __launch_bounds__(kBwdThreads, LH_BWD_MIN_BLOCKS)
                     }
                 }
             }
-        }
-        // base-colour factor of the pixel's MeshInfo record
-        float* bcf_dst = mg ? reinterpret_cast<float*>(mg->base_color_factor) : nullptr;
-        if (__any_sync(kFull, bcf_dst != nullptr)) {
-            const Run r = run_of((unsigned long long)bcf_dst);
-            const float bx = run_sum(bcf_dst ? g.bcf.x : 0.0f, r);
-            const float by = run_sum(bcf_dst ? g.bcf.y : 0.0f, r);
-            const float bz = run_sum(bcf_dst ? g.bcf.z : 0.0f, r);
-            if (r.head && bcf_dst) {
-                cache_add(cache, bcf_dst, bx);
-                cache_add(cache, bcf_dst + 1, by);
-                cache_add(cache, bcf_dst + 2, bz);
-            }
-        }
-        if (tex_targets) {
-            // base colour (rgb of the texel) and metallic-roughness (g, b)
-            float* ba[4] = {nullptr, nullptr, nullptr, nullptr};
-            float* ma[4] = {nullptr, nullptr, nullptr, nullptr};
-            bool base_small = false, mr_small = false;
-            if (o.ok && g.base_index < f.n_textures && tex_targets[g.base_index]) {
-                const lh_texture& tx = f.textures[g.base_index];
-                float4* dst = reinterpret_cast<float4*>(tex_targets[g.base_index]);
-#pragma unroll
-                for (int q = 0; q < 4; q++)
-                    ba[q] = reinterpret_cast<float*>(dst + (size_t)g.base_ij[2 + (q >> 1)] * tx.width + g.base_ij[q & 1]);
-                base_small = tx.width * tx.height <= kSmallTexture;
-            }
-            if (o.ok && g.mr_index < f.n_textures && tex_targets[g.mr_index]) {
-                const lh_texture& tx = f.textures[g.mr_index];
-                float4* dst = reinterpret_cast<float4*>(tex_targets[g.mr_index]);
-#pragma unroll
-                for (int q = 0; q < 4; q++)
-                    ma[q] = reinterpret_cast<float*>(dst + (size_t)g.mr_ij[2 + (q >> 1)] * tx.width + g.mr_ij[q & 1]);
-                mr_small = tx.width * tx.height <= kSmallTexture;
-            }
-            scatter_texels<3>(cache, ba, g.base_texel, 0, base_small);
-            scatter_texels<2>(cache, ma, g.mr_texel, 1, mr_small);  // roughness (g), metallic (b)
         }
     }
     // light direction / colour: one atomic per value per block

@@ -19,6 +19,12 @@ namespace {
 
 constexpr uint32_t kVersion = 1;
 
+// The resolve adjoint captured with a graphed frame (all zero: none).
+struct GraphBackward {
+    uint64_t grad;
+    lh_grad_targets targets;
+};
+
 struct Alloc {
     void* p = nullptr;
     size_t bytes = 0;
@@ -82,9 +88,38 @@ struct lh_ctx {
     lh_tuning graph_tuning{};
     cudaStream_t capture_stream = nullptr;
     bool capturing = false;
+    GraphBackward graph_backward{};
+    // 2D tensor map of d_vis for the TMA-staged resolve (false: rows are not
+    // 16-byte aligned or the driver lacks the encoder)
+    alignas(64) CUtensorMap vis_map;
+    bool vis_map_ok = false;
 };
 
 namespace {
+
+// Tensor map of the main visibility buffer: u64 elements, W x H, boxes of
+// 32 x 8 (the resolve's tile).  cuTensorMapEncodeTiled is reached through
+// the runtime's driver entry point, so nothing links against libcuda.
+bool encode_vis_map(lh_ctx* c) {
+    const uint64_t W = c->cfg.width, H = c->cfg.height;
+    if ((W * 8) % 16 != 0) return false;
+    using Encode = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+        return false;
+    const cuuint64_t dims[2] = {W, H};
+    const cuuint64_t strides[1] = {W * 8};
+    const cuuint32_t box[2] = {32, 8};
+    const cuuint32_t elem[2] = {1, 1};
+    return reinterpret_cast<Encode>(fn)(&c->vis_map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, c->d_vis, dims, strides, box,
+                                        elem, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 
 lh_status fail(lh_ctx* c, lh_status st, const std::string& msg) {
     if (c) c->err = msg;
@@ -268,7 +303,8 @@ lh_status enqueue_frame(lh_ctx* c, uint32_t n_probes, uint32_t n_instances, bool
     if (schedule == LH_SCHEDULE_PERSISTENT) {
         // stages 0..7 in one launch: the time lands in stage 0 ("clear")
         if (e == cudaSuccess)
-            e = launch_frame_persistent(f, n_persp, t.small_px, t.medium_px, t.cull_blocks_per_sm, s, c->sms);
+            e = launch_frame_persistent(f, n_persp, t.small_px, t.medium_px, t.raster_batch, t.cull_blocks_per_sm, s,
+                                        c->sms);
         e = mark(e);
         e = skip_to(8, e);
     } else if (schedule == LH_SCHEDULE_PER_VIEW) {
@@ -277,7 +313,7 @@ lh_status enqueue_frame(lh_ctx* c, uint32_t n_probes, uint32_t n_instances, bool
             e = launch_cull_instances(f, v, 1, s);
             if (e == cudaSuccess) e = launch_cull_meshlets(f, v, 1, cull_blocks, s);
             if (e == cudaSuccess)
-                e = launch_raster_kind(f, v, 1, kViewVisibility, t.small_px, t.medium_px, s, c->sms);
+                e = launch_raster_kind(f, v, 1, kViewVisibility, t.small_px, t.medium_px, t.raster_batch, s, c->sms);
         }
         e = skip_to(4, e);
         if (e == cudaSuccess) e = mark(launch_depth_reduce_fit(f, s, c->sms));
@@ -285,7 +321,7 @@ lh_status enqueue_frame(lh_ctx* c, uint32_t n_probes, uint32_t n_instances, bool
             e = launch_cull_instances(f, n_persp + k, 1, s);
             if (e == cudaSuccess) e = launch_cull_meshlets(f, n_persp + k, 1, cull_blocks, s);
             if (e == cudaSuccess)
-                e = launch_raster_kind(f, n_persp + k, 1, kViewShadow, t.small_px, t.medium_px, s, c->sms);
+                e = launch_raster_kind(f, n_persp + k, 1, kViewShadow, t.small_px, t.medium_px, t.raster_batch, s, c->sms);
         }
         e = skip_to(8, e);
     } else {
@@ -294,17 +330,18 @@ lh_status enqueue_frame(lh_ctx* c, uint32_t n_probes, uint32_t n_instances, bool
         if (e == cudaSuccess) e = mark(launch_cull_instances(f, 0, n_persp, s));
         if (e == cudaSuccess) e = mark(launch_cull_meshlets(f, 0, n_persp, cull_blocks, s));
         if (e == cudaSuccess)
-            e = mark(launch_raster_kind(f, 0, n_persp, kViewVisibility, t.small_px, t.medium_px, s, c->sms));
+            e = mark(launch_raster_kind(f, 0, n_persp, kViewVisibility, t.small_px, t.medium_px, t.raster_batch, s, c->sms));
         // depth range + cascade fit (main view only)
         if (e == cudaSuccess) e = mark(launch_depth_reduce_fit(f, s, c->sms));
         // cascades
         if (e == cudaSuccess) e = mark(launch_cull_instances(f, n_persp, 4, s));
         if (e == cudaSuccess) e = mark(launch_cull_meshlets(f, n_persp, 4, cull_blocks, s));
         if (e == cudaSuccess)
-            e = mark(launch_raster_kind(f, n_persp, 4, kViewShadow, t.small_px, t.medium_px, s, c->sms));
+            e = mark(launch_raster_kind(f, n_persp, 4, kViewShadow, t.small_px, t.medium_px, t.raster_batch, s, c->sms));
     }
     // lighting resolve of the main view
-    if (e == cudaSuccess) e = mark(launch_resolve(f, c->cfg.width, c->cfg.height, s));
+    if (e == cudaSuccess)
+        e = mark(launch_resolve(f, c->cfg.width, c->cfg.height, c->vis_map_ok ? &c->vis_map : nullptr, s, c->sms));
     if (e != cudaSuccess) return cuda_fail(c, e, "frame launch");
     return LH_OK;
 }
@@ -376,7 +413,7 @@ lh_status lh_create(const lh_config* config, lh_ctx** out) {
     if (!c) return LH_ERR_OUT_OF_MEMORY;
     c->cfg = cfg;
     c->device = cfg.device;
-    c->tuning = lh_tuning{8u, 256u, 2.0f, LH_SCHEDULE_DEFAULT};
+    c->tuning = lh_tuning{8u, 256u, 2.0f, LH_SCHEDULE_DEFAULT, 0u};
     cudaError_t e = cudaSetDevice(c->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device);
     c->max_views = 5 + cfg.max_probes;
@@ -407,6 +444,7 @@ lh_status lh_create(const lh_config* config, lh_ctx** out) {
         e = cudaMemcpy(c->d_srgb, lut, sizeof(lut), cudaMemcpyHostToDevice);
     }
     if (e == cudaSuccess) e = cudaMemset(c->d_misc, 0, sizeof(MiscStorage));
+    if (e == cudaSuccess) c->vis_map_ok = encode_vis_map(c);
     c->staging_bytes = sizeof(Uniforms) * (1 + cfg.max_probes) + 64;
     for (int i = 0; i < 2 && e == cudaSuccess; i++) {
         e = cudaMallocHost(reinterpret_cast<void**>(&c->h_staging[i]), c->staging_bytes);
@@ -511,8 +549,12 @@ static lh_status frame_impl(lh_ctx* c, const Uniforms* u, const Uniforms* probes
     return LH_OK;
 }
 
-lh_status lh_frame_graph(lh_ctx* c, const Uniforms* u, const Uniforms* probes, uint32_t n_probes, void* stream,
-                         lh_frame_out* out) {
+namespace {
+
+// Batched frame replayed from a captured CUDA graph; with `bw` the resolve
+// adjoint is captured into the same graph after the frame.
+lh_status frame_graph_impl(lh_ctx* c, const Uniforms* u, const Uniforms* probes, uint32_t n_probes,
+                           const GraphBackward* bw, void* stream, lh_frame_out* out) {
     lh_status st = check_ctx(c);
     if (st != LH_OK) return st;
     if (!u) return fail(c, LH_ERR_INVALID_ARGUMENT, "uniforms is NULL");
@@ -537,7 +579,11 @@ lh_status lh_frame_graph(lh_ctx* c, const Uniforms* u, const Uniforms* probes, u
         }
     }
     const bool tuning_changed = std::memcmp(&c->graph_tuning, &c->tuning, sizeof(lh_tuning)) != 0;
-    if (!c->graph_exec || c->graph_probes != n_probes || c->graph_instances != n_inst || tuning_changed) {
+    const GraphBackward none{};
+    const GraphBackward& want = bw ? *bw : none;
+    const bool backward_changed = std::memcmp(&c->graph_backward, &want, sizeof(GraphBackward)) != 0;
+    if (!c->graph_exec || c->graph_probes != n_probes || c->graph_instances != n_inst || tuning_changed ||
+        backward_changed) {
         if (c->graph_exec) {
             cudaGraphExecDestroy(c->graph_exec);
             c->graph_exec = nullptr;
@@ -550,6 +596,13 @@ lh_status lh_frame_graph(lh_ctx* c, const Uniforms* u, const Uniforms* probes, u
         if (e != cudaSuccess) return cuda_fail(c, e, "begin capture");
         c->capturing = true;
         st = enqueue_frame(c, n_probes, n_inst, true, c->capture_stream);
+        if (st == LH_OK && bw) {
+            const FrameDev f = frame_dev(c, 5 + n_probes, n_inst);
+            cudaError_t eb = launch_resolve_backward(f, c->cfg.width, c->cfg.height,
+                                                     reinterpret_cast<const float4*>(bw->grad), bw->targets,
+                                                     c->capture_stream);
+            if (eb != cudaSuccess) st = cuda_fail(c, eb, "resolve backward");
+        }
         c->capturing = false;
         cudaGraph_t g = nullptr;
         e = cudaStreamEndCapture(c->capture_stream, &g);
@@ -564,6 +617,7 @@ lh_status lh_frame_graph(lh_ctx* c, const Uniforms* u, const Uniforms* probes, u
         c->graph_probes = n_probes;
         c->graph_instances = n_inst;
         c->graph_tuning = c->tuning;
+        c->graph_backward = want;
     }
     if ((st = upload_frame_constants(c, u, probes, n_probes, s)) != LH_OK) return st;
     e = cudaGraphLaunch(c->graph_exec, s);
@@ -571,6 +625,28 @@ lh_status lh_frame_graph(lh_ctx* c, const Uniforms* u, const Uniforms* probes, u
     c->last_stream = s;
     if (out) fill_out(c, out);
     return LH_OK;
+}
+
+}  // namespace
+
+lh_status lh_frame_graph(lh_ctx* c, const Uniforms* u, const Uniforms* probes, uint32_t n_probes, void* stream,
+                         lh_frame_out* out) {
+    return frame_graph_impl(c, u, probes, n_probes, nullptr, stream, out);
+}
+
+lh_status lh_frame_graph_backward(lh_ctx* c, const Uniforms* u, const Uniforms* probes, uint32_t n_probes,
+                                  uint64_t d_grad_hdr, const lh_grad_targets* targets, void* stream,
+                                  lh_frame_out* out) {
+    lh_status st = check_ctx(c);
+    if (st != LH_OK) return st;
+    if (!d_grad_hdr || !targets) return fail(c, LH_ERR_INVALID_ARGUMENT, "null gradient or targets");
+    if ((d_grad_hdr & 15) || (targets->instance_grads & 7) || (targets->texture_grads & 7) ||
+        (targets->light_dir & 3) || (targets->light_color & 3))
+        return fail(c, LH_ERR_INVALID_ARGUMENT, "misaligned gradient buffer");
+    GraphBackward bw{};
+    bw.grad = d_grad_hdr;
+    bw.targets = *targets;
+    return frame_graph_impl(c, u, probes, n_probes, &bw, stream, out);
 }
 
 lh_status lh_get_outputs(lh_ctx* c, lh_frame_out* out) {
@@ -672,7 +748,7 @@ void lh_destroy(lh_ctx* c) {
 lh_status lh_set_tuning(lh_ctx* c, const lh_tuning* t) {
     if (!c || !t) return LH_ERR_INVALID_ARGUMENT;
     if (t->small_px > 4096 || t->medium_px < t->small_px || !(t->cull_blocks_per_sm > 0.0f) ||
-        t->cull_blocks_per_sm > 64.0f || t->schedule > LH_SCHEDULE_PER_VIEW)
+        t->cull_blocks_per_sm > 64.0f || t->schedule > LH_SCHEDULE_PER_VIEW || t->raster_batch > 64)
         return LH_ERR_INVALID_ARGUMENT;
     c->tuning = *t;
     return LH_OK;

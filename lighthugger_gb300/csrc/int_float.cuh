@@ -1,11 +1,13 @@
-// Integer -> float conversions that stay on the integer and FP32 pipes.
+// Integer -> float conversions for the rasteriser's edge functions.
 //
-// The 64-bit integer conversion instructions execute on the FP64 unit, which
-// GB300 keeps narrow; the rasteriser converts two edge functions per covered
-// fragment.  These routines return exactly what the round-to-nearest-even
-// conversions return (__int2float_rn / __ll2float_rn, and static_cast<float>
-// on the host), so depths stay bit exact.  Host-compilable for the CPU check
-// in tests/native.
+// Two edge functions are converted per covered fragment.  Small values (the
+// common case: fragments of small triangles) go through the significand of
+// 1.5 * 2^23 -- one integer add and one float subtract -- instead of a
+// conversion instruction.  Every routine returns exactly what the
+// round-to-nearest-even conversion returns (__int2float_rn / __ll2float_rn,
+// static_cast<float> on the host), so depths stay bit exact.  i64_to_f32_rn
+// is the integer-only 64-bit conversion; host-compilable for the CPU check in
+// tests/native.
 #pragma once
 
 #include <cstdint>
@@ -64,7 +66,11 @@ LH_IF_HD float i64_to_f32_rn(int64_t v) {
 // integer add and one float subtract), the rest take the general routine.
 LH_IF_HD float i32_to_f32_rn(int32_t v) {
     if (v > -(1 << 22) && v < (1 << 22)) return bits_to_float(0x4B400000u + (uint32_t)v) - 12582912.0f;
+#if defined(__CUDA_ARCH__)
+    return __int2float_rn(v);
+#else
     return i64_to_f32_rn((int64_t)v);
+#endif
 }
 
 }  // namespace lh

@@ -239,6 +239,26 @@ __device__ __forceinline__ int64_t cross3(const SnapV& a, const SnapV& b, const 
            ((int64_t)c.X * a.Y - (int64_t)a.X * c.Y);
 }
 
+// Twice the signed area (= cross3) from vertex differences: 32-bit products
+// when every difference is below 2^15 in magnitude.
+__device__ __forceinline__ int64_t cross_rel(const SnapV& a, const SnapV& b, const SnapV& c) {
+    const int32_t ux = b.X - a.X, uy = b.Y - a.Y, vx = c.X - a.X, vy = c.Y - a.Y;
+    if ((uint32_t)(ux + 0x7FFF) < 0xFFFFu && (uint32_t)(uy + 0x7FFF) < 0xFFFFu && (uint32_t)(vx + 0x7FFF) < 0xFFFFu &&
+        (uint32_t)(vy + 0x7FFF) < 0xFFFFu)
+        return (int64_t)(ux * vy - vx * uy);
+    return (int64_t)ux * vy - (int64_t)vx * uy;
+}
+
+// Whether the triangle's bounding box holds a pixel centre of the W x H
+// target (the bbox rule of make_setup); false means no coverage at all.
+__device__ __forceinline__ bool covers_centre(const SnapV& v0, const SnapV& v1, const SnapV& v2, uint32_t W,
+                                              uint32_t H) {
+    const int32_t minX = min(v0.X, min(v1.X, v2.X)), maxX = max(v0.X, max(v1.X, v2.X));
+    const int32_t minY = min(v0.Y, min(v1.Y, v2.Y)), maxY = max(v0.Y, max(v1.Y, v2.Y));
+    return max((minX + 127) >> 8, 0) <= min((maxX - 128) >> 8, (int32_t)W - 1) &&
+           max((minY + 127) >> 8, 0) <= min((maxY - 128) >> 8, (int32_t)H - 1);
+}
+
 // Triangle ready for coverage: orientation normalised (interior has every
 // edge function >= 0), bias 1 for edges that are not top-left.
 struct TriSetup {
@@ -247,8 +267,11 @@ struct TriSetup {
     uint32_t id;
     int32_t px0, py0, px1, py1;
     uint32_t bias;  // bit0 edge12, bit1 edge20, bit2 edge01 not top-left;
-                    // bit3: every edge product in the bbox fits 32 bits
+                    // bit3: every edge product in the bbox fits 32 bits;
+                    // bit4 (kBiasAlpha): alpha-tested
+    uint32_t verts;  // alpha-tested: meshlet vertices m0 | m1 << 8 | m2 << 16
 };
+constexpr uint32_t kBiasAlpha = 16u;
 
 __device__ __forceinline__ bool top_left(int32_t ax, int32_t ay, int32_t bx, int32_t by) {
     int32_t dy = by - ay, dx = bx - ax;
@@ -269,7 +292,7 @@ __device__ __forceinline__ bool make_setup(SnapV v0, SnapV v1, SnapV v2, uint32_
     t.py1 = min((maxY - 128) >> 8, (int32_t)H - 1);
     if (t.px0 > t.px1 || t.py0 > t.py1) return false;
     t.X0 = v0.X; t.Y0 = v0.Y; t.X1 = v1.X; t.Y1 = v1.Y; t.X2 = v2.X; t.Y2 = v2.Y;
-    float fA = i64_to_f32_rn(A);
+    float fA = __ll2float_rn(A);
     t.z0 = v0.z;
     t.s1 = (v1.z - v0.z) / fA;
     t.s2 = (v2.z - v0.z) / fA;
@@ -280,6 +303,21 @@ __device__ __forceinline__ bool make_setup(SnapV v0, SnapV v1, SnapV v2, uint32_
     // product of an edge function is at most ext_x * ext_y in magnitude
     if ((int64_t)(maxX - minX) * (int64_t)(maxY - minY) < (1ll << 30)) t.bias |= 8u;
     return true;
+}
+
+// An edge function value as float (round to nearest even): the 32-bit route
+// when it fits, else the conversion instruction (LH_EDGE_CONV=2: the
+// integer-only routine; same bits either way).
+#ifndef LH_EDGE_CONV
+#define LH_EDGE_CONV 1
+#endif
+__device__ __forceinline__ float edge_to_float(int64_t e) {
+    if (e == (int64_t)(int32_t)e) return i32_to_f32_rn((int32_t)e);
+#if LH_EDGE_CONV == 2
+    return i64_to_f32_rn(e);
+#else
+    return __ll2float_rn(e);
+#endif
 }
 
 // Coverage + depth of pixel (px, py); returns false when not covered.
@@ -303,8 +341,8 @@ __device__ __forceinline__ bool cover(const TriSetup& t, int32_t px, int32_t py,
         if (e12 < (int64_t)(t.bias & 1u) || e20 < (int64_t)((t.bias >> 1) & 1u) ||
             e01 < (int64_t)((t.bias >> 2) & 1u))
             return false;
-        f20 = i64_to_f32_rn(e20);
-        f01 = i64_to_f32_rn(e01);
+        f20 = edge_to_float(e20);
+        f01 = edge_to_float(e01);
     }
     float d = (t.z0 + f20 * t.s1) + f01 * t.s2;
     d = d > 0.0f ? d : 0.0f;

@@ -1,6 +1,7 @@
 // Device-visible frame description shared by the kernels and the C ABI.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -105,13 +106,17 @@ cudaError_t launch_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint32_
 // Raster all views [view_begin, view_begin + n_views) of one kind (kViewVisibility
 // or kViewShadow): main kernel, clipper, band kernel.
 cudaError_t launch_raster_kind(const FrameDev& f, uint32_t view_begin, uint32_t n_views, int kind, uint32_t small_px,
-                               uint32_t medium_px, cudaStream_t s, int sms);
+                               uint32_t medium_px, uint32_t raster_batch, cudaStream_t s, int sms);
 cudaError_t launch_depth_reduce_fit(const FrameDev& f, cudaStream_t s, int sms);
 // Clear + cull + raster of every view in one cooperative persistent launch.
 cudaError_t launch_frame_persistent(const FrameDev& f, uint32_t n_persp, uint32_t small_px, uint32_t medium_px,
+                                    uint32_t raster_batch,
                                     float blocks_per_sm, cudaStream_t s, int sms);
 int persistent_blocks_per_sm();
-cudaError_t launch_resolve(const FrameDev& f, uint32_t width, uint32_t height, cudaStream_t s);
+// vis_map: 2D tensor map of the main visibility buffer (u64, box 32 x 8) for
+// the TMA-staged resolve, or null for per-thread loads.
+cudaError_t launch_resolve(const FrameDev& f, uint32_t width, uint32_t height, const CUtensorMap* vis_map,
+                           cudaStream_t s, int sms);
 cudaError_t launch_resolve_backward(const FrameDev& f, uint32_t width, uint32_t height, const float4* grad,
                                     const lh_grad_targets& t, cudaStream_t s);
 cudaError_t launch_sum_meshlets(const Instance* instances, uint32_t n, unsigned long long* out, cudaStream_t s);

@@ -114,12 +114,13 @@ int persistent_blocks_per_sm() {
 }
 
 cudaError_t launch_frame_persistent(const FrameDev& f, uint32_t n_persp, uint32_t small_px, uint32_t medium_px,
+                                    uint32_t raster_batch,
                                     float blocks_per_sm, cudaStream_t s, int sms) {
     const int resident = persistent_blocks_per_sm();
     if (resident <= 0) return cudaErrorCooperativeLaunchTooLarge;
     (void)blocks_per_sm;
     const int per_sm = resident;  // every resident slot: the raster phases need the occupancy
-    RasterTune tune{small_px, medium_px};
+    RasterTune tune{small_px, medium_px, raster_batch};
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(sms * per_sm));
     cfg.blockDim = dim3(kPersistentThreads);

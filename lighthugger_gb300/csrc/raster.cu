@@ -17,17 +17,17 @@ __global__ void __launch_bounds__(128) k_raster_clip(FrameDev f) {
 }
 
 template <int KIND>
-__global__ void __launch_bounds__(256) k_raster_big(FrameDev f) {
+__global__ void __launch_bounds__(256, 4) k_raster_big(FrameDev f) {
     phase_raster_big<KIND>(f);
 }
 
 }  // namespace
 
 cudaError_t launch_raster_kind(const FrameDev& f, uint32_t view_begin, uint32_t n_views, int kind, uint32_t small_px,
-                               uint32_t medium_px, cudaStream_t s, int sms) {
+                               uint32_t medium_px, uint32_t raster_batch, cudaStream_t s, int sms) {
     if (n_views == 0) return cudaSuccess;
     if (n_views > kMaxViews) return cudaErrorInvalidValue;
-    RasterTune tune{small_px, medium_px};
+    RasterTune tune{small_px, medium_px, raster_batch};
     // raster words: clip count, claims, reduce counter, packed big-triangle word
     cudaError_t e = cudaMemsetAsync(f.status + kStClipCount, 0, sizeof(uint32_t) * (kStBigPacked + 2 - kStClipCount), s);
     if (e != cudaSuccess) return e;

@@ -6,7 +6,11 @@
 // shadowmap_opaque_vertex (rasterization.glsl:101-111) with depth LESS /
 // clear 1 / front-face culling (pipelines.cpp:15-19,73-77,257-270), driven
 // by drawIndirectCount over the draw lists (src/rendering.cpp:197-266,
-// 325-438).  Alpha-clip draws are rasterised as opaque (no alpha test).
+// 325-438).  Alpha-clip draws (visbuffer_alpha_clip_vertex/pixel and
+// shadowmap_alpha_clip*, rasterization.glsl:60-97,113-145) are double sided
+// (pipelines.cpp:272-285,302-315) and alpha tested per fragment: the base
+// texture's alpha, sampled bilinearly at the perspective-correct uv of the
+// pixel centre, must not be below 0.5.
 //
 // Layout of the work:
 //  k_raster       one warp per visible meshlet (claimed dynamically across
@@ -37,6 +41,7 @@ constexpr int kRasterWarps = 8;
 struct RasterTune {
     uint32_t small_px;   // lane path up to this many bbox pixels
     uint32_t medium_px;  // warp path up to this many; larger: band queue
+    uint32_t batch;      // meshlets claimed per atomic (0: automatic)
 };
 
 __device__ __forceinline__ const lh_mat4& view_matrix(const FrameDev& f, const ViewDev* vw) {
@@ -57,6 +62,127 @@ __device__ __forceinline__ MeshInfoRaster load_mesh_info_raster(const MeshInfo* 
     r.meshlets = __ldg(w + 5);
     r.flags = (uint32_t)((__ldg(w + 6) >> 16) & 0xFFu);
     return r;
+}
+
+// ------------------------------------------------------------ alpha clip
+// One vertex of an alpha-tested triangle: clip x, y, w and the uv the
+// reference's vertex shader forms (uv * texture_scale + texture_offset).
+struct AlphaVert {
+    float x, y, w, u, v;
+};
+
+// Fields of a MeshInfo the alpha test needs.
+struct MeshInfoAlpha {
+    uint64_t uvs;
+    float ts_x, ts_y, to_x, to_y;
+    uint32_t tex;
+};
+__device__ __forceinline__ MeshInfoAlpha load_mesh_info_alpha(const MeshInfo* mi) {
+    MeshInfoAlpha r;
+    r.uvs = __ldg(&mi->uvs);
+    r.ts_x = __ldg(&mi->texture_scale.x);
+    r.ts_y = __ldg(&mi->texture_scale.y);
+    r.to_x = __ldg(&mi->texture_offset.x);
+    r.to_y = __ldg(&mi->texture_offset.y);
+    r.tex = __ldg(&mi->base_color_texture_index);
+    return r;
+}
+__device__ __forceinline__ AlphaVert alpha_vert(f4 c, const MeshInfoAlpha& ma, uint32_t flags, uint32_t index) {
+    const f2 uv = load_uv_raw(ma.uvs, flags, index);
+    return AlphaVert{c.x, c.y, c.w, uv.x * ma.ts_x + ma.to_x, uv.y * ma.ts_y + ma.to_y};
+}
+
+// 2D homogeneous edge functions of the unclipped triangle (Olano and Greer,
+// "Triangle scan conversion using 2D homogeneous coordinates", 1997):
+// E_k(nx, ny) = a_k nx + b_k ny + c_k with (a_k, b_k, c_k) = v_i x v_j for
+// (i, j) = (1, 2), (2, 0), (0, 1) over v = (x, y, w); the perspective-correct
+// barycentrics are E_k / (E_0 + E_1 + E_2), for clipped triangles too.
+struct AlphaTri {
+    float a[3], b[3], c[3];
+    float u[3], v[3];
+    uint32_t tex;
+};
+__device__ __forceinline__ void alpha_edge(const AlphaVert& p, const AlphaVert& q, float& a, float& b, float& c) {
+    a = p.y * q.w - q.y * p.w;
+    b = p.w * q.x - q.w * p.x;
+    c = p.x * q.y - q.x * p.y;
+}
+__device__ __forceinline__ AlphaTri alpha_setup(const AlphaVert& v0, const AlphaVert& v1, const AlphaVert& v2,
+                                                uint32_t tex) {
+    AlphaTri t;
+    alpha_edge(v1, v2, t.a[0], t.b[0], t.c[0]);
+    alpha_edge(v2, v0, t.a[1], t.b[1], t.c[1]);
+    alpha_edge(v0, v1, t.a[2], t.b[2], t.c[2]);
+    t.u[0] = v0.u;
+    t.u[1] = v1.u;
+    t.u[2] = v2.u;
+    t.v[0] = v0.v;
+    t.v[1] = v1.v;
+    t.v[2] = v2.v;
+    t.tex = tex;
+    return t;
+}
+
+// Alpha of the bilinear, repeat-addressed sample of texture `index` at uv.
+__device__ __forceinline__ float sample_alpha(const FrameDev& f, uint32_t index, float uvx, float uvy) {
+    if (index >= f.n_textures) return 0.0f;
+    const lh_texture t = f.textures[index];
+    const uchar4* tex = reinterpret_cast<const uchar4*>(t.texels);
+    float u = uvx * (float)t.width - 0.5f, v = uvy * (float)t.height - 0.5f;
+    if (!(fabsf(u) < 1e9f)) u = 0.0f;
+    if (!(fabsf(v) < 1e9f)) v = 0.0f;
+    const float fu = floorf(u), fv = floorf(v);
+    const float a = u - fu, b = v - fv;
+    const int32_t i0 = (int32_t)fu, j0 = (int32_t)fv, W = (int32_t)t.width, H = (int32_t)t.height;
+    const int32_t ia = wrap_texel(i0, W), ib = wrap_texel(i0 + 1, W), ja = wrap_texel(j0, H), jb = wrap_texel(j0 + 1, H);
+    auto al = [&](int32_t i, int32_t j) { return (float)__ldg(tex + ((size_t)j * W + i)).w / 255.0f; };
+    const float t00 = al(ia, ja), t10 = al(ib, ja), t01 = al(ia, jb), t11 = al(ib, jb);
+    const float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+    return ((t00 * w00 + t10 * w10) + t01 * w01) + t11 * w11;
+}
+
+// True when the fragment at pixel (px, py) of a W x H target survives.
+__device__ __forceinline__ bool alpha_pass(const FrameDev& f, const AlphaTri& t, int32_t px, int32_t py, uint32_t W,
+                                           uint32_t H) {
+    const float nx = (((float)px + 0.5f) / (float)W) * 2.0f - 1.0f;
+    const float ny = (((float)py + 0.5f) / (float)H) * 2.0f - 1.0f;
+    const float e0 = (t.a[0] * nx + t.b[0] * ny) + t.c[0];
+    const float e1 = (t.a[1] * nx + t.b[1] * ny) + t.c[1];
+    const float e2 = (t.a[2] * nx + t.b[2] * ny) + t.c[2];
+    const float sum = (e0 + e1) + e2;
+    const float l0 = e0 / sum, l1 = e1 / sum, l2 = e2 / sum;
+    const float u = (l0 * t.u[0] + l1 * t.u[1]) + l2 * t.u[2];
+    const float v = (l0 * t.v[0] + l1 * t.v[1]) + l2 * t.v[2];
+    return !(sample_alpha(f, t.tex, u, v) < 0.5f);
+}
+
+// The alpha set-up of triangle `id` (packed tri / draw slot) of view
+// `view`, from the scene buffers (the band and clip paths).
+__device__ AlphaTri alpha_tri_global(const FrameDev& f, uint32_t view, uint32_t id) {
+    const ViewDev* vw = f.views + view;
+    const uint32_t slot = id & ((1u << 24) - 1u), tri = id >> 24;
+    const MeshletReference ref = vw->refs[slot];
+    const Instance* inst = f.instances + ref.instance_index;
+    lh_mat4 transform;
+    const float4* src = reinterpret_cast<const float4*>(inst);
+    float4* dst = reinterpret_cast<float4*>(&transform);
+    for (int i = 0; i < 4; i++) dst[i] = __ldg(src + i);
+    const MeshInfo* mip = mesh_info_of(inst);
+    const MeshInfoRaster mi = load_mesh_info_raster(mip);
+    const MeshInfoAlpha ma = load_mesh_info_alpha(mip);
+    const Meshlet* ml = reinterpret_cast<const Meshlet*>(mi.meshlets) + ref.meshlet_index;
+    const uint32_t tri_off = __ldg(&ml->triangle_offset), idx_off = __ldg(&ml->index_offset);
+    const uint8_t* micro = reinterpret_cast<const uint8_t*>(mi.micro_indices) + tri_off + tri * 3;
+    const lh_mat4& vp = view_matrix(f, vw);
+    AlphaVert av[3];
+    for (int k = 0; k < 3; k++) {
+        const uint32_t idx = (mi.flags & MESH_INFO_FLAGS_32_BIT_INDICES)
+                                 ? __ldg(reinterpret_cast<const uint32_t*>(mi.indices) + idx_off + __ldg(micro + k))
+                                 : __ldg(reinterpret_cast<const uint16_t*>(mi.indices) + idx_off + __ldg(micro + k));
+        const f3 w = world_pos(transform, load_position(mi.positions, mi.flags, idx));
+        av[k] = alpha_vert(mul(vp, f4{w.x, w.y, w.z, 1.0f}), ma, mi.flags, idx);
+    }
+    return alpha_setup(av[0], av[1], av[2], ma.tex);
 }
 __device__ __forceinline__ uint32_t load_index_raw(uint64_t indices, uint32_t flags, uint32_t i) {
     if (flags & MESH_INFO_FLAGS_32_BIT_INDICES) return __ldg(reinterpret_cast<const uint32_t*>(indices) + i);
@@ -99,6 +225,19 @@ __device__ void push_big(const FrameDev& f, const TriSetup& t, uint32_t view) {
     f.big_base[idx] = (uint32_t)base;
 }
 
+// Where a warp's alpha-tested triangles find their vertices: the warp's
+// shared AlphaVert array (indexed by TriSetup::verts) and the meshlet's
+// base texture.
+struct AlphaSrc {
+    const AlphaVert* av;
+    uint32_t tex;
+    uint32_t H;
+};
+
+__device__ __forceinline__ AlphaTri alpha_of(const TriSetup& t, const AlphaSrc& as) {
+    return alpha_setup(as.av[t.verts & 0xFFu], as.av[(t.verts >> 8) & 0xFFu], as.av[(t.verts >> 16) & 0xFFu], as.tex);
+}
+
 template <int KIND>
 __device__ __forceinline__ void raster_lane(const TriSetup& t, void* target, uint32_t W) {
     for (int32_t py = t.py0; py <= t.py1; py++)
@@ -125,6 +264,39 @@ __device__ __forceinline__ void raster_warp(const TriSetup& t, void* target, uin
     }
 }
 
+// The alpha-tested variants are not inlined: their set-up and sampling
+// state stays out of the register allocation of the opaque paths (the
+// launch bounds cap the whole call tree; alpha triangles are the rare case).
+template <int KIND>
+__device__ __noinline__ void raster_lane_alpha(const FrameDev& f, const TriSetup& t, void* target, uint32_t W,
+                                               const AlphaSrc& as) {
+    const AlphaTri at = alpha_of(t, as);
+    for (int32_t py = t.py0; py <= t.py1; py++)
+        for (int32_t px = t.px0; px <= t.px1; px++) {
+            float d;
+            if (cover(t, px, py, d) && alpha_pass(f, at, px, py, W, as.H))
+                write_fragment<KIND>(target, W, px, py, d, t.id);
+        }
+}
+
+template <int KIND>
+__device__ __noinline__ void raster_warp_alpha(const FrameDev& f, const TriSetup& t, void* target, uint32_t W,
+                                               uint32_t lane, const AlphaSrc& as) {
+    const uint32_t w = (uint32_t)(t.px1 - t.px0 + 1);
+    const uint32_t npx = w * (uint32_t)(t.py1 - t.py0 + 1);
+    const float inv_w = 1.0f / (float)w;
+    const AlphaTri at = alpha_of(t, as);
+    for (uint32_t p = lane; p < npx; p += 32) {
+        int32_t ry = (int32_t)(((float)p + 0.5f) * inv_w);
+        int32_t rx = (int32_t)p - ry * (int32_t)w;
+        if (rx < 0) { ry--; rx += (int32_t)w; }
+        else if (rx >= (int32_t)w) { ry++; rx -= (int32_t)w; }
+        int32_t px = t.px0 + rx, py = t.py0 + ry;
+        float d;
+        if (cover(t, px, py, d) && alpha_pass(f, at, px, py, W, as.H)) write_fragment<KIND>(target, W, px, py, d, t.id);
+    }
+}
+
 __device__ __forceinline__ TriSetup shfl_setup(const TriSetup& s, int src) {
     TriSetup r;
     const uint32_t* a = reinterpret_cast<const uint32_t*>(&s);
@@ -145,6 +317,7 @@ __device__ void phase_raster(const FrameDev& f, uint32_t view_begin, uint32_t n_
     __shared__ SnapV s_v[kRasterWarps][MAX_MESHLET_UNIQUE_VERTICES];
     __shared__ uint8_t s_oc[kRasterWarps][MAX_MESHLET_UNIQUE_VERTICES];
     __shared__ uint32_t s_micro[kRasterWarps][(MAX_MESHLET_TRIANGLES * 3 + 3) / 4];
+    __shared__ AlphaVert s_av[kRasterWarps][MAX_MESHLET_UNIQUE_VERTICES];
     const uint32_t md = f.max_draws;
     if (threadIdx.x == 0) {
         uint32_t run = 0;
@@ -167,11 +340,27 @@ __device__ void phase_raster(const FrameDev& f, uint32_t view_begin, uint32_t n_
     SnapV* sv = s_v[warp];
     uint8_t* so = s_oc[warp];
     const uint8_t* mic = reinterpret_cast<const uint8_t*>(s_micro[warp]);
+    // Work units: a meshlet, or a quarter of its triangles when the views
+    // hold fewer than two meshlets per warp of the grid (shadow cascades).
+    // Units are claimed `batch` per atomic: one keeps consecutive (nearby)
+    // meshlets on different warps; with millions of units (many views) the
+    // claim word itself becomes the contended address and 4 pays.
+    const uint32_t warps_total = gridDim.x * (blockDim.x >> 5);
+    const uint32_t split = total < 2u * warps_total ? 4u : 1u;
+    const uint32_t units = total * split;
+    const uint32_t batch = tune.batch ? tune.batch : (units > 256u * warps_total ? 4u : 1u);
+    uint32_t unit = 0, unit_end = 0;
     for (;;) {
-        uint32_t item = 0;
-        if (lane == 0) item = atomicAdd(claim_word, 1u);
-        item = __shfl_sync(0xFFFFFFFFu, item, 0);
-        if (item >= total) break;
+        if (unit == unit_end) {
+            uint32_t first = 0;
+            if (lane == 0) first = atomicAdd(claim_word, batch);
+            first = __shfl_sync(0xFFFFFFFFu, first, 0);
+            if (first >= units) break;
+            unit = first;
+            unit_end = min(first + batch, units);
+        }
+        const uint32_t item = unit / split, part = unit % split;
+        unit++;
         uint32_t v = 0;
         while (item >= s_prefix[v + 1]) v++;
         const uint32_t view = view_begin + v;
@@ -191,8 +380,16 @@ __device__ void phase_raster(const FrameDev& f, uint32_t view_begin, uint32_t n_
         const uint32_t nv = mb.m.index_count, nt = mb.m.triangle_count;
         if (nv > MAX_MESHLET_UNIQUE_VERTICES || nt > MAX_MESHLET_TRIANGLES) {
             // beyond the meshletiser limits: malformed, skipped and flagged
-            if (lane == 0) atomicOr(&f.status[kStFlags], LH_FLAG_BAD_MESHLET);
+            if (lane == 0 && part == 0) atomicOr(&f.status[kStFlags], LH_FLAG_BAD_MESHLET);
             continue;
+        }
+        if (part * 32u >= nt) continue;  // this quarter holds no triangles
+        const bool alpha = slot >= md;  // the alpha-clip draw class
+        AlphaSrc as{s_av[warp], 0u, H};
+        MeshInfoAlpha ma{};
+        if (alpha) {
+            ma = load_mesh_info_alpha(mesh_info_of(inst));
+            as.tex = ma.tex;
         }
         for (uint32_t j = lane; j < nv; j += 32) {
             uint32_t idx = load_index_raw(mi.indices, mi.flags, mb.m.index_offset + j);
@@ -203,6 +400,7 @@ __device__ void phase_raster(const FrameDev& f, uint32_t view_begin, uint32_t n_
             if (!oc) s = snap(c, hw, hh);
             sv[j] = s;
             so[j] = (uint8_t)oc;
+            if (alpha) s_av[warp][j] = alpha_vert(c, ma, mi.flags, idx);
         }
         const uint64_t mbase = mi.micro_indices + mb.m.triangle_offset;
         const uint32_t nbytes = nt * 3;
@@ -214,7 +412,7 @@ __device__ void phase_raster(const FrameDev& f, uint32_t view_begin, uint32_t n_
             for (uint32_t j = lane; j < nbytes; j += 32) d[j] = __ldg(reinterpret_cast<const uint8_t*>(mbase) + j);
         }
         __syncwarp();
-        for (uint32_t base = 0; base < nt; base += 32) {
+        for (uint32_t base = part * 32u; base < nt; base += 32u * split) {
             const uint32_t t = base + lane;
             bool medium = false;
             TriSetup st;
@@ -232,13 +430,30 @@ __device__ void phase_raster(const FrameDev& f, uint32_t view_begin, uint32_t n_
                         else atomicOr(&f.status[kStFlags], LH_FLAG_QUEUE_OVERFLOW);
                     } else {
                         SnapV a = sv[m0], b = sv[m1], c = sv[m2];
+                        // most visible triangles hold no pixel centre: the
+                        // 32-bit bbox test rejects them before the area
+#ifndef LH_RASTER_BBOX_FIRST
+#define LH_RASTER_BBOX_FIRST 1
+#endif
+#if LH_RASTER_BBOX_FIRST
+                        int64_t cr = covers_centre(a, b, c, W, H) ? cross_rel(a, b, c) : 0;
+#else
                         int64_t cr = cross3(a, b, c);
-                        bool keep = KIND == 0 ? cr < 0 : cr > 0;
+#endif
+                        // alpha clip is double sided
+                        bool keep = alpha ? cr != 0 : (KIND == 0 ? cr < 0 : cr > 0);
                         if (keep) {
                             if (cr > 0) { SnapV tmp = b; b = c; c = tmp; }
                             if (make_setup(a, b, c, LH_PACK_ID(t, slot), W, H, st)) {
+                                if (alpha) {
+                                    st.bias |= kBiasAlpha;
+                                    st.verts = m0 | (m1 << 8) | (m2 << 16);
+                                }
                                 uint32_t npx = (uint32_t)(st.px1 - st.px0 + 1) * (uint32_t)(st.py1 - st.py0 + 1);
-                                if (npx <= tune.small_px) raster_lane<KIND>(st, target, W);
+                                if (npx <= tune.small_px) {
+                                    if (alpha) raster_lane_alpha<KIND>(f, st, target, W, as);
+                                    else raster_lane<KIND>(st, target, W);
+                                }
                                 else if (npx <= tune.medium_px) medium = true;
                                 else push_big(f, st, view);
                             }
@@ -251,12 +466,12 @@ __device__ void phase_raster(const FrameDev& f, uint32_t view_begin, uint32_t n_
                 int src = __ffs(mask) - 1;
                 mask &= mask - 1;
                 TriSetup b = shfl_setup(st, src);
-                raster_warp<KIND>(b, target, W, lane);
+                if (b.bias & kBiasAlpha) raster_warp_alpha<KIND>(f, b, target, W, lane, as);
+                else raster_warp<KIND>(b, target, W, lane);
             }
         }
         __syncwarp();
     }
-    __syncthreads();
 }
 
 // Sutherland-Hodgman against w-z, z, g*w-x, g*w+x, g*w-y, g*w+y >= 0.
@@ -304,6 +519,7 @@ __device__ void phase_raster_clip(const FrameDev& f, uint32_t gtid, uint32_t gst
         load_meshlet(reinterpret_cast<const Meshlet*>(mi.meshlets) + ref.meshlet_index, mb);
         const lh_mat4& vp = view_matrix(f, vw);
         const uint8_t* micro = reinterpret_cast<const uint8_t*>(mi.micro_indices) + mb.m.triangle_offset + it.tri * 3;
+        const bool alpha = it.slot >= f.max_draws;  // alpha clip: double sided, alpha tested
         f4 poly[9];
         for (int k = 0; k < 3; k++) {
             uint32_t idx = load_index_raw(mi.indices, mi.flags, mb.m.index_offset + micro[k]);
@@ -325,8 +541,8 @@ __device__ void phase_raster_clip(const FrameDev& f, uint32_t gtid, uint32_t gst
             pc += (int64_t)a.X * b.Y - (int64_t)b.X * a.Y;
         }
         if (pc == 0) continue;
-        if (KIND == 0 && pc > 0) continue;
-        if (KIND == 1 && pc < 0) continue;
+        if (!alpha && KIND == 0 && pc > 0) continue;
+        if (!alpha && KIND == 1 && pc < 0) continue;
         const uint32_t id = LH_PACK_ID(it.tri, it.slot);
         for (int k = 1; k + 1 < np; k++) {
             SnapV a = s[0], b = s[k], c = s[k + 1];
@@ -334,7 +550,10 @@ __device__ void phase_raster_clip(const FrameDev& f, uint32_t gtid, uint32_t gst
             if (tc == 0 || ((tc < 0) != (pc < 0))) continue;
             if (tc > 0) { SnapV tmp = b; b = c; c = tmp; }
             TriSetup st;
-            if (make_setup(a, b, c, id, W, H, st)) push_big(f, st, it.view);
+            if (make_setup(a, b, c, id, W, H, st)) {
+                if (alpha) st.bias |= kBiasAlpha;
+                push_big(f, st, it.view);
+            }
         }
     }
 }
@@ -350,6 +569,27 @@ __device__ __forceinline__ bool edge_rejects(int32_t ax, int32_t ay, int32_t bx,
                                              int32_t y0, int32_t y1, int64_t bias) {
     return edge_at(ax, ay, bx, by, x0, y0) < bias && edge_at(ax, ay, bx, by, x1, y0) < bias &&
            edge_at(ax, ay, bx, by, x0, y1) < bias && edge_at(ax, ay, bx, by, x1, y1) < bias;
+}
+
+// The pixels [x0, x1] x [y0, y1] of an alpha-tested big triangle, one
+// column per lane (not inlined, as the other alpha paths).
+template <int KIND>
+__device__ __noinline__ void raster_chunk_alpha(const FrameDev& f, const BigTri& b, int32_t x0, int32_t x1, int32_t y0,
+                                                int32_t y1, uint32_t lane) {
+    const ViewDev* vw = f.views + b.view;
+    void* target = vw->target;
+    const uint32_t W = vw->width, H = vw->height;
+    const AlphaTri at = alpha_tri_global(f, b.view, b.id);
+    TriSetup t;
+    t.X0 = b.X0; t.Y0 = b.Y0; t.X1 = b.X1; t.Y1 = b.Y1; t.X2 = b.X2; t.Y2 = b.Y2;
+    t.z0 = b.z0; t.s1 = b.s1; t.s2 = b.s2;
+    t.id = b.id;
+    t.bias = b.bias;
+    for (int32_t py = y0; py <= y1; py++)
+        for (int32_t px = x0 + (int32_t)lane; px <= x1; px += 32) {
+            float d;
+            if (cover(t, px, py, d) && alpha_pass(f, at, px, py, W, H)) write_fragment<KIND>(target, W, px, py, d, t.id);
+        }
 }
 
 // One warp per 16 x 64-pixel chunk of a big triangle; chunks whose
@@ -388,19 +628,29 @@ __device__ void phase_raster_big(const FrameDev& f) {
             edge_rejects(b.X2, b.Y2, b.X0, b.Y0, x0, x1, y0, y1, (b.bias >> 1) & 1u) ||
             edge_rejects(b.X0, b.Y0, b.X1, b.Y1, x0, x1, y0, y1, (b.bias >> 2) & 1u))
             continue;
-        TriSetup t;
-        t.X0 = b.X0; t.Y0 = b.Y0; t.X1 = b.X1; t.Y1 = b.Y1; t.X2 = b.X2; t.Y2 = b.Y2;
-        t.z0 = b.z0; t.s1 = b.s1; t.s2 = b.s2;
-        t.id = b.id;
-        t.bias = b.bias;
         const ViewDev* vw = f.views + b.view;
         void* target = vw->target;
         const uint32_t W = vw->width;
-        for (int32_t py = y0; py <= y1; py++)
-            for (int32_t px = x0 + (int32_t)lane; px <= x1; px += 32) {
-                float d;
-                if (cover(t, px, py, d)) write_fragment<KIND>(target, W, px, py, d, t.id);
+        if (b.bias & kBiasAlpha) {
+            raster_chunk_alpha<KIND>(f, b, x0, x1, y0, y1, lane);
+            continue;
+        }
+        // edge functions at the top of the lane's column, then one add per
+        // row (the same integers cover() forms, so the same coverage/depth)
+        const int64_t d12 = -(int64_t)(b.X2 - b.X1) * 256, d20 = -(int64_t)(b.X0 - b.X2) * 256,
+                      d01 = -(int64_t)(b.X1 - b.X0) * 256;
+        const int64_t b12 = b.bias & 1u, b20 = (b.bias >> 1) & 1u, b01 = (b.bias >> 2) & 1u;
+        for (int32_t px = x0 + (int32_t)lane; px <= x1; px += 32) {
+            int64_t e12 = edge_at(b.X1, b.Y1, b.X2, b.Y2, px, y0), e20 = edge_at(b.X2, b.Y2, b.X0, b.Y0, px, y0),
+                    e01 = edge_at(b.X0, b.Y0, b.X1, b.Y1, px, y0);
+            for (int32_t py = y0; py <= y1; py++, e12 += d12, e20 += d20, e01 += d01) {
+                if (e12 < b12 || e20 < b20 || e01 < b01) continue;
+                float d = (b.z0 + edge_to_float(e20) * b.s1) + edge_to_float(e01) * b.s2;
+                d = d > 0.0f ? d : 0.0f;
+                d = d < 1.0f ? d : 1.0f;
+                write_fragment<KIND>(target, W, px, py, d, b.id);
             }
+        }
     }
 }
 

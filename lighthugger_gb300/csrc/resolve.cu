@@ -5,7 +5,11 @@
 // reset_buffers.glsl:9-57), read_depth (compute/read_depth.glsl:22-83),
 // generate_shadow_matrices (compute/generate_shadow_matrices.glsl:15-110) and
 // render_geometry (src/shaders/render_geometry.comp:70-266).
+#include <algorithm>
+#include <cstring>
+
 #include "frame_phases.cuh"
+#include "tma.cuh"
 
 namespace lh {
 namespace {
@@ -150,14 +154,12 @@ __device__ __forceinline__ f3 interp_deriv(const Bary& b, float v0, float v1, fl
     return {dot(m, b.lambda), dot(m, b.ddx), dot(m, b.ddy)};
 }
 
-// render_geometry.comp:70-266, one thread per pixel (blocks of 32 x 8).
-__global__ void __launch_bounds__(256) k_resolve(FrameDev f) {
+// render_geometry.comp:70-266 for pixel (x, y) of the main view, whose
+// visibility word is `vis`.
+__device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uint32_t y, unsigned long long vis) {
     const Uniforms& u = *f.uniforms;
     const uint32_t W = u.window_size.x, H = u.window_size.y;
-    const uint32_t x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
-    if (x >= W || y >= H) return;
     const f2 ndc{(float)x / (float)W * 2.0f - 1.0f, (float)y / (float)H * 2.0f - 1.0f};
-    const unsigned long long vis = __ldcs(reinterpret_cast<const unsigned long long*>(f.visibility) + (size_t)y * W + x);
     float4* out = f.hdr + (size_t)y * W + x;
     if (u2f((uint32_t)(vis >> 32)) == 0.0f) {
         f4 un = mul(u.perspective_inverse, f4{ndc.x, ndc.y, 0.0f, 1.0f});
@@ -259,6 +261,68 @@ __global__ void __launch_bounds__(256) k_resolve(FrameDev f) {
     __stcs(out, make_float4(o.x, o.y, o.z, 1.0f));
 }
 
+constexpr uint32_t kResolveRows = 8;  // tiles of 32 x 8 pixels, one warp per row
+
+// One thread per pixel; a grid of resident blocks strides over the tiles.
+// With kTma the visibility tile of each step is staged in shared memory by
+// a TMA load issued two steps ahead (double buffered, one mbarrier per
+// buffer); otherwise (rows not 16-byte aligned) each thread loads its word.
+template <bool kTma>
+__global__ void __launch_bounds__(256, 3)
+    k_resolve(FrameDev f, const __grid_constant__ CUtensorMap vis_map, uint32_t tiles_x, uint32_t n_tiles) {
+    __shared__ __align__(128) unsigned long long s_vis[2][kResolveRows][32];
+    __shared__ __align__(8) uint64_t s_bar[2];
+    const uint32_t W = f.uniforms->window_size.x, H = f.uniforms->window_size.y;
+    const uint32_t tid = threadIdx.y * 32 + threadIdx.x;
+    constexpr uint32_t kTileBytes = sizeof(s_vis[0]);
+    if (kTma) {
+        if (tid == 0) {
+            mbar_init(&s_bar[0], 1);
+            mbar_init(&s_bar[1], 1);
+            mbar_init_fence();
+        }
+        __syncthreads();
+        if (tid == 0) {
+            for (uint32_t k = 0; k < 2; k++) {
+                const uint32_t tile = blockIdx.x + k * gridDim.x;
+                if (tile >= n_tiles) break;
+                mbar_expect_tx(&s_bar[k], kTileBytes);
+                tma_load_2d(s_vis[k], &vis_map, (int32_t)((tile % tiles_x) * 32),
+                            (int32_t)((tile / tiles_x) * kResolveRows), &s_bar[k]);
+            }
+        }
+    }
+    uint32_t k = 0;
+    for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, k++) {
+        const uint32_t x = (tile % tiles_x) * 32 + threadIdx.x, y = (tile / tiles_x) * kResolveRows + threadIdx.y;
+        const bool inside = x < W && y < H;
+        unsigned long long vis = 0;
+        if (kTma) {
+            const uint32_t st = k & 1u;
+            const bool ok = mbar_wait(&s_bar[st], (k >> 1) & 1u);
+            if (__syncthreads_or(!ok)) {
+                // a copy that never landed: report it and stop this block
+                if (tid == 0) {
+                    atomicOr(&f.status[kStFlags], LH_FLAG_TIMEOUT);
+                    mbar_wait(&s_bar[st ^ 1u], ((k + 1) >> 1) & 1u);  // the other buffer's copy, bounded
+                }
+                break;
+            }
+            vis = s_vis[st][threadIdx.y][threadIdx.x];
+            __syncthreads();  // buffer st is free again
+            const uint32_t next = tile + 2 * gridDim.x;
+            if (tid == 0 && next < n_tiles) {
+                mbar_expect_tx(&s_bar[st], kTileBytes);
+                tma_load_2d(s_vis[st], &vis_map, (int32_t)((next % tiles_x) * 32),
+                            (int32_t)((next / tiles_x) * kResolveRows), &s_bar[st]);
+            }
+        } else if (inside) {
+            vis = __ldcs(reinterpret_cast<const unsigned long long*>(f.visibility) + (size_t)y * W + x);
+        }
+        if (inside) resolve_pixel(f, x, y, vis);
+    }
+}
+
 // grid = (blocks, n_views)
 __global__ void __launch_bounds__(256) k_clear_targets(FrameDev f) {
     phase_clear_view(f, blockIdx.y, (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, (uint64_t)gridDim.x * blockDim.x,
@@ -289,9 +353,19 @@ cudaError_t launch_depth_reduce_fit(const FrameDev& f, cudaStream_t s, int sms) 
     return cudaGetLastError();
 }
 
-cudaError_t launch_resolve(const FrameDev& f, uint32_t width, uint32_t height, cudaStream_t s) {
-    dim3 grid((width + 31) / 32, (height + 7) / 8);
-    k_resolve<<<grid, dim3(32, 8), 0, s>>>(f);
+cudaError_t launch_resolve(const FrameDev& f, uint32_t width, uint32_t height, const CUtensorMap* vis_map,
+                           cudaStream_t s, int sms) {
+    const uint32_t tiles_x = (width + 31) / 32, tiles_y = (height + kResolveRows - 1) / kResolveRows;
+    const uint32_t n_tiles = tiles_x * tiles_y;
+    if (n_tiles == 0) return cudaSuccess;
+    const uint32_t grid = std::min<uint32_t>(n_tiles, (uint32_t)sms * 3u);
+    if (vis_map) {
+        k_resolve<true><<<grid, dim3(32, kResolveRows), 0, s>>>(f, *vis_map, tiles_x, n_tiles);
+    } else {
+        CUtensorMap none;
+        std::memset(&none, 0, sizeof(none));
+        k_resolve<false><<<grid, dim3(32, kResolveRows), 0, s>>>(f, none, tiles_x, n_tiles);
+    }
     return cudaGetLastError();
 }
 

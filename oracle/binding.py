@@ -41,6 +41,9 @@ def lib():
         L.lho_frame.restype = C.c_int
         L.lho_raster_triangle.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p]
         L.lho_raster_triangle.restype = C.c_int
+        L.lho_raster_triangle_alpha.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                                C.c_uint32, C.c_uint32, C.c_void_p]
+        L.lho_raster_triangle_alpha.restype = C.c_int
         L.lho_resolve_f64.argtypes = [C.POINTER(FrameDesc), C.POINTER(FrameOut), C.c_void_p]
         L.lho_resolve_f64.restype = C.c_int
         _lib = L
@@ -156,4 +159,26 @@ def raster_triangle(clip, tri_id, kind, width, height, target=None):
     st = lib().lho_raster_triangle(clip.ctypes.data, tri_id, kind, width, height, target.ctypes.data)
     if st != 0:
         raise RuntimeError("lho_raster_triangle failed: %d" % st)
+    return target
+
+
+class _Texture(C.Structure):
+    """lh_texture (include/lh/lh.h)."""
+    _fields_ = [("texels", C.c_uint64), ("width", C.c_uint32), ("height", C.c_uint32), ("srgb", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
+def raster_triangle_alpha(clip, uv, texels, tex_w, tex_h, tri_id, kind, width, height, target=None):
+    """Rasterise one alpha-clip triangle: clip (3x4), per-vertex uv (3x2),
+    RGBA8 texels (tex_h x tex_w x 4, linear)."""
+    clip = np.ascontiguousarray(clip, dtype=np.float32).reshape(12)
+    uv = np.ascontiguousarray(uv, dtype=np.float32).reshape(6)
+    texels = np.ascontiguousarray(texels, dtype=np.uint8)
+    tex = _Texture(texels=texels.ctypes.data, width=tex_w, height=tex_h, srgb=0)
+    if target is None:
+        target = np.zeros((height, width), np.uint64) if kind == 0 else np.full((height, width), 0x3F800000, np.uint64)
+    st = lib().lho_raster_triangle_alpha(clip.ctypes.data, uv.ctypes.data, C.byref(tex), tri_id, kind, width, height,
+                                         target.ctypes.data)
+    if st != 0:
+        raise RuntimeError("lho_raster_triangle_alpha failed: %d" % st)
     return target

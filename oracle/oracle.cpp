@@ -372,6 +372,54 @@ static bool top_left(const SnapV& a, const SnapV& b) {
     return dy > 0 || (dy == 0 && dx < 0);
 }
 
+// Alpha test of the alpha-clip pipelines (rasterization.glsl:66-97,
+// 118-145): a fragment is discarded when the base-colour texture's alpha,
+// sampled bilinearly with repeat addressing at the perspective-correct uv of
+// the pixel centre, is below 0.5.  The perspective-correct barycentrics come
+// from the 2D homogeneous edge functions of the unclipped triangle (Olano and
+// Greer, "Triangle scan conversion using 2D homogeneous coordinates", 1997):
+// for clip positions v_k = (x_k, y_k, w_k), E_k(nx, ny) = a_k nx + b_k ny + c_k
+// with (a_k, b_k, c_k) = v_i x v_j for (i, j) = (1, 2), (2, 0), (0, 1), and
+// lambda_k = E_k / (E_0 + E_1 + E_2) -- which holds for clipped triangles too.
+// uv_k = uv(vertex k) * texture_scale + texture_offset, per vertex as the
+// reference's vertex shaders form it.
+struct AlphaTest {
+    float a[3], b[3], c[3];
+    float u[3], v[3];
+    uint32_t tex;  // base_color_texture_index
+};
+
+static AlphaTest alpha_setup(const ClipV c[3], const float u[3], const float v[3], uint32_t tex) {
+    AlphaTest t;
+    for (int k = 0; k < 3; k++) {
+        const ClipV& p = c[(k + 1) % 3];
+        const ClipV& q = c[(k + 2) % 3];
+        t.a[k] = p.y * q.w - q.y * p.w;
+        t.b[k] = p.w * q.x - q.w * p.x;
+        t.c[k] = p.x * q.y - q.x * p.y;
+        t.u[k] = u[k];
+        t.v[k] = v[k];
+    }
+    t.tex = tex;
+    return t;
+}
+
+template <class T> struct Tex4 { T r, g, b, a; };
+template <class T> static Tex4<T> sample_repeat(const lho_frame_desc* d, uint32_t index, V2<T> uv);
+
+// True when the fragment at pixel (px, py) of a W x H target survives.
+static bool alpha_pass(const lho_frame_desc* d, const AlphaTest& t, int32_t px, int32_t py, uint32_t W, uint32_t H) {
+    const float nx = (((float)px + 0.5f) / (float)W) * 2.0f - 1.0f;
+    const float ny = (((float)py + 0.5f) / (float)H) * 2.0f - 1.0f;
+    float e[3];
+    for (int k = 0; k < 3; k++) e[k] = (t.a[k] * nx + t.b[k] * ny) + t.c[k];
+    const float s = (e[0] + e[1]) + e[2];
+    const float l0 = e[0] / s, l1 = e[1] / s, l2 = e[2] / s;
+    const float u = (l0 * t.u[0] + l1 * t.u[1]) + l2 * t.u[2];
+    const float v = (l0 * t.v[0] + l1 * t.v[1]) + l2 * t.v[2];
+    return !(sample_repeat<float>(d, t.tex, V2<float>{u, v}).a < 0.5f);
+}
+
 struct Target {
     uint32_t kind;  // 0 visibility (u64 max), 1 shadow depth (u32 min)
     uint32_t W, H;
@@ -379,6 +427,8 @@ struct Target {
     uint32_t* depth;
     uint32_t id;
     uint64_t* stats;  // per-thread counters (may be null)
+    const AlphaTest* alpha = nullptr;  // alpha-clip draw: double sided, alpha tested
+    const lho_frame_desc* desc = nullptr;
 };
 
 // Rasterise one snapped triangle whose orientation is already normalised
@@ -407,6 +457,7 @@ static void raster_tri(const Target& t, SnapV v0, SnapV v1, SnapV v2) {
             int64_t Px = (int64_t)px * 256 + 128;
             int64_t e12 = edge(v1, v2, Px, Py), e20 = edge(v2, v0, Px, Py), e01 = edge(v0, v1, Px, Py);
             if (e12 < b12 || e20 < b20 || e01 < b01) continue;
+            if (t.alpha && !alpha_pass(t.desc, *t.alpha, px, py, t.W, t.H)) continue;
             float dpt = (v0.z + (float)e20 * s1) + (float)e01 * s2;
             dpt = dpt > 0.0f ? dpt : 0.0f;
             dpt = dpt < 1.0f ? dpt : 1.0f;
@@ -482,8 +533,9 @@ static void raster_primitive(const Target& t, const ClipV c[3]) {
     int64_t pc = poly_cross(s, n);
     // cross < 0 <=> Vulkan area > 0 <=> counter-clockwise <=> front facing
     if (pc == 0) return;
-    if (t.kind == 0 && pc > 0) return;  // visibility: cull back faces
-    if (t.kind == 1 && pc < 0) return;  // shadow: cull front faces
+    if (!t.alpha && t.kind == 0 && pc > 0) return;  // visibility: cull back faces
+    if (!t.alpha && t.kind == 1 && pc < 0) return;  // shadow: cull front faces
+    // (alpha clip: FILL_RASTERIZATION_DOUBLE_SIDED, pipelines.cpp:272-285,302-315)
     for (int i = 1; i + 1 < n; i++) {
         SnapV a = s[0], b = s[i], d = s[i + 1];
         SnapV tri[3] = {a, b, d};
@@ -496,7 +548,7 @@ static void raster_primitive(const Target& t, const ClipV c[3]) {
 
 // rasterization.glsl:12-34 (load_vertex_data) for one triangle of a draw.
 static bool triangle_clip(const lho_frame_desc* d, const lh_mat4& vp, const MeshletReference& ref, uint32_t tri,
-                          ClipV out[3], uint32_t* flags) {
+                          ClipV out[3], uint32_t* flags, AlphaTest* alpha = nullptr) {
     const Instance& inst = d->instances[ref.instance_index];
     const MeshInfo& mi = mesh_info_of(inst);
     const Meshlet& ml = meshlet_of(mi, ref.meshlet_index);
@@ -508,13 +560,21 @@ static bool triangle_clip(const lho_frame_desc* d, const lh_mat4& vp, const Mesh
         vec3 w = calculate_world_pos<float>(inst, mi, index);
         vec4 c = mul<float>(vp, vec4{w.x, w.y, w.z, 1.0f});
         out[k] = ClipV{c.x, c.y, c.z, c.w};
+        if (alpha) {
+            V2<float> uv = load_uv_raw<float>(mi, index);
+            alpha->u[k] = uv.x * mi.texture_scale.x + mi.texture_offset.x;
+            alpha->v[k] = uv.y * mi.texture_scale.y + mi.texture_offset.y;
+        }
     }
+    if (alpha) *alpha = alpha_setup(out, alpha->u, alpha->v, mi.base_color_texture_index);
     return true;
 }
 
-// Visibility raster (rasterization.glsl:38-58 with the state of
-// src/pipelines.cpp:287-300): every opaque and alpha-clip draw of the view
-// (alpha testing is not applied: see the alpha-clip note in the kernels).
+// Visibility or shadow raster of one view: the opaque draws
+// (rasterization.glsl:38-58, 101-111 with the state of
+// src/pipelines.cpp:257-270,287-300), then the alpha-clip draws, double
+// sided and alpha tested (rasterization.glsl:60-97, 113-145;
+// pipelines.cpp:272-285,302-315).
 static void raster_view(Frame& F, uint32_t view, const Target& tgt_proto, const lh_mat4& vp) {
     ViewLists L = F.lists(view);
     uint32_t md = F.d->max_draws;
@@ -538,12 +598,16 @@ static void raster_view(Frame& F, uint32_t view, const Target& tgt_proto, const 
                 fl |= LH_FLAG_BAD_MESHLET;
                 continue;
             }
+            const bool alpha = slot >= md;  // the alpha-clip draw class
             for (uint32_t tri = 0; tri < ml.triangle_count; tri++) {
                 ClipV c[3];
-                if (!triangle_clip(F.d, vp, ref, tri, c, &fl)) continue;
+                AlphaTest at;
+                if (!triangle_clip(F.d, vp, ref, tri, c, &fl, alpha ? &at : nullptr)) continue;
                 Target t = tgt_proto;
                 t.id = LH_PACK_ID(tri, slot);
                 t.stats = st;
+                t.alpha = alpha ? &at : nullptr;
+                t.desc = F.d;
                 raster_primitive(t, c);
             }
             uint64_t frags = st[1] - st[7];
@@ -696,7 +760,6 @@ static void init_srgb() {
     }
 }
 
-template <class T> struct Tex4 { T r, g, b, a; };
 
 // Bilinear filtering of level 0 with repeat addressing (the reference's
 // repeat_sampler, src/main.cpp:550-560, without mip levels / anisotropy).
@@ -1030,6 +1093,35 @@ int lho_raster_triangle(const float clip[12], uint32_t id, uint32_t kind, uint32
     ClipV c[3];
     for (int k = 0; k < 3; k++) c[k] = ClipV{clip[k * 4], clip[k * 4 + 1], clip[k * 4 + 2], clip[k * 4 + 3]};
     Target t{kind, width, height, nullptr, nullptr, id, nullptr};
+    std::vector<uint32_t> depth;
+    if (kind == 0) {
+        t.vis = target;
+    } else {
+        depth.resize((size_t)width * height);
+        for (size_t i = 0; i < depth.size(); i++) depth[i] = (uint32_t)target[i];
+        t.depth = depth.data();
+    }
+    raster_primitive(t, c);
+    if (kind == 1)
+        for (size_t i = 0; i < depth.size(); i++) target[i] = depth[i];
+    return LH_OK;
+}
+
+int lho_raster_triangle_alpha(const float clip[12], const float uv[6], const lh_texture* texture, uint32_t id,
+                              uint32_t kind, uint32_t width, uint32_t height, uint64_t* target) {
+    if (!clip || !uv || !texture || !target || width == 0 || height == 0 || kind > 1) return LH_ERR_INVALID_ARGUMENT;
+    init_srgb();
+    ClipV c[3];
+    for (int k = 0; k < 3; k++) c[k] = ClipV{clip[k * 4], clip[k * 4 + 1], clip[k * 4 + 2], clip[k * 4 + 3]};
+    const float u[3] = {uv[0], uv[2], uv[4]}, v[3] = {uv[1], uv[3], uv[5]};
+    lho_frame_desc d;
+    std::memset(&d, 0, sizeof(d));
+    d.textures = texture;
+    d.n_textures = 1;
+    const AlphaTest at = alpha_setup(c, u, v, 0);
+    Target t{kind, width, height, nullptr, nullptr, id, nullptr};
+    t.alpha = &at;
+    t.desc = &d;
     std::vector<uint32_t> depth;
     if (kind == 0) {
         t.vis = target;

