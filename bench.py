@@ -241,6 +241,7 @@ def run_gpu(args):
         "clear": npx * 8 + 4 * d.shadow_size ** 2 * 4,
     }
     dom = max(algo, key=lambda k: stage_ms.get(k, 0.0))
+    tri_main, tri_shadow = visible_triangles(r, st, 0), sum(visible_triangles(r, st, v) for v in range(1, 5))
     peak, peak_kind = _measured_peak_hbm()
     achieved = algo[dom] / (stage_ms[dom] * 1e-3) / 1e9 if stage_ms.get(dom) else 0.0
     tri_total = d.total_triangles
@@ -255,6 +256,9 @@ def run_gpu(args):
         "shadow_visible_meshlets": [int(st.visible_opaque[k]) for k in range(1, 5)],
         "big_triangles_last_pass": int(st.big_triangles), "clipped_triangles_last_pass": int(st.clipped_triangles),
         "stage_ms": {k: round(v, 4) for k, v in stage_ms.items()},
+        "raster": {"visible_triangles": tri_main, "shadow_triangles": tri_shadow,
+                   "gtri_per_s": tri_main / (stage_ms["raster"] * 1e-3) / 1e9,
+                   "shadow_gtri_per_s": tri_shadow / (stage_ms["shadow_raster"] * 1e-3) / 1e9},
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": 560 + 8, "d2h_bytes_per_step": npx * 16},
         "gpu_launches": 13 * args.steps,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -278,6 +282,22 @@ def run_gpu(args):
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def visible_triangles(r, st, view):
+    """Triangles of the view's visible meshlets: the draw commands' vertex
+    counts / 3 (DrawIndirectCommand{3 * triangles, 1, 0, slot})."""
+    import numpy as np
+    o = r.out
+    base = o.draw_calls + view * o.draw_call_section_bytes
+    total = 0
+    classes = ((0, min(st.visible_opaque[view], o.max_draws)),
+               (o.max_draws, min(st.visible_alpha_clip[view], o.max_draws)))
+    for first, n in classes:
+        if n:
+            cmds = r.download(base + 8 + 16 * first, 16 * n, np.uint32).reshape(n, 4)
+            total += int(cmds[:, 0].astype(np.int64).sum()) // 3
+    return total
 
 
 def bench_batched(lh, torch, args, device):

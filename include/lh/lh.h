@@ -187,6 +187,16 @@ lh_status lh_frame_graph_backward(lh_ctx* ctx, const Uniforms* uniforms, const U
                                   uint64_t d_grad_hdr, const lh_grad_targets* targets, void* stream,
                                   lh_frame_out* out);
 
+/* Display transform of the last frame's HDR image (display_transform.comp:
+ * 5-81): the tony_mc_mapface encoding stimulus / (stimulus + 1) into a 48^3
+ * LUT sampled trilinearly (clamp to edge) at texel centres, the cascade
+ * overlay when Uniforms.debug_shadowmaps is set, and the sRGB transfer
+ * function, rounded to RGBA8.  d_lut: float4[48][48][48] (x fastest, indexed
+ * by the encoded r, g, b), or 0 for the built-in identity stand-in (the
+ * reference's LUT asset is not part of its sources).  d_out: uchar4[h][w].
+ * Stream ordered, after the frame on the same stream. */
+lh_status lh_display_transform(lh_ctx* ctx, uint64_t d_lut, uint64_t d_out, void* stream);
+
 /* Pointers to the context's result buffers (valid until lh_destroy). */
 lh_status lh_get_outputs(lh_ctx* ctx, lh_frame_out* out);
 

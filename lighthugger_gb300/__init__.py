@@ -145,6 +145,7 @@ def lib():
     L.lh_resolve_backward.argtypes = [P, C.c_uint64, C.POINTER(GradTargets), P]
     L.lh_frame_graph_backward.argtypes = [P, P, P, C.c_uint32, C.c_uint64, C.POINTER(GradTargets), P,
                                           C.POINTER(FrameOut)]
+    L.lh_display_transform.argtypes = [P, C.c_uint64, C.c_uint64, P]
     L.lh_set_profiling.argtypes = [P, C.c_int]
     L.lh_get_stage_times.argtypes = [P, C.POINTER(C.c_float), C.c_uint32]
     L.lh_set_tuning.argtypes = [P, C.POINTER(Tuning)]
@@ -157,7 +158,7 @@ def lib():
     L.lh_make_uniforms.argtypes = [C.POINTER(Camera), C.POINTER(Uniforms)]
     for name in ("lh_create", "lh_set_scene", "lh_frame", "lh_frame_batched", "lh_frame_graph", "lh_get_outputs",
                  "lh_read_status",
-                 "lh_download", "lh_resolve_backward", "lh_frame_graph_backward", "lh_set_profiling", "lh_get_stage_times", "lh_set_tuning", "lh_get_tuning", "lh_scene_create", "lh_scene_describe",
+                 "lh_download", "lh_resolve_backward", "lh_frame_graph_backward", "lh_display_transform", "lh_set_profiling", "lh_get_stage_times", "lh_set_tuning", "lh_get_tuning", "lh_scene_create", "lh_scene_describe",
                  "lh_scene_upload", "lh_make_uniforms"):
         getattr(L, name).restype = C.c_int32
     _lib = L
@@ -331,6 +332,12 @@ class Renderer:
                                              grad_ptr, C.byref(targets), s, C.byref(self.out)),
                "lh_frame_graph_backward", self.ctx)
         return self.out
+
+    def display_transform(self, out_ptr, lut_ptr=0, stream=None):
+        """RGBA8 display image of the last frame into device buffer out_ptr
+        (uchar4[h][w]); lut_ptr: float4[48][48][48] or 0 for the stand-in."""
+        s = stream if stream is not None else self.stream
+        _check(lib().lh_display_transform(self.ctx, lut_ptr, out_ptr, s), "lh_display_transform", self.ctx)
 
     def status(self):
         st = DeviceStatus()

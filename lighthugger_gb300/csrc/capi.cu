@@ -89,6 +89,7 @@ struct lh_ctx {
     cudaStream_t capture_stream = nullptr;
     bool capturing = false;
     GraphBackward graph_backward{};
+    float4* d_lut_standin = nullptr;  // identity 48^3 LUT for lh_display_transform
     // 2D tensor map of d_vis for the TMA-staged resolve (false: rows are not
     // 16-byte aligned or the driver lacks the encoder)
     alignas(64) CUtensorMap vis_map;
@@ -98,7 +99,7 @@ struct lh_ctx {
 namespace {
 
 // Tensor map of the main visibility buffer: u64 elements, W x H, boxes of
-// 32 x 8 (the resolve's tile).  cuTensorMapEncodeTiled is reached through
+// 32 x 1 (one warp's row segment in the resolve).  cuTensorMapEncodeTiled is reached through
 // the runtime's driver entry point, so nothing links against libcuda.
 bool encode_vis_map(lh_ctx* c) {
     const uint64_t W = c->cfg.width, H = c->cfg.height;
@@ -113,7 +114,7 @@ bool encode_vis_map(lh_ctx* c) {
         return false;
     const cuuint64_t dims[2] = {W, H};
     const cuuint64_t strides[1] = {W * 8};
-    const cuuint32_t box[2] = {32, 8};
+    const cuuint32_t box[2] = {32, 1};
     const cuuint32_t elem[2] = {1, 1};
     return reinterpret_cast<Encode>(fn)(&c->vis_map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, c->d_vis, dims, strides, box,
                                         elem, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -697,6 +698,34 @@ lh_status lh_resolve_backward(lh_ctx* c, uint64_t d_grad_hdr, const lh_grad_targ
     cudaError_t e = launch_resolve_backward(f, c->cfg.width, c->cfg.height, reinterpret_cast<const float4*>(d_grad_hdr),
                                             *targets, s);
     if (e != cudaSuccess) return cuda_fail(c, e, "resolve backward");
+    c->last_stream = s;
+    return LH_OK;
+}
+
+lh_status lh_display_transform(lh_ctx* c, uint64_t d_lut, uint64_t d_out, void* stream) {
+    lh_status st = check_ctx(c);
+    if (st != LH_OK) return st;
+    if (!d_out || (d_out & 3) || (d_lut & 15)) return fail(c, LH_ERR_INVALID_ARGUMENT, "null or misaligned buffer");
+    if (!c->d_reset) return fail(c, LH_ERR_NO_SCENE, "lh_set_scene was not called");
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaSuccess;
+    if (!d_lut && !c->d_lut_standin) {
+        // identity on the encoded cube: texel (x, y, z) holds (x, y, z) / 47
+        std::vector<float4> lut(48 * 48 * 48);
+        for (int z = 0; z < 48; z++)
+            for (int y = 0; y < 48; y++)
+                for (int x = 0; x < 48; x++)
+                    lut[((size_t)z * 48 + y) * 48 + x] = make_float4(x / 47.0f, y / 47.0f, z / 47.0f, 1.0f);
+        e = cudaStreamSynchronize(s);
+        if (e == cudaSuccess) e = dalloc(c, &c->d_lut_standin, lut.size() * sizeof(float4));
+        if (e == cudaSuccess)
+            e = cudaMemcpy(c->d_lut_standin, lut.data(), lut.size() * sizeof(float4), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_fail(c, e, "stand-in LUT");
+    }
+    const float4* lut = d_lut ? reinterpret_cast<const float4*>(d_lut) : c->d_lut_standin;
+    FrameDev f = frame_dev(c, c->n_views_last, c->n_instances);
+    e = launch_display_transform(f, c->cfg.width, c->cfg.height, lut, reinterpret_cast<uchar4*>(d_out), s);
+    if (e != cudaSuccess) return cuda_fail(c, e, "display transform");
     c->last_stream = s;
     return LH_OK;
 }

@@ -359,10 +359,12 @@ __device__ __forceinline__ void write_fragment(void* target, uint32_t W, int32_t
                                                uint32_t id) {
     size_t pix = (size_t)py * W + px;
     if (KIND == 0) {
-        unsigned long long key = ((unsigned long long)f2u(depth) << 32) | id;
-        atomicMax(reinterpret_cast<unsigned long long*>(target) + pix, key);
+        const unsigned long long key = ((unsigned long long)f2u(depth) << 32) | id;
+        asm volatile("red.relaxed.gpu.global.max.u64 [%0], %1;" ::"l"(reinterpret_cast<unsigned long long*>(target) + pix),
+                     "l"(key));
     } else {
-        atomicMin(reinterpret_cast<uint32_t*>(target) + pix, f2u(depth));
+        asm volatile("red.relaxed.gpu.global.min.u32 [%0], %1;" ::"l"(reinterpret_cast<uint32_t*>(target) + pix),
+                     "r"(f2u(depth)));
     }
 }
 

@@ -70,6 +70,7 @@ enum StatusWord : uint32_t {
     kStMlClaim = 6,    // meshlet-cull (view, tile) claims
     kStBarrier = 7,    // grid barrier of the persistent kernel
     kStBigPacked = 8,  // u64 (words 8-9): big-triangle count << 40 | chunk count
+    kStRasterClaimAlpha = 10,  // raster claims of the alpha-clip class
     kStWords = 16
 };
 
@@ -113,10 +114,12 @@ cudaError_t launch_frame_persistent(const FrameDev& f, uint32_t n_persp, uint32_
                                     uint32_t raster_batch,
                                     float blocks_per_sm, cudaStream_t s, int sms);
 int persistent_blocks_per_sm();
-// vis_map: 2D tensor map of the main visibility buffer (u64, box 32 x 8) for
+// vis_map: 2D tensor map of the main visibility buffer (u64, box 32 x 1) for
 // the TMA-staged resolve, or null for per-thread loads.
 cudaError_t launch_resolve(const FrameDev& f, uint32_t width, uint32_t height, const CUtensorMap* vis_map,
                            cudaStream_t s, int sms);
+cudaError_t launch_display_transform(const FrameDev& f, uint32_t width, uint32_t height, const float4* lut, uchar4* out,
+                                     cudaStream_t s);
 cudaError_t launch_resolve_backward(const FrameDev& f, uint32_t width, uint32_t height, const float4* grad,
                                     const lh_grad_targets& t, cudaStream_t s);
 cudaError_t launch_sum_meshlets(const Instance* instances, uint32_t n, unsigned long long* out, cudaStream_t s);

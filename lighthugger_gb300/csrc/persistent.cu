@@ -50,7 +50,7 @@ __device__ void grid_barrier(const FrameDev& f, uint32_t& epoch) {
 
 // Resets the raster words between the visibility and the shadow passes.
 __device__ void reset_raster_words(const FrameDev& f) {
-    for (uint32_t w = kStClipCount + threadIdx.x; w < kStBigPacked + 2; w += blockDim.x)
+    for (uint32_t w = kStClipCount + threadIdx.x; w <= kStRasterClaimAlpha; w += blockDim.x)
         if (w != kStBarrier && w != kStReduceDone) f.status[w] = 0u;
 }
 
@@ -58,6 +58,7 @@ constexpr int kPersistentThreads = 256;
 
 __global__ void __launch_bounds__(kPersistentThreads, 3) k_frame_persistent(FrameDev f, uint32_t n_persp,
                                                                            RasterTune tune) {
+    __shared__ RasterSmemAlpha s_raster;  // reused by every raster phase
     uint32_t epoch = 0;
     const uint64_t gtid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, gstride = (uint64_t)gridDim.x * blockDim.x;
     const uint32_t n_views = n_persp + 4;
@@ -71,7 +72,8 @@ __global__ void __launch_bounds__(kPersistentThreads, 3) k_frame_persistent(Fram
     grid_barrier(f, epoch);
     phase_cull_meshlets(f, 0, n_persp, &f.status[kStMlClaim]);
     grid_barrier(f, epoch);
-    phase_raster<0>(f, 0, n_persp, tune, &f.status[kStRasterClaim]);
+    phase_raster<0, false>(f, 0, n_persp, tune, &f.status[kStRasterClaim], s_raster, nullptr);
+    phase_raster<0, true>(f, 0, n_persp, tune, &f.status[kStRasterClaimAlpha], s_raster, s_raster.av);
     grid_barrier(f, epoch);
     phase_raster_clip<0>(f, (uint32_t)gtid, (uint32_t)gstride);
     grid_barrier(f, epoch);
@@ -91,7 +93,8 @@ __global__ void __launch_bounds__(kPersistentThreads, 3) k_frame_persistent(Fram
     grid_barrier(f, epoch);
     phase_cull_meshlets(f, n_persp, 4, &f.status[kStMlClaim]);
     grid_barrier(f, epoch);
-    phase_raster<1>(f, n_persp, 4, tune, &f.status[kStRasterClaim]);
+    phase_raster<1, false>(f, n_persp, 4, tune, &f.status[kStRasterClaim], s_raster, nullptr);
+    phase_raster<1, true>(f, n_persp, 4, tune, &f.status[kStRasterClaimAlpha], s_raster, s_raster.av);
     grid_barrier(f, epoch);
     phase_raster_clip<1>(f, (uint32_t)gtid, (uint32_t)gstride);
     grid_barrier(f, epoch);

@@ -8,7 +8,16 @@ namespace {
 template <int KIND>
 __global__ void __launch_bounds__(kRasterWarps * 32, 3) k_raster(FrameDev f, uint32_t view_begin, uint32_t n_views,
                                                                  RasterTune tune) {
-    phase_raster<KIND>(f, view_begin, n_views, tune, &f.status[kStRasterClaim]);
+    __shared__ RasterSmem sm;
+    phase_raster<KIND, false>(f, view_begin, n_views, tune, &f.status[kStRasterClaim], sm, nullptr);
+}
+
+// The alpha-clip draw class (double sided, alpha tested).
+template <int KIND>
+__global__ void __launch_bounds__(kRasterWarps * 32, 3) k_raster_alpha(FrameDev f, uint32_t view_begin,
+                                                                       uint32_t n_views, RasterTune tune) {
+    __shared__ RasterSmemAlpha sm;
+    phase_raster<KIND, true>(f, view_begin, n_views, tune, &f.status[kStRasterClaimAlpha], sm, sm.av);
 }
 
 template <int KIND>
@@ -29,14 +38,17 @@ cudaError_t launch_raster_kind(const FrameDev& f, uint32_t view_begin, uint32_t 
     if (n_views > kMaxViews) return cudaErrorInvalidValue;
     RasterTune tune{small_px, medium_px, raster_batch};
     // raster words: clip count, claims, reduce counter, packed big-triangle word
-    cudaError_t e = cudaMemsetAsync(f.status + kStClipCount, 0, sizeof(uint32_t) * (kStBigPacked + 2 - kStClipCount), s);
+    cudaError_t e =
+        cudaMemsetAsync(f.status + kStClipCount, 0, sizeof(uint32_t) * (kStRasterClaimAlpha + 1 - kStClipCount), s);
     if (e != cudaSuccess) return e;
     if (kind == kViewVisibility) {
         k_raster<0><<<sms * 3, kRasterWarps * 32, 0, s>>>(f, view_begin, n_views, tune);
+        k_raster_alpha<0><<<sms * 3, kRasterWarps * 32, 0, s>>>(f, view_begin, n_views, tune);
         k_raster_clip<0><<<sms, 128, 0, s>>>(f);
         k_raster_big<0><<<sms * 4, 256, 0, s>>>(f);
     } else {
         k_raster<1><<<sms * 3, kRasterWarps * 32, 0, s>>>(f, view_begin, n_views, tune);
+        k_raster_alpha<1><<<sms * 3, kRasterWarps * 32, 0, s>>>(f, view_begin, n_views, tune);
         k_raster_clip<1><<<sms, 128, 0, s>>>(f);
         k_raster_big<1><<<sms * 4, 256, 0, s>>>(f);
     }

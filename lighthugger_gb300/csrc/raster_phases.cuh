@@ -306,27 +306,146 @@ __device__ __forceinline__ TriSetup shfl_setup(const TriSetup& s, int src) {
     return r;
 }
 
-// One warp per visible meshlet of views [view_begin, view_begin + n_views),
-// claimed from `claim_word`.  Persistent: returns when the claims run out.
-template <int KIND>
+// Shared memory of the raster phase (declared by the calling kernel, so that
+// the persistent kernel's phases reuse one copy).  The alpha-clip class adds
+// an AlphaVert array per warp (RasterSmemAlpha).
+constexpr uint32_t kMicroWords = (MAX_MESHLET_TRIANGLES * 3 + 3) / 4;
+struct RasterSmem {
+    uint32_t prefix[kMaxViews + 1];
+    __align__(16) lh_mat4 vp[kMaxViews];
+    SnapV v[kRasterWarps][MAX_MESHLET_UNIQUE_VERTICES];
+    uint8_t oc[kRasterWarps][MAX_MESHLET_UNIQUE_VERTICES];
+    uint32_t micro[kRasterWarps][kMicroWords];
+};
+struct RasterSmemAlpha : RasterSmem {
+    AlphaVert av[kRasterWarps][MAX_MESHLET_UNIQUE_VERTICES];
+};
+
+// One claimed meshlet (or quarter of one) of a view, as the warp works on it.
+struct MeshletWork {
+    uint32_t view, slot, part, split, nv, nt, W, H;
+    void* target;
+    float hw, hh;
+    const lh_mat4* vp;  // the view's matrix (shared memory)
+    lh_mat4 transform;  // the instance's
+    MeshInfoRaster mi;
+    uint32_t index_offset, triangle_offset;
+    const Instance* inst;
+};
+
+// The warp's pass over one meshlet: its vertices transformed and snapped into
+// shared memory, then one lane per triangle (set-up, face culling, binning).
+// ALPHA: the alpha-clip class (double sided, alpha tested per fragment).
+template <int KIND, bool ALPHA>
+__device__ __forceinline__ void raster_meshlet(const FrameDev& f, const MeshletWork w, RasterTune tune, SnapV* sv,
+                                               uint8_t* so, uint32_t* micro_words, AlphaVert* av, uint32_t lane) {
+    const uint32_t nv = w.nv, nt = w.nt, W = w.W, H = w.H;
+    const MeshInfoRaster& mi = w.mi;
+    AlphaSrc as{av, 0u, H};
+    MeshInfoAlpha ma{};
+    if (ALPHA) {
+        ma = load_mesh_info_alpha(mesh_info_of(w.inst));
+        as.tex = ma.tex;
+    }
+    for (uint32_t j = lane; j < nv; j += 32) {
+        uint32_t idx = load_index_raw(mi.indices, mi.flags, w.index_offset + j);
+        f3 wp = world_pos(w.transform, load_position(mi.positions, mi.flags, idx));
+        f4 c = mul(*w.vp, f4{wp.x, wp.y, wp.z, 1.0f});
+        uint32_t oc = outcode(c);
+        SnapV s{0, 0, 0.0f};
+        if (!oc) s = snap(c, w.hw, w.hh);
+        sv[j] = s;
+        so[j] = (uint8_t)oc;
+        if (ALPHA) av[j] = alpha_vert(c, ma, mi.flags, idx);
+    }
+    const uint64_t mbase = mi.micro_indices + w.triangle_offset;
+    const uint32_t nbytes = nt * 3;
+    if ((mbase & 3) == 0) {
+        for (uint32_t j = lane; j < (nbytes + 3) / 4; j += 32)
+            micro_words[j] = __ldg(reinterpret_cast<const uint32_t*>(mbase) + j);
+    } else {
+        uint8_t* d = reinterpret_cast<uint8_t*>(micro_words);
+        for (uint32_t j = lane; j < nbytes; j += 32) d[j] = __ldg(reinterpret_cast<const uint8_t*>(mbase) + j);
+    }
+    __syncwarp();
+    const uint8_t* mic = reinterpret_cast<const uint8_t*>(micro_words);
+    for (uint32_t base = w.part * 32u; base < nt; base += 32u * w.split) {
+        const uint32_t t = base + lane;
+        bool medium = false;
+        TriSetup st;
+        if (t < nt) {
+            const uint32_t m0 = mic[3 * t], m1 = mic[3 * t + 1], m2 = mic[3 * t + 2];
+            if (m0 >= nv || m1 >= nv || m2 >= nv) {
+                atomicOr(&f.status[kStFlags], LH_FLAG_BAD_MESHLET);
+            } else {
+                const uint32_t o0 = so[m0], o1 = so[m1], o2 = so[m2];
+                if (((o0 | o1 | o2) & 64u) || (o0 & o1 & o2)) {
+                    // non-finite / w <= 0, or entirely outside one plane
+                } else if (o0 | o1 | o2) {
+                    uint32_t pos = atomicAdd(&f.status[kStClipCount], 1u);
+                    if (pos < f.clip_cap) f.clip[pos] = ClipItem{w.view, w.slot, t, 0u};
+                    else atomicOr(&f.status[kStFlags], LH_FLAG_QUEUE_OVERFLOW);
+                } else {
+                    SnapV a = sv[m0], b = sv[m1], c = sv[m2];
+                    // most visible triangles hold no pixel centre: the 32-bit
+                    // bbox test rejects them before the area
+                    int64_t cr = covers_centre(a, b, c, W, H) ? cross_rel(a, b, c) : 0;
+                    // alpha clip is double sided
+                    bool keep = ALPHA ? cr != 0 : (KIND == 0 ? cr < 0 : cr > 0);
+                    if (keep) {
+                        if (cr > 0) { SnapV tmp = b; b = c; c = tmp; }
+                        if (make_setup(a, b, c, LH_PACK_ID(t, w.slot), W, H, st)) {
+                            if (ALPHA) {
+                                st.bias |= kBiasAlpha;
+                                st.verts = m0 | (m1 << 8) | (m2 << 16);
+                            }
+                            uint32_t npx = (uint32_t)(st.px1 - st.px0 + 1) * (uint32_t)(st.py1 - st.py0 + 1);
+                            if (npx <= tune.small_px) {
+                                if (ALPHA) raster_lane_alpha<KIND>(f, st, w.target, W, as);
+                                else raster_lane<KIND>(st, w.target, W);
+                            } else if (npx <= tune.medium_px) {
+                                medium = true;
+                            } else {
+                                push_big(f, st, w.view);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        uint32_t mask = __ballot_sync(0xFFFFFFFFu, medium);
+        while (mask) {
+            int src = __ffs(mask) - 1;
+            mask &= mask - 1;
+            TriSetup b = shfl_setup(st, src);
+            if (ALPHA) raster_warp_alpha<KIND>(f, b, w.target, W, lane, as);
+            else raster_warp<KIND>(b, w.target, W, lane);
+        }
+    }
+    __syncwarp();
+}
+
+// One warp per visible meshlet of views [view_begin, view_begin + n_views)
+// of one draw class (opaque, or ALPHA: alpha clip), claimed from
+// `claim_word`.  Persistent: returns when the claims run out.  The classes
+// are separate instantiations (separate launches) so that the opaque path
+// carries none of the alpha test's state.
+template <int KIND, bool ALPHA>
 __device__ void phase_raster(const FrameDev& f, uint32_t view_begin, uint32_t n_views, RasterTune tune,
-                             uint32_t* claim_word) {
-    __shared__ uint32_t s_prefix[kMaxViews + 1];
-    __shared__ uint32_t s_nop[kMaxViews];
-    __shared__ __align__(16) lh_mat4 s_vp[kMaxViews];
-    __shared__ SnapV s_v[kRasterWarps][MAX_MESHLET_UNIQUE_VERTICES];
-    __shared__ uint8_t s_oc[kRasterWarps][MAX_MESHLET_UNIQUE_VERTICES];
-    __shared__ uint32_t s_micro[kRasterWarps][(MAX_MESHLET_TRIANGLES * 3 + 3) / 4];
-    __shared__ AlphaVert s_av[kRasterWarps][MAX_MESHLET_UNIQUE_VERTICES];
+                             uint32_t* claim_word, RasterSmem& sm, AlphaVert (*s_av)[MAX_MESHLET_UNIQUE_VERTICES]) {
+    uint32_t* s_prefix = sm.prefix;
+    lh_mat4* s_vp = sm.vp;
+    SnapV(*s_v)[MAX_MESHLET_UNIQUE_VERTICES] = sm.v;
+    uint8_t(*s_oc)[MAX_MESHLET_UNIQUE_VERTICES] = sm.oc;
+    uint32_t(*s_micro)[kMicroWords] = sm.micro;
     const uint32_t md = f.max_draws;
+    __syncthreads();  // `sm` may still be in use by a previous phase of the block
     if (threadIdx.x == 0) {
         uint32_t run = 0;
         for (uint32_t v = 0; v < n_views; v++) {
             const uint32_t* cnt = reinterpret_cast<const uint32_t*>(f.views[view_begin + v].draws);
-            uint32_t nop = min(cnt[0], md), nal = min(cnt[1], md);
             s_prefix[v] = run;
-            s_nop[v] = nop;
-            run += nop + nal;
+            run += min(cnt[ALPHA ? 1 : 0], md);
         }
         s_prefix[n_views] = run;
     }
@@ -339,7 +458,6 @@ __device__ void phase_raster(const FrameDev& f, uint32_t view_begin, uint32_t n_
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     SnapV* sv = s_v[warp];
     uint8_t* so = s_oc[warp];
-    const uint8_t* mic = reinterpret_cast<const uint8_t*>(s_micro[warp]);
     // Work units: a meshlet, or a quarter of its triangles when the views
     // hold fewer than two meshlets per warp of the grid (shadow cascades).
     // Units are claimed `batch` per atomic: one keeps consecutive (nearby)
@@ -366,7 +484,7 @@ __device__ void phase_raster(const FrameDev& f, uint32_t view_begin, uint32_t n_
         const uint32_t view = view_begin + v;
         const ViewDev* vw = f.views + view;
         const uint32_t local = item - s_prefix[v];
-        const uint32_t slot = local < s_nop[v] ? local : md + (local - s_nop[v]);
+        const uint32_t slot = ALPHA ? md + local : local;
         const MeshletReference ref = vw->refs[slot];
         const Instance* inst = f.instances + ref.instance_index;
         lh_mat4 transform;
@@ -384,93 +502,9 @@ __device__ void phase_raster(const FrameDev& f, uint32_t view_begin, uint32_t n_
             continue;
         }
         if (part * 32u >= nt) continue;  // this quarter holds no triangles
-        const bool alpha = slot >= md;  // the alpha-clip draw class
-        AlphaSrc as{s_av[warp], 0u, H};
-        MeshInfoAlpha ma{};
-        if (alpha) {
-            ma = load_mesh_info_alpha(mesh_info_of(inst));
-            as.tex = ma.tex;
-        }
-        for (uint32_t j = lane; j < nv; j += 32) {
-            uint32_t idx = load_index_raw(mi.indices, mi.flags, mb.m.index_offset + j);
-            f3 w = world_pos(transform, load_position(mi.positions, mi.flags, idx));
-            f4 c = mul(s_vp[v], f4{w.x, w.y, w.z, 1.0f});
-            uint32_t oc = outcode(c);
-            SnapV s{0, 0, 0.0f};
-            if (!oc) s = snap(c, hw, hh);
-            sv[j] = s;
-            so[j] = (uint8_t)oc;
-            if (alpha) s_av[warp][j] = alpha_vert(c, ma, mi.flags, idx);
-        }
-        const uint64_t mbase = mi.micro_indices + mb.m.triangle_offset;
-        const uint32_t nbytes = nt * 3;
-        if ((mbase & 3) == 0) {
-            for (uint32_t j = lane; j < (nbytes + 3) / 4; j += 32)
-                s_micro[warp][j] = __ldg(reinterpret_cast<const uint32_t*>(mbase) + j);
-        } else {
-            uint8_t* d = reinterpret_cast<uint8_t*>(s_micro[warp]);
-            for (uint32_t j = lane; j < nbytes; j += 32) d[j] = __ldg(reinterpret_cast<const uint8_t*>(mbase) + j);
-        }
-        __syncwarp();
-        for (uint32_t base = part * 32u; base < nt; base += 32u * split) {
-            const uint32_t t = base + lane;
-            bool medium = false;
-            TriSetup st;
-            if (t < nt) {
-                const uint32_t m0 = mic[3 * t], m1 = mic[3 * t + 1], m2 = mic[3 * t + 2];
-                if (m0 >= nv || m1 >= nv || m2 >= nv) {
-                    atomicOr(&f.status[kStFlags], LH_FLAG_BAD_MESHLET);
-                } else {
-                    const uint32_t o0 = so[m0], o1 = so[m1], o2 = so[m2];
-                    if (((o0 | o1 | o2) & 64u) || (o0 & o1 & o2)) {
-                        // non-finite / w <= 0, or entirely outside one plane
-                    } else if (o0 | o1 | o2) {
-                        uint32_t pos = atomicAdd(&f.status[kStClipCount], 1u);
-                        if (pos < f.clip_cap) f.clip[pos] = ClipItem{view, slot, t, 0u};
-                        else atomicOr(&f.status[kStFlags], LH_FLAG_QUEUE_OVERFLOW);
-                    } else {
-                        SnapV a = sv[m0], b = sv[m1], c = sv[m2];
-                        // most visible triangles hold no pixel centre: the
-                        // 32-bit bbox test rejects them before the area
-#ifndef LH_RASTER_BBOX_FIRST
-#define LH_RASTER_BBOX_FIRST 1
-#endif
-#if LH_RASTER_BBOX_FIRST
-                        int64_t cr = covers_centre(a, b, c, W, H) ? cross_rel(a, b, c) : 0;
-#else
-                        int64_t cr = cross3(a, b, c);
-#endif
-                        // alpha clip is double sided
-                        bool keep = alpha ? cr != 0 : (KIND == 0 ? cr < 0 : cr > 0);
-                        if (keep) {
-                            if (cr > 0) { SnapV tmp = b; b = c; c = tmp; }
-                            if (make_setup(a, b, c, LH_PACK_ID(t, slot), W, H, st)) {
-                                if (alpha) {
-                                    st.bias |= kBiasAlpha;
-                                    st.verts = m0 | (m1 << 8) | (m2 << 16);
-                                }
-                                uint32_t npx = (uint32_t)(st.px1 - st.px0 + 1) * (uint32_t)(st.py1 - st.py0 + 1);
-                                if (npx <= tune.small_px) {
-                                    if (alpha) raster_lane_alpha<KIND>(f, st, target, W, as);
-                                    else raster_lane<KIND>(st, target, W);
-                                }
-                                else if (npx <= tune.medium_px) medium = true;
-                                else push_big(f, st, view);
-                            }
-                        }
-                    }
-                }
-            }
-            uint32_t mask = __ballot_sync(0xFFFFFFFFu, medium);
-            while (mask) {
-                int src = __ffs(mask) - 1;
-                mask &= mask - 1;
-                TriSetup b = shfl_setup(st, src);
-                if (b.bias & kBiasAlpha) raster_warp_alpha<KIND>(f, b, target, W, lane, as);
-                else raster_warp<KIND>(b, target, W, lane);
-            }
-        }
-        __syncwarp();
+        const MeshletWork w{view,   slot, part, split, nv,        nt, W, H, target, hw, hh, &s_vp[v],
+                            transform, mi, mb.m.index_offset, mb.m.triangle_offset, inst};
+        raster_meshlet<KIND, ALPHA>(f, w, tune, sv, so, s_micro[warp], ALPHA ? s_av[warp] : nullptr, lane);
     }
 }
 

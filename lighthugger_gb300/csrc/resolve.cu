@@ -154,10 +154,64 @@ __device__ __forceinline__ f3 interp_deriv(const Bary& b, float v0, float v1, fl
     return {dot(m, b.lambda), dot(m, b.ddx), dot(m, b.ddy)};
 }
 
-// render_geometry.comp:70-266 for pixel (x, y) of the main view, whose
+// DEBUG_COLOURS (shaders/common/debug.glsl:1-11) and temperature()
+// (debug.glsl:15-37) for the debug views.
+__constant__ float c_debug_colours[10][3] = {
+    {0.0f / 255.0f, 2.0f / 255.0f, 91.0f / 255.0f},     {0.0f / 255.0f, 108.0f / 255.0f, 251.0f / 255.0f},
+    {0.0f / 255.0f, 221.0f / 255.0f, 221.0f / 255.0f},  {51.0f / 255.0f, 221.0f / 255.0f, 0.0f / 255.0f},
+    {255.0f / 255.0f, 252.0f / 255.0f, 0.0f / 255.0f},  {255.0f / 255.0f, 180.0f / 255.0f, 0.0f / 255.0f},
+    {255.0f / 255.0f, 104.0f / 255.0f, 0.0f / 255.0f},  {226.0f / 255.0f, 22.0f / 255.0f, 0.0f / 255.0f},
+    {191.0f / 255.0f, 0.0f / 255.0f, 83.0f / 255.0f},   {145.0f / 255.0f, 0.0f / 255.0f, 65.0f / 255.0f}};
+__device__ __forceinline__ f3 debug_colour(uint32_t i) {
+    return {c_debug_colours[i][0], c_debug_colours[i][1], c_debug_colours[i][2]};
+}
+__device__ __forceinline__ float smoothstep_(float e0, float e1, float x) {
+    float t = (x - e0) / (e1 - e0);
+    t = t < 0.0f ? 0.0f : (t > 1.0f ? 1.0f : t);
+    return t * t * (3.0f - 2.0f * t);
+}
+__device__ f3 temperature(float t) {
+    const float s = t * 10.0f;
+    const int cur = (int)s <= 9 ? (int)s : 9;
+    const int prv = cur >= 1 ? cur - 1 : 0;
+    const int nxt = cur < 9 ? cur + 1 : 9;
+    const float blur = 0.8f;
+    const float wc = smoothstep_((float)cur - blur, (float)cur + blur, s) *
+                     (1.0f - smoothstep_((float)(cur + 1) - blur, (float)(cur + 1) + blur, s));
+    const float wp = 1.0f - smoothstep_((float)cur - blur, (float)cur + blur, s);
+    const float wn = smoothstep_((float)(cur + 1) - blur, (float)(cur + 1) + blur, s);
+    const f3 r = debug_colour(cur) * wc + debug_colour(prv) * wp + debug_colour(nxt) * wn;
+    return {clampf(r.x, 0.0f, 1.0f), clampf(r.y, 0.0f, 1.0f), clampf(r.z, 0.0f, 1.0f)};
+}
+
+// The debug views (render_geometry.comp:268-308) that replace the lit
+// colour with material / index / normal colours; not inlined, so the lit
+// path's registers do not carry them.  They do not depend on the lighting,
+// which the kernel then skips.
+__device__ __noinline__ f3 debug_view(int32_t mode, f3 base, uint32_t cascade, uint32_t tri, uint32_t meshlet_index,
+                                      f3 normal) {
+    switch (mode) {
+        case 1: return base * debug_colour(cascade);        // UNIFORMS_DEBUG_CASCADES
+        case 2: return debug_colour(tri % 10);              // UNIFORMS_DEBUG_TRIANGLE_INDEX
+        case 3: return debug_colour(meshlet_index % 10);    // UNIFORMS_DEBUG_INSTANCE_INDEX
+        default: return normal * 0.5f + f3{0.5f, 0.5f, 0.5f};  // UNIFORMS_DEBUG_NORMALS
+    }
+}
+
+// UNIFORMS_DEBUG_SHADER_CLOCK: the pixel's shading time as a heat map.
+__device__ __noinline__ f3 clock_view(long long start_time) {
+    const float dt = (float)(clock64() - start_time) / 65000.0f;
+    return temperature(dt < 0.0f ? 0.0f : (dt > 1.0f ? 1.0f : dt));
+}
+
+// render_geometry.comp:70-308 for pixel (x, y) of the main view, whose
 // visibility word is `vis`.
-__device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uint32_t y, unsigned long long vis) {
+// `clock_slot`: the thread's shared-memory word for the clock view's start
+// time (kept out of registers).
+__device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uint32_t y, unsigned long long vis,
+                                              long long* clock_slot) {
     const Uniforms& u = *f.uniforms;
+    if (u.debug == 4) *clock_slot = clock64();
     const uint32_t W = u.window_size.x, H = u.window_size.y;
     const f2 ndc{(float)x / (float)W * 2.0f - 1.0f, (float)y / (float)H * 2.0f - 1.0f};
     float4* out = f.hdr + (size_t)y * W + x;
@@ -246,6 +300,11 @@ __device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uin
                               (tt.z * mn.x + bb.z * mn.y) + normal.z * mn.z});
     }
     // AMBIENT_SH (render_geometry.comp:40-57): only sh[0] = sh[2] = 0.025.
+    if (u.debug != 0 && u.debug != 4) {
+        const f3 o = debug_view(u.debug, base, ci, tri, ref.meshlet_index, normal);
+        __stcs(out, make_float4(o.x, o.y, o.z, 1.0f));
+        return;
+    }
     const float amb_level = 0.025f;
     const f3 zero{0.0f, 0.0f, 0.0f}, sh0{amb_level, amb_level, amb_level};
     f3 amb = ((((((((sh0 + zero * normal.x) + sh0 * normal.y) + zero * normal.z) + zero * (normal.x * normal.z)) +
@@ -258,69 +317,78 @@ __device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uin
     f3 sun = (BRDF(view_vector, ld3(u.sun_dir), normal, roughness, metallic, base, alpha) * sun_intensity) *
              ld3(u.sun_intensity);
     f3 o = sun + ambient;
+    if (u.debug == 4) o = clock_view(*clock_slot);
     __stcs(out, make_float4(o.x, o.y, o.z, 1.0f));
 }
 
-constexpr uint32_t kResolveRows = 8;  // tiles of 32 x 8 pixels, one warp per row
+constexpr uint32_t kResolveWarps = 8;   // warps per block
+constexpr uint32_t kResolveStages = 4;  // visibility rows in flight per warp
 
-// One thread per pixel; a grid of resident blocks strides over the tiles.
-// With kTma the visibility tile of each step is staged in shared memory by
-// a TMA load issued two steps ahead (double buffered, one mbarrier per
-// buffer); otherwise (rows not 16-byte aligned) each thread loads its word.
+// One thread per pixel, one warp per 32-pixel row segment; the grid's warps
+// stride over the segments.  With kTma each warp stages the visibility words
+// of its next kResolveStages segments in shared memory with TMA row loads
+// (box 32 x 1, one mbarrier per stage), issued by its lane 0; nothing
+// synchronises beyond the warp.  Without (rows not 16-byte aligned) each
+// thread loads its own word.
 template <bool kTma>
-__global__ void __launch_bounds__(256, 3)
-    k_resolve(FrameDev f, const __grid_constant__ CUtensorMap vis_map, uint32_t tiles_x, uint32_t n_tiles) {
-    __shared__ __align__(128) unsigned long long s_vis[2][kResolveRows][32];
-    __shared__ __align__(8) uint64_t s_bar[2];
+__global__ void __launch_bounds__(kResolveWarps * 32, 3)
+    k_resolve(FrameDev f, const __grid_constant__ CUtensorMap vis_map, uint32_t segs_x, uint32_t n_segs) {
+    __shared__ __align__(128) unsigned long long s_vis[kResolveWarps][kResolveStages][32];
+    __shared__ __align__(8) uint64_t s_bar[kResolveWarps][kResolveStages];
+    __shared__ long long s_clock[kResolveWarps][32];
     const uint32_t W = f.uniforms->window_size.x, H = f.uniforms->window_size.y;
-    const uint32_t tid = threadIdx.y * 32 + threadIdx.x;
-    constexpr uint32_t kTileBytes = sizeof(s_vis[0]);
+    const uint32_t lane = threadIdx.x, warp = threadIdx.y;
+    const uint32_t gwarp = blockIdx.x * kResolveWarps + warp, nwarps = gridDim.x * kResolveWarps;
+    unsigned long long(*vis_buf)[32] = s_vis[warp];
+    uint64_t* bar = s_bar[warp];
     if (kTma) {
-        if (tid == 0) {
-            mbar_init(&s_bar[0], 1);
-            mbar_init(&s_bar[1], 1);
+        if (lane == 0) {
+            for (uint32_t k = 0; k < kResolveStages; k++) mbar_init(&bar[k], 1);
             mbar_init_fence();
-        }
-        __syncthreads();
-        if (tid == 0) {
-            for (uint32_t k = 0; k < 2; k++) {
-                const uint32_t tile = blockIdx.x + k * gridDim.x;
-                if (tile >= n_tiles) break;
-                mbar_expect_tx(&s_bar[k], kTileBytes);
-                tma_load_2d(s_vis[k], &vis_map, (int32_t)((tile % tiles_x) * 32),
-                            (int32_t)((tile / tiles_x) * kResolveRows), &s_bar[k]);
+            for (uint32_t k = 0; k < kResolveStages; k++) {
+                const uint32_t seg = gwarp + k * nwarps;
+                if (seg >= n_segs) break;
+                mbar_expect_tx(&bar[k], 32 * 8);
+                tma_load_2d(vis_buf[k], &vis_map, (int32_t)((seg % segs_x) * 32), (int32_t)(seg / segs_x), &bar[k]);
             }
         }
+        __syncwarp();
     }
     uint32_t k = 0;
-    for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, k++) {
-        const uint32_t x = (tile % tiles_x) * 32 + threadIdx.x, y = (tile / tiles_x) * kResolveRows + threadIdx.y;
-        const bool inside = x < W && y < H;
+    for (uint32_t seg = gwarp; seg < n_segs; seg += nwarps, k++) {
+        const uint32_t x = (seg % segs_x) * 32 + lane, y = seg / segs_x;
+        const bool inside = x < W;
         unsigned long long vis = 0;
         if (kTma) {
-            const uint32_t st = k & 1u;
-            const bool ok = mbar_wait(&s_bar[st], (k >> 1) & 1u);
-            if (__syncthreads_or(!ok)) {
-                // a copy that never landed: report it and stop this block
-                if (tid == 0) {
+            const uint32_t st = k % kResolveStages;
+            const bool ok = mbar_wait(&bar[st], (k / kResolveStages) & 1u);
+            if (__any_sync(0xFFFFFFFFu, !ok)) {
+                // a copy that never landed: report it, wait (bounded) for the
+                // warp's other copies in flight, and stop this warp
+                if (lane == 0) {
                     atomicOr(&f.status[kStFlags], LH_FLAG_TIMEOUT);
-                    mbar_wait(&s_bar[st ^ 1u], ((k + 1) >> 1) & 1u);  // the other buffer's copy, bounded
+                    for (uint32_t j = 1; j < kResolveStages; j++) {
+                        const uint32_t kk = k + j;
+                        if (seg + j * nwarps >= n_segs) break;
+                        mbar_wait(&bar[kk % kResolveStages], (kk / kResolveStages) & 1u);
+                    }
                 }
                 break;
             }
-            vis = s_vis[st][threadIdx.y][threadIdx.x];
-            __syncthreads();  // buffer st is free again
-            const uint32_t next = tile + 2 * gridDim.x;
-            if (tid == 0 && next < n_tiles) {
-                mbar_expect_tx(&s_bar[st], kTileBytes);
-                tma_load_2d(s_vis[st], &vis_map, (int32_t)((next % tiles_x) * 32),
-                            (int32_t)((next / tiles_x) * kResolveRows), &s_bar[st]);
+            vis = vis_buf[st][lane];
+            __syncwarp();  // stage st is free again
+            const uint32_t next = seg + kResolveStages * nwarps;
+            if (lane == 0 && next < n_segs) {
+                mbar_expect_tx(&bar[st], 32 * 8);
+                tma_load_2d(vis_buf[st], &vis_map, (int32_t)((next % segs_x) * 32), (int32_t)(next / segs_x),
+                            &bar[st]);
             }
         } else if (inside) {
             vis = __ldcs(reinterpret_cast<const unsigned long long*>(f.visibility) + (size_t)y * W + x);
         }
-        if (inside) resolve_pixel(f, x, y, vis);
+        if (inside) resolve_pixel(f, x, y, vis, &s_clock[warp][lane]);
     }
+    (void)H;
 }
 
 // grid = (blocks, n_views)
@@ -355,16 +423,16 @@ cudaError_t launch_depth_reduce_fit(const FrameDev& f, cudaStream_t s, int sms) 
 
 cudaError_t launch_resolve(const FrameDev& f, uint32_t width, uint32_t height, const CUtensorMap* vis_map,
                            cudaStream_t s, int sms) {
-    const uint32_t tiles_x = (width + 31) / 32, tiles_y = (height + kResolveRows - 1) / kResolveRows;
-    const uint32_t n_tiles = tiles_x * tiles_y;
-    if (n_tiles == 0) return cudaSuccess;
-    const uint32_t grid = std::min<uint32_t>(n_tiles, (uint32_t)sms * 3u);
+    const uint32_t segs_x = (width + 31) / 32;
+    const uint32_t n_segs = segs_x * height;
+    if (n_segs == 0) return cudaSuccess;
+    const uint32_t grid = std::min<uint32_t>((n_segs + kResolveWarps - 1) / kResolveWarps, (uint32_t)sms * 3u);
     if (vis_map) {
-        k_resolve<true><<<grid, dim3(32, kResolveRows), 0, s>>>(f, *vis_map, tiles_x, n_tiles);
+        k_resolve<true><<<grid, dim3(32, kResolveWarps), 0, s>>>(f, *vis_map, segs_x, n_segs);
     } else {
         CUtensorMap none;
         std::memset(&none, 0, sizeof(none));
-        k_resolve<false><<<grid, dim3(32, kResolveRows), 0, s>>>(f, none, tiles_x, n_tiles);
+        k_resolve<false><<<grid, dim3(32, kResolveWarps), 0, s>>>(f, none, segs_x, n_segs);
     }
     return cudaGetLastError();
 }

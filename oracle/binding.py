@@ -44,6 +44,9 @@ def lib():
         L.lho_raster_triangle_alpha.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
                                                 C.c_uint32, C.c_uint32, C.c_void_p]
         L.lho_raster_triangle_alpha.restype = C.c_int
+        L.lho_display_transform.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32,
+                                            C.c_uint32, C.c_void_p]
+        L.lho_display_transform.restype = C.c_int
         L.lho_resolve_f64.argtypes = [C.POINTER(FrameDesc), C.POINTER(FrameOut), C.c_void_p]
         L.lho_resolve_f64.restype = C.c_int
         _lib = L
@@ -182,3 +185,19 @@ def raster_triangle_alpha(clip, uv, texels, tex_w, tex_h, tri_id, kind, width, h
     if st != 0:
         raise RuntimeError("lho_raster_triangle_alpha failed: %d" % st)
     return target
+
+
+def display_transform(hdr, lut=None, shadow_maps=None, debug_shadowmaps=0):
+    """RGBA8 display image of a float HDR image [h, w, 4] (lut: float32
+    [48, 48, 48, 4] or None for the identity stand-in)."""
+    hdr = np.ascontiguousarray(hdr, np.float32)
+    H, W = hdr.shape[:2]
+    out = np.zeros((H, W, 4), np.uint8)
+    lut_p = np.ascontiguousarray(lut, np.float32) if lut is not None else None
+    sm = np.ascontiguousarray(shadow_maps, np.float32) if shadow_maps is not None else None
+    S = sm.shape[-1] if sm is not None else 0
+    st = lib().lho_display_transform(hdr.ctypes.data, W, H, lut_p.ctypes.data if lut_p is not None else None,
+                                     sm.ctypes.data if sm is not None else None, S, debug_shadowmaps, out.ctypes.data)
+    if st != 0:
+        raise RuntimeError("lho_display_transform failed: %d" % st)
+    return out

@@ -911,7 +911,18 @@ template <class T> static V3<T> sky(V3<T> ray) {
     return {(T)0.25 + (T)0.10 * ray.y, (T)0.35 + (T)0.15 * ray.y, (T)0.55 + (T)0.25 * ray.y};
 }
 
-// render_geometry.comp:70-266 for one pixel.
+// DEBUG_COLOURS (shaders/common/debug.glsl:1-11).
+static const float kDebugColours[10][3] = {
+    {0.0f / 255.0f, 2.0f / 255.0f, 91.0f / 255.0f},     {0.0f / 255.0f, 108.0f / 255.0f, 251.0f / 255.0f},
+    {0.0f / 255.0f, 221.0f / 255.0f, 221.0f / 255.0f},  {51.0f / 255.0f, 221.0f / 255.0f, 0.0f / 255.0f},
+    {255.0f / 255.0f, 252.0f / 255.0f, 0.0f / 255.0f},  {255.0f / 255.0f, 180.0f / 255.0f, 0.0f / 255.0f},
+    {255.0f / 255.0f, 104.0f / 255.0f, 0.0f / 255.0f},  {226.0f / 255.0f, 22.0f / 255.0f, 0.0f / 255.0f},
+    {191.0f / 255.0f, 0.0f / 255.0f, 83.0f / 255.0f},   {145.0f / 255.0f, 0.0f / 255.0f, 65.0f / 255.0f}};
+template <class T> static V3<T> debug_colour(uint32_t i) {
+    return {(T)kDebugColours[i][0], (T)kDebugColours[i][1], (T)kDebugColours[i][2]};
+}
+
+// render_geometry.comp:70-308 for one pixel.
 template <class T> static V4<T> resolve_pixel(const lho_frame_desc* d, const lho_frame_out* o, uint32_t x, uint32_t y) {
     const Uniforms& u = *d->uniforms;
     uint32_t W = u.window_size.x, H = u.window_size.y;
@@ -1008,6 +1019,15 @@ template <class T> static V4<T> resolve_pixel(const lho_frame_desc* d, const lho
     V3<T> sun = (BRDF<T>(view_vector, v3<T>(u.sun_dir), normal, roughness, metallic, base, alpha) * sun_intensity) *
                 v3<T>(u.sun_intensity);
     V3<T> out = sun + ambient;
+    // debug views (render_geometry.comp:268-308); the shader-clock heat map
+    // measures time and has no CPU counterpart (left as the lit colour)
+    switch (u.debug) {
+        case 1: out = base * debug_colour<T>(ci); break;                // UNIFORMS_DEBUG_CASCADES
+        case 2: out = debug_colour<T>(tri % 10); break;                 // UNIFORMS_DEBUG_TRIANGLE_INDEX
+        case 3: out = debug_colour<T>(ref.meshlet_index % 10); break;   // UNIFORMS_DEBUG_INSTANCE_INDEX
+        case 5: out = normal * (T)0.5 + V3<T>{(T)0.5, (T)0.5, (T)0.5}; break;  // UNIFORMS_DEBUG_NORMALS
+        default: break;
+    }
     return {out.x, out.y, out.z, (T)1};
 }
 
@@ -1133,6 +1153,92 @@ int lho_raster_triangle_alpha(const float clip[12], const float uv[6], const lh_
     raster_primitive(t, c);
     if (kind == 1)
         for (size_t i = 0; i < depth.size(); i++) target[i] = depth[i];
+    return LH_OK;
+}
+
+// ------------------------------------------------------------ display transform
+// display_transform.comp:5-81.  Trilinear LUT sampling with clamp to edge
+// (clamp_sampler, main.cpp:561-566), lerped along x, then y, then z.
+static void lut_sample(const float* lut, const float uvw[3], float out[3]) {
+    const int N = 48;
+    float a[3];
+    int i0[3], i1[3];
+    for (int k = 0; k < 3; k++) {
+        float t = uvw[k] * (float)N - 0.5f;
+        float fl = std::floor(t);
+        a[k] = t - fl;
+        int i = (int)fl;
+        i0[k] = std::min(std::max(i, 0), N - 1);
+        i1[k] = std::min(std::max(i + 1, 0), N - 1);
+    }
+    auto t = [&](int x, int y, int z, int c) { return lut[(((size_t)z * N + y) * N + x) * 4 + c]; };
+    for (int c = 0; c < 3; c++) {
+        float c00 = t(i0[0], i0[1], i0[2], c) * (1.0f - a[0]) + t(i1[0], i0[1], i0[2], c) * a[0];
+        float c10 = t(i0[0], i1[1], i0[2], c) * (1.0f - a[0]) + t(i1[0], i1[1], i0[2], c) * a[0];
+        float c01 = t(i0[0], i0[1], i1[2], c) * (1.0f - a[0]) + t(i1[0], i0[1], i1[2], c) * a[0];
+        float c11 = t(i0[0], i1[1], i1[2], c) * (1.0f - a[0]) + t(i1[0], i1[1], i1[2], c) * a[0];
+        float c0 = c00 * (1.0f - a[1]) + c10 * a[1], c1 = c01 * (1.0f - a[1]) + c11 * a[1];
+        out[c] = c0 * (1.0f - a[2]) + c1 * a[2];
+    }
+}
+
+static float srgb_oetf(float v) { return v <= 0.003130f ? v * 12.92f : 1.055f * std::pow(v, 1.0f / 2.4f) - 0.055f; }
+
+static uint8_t unorm8(float v) {
+    v = v > 0.0f ? v : 0.0f;
+    v = v < 1.0f ? v : 1.0f;
+    return (uint8_t)std::floor(v * 255.0f + 0.5f);
+}
+
+int lho_display_transform(const float* hdr, uint32_t W, uint32_t H, const float* lut, const float* shadow_maps,
+                          uint32_t S, uint32_t debug_shadowmaps, uint8_t* out) {
+    if (!hdr || !out || (debug_shadowmaps && (!shadow_maps || !S))) return LH_ERR_INVALID_ARGUMENT;
+    std::vector<float> identity;
+    if (!lut) {
+        identity.resize(48 * 48 * 48 * 4);
+        for (int z = 0; z < 48; z++)
+            for (int y = 0; y < 48; y++)
+                for (int x = 0; x < 48; x++) {
+                    float* p = &identity[(((size_t)z * 48 + y) * 48 + x) * 4];
+                    p[0] = x / 47.0f;
+                    p[1] = y / 47.0f;
+                    p[2] = z / 47.0f;
+                    p[3] = 1.0f;
+                }
+        lut = identity.data();
+    }
+    const float scale = (48.0f - 1.0f) / 48.0f, bias = 0.5f / 48.0f;
+    for (uint32_t y = 0; y < H; y++)
+        for (uint32_t x = 0; x < W; x++) {
+            const float* s = hdr + ((size_t)y * W + x) * 4;
+            float uvw[3], v[3];
+            for (int c = 0; c < 3; c++) uvw[c] = (s[c] / (s[c] + 1.0f)) * scale + bias;
+            lut_sample(lut, uvw, v);
+            if (debug_shadowmaps) {
+                const float uvx = ((float)x + 0.5f) / (float)W, uvy = ((float)y + 0.5f) / (float)H;
+                const float pct = 0.5f;
+                if (uvx < pct && uvy < pct) {
+                    const float sx = uvx * 2.0f / pct, sy = uvy * 2.0f / pct;
+                    const uint32_t cascade = (sy > 1.0f ? 2u : 0u) + (sx > 1.0f ? 1u : 0u);
+                    const float* m = shadow_maps + (size_t)cascade * S * S;
+                    const float u = sx - std::floor(sx), w = sy - std::floor(sy);
+                    const float tu = u * (float)S - 0.5f, tv = w * (float)S - 0.5f;
+                    const float fu = std::floor(tu), fv = std::floor(tv);
+                    const float a = tu - fu, b = tv - fv;
+                    auto cl = [&](int i) { return std::min(std::max(i, 0), (int)S - 1); };
+                    const int i0 = cl((int)fu), i1 = cl((int)fu + 1), j0 = cl((int)fv), j1 = cl((int)fv + 1);
+                    const float t00 = m[(size_t)j0 * S + i0], t10 = m[(size_t)j0 * S + i1],
+                                t01 = m[(size_t)j1 * S + i0], t11 = m[(size_t)j1 * S + i1];
+                    const float d = ((t00 * ((1.0f - a) * (1.0f - b)) + t10 * (a * (1.0f - b))) + t01 * ((1.0f - a) * b)) +
+                                    t11 * (a * b);
+                    const float g = (d - 0.5f) * 100.0f + 0.5f;
+                    v[0] = v[1] = v[2] = g;
+                }
+            }
+            uint8_t* o = out + ((size_t)y * W + x) * 4;
+            for (int c = 0; c < 3; c++) o[c] = unorm8(srgb_oetf(v[c]));
+            o[3] = 255;
+        }
     return LH_OK;
 }
 

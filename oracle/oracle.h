@@ -97,6 +97,13 @@ int lho_raster_triangle(const float clip[12], uint32_t id, uint32_t kind, uint32
 int lho_raster_triangle_alpha(const float clip[12], const float uv[6], const lh_texture* texture, uint32_t id,
                               uint32_t kind, uint32_t width, uint32_t height, uint64_t* target);
 
+/* Display transform (display_transform.comp:5-81) of a float RGBA HDR image
+ * into RGBA8: tony_mc_mapface encoding into a 48^3 LUT (float4, x fastest;
+ * null = the identity stand-in), the cascade overlay when debug_shadowmaps,
+ * sRGB transfer function, round to nearest. */
+int lho_display_transform(const float* hdr, uint32_t width, uint32_t height, const float* lut, const float* shadow_maps,
+                          uint32_t shadow_size, uint32_t debug_shadowmaps, uint8_t* out);
+
 /* Forward resolve of one frame in float64 (the FP64 reference for error
  * statements); same inputs as lho_frame with visibility and shadow maps
  * already filled in `out`. */

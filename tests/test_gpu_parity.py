@@ -183,3 +183,26 @@ def test_near_plane_clipping_parity(native, oracle, gap):
     assert stats["covered"] > 0.05 * d.width * d.height  # the surface fills part of the view
     if gap < 0.01:
         assert fr.raster_stats["visibility"]["clipped"] > 0
+
+
+@pytest.mark.parametrize("mode", [1, 2, 3, 5])
+def test_debug_views(native, oracle, mode):
+    """Uniforms.debug (render_geometry.comp:268-308): cascades, triangle
+    index, meshlet index and normal colours match the oracle."""
+    import ctypes
+    lh = native
+    scene = lh.Scene(1).upload(0)
+    d = scene.desc
+    u = lh.Uniforms.from_buffer_copy(bytes(scene.uniforms))
+    ctypes.memmove(ctypes.addressof(u) + 552, ctypes.byref(ctypes.c_int32(mode)), 4)
+    cfg = lh.Config(width=d.width, height=d.height, shadow_size=d.shadow_size, max_instances=1024, max_draws=200000)
+    r = lh.Renderer(cfg)
+    r.set_scene(scene)
+    r.frame(u)
+    st = r.status()
+    fr = oracle.run_scene(scene, shadow_size=d.shadow_size, max_instances=1024, max_draws=200000, uniforms=u)
+    _assert_parity(r, fr, 200000, 1024, st)
+    hdr = r.hdr()
+    lit = oracle.run_scene(scene, shadow_size=d.shadow_size, max_instances=1024, max_draws=200000)
+    covered = (r.visibility() >> np.uint64(32)) != 0
+    assert not np.array_equal(hdr[covered], lit.hdr[covered])  # the view replaced the lighting

@@ -209,3 +209,35 @@ def test_alpha_clip_uv_is_perspective_correct(oracle):
     clear = np.abs(alpha - 0.5) > 1e-3
     assert clear.sum() > 200
     assert np.array_equal(covered(t)[clear], (alpha >= 0.5)[clear])
+
+
+def test_display_transform_known_values(oracle):
+    # identity stand-in LUT: display = stimulus / (1 + stimulus), then the
+    # sRGB transfer function and rounding to 8 bits
+    stim = np.array([0.0, 1.0, 3.0, 1e-4], np.float32)
+    hdr = np.zeros((1, 4, 4), np.float32)
+    hdr[0, :, 0] = hdr[0, :, 1] = hdr[0, :, 2] = stim
+    out = oracle.display_transform(hdr)
+    enc = stim.astype(np.float64) / (stim + 1.0)
+    srgb = np.where(enc <= 0.00313, enc * 12.92, 1.055 * enc ** (1 / 2.4) - 0.055)
+    expect = np.floor(np.clip(srgb, 0, 1) * 255 + 0.5)
+    assert np.array_equal(out[0, :, 0], expect.astype(np.uint8)), (out[0, :, 0], expect)
+    assert (out[..., 3] == 255).all()
+    # a full LUT of one colour maps everything to it
+    lut = np.zeros((48, 48, 48, 4), np.float32)
+    lut[..., 1] = 0.5
+    out = oracle.display_transform(hdr, lut=lut)
+    assert (out[0, :, 0] == 0).all() and (out[0, :, 1] == 188).all()
+
+
+def test_display_transform_shadow_overlay(oracle):
+    # debug_shadowmaps: the top-left quarter shows the 4 cascades at
+    # (depth - 0.5) * 100 + 0.5; a map of 0.5 reads back as 0.5 -> 188
+    W = H = 16
+    hdr = np.zeros((H, W, 4), np.float32)
+    maps = np.full((4, 8, 8), 0.5, np.float32)
+    maps[3] = 0.51  # cascade 3 (bottom-right of the quarter): 1.5 -> white
+    out = oracle.display_transform(hdr, shadow_maps=maps, debug_shadowmaps=1)
+    assert (out[:4, :4, 0] == 188).all()
+    assert (out[4:8, 4:8, 0] == 255).all()
+    assert (out[8:, :, 0] == 0).all() and (out[:, 8:, 0] == 0).all()
