@@ -233,10 +233,18 @@ def run_gpu(args):
     vis_ml = st.visible_opaque[0] + st.visible_alpha_clip[0]
     cand_sh = sum(st.candidate_meshlets[1:5])
     vis_sh = sum(st.visible_opaque[1:5])
+    # resolve: visibility words read, HDR written, plus what it gathers once:
+    # the 4 shadow layers, the textures, and the geometry of the triangles
+    # left in the visibility buffer (micro indices, ~0.52 unique vertices per
+    # triangle of index + fp32 position / normal / uv)
+    vis_ids = np.unique(r.visibility().reshape(-1) & np.uint64(0xFFFFFFFF))
+    shown_tris = int(vis_ids.size)
+    tex_bytes = sum(int(d.host_textures[i].width) * int(d.host_textures[i].height) * 4 for i in range(d.n_textures))
     algo = {
         "cull_meshlets": cand * (MESHLET_BYTES + PREFIX_ENTRY_BYTES) + vis_ml * DRAW_WRITE_BYTES,
         "shadow_cull_meshlets": cand_sh * (MESHLET_BYTES + PREFIX_ENTRY_BYTES) + vis_sh * DRAW_WRITE_BYTES,
-        "resolve": npx * (VIS_PIXEL_BYTES + HDR_PIXEL_BYTES),
+        "resolve": npx * (VIS_PIXEL_BYTES + HDR_PIXEL_BYTES) + 4 * d.shadow_size ** 2 * 4 + tex_bytes +
+        int(shown_tris * (3 + 0.52 * (4 + 32))),
         "depth_fit": npx * VIS_PIXEL_BYTES,
         "clear": npx * 8 + 4 * d.shadow_size ** 2 * 4,
     }

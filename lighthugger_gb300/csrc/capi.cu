@@ -99,7 +99,7 @@ struct lh_ctx {
 namespace {
 
 // Tensor map of the main visibility buffer: u64 elements, W x H, boxes of
-// 32 x 1 (one warp's row segment in the resolve).  cuTensorMapEncodeTiled is reached through
+// 128 x 1 (one warp's row of a resolve strip).  cuTensorMapEncodeTiled is reached through
 // the runtime's driver entry point, so nothing links against libcuda.
 bool encode_vis_map(lh_ctx* c) {
     const uint64_t W = c->cfg.width, H = c->cfg.height;
@@ -114,7 +114,7 @@ bool encode_vis_map(lh_ctx* c) {
         return false;
     const cuuint64_t dims[2] = {W, H};
     const cuuint64_t strides[1] = {W * 8};
-    const cuuint32_t box[2] = {32, 1};
+    const cuuint32_t box[2] = {128, 1};
     const cuuint32_t elem[2] = {1, 1};
     return reinterpret_cast<Encode>(fn)(&c->vis_map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, c->d_vis, dims, strides, box,
                                         elem, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,

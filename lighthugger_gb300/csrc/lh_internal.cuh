@@ -114,7 +114,7 @@ cudaError_t launch_frame_persistent(const FrameDev& f, uint32_t n_persp, uint32_
                                     uint32_t raster_batch,
                                     float blocks_per_sm, cudaStream_t s, int sms);
 int persistent_blocks_per_sm();
-// vis_map: 2D tensor map of the main visibility buffer (u64, box 32 x 1) for
+// vis_map: 2D tensor map of the main visibility buffer (u64, box 128 x 1) for
 // the TMA-staged resolve, or null for per-thread loads.
 cudaError_t launch_resolve(const FrameDev& f, uint32_t width, uint32_t height, const CUtensorMap* vis_map,
                            cudaStream_t s, int sms);

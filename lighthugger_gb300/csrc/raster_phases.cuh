@@ -347,6 +347,8 @@ __device__ __forceinline__ void raster_meshlet(const FrameDev& f, const MeshletW
         ma = load_mesh_info_alpha(mesh_info_of(w.inst));
         as.tex = ma.tex;
     }
+    int32_t min_x = INT32_MAX, max_x = INT32_MIN, min_y = INT32_MAX, max_y = INT32_MIN;
+    uint32_t any_oc = 0;
     for (uint32_t j = lane; j < nv; j += 32) {
         uint32_t idx = load_index_raw(mi.indices, mi.flags, w.index_offset + j);
         f3 wp = world_pos(w.transform, load_position(mi.positions, mi.flags, idx));
@@ -356,7 +358,24 @@ __device__ __forceinline__ void raster_meshlet(const FrameDev& f, const MeshletW
         if (!oc) s = snap(c, w.hw, w.hh);
         sv[j] = s;
         so[j] = (uint8_t)oc;
+        any_oc |= oc;
+        min_x = min(min_x, s.X);
+        max_x = max(max_x, s.X);
+        min_y = min(min_y, s.Y);
+        max_y = max(max_y, s.Y);
         if (ALPHA) av[j] = alpha_vert(c, ma, mi.flags, idx);
+    }
+    // A meshlet whose snapped vertices (all inside the guard band) span no
+    // pixel centre produces no fragment: every triangle's bbox lies inside
+    // the vertices' bbox.  Common for far meshlets in small views.
+    if (nv > 0 && !__any_sync(0xFFFFFFFFu, any_oc != 0)) {
+        min_x = __reduce_min_sync(0xFFFFFFFFu, min_x);
+        max_x = __reduce_max_sync(0xFFFFFFFFu, max_x);
+        min_y = __reduce_min_sync(0xFFFFFFFFu, min_y);
+        max_y = __reduce_max_sync(0xFFFFFFFFu, max_y);
+        if (max((min_x + 127) >> 8, 0) > min((max_x - 128) >> 8, (int32_t)W - 1) ||
+            max((min_y + 127) >> 8, 0) > min((max_y - 128) >> 8, (int32_t)H - 1))
+            return;
     }
     const uint64_t mbase = mi.micro_indices + w.triangle_offset;
     const uint32_t nbytes = nt * 3;
@@ -605,6 +624,26 @@ __device__ __forceinline__ bool edge_rejects(int32_t ax, int32_t ay, int32_t bx,
            edge_at(ax, ay, bx, by, x0, y1) < bias && edge_at(ax, ay, bx, by, x1, y1) < bias;
 }
 
+// Number of entries of the ascending array base[0, n) that are <= c (the
+// upper bound), found by the whole warp: 32 probes per round narrow the
+// range 32-fold, so a queue of 16k triangles takes 3 dependent loads instead
+// of 14.
+__device__ __forceinline__ uint32_t upper_bound_warp(const uint32_t* base, uint32_t n, uint32_t c, uint32_t lane) {
+    uint32_t lo = 0, hi = n;  // the answer lies in [lo, hi]
+    for (;;) {
+        const uint32_t span = hi - lo;
+        const uint32_t step = span <= 32u ? 1u : (span + 31u) / 32u;
+        const uint32_t p = lo + lane * step;
+        const bool le = p < hi && __ldcg(base + p) <= c;
+        const uint32_t k = __popc(__ballot_sync(0xFFFFFFFFu, le));  // true lanes form a prefix
+        if (step == 1u) return lo + k;
+        const uint32_t nlo = k ? lo + (k - 1u) * step + 1u : lo;
+        const uint32_t nhi = (k < 32u && lo + k * step < hi) ? lo + k * step : hi;
+        lo = nlo;
+        hi = nhi;
+    }
+}
+
 // The pixels [x0, x1] x [y0, y1] of an alpha-tested big triangle, one
 // column per lane (not inlined, as the other alpha paths).
 template <int KIND>
@@ -635,25 +674,27 @@ __device__ void phase_raster_big(const FrameDev& f) {
     const unsigned long long total = packed & ((1ull << 40) - 1);
     const uint32_t lane = threadIdx.x & 31;
     if (ntri == 0) return;
+    constexpr uint32_t kChunkBatch = 4;  // chunks claimed per atomic
+    // chunk numbers fit 32 bits (push_big drops triangles beyond)
+    const uint32_t total32 = (uint32_t)min(total, 0xFFFFFFFFull);
+    uint32_t c = 0, c_end = 0;
     for (;;) {
-        unsigned long long c = 0;
-        if (lane == 0) c = atomicAdd(&f.status[kStBigClaim], 1u);
-        c = __shfl_sync(0xFFFFFFFFu, c, 0);
-        if (c >= total) break;
-        // upper_bound over the ascending chunk bases, minus one
-        uint32_t first = 0, count = ntri;
-        while (count > 0) {
-            uint32_t step = count / 2, cur = first + step;
-            bool greater = c >= f.big_base[cur];
-            first = greater ? cur + 1 : first;
-            count = greater ? count - (step + 1) : step;
+        if (c == c_end) {
+            uint32_t first_c = 0;
+            if (lane == 0) first_c = atomicAdd(&f.status[kStBigClaim], kChunkBatch);
+            first_c = __shfl_sync(0xFFFFFFFFu, first_c, 0);
+            if (first_c >= total32) break;
+            c = first_c;
+            c_end = first_c + min(kChunkBatch, total32 - first_c);
         }
+        const uint32_t first = upper_bound_warp(f.big_base, ntri, c, lane);
+        c++;
         if (first == 0) continue;
         const uint32_t i = first - 1;
         const BigTri b = f.big[i];
         const uint32_t nbx = (uint32_t)(b.px1 - b.px0) / kChunkCols + 1;
         const uint32_t nby = (uint32_t)(b.py1 - b.py0) / kChunkRows + 1;
-        const unsigned long long local = c - f.big_base[i];
+        const unsigned long long local = (c - 1u) - f.big_base[i];
         if (local >= (unsigned long long)nbx * nby) continue;  // chunk of a dropped triangle
         const int32_t cx = (int32_t)(local % nbx), cy = (int32_t)(local / nbx);
         const int32_t x0 = b.px0 + cx * kChunkCols, x1 = min(b.px1, x0 + kChunkCols - 1);

@@ -35,8 +35,8 @@ __device__ Tex4 sample_repeat(const FrameDev& f, uint32_t index, f2 uv) {
         uchar4 p = __ldg(reinterpret_cast<const uchar4*>(tex) + ((size_t)j * W + i));
         Tex4 r;
         if (t.srgb) { r.r = f.srgb_lut[p.x]; r.g = f.srgb_lut[p.y]; r.b = f.srgb_lut[p.z]; }
-        else { r.r = (float)p.x / 255.0f; r.g = (float)p.y / 255.0f; r.b = (float)p.z / 255.0f; }
-        r.a = (float)p.w / 255.0f;
+        else { r.r = (float)p.x * (1.0f / 255.0f); r.g = (float)p.y * (1.0f / 255.0f); r.b = (float)p.z * (1.0f / 255.0f); }
+        r.a = (float)p.w * (1.0f / 255.0f);
         return r;
     };
     Tex4 t00 = texel(ia, ja), t10 = texel(ib, ja), t01 = texel(ia, jb), t11 = texel(ib, jb);
@@ -72,7 +72,17 @@ __device__ float sample_shadow(const FrameDev& f, f2 uv, float layer_f, float re
 constexpr float kPi = 3.14159265358979323846f;
 
 // pbr.glsl:3-96
-__device__ __forceinline__ float F_Schlick1(float u, float f0, float f90) { return f0 + (f90 - f0) * powf(1.0f - u, 5.0f); }
+// The BRDF feeds no discrete decision, so it runs on approximate division,
+// reciprocal square root and multiplied-out integer powers (a few ulp; the
+// radiance is checked at 2^-10).  Everything that selects something -- the
+// barycentrics and world position (cascade, PCF taps, compare results) and
+// the view vector (face flip) -- stays in the oracle's IEEE arithmetic.
+__device__ __forceinline__ float pow5f(float x) {
+    const float x2 = x * x;
+    return x2 * x2 * x;
+}
+__device__ __forceinline__ f3 fast_normalize(f3 v) { return v * rsqrtf(dot(v, v)); }
+__device__ __forceinline__ float F_Schlick1(float u, float f0, float f90) { return f0 + (f90 - f0) * pow5f(1.0f - u); }
 __device__ __forceinline__ float Fd_Burley(float NoV, float NoL, float LoH, float rough) {
     float f90 = 0.5f + 2.0f * rough * LoH * LoH;
     float light = F_Schlick1(NoL, 1.0f, f90);
@@ -82,17 +92,17 @@ __device__ __forceinline__ float Fd_Burley(float NoV, float NoL, float LoH, floa
 __device__ __forceinline__ float D_GGX(float NoH, float a) {
     float a2 = a * a;
     float fq = (NoH * a2 - NoH) * NoH + 1.0f;
-    return a2 / (kPi * fq * fq);
+    return __fdividef(a2, kPi * fq * fq);
 }
 __device__ __forceinline__ float V_SmithGGXCorrelated(float NoV, float NoL, float a) {
     float a2 = a * a;
     float GGXL = NoV * sqrtf((-NoL * a2 + NoL) * NoL + a2);
     float GGXV = NoL * sqrtf((-NoV * a2 + NoV) * NoV + a2);
-    return 0.5f / (GGXV + GGXL);
+    return __fdividef(0.5f, GGXV + GGXL);
 }
 __device__ __forceinline__ float clampf(float x, float lo, float hi) { return gmin(gmax(x, lo), hi); }
 __device__ f3 BRDF(f3 v, f3 l, f3 n, float pr, float metallic, f3 base, bool thin) {
-    f3 h = normalize(v + l);
+    f3 h = fast_normalize(v + l);
     f3 diffuse = base * (1.0f - metallic);
     float refl = (1.5f - 1.0f) / (1.5f + 1.0f);
     refl = refl * refl;
@@ -103,7 +113,7 @@ __device__ f3 BRDF(f3 v, f3 l, f3 n, float pr, float metallic, f3 base, bool thi
     float LoH = clampf(dot(l, h), 0.0f, 1.0f);
     float rough = pr * pr;
     float D = D_GGX(NoH, rough);
-    float p = powf(1.0f - LoH, 5.0f);
+    float p = pow5f(1.0f - LoH);
     f3 F{f0.x + (1.0f - f0.x) * p, f0.y + (1.0f - f0.y) * p, f0.z + (1.0f - f0.z) * p};
     float V = V_SmithGGXCorrelated(NoV, NoL, rough);
     f3 Fr = F * (D * V);
@@ -120,7 +130,9 @@ __device__ f3 BRDF(f3 v, f3 l, f3 n, float pr, float metallic, f3 base, bool thi
 
 struct Bary { f3 lambda, ddx, ddy; };
 
-// vbuffer.glsl:11-63
+// vbuffer.glsl:11-63.  kDeriv: also the screen derivatives of lambda, which
+// only the normal-map path reads (computed there, not for every pixel).
+template <bool kDeriv>
 __device__ Bary calc_full_bary(f4 p0, f4 p1, f4 p2, f2 ndc, f2 win) {
     Bary r;
     f3 invW{1.0f / p0.w, 1.0f / p1.w, 1.0f / p2.w};
@@ -137,6 +149,7 @@ __device__ Bary calc_full_bary(f4 p0, f4 p1, f4 p2, f2 ndc, f2 win) {
     r.lambda.x = interpW * ((invW.x + dv.x * r.ddx.x) + dv.y * r.ddy.x);
     r.lambda.y = interpW * ((0.0f + dv.x * r.ddx.y) + dv.y * r.ddy.y);
     r.lambda.z = interpW * ((0.0f + dv.x * r.ddx.z) + dv.y * r.ddy.z);
+    if (!kDeriv) return r;
     r.ddx = r.ddx * (2.0f / win.x);
     r.ddy = r.ddy * (2.0f / win.y);
     ddxSum *= 2.0f / win.x;
@@ -206,6 +219,32 @@ __device__ __noinline__ f3 clock_view(long long start_time) {
 
 // render_geometry.comp:70-308 for pixel (x, y) of the main view, whose
 // visibility word is `vis`.
+// Normal mapping (render_geometry.comp:25-38, 225-232): the cotangent frame
+// from the screen derivatives of the world position and uv.  Not inlined:
+// the scenes' materials rarely carry normal maps.
+__device__ __noinline__ f3 apply_normal_map(const FrameDev& f, uint32_t tex, f2 uv, const lh_mat4& PV, f3 pa, f3 pb,
+                                            f3 pc, f3 us, f3 vs, f2 ndc, f2 win, f3 normal) {
+    Tex4 nt = sample_repeat(f, tex, uv);
+    f3 mn{nt.r * 255.0f / 127.0f - 128.0f / 127.0f, nt.g * 255.0f / 127.0f - 128.0f / 127.0f,
+          nt.b * 255.0f / 127.0f - 128.0f / 127.0f};
+    // screen derivatives of the world position and uv (the same barycentrics
+    // again, with their derivatives)
+    const Bary bd = calc_full_bary<true>(mul(PV, f4{pa.x, pa.y, pa.z, 1.0f}), mul(PV, f4{pb.x, pb.y, pb.z, 1.0f}),
+                                         mul(PV, f4{pc.x, pc.y, pc.z, 1.0f}), ndc, win);
+    const f3 wx = interp_deriv(bd, pa.x, pb.x, pc.x), wy = interp_deriv(bd, pa.y, pb.y, pc.y),
+             wz = interp_deriv(bd, pa.z, pb.z, pc.z);
+    const f3 wdx{wx.y, wy.y, wz.y}, wdy{wx.z, wy.z, wz.z};
+    const f3 uvx = interp_deriv(bd, us.x, us.y, us.z), uvy = interp_deriv(bd, vs.x, vs.y, vs.z);
+    const f2 uvdx{uvx.y, uvy.y}, uvdy{uvx.z, uvy.z};
+    f3 dpy = cross(wdy, normal), dpx = cross(normal, wdx);
+    f3 t = dpy * uvdx.x + dpx * uvdy.x;
+    f3 b = dpy * uvdx.y + dpx * uvdy.y;
+    float invmax = 1.0f / sqrtf(gmax(dot(t, t), dot(b, b)));
+    f3 tt = t * invmax, bb = b * invmax;
+    return normalize(f3{(tt.x * mn.x + bb.x * mn.y) + normal.x * mn.z, (tt.y * mn.x + bb.y * mn.y) + normal.y * mn.z,
+                        (tt.z * mn.x + bb.z * mn.y) + normal.z * mn.z});
+}
+
 // `clock_slot`: the thread's shared-memory word for the clock view's start
 // time (kept out of registers).
 __device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uint32_t y, unsigned long long vis,
@@ -244,27 +283,32 @@ __device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uin
     f3 pb = world_pos(T, load_position(mi.positions, flags, idx[1]));
     f3 pc = world_pos(T, load_position(mi.positions, flags, idx[2]));
     const lh_mat4& PV = u.combined_perspective_view;
-    Bary bary = calc_full_bary(mul(PV, f4{pa.x, pa.y, pa.z, 1.0f}), mul(PV, f4{pb.x, pb.y, pb.z, 1.0f}),
-                               mul(PV, f4{pc.x, pc.y, pc.z, 1.0f}), ndc, f2{(float)W, (float)H});
-    f3 wx = interp_deriv(bary, pa.x, pb.x, pc.x), wy = interp_deriv(bary, pa.y, pb.y, pc.y),
-       wz = interp_deriv(bary, pa.z, pb.z, pc.z);
-    f3 world{wx.x, wy.x, wz.x}, wdx{wx.y, wy.y, wz.y}, wdy{wx.z, wy.z, wz.z};
+    const Bary bary = calc_full_bary<false>(mul(PV, f4{pa.x, pa.y, pa.z, 1.0f}), mul(PV, f4{pb.x, pb.y, pb.z, 1.0f}),
+                                            mul(PV, f4{pc.x, pc.y, pc.z, 1.0f}), ndc, f2{(float)W, (float)H});
+    const f3 world{dot(f3{pa.x, pb.x, pc.x}, bary.lambda), dot(f3{pa.y, pb.y, pc.y}, bary.lambda),
+                   dot(f3{pa.z, pb.z, pc.z}, bary.lambda)};
     f2 ua = load_uv_raw(mi.uvs, flags, idx[0]), ub = load_uv_raw(mi.uvs, flags, idx[1]),
        uc = load_uv_raw(mi.uvs, flags, idx[2]);
     f2 ts{mi.texture_scale.x, mi.texture_scale.y};
-    f3 uvx = interp_deriv(bary, ua.x * ts.x, ub.x * ts.x, uc.x * ts.x);
-    f3 uvy = interp_deriv(bary, ua.y * ts.y, ub.y * ts.y, uc.y * ts.y);
-    f2 uv{uvx.x + mi.texture_offset.x, uvy.x + mi.texture_offset.y};
-    f2 uvdx{uvx.y, uvy.y}, uvdy{uvx.z, uvy.z};
+    const f3 us{ua.x * ts.x, ub.x * ts.x, uc.x * ts.x}, vs{ua.y * ts.y, ub.y * ts.y, uc.y * ts.y};
+    f2 uv{dot(us, bary.lambda) + mi.texture_offset.x, dot(vs, bary.lambda) + mi.texture_offset.y};
     f3 view_vector = normalize(ld3(u.camera_pos) - world);
-    f3 na = normalize(load_normal_raw(mi.normals, flags, idx[0]));
-    f3 nb = normalize(load_normal_raw(mi.normals, flags, idx[1]));
-    f3 nc = normalize(load_normal_raw(mi.normals, flags, idx[2]));
+    f3 na = fast_normalize(load_normal_raw(mi.normals, flags, idx[0]));
+    f3 nb = fast_normalize(load_normal_raw(mi.normals, flags, idx[1]));
+    f3 nc = fast_normalize(load_normal_raw(mi.normals, flags, idx[2]));
     f3 normal{interp_deriv(bary, na.x, nb.x, nc.x).x, interp_deriv(bary, na.y, nb.y, nc.y).x,
               interp_deriv(bary, na.z, nb.z, nc.z).x};
-    normal = normalize(mul3(inst->normal_transform, normal));
+    normal = fast_normalize(mul3(inst->normal_transform, normal));
     f3 gn = cross(pb - pa, pc - pa);
     if (dot(gn, view_vector) < 0.0f) normal = -normal;
+    // materials first (they need the geometry the shadow code below does not,
+    // so its registers free up early; the order changes no result)
+    Tex4 bc = sample_repeat(f, mi.base_tex, uv);
+    f3 base{bc.r * mi.base_color_factor.x, bc.g * mi.base_color_factor.y, bc.b * mi.base_color_factor.z};
+    Tex4 mr = sample_repeat(f, mi.mr_tex, uv);
+    float roughness = mr.g, metallic = mr.b;
+    if (mi.normal_tex != UNUSED_TEXTURE_INDEX)
+        normal = apply_normal_map(f, mi.normal_tex, uv, PV, pa, pb, pc, us, vs, ndc, f2{(float)W, (float)H}, normal);
     uint32_t ci;
     f4 sc{0.0f, 0.0f, 0.0f, 0.0f};
     for (ci = 0; ci < 4; ci++) {
@@ -283,22 +327,6 @@ __device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uin
         }
     shadow_sum /= 9.0f;
     if (sc.z > 1.0f) shadow_sum = 1.0f;
-    Tex4 bc = sample_repeat(f, mi.base_tex, uv);
-    f3 base{bc.r * mi.base_color_factor.x, bc.g * mi.base_color_factor.y, bc.b * mi.base_color_factor.z};
-    Tex4 mr = sample_repeat(f, mi.mr_tex, uv);
-    float roughness = mr.g, metallic = mr.b;
-    if (mi.normal_tex != UNUSED_TEXTURE_INDEX) {
-        Tex4 nt = sample_repeat(f, mi.normal_tex, uv);
-        f3 mn{nt.r * 255.0f / 127.0f - 128.0f / 127.0f, nt.g * 255.0f / 127.0f - 128.0f / 127.0f,
-              nt.b * 255.0f / 127.0f - 128.0f / 127.0f};
-        f3 dpy = cross(wdy, normal), dpx = cross(normal, wdx);
-        f3 t = dpy * uvdx.x + dpx * uvdy.x;
-        f3 b = dpy * uvdx.y + dpx * uvdy.y;
-        float invmax = 1.0f / sqrtf(gmax(dot(t, t), dot(b, b)));
-        f3 tt = t * invmax, bb = b * invmax;
-        normal = normalize(f3{(tt.x * mn.x + bb.x * mn.y) + normal.x * mn.z, (tt.y * mn.x + bb.y * mn.y) + normal.y * mn.z,
-                              (tt.z * mn.x + bb.z * mn.y) + normal.z * mn.z});
-    }
     // AMBIENT_SH (render_geometry.comp:40-57): only sh[0] = sh[2] = 0.025.
     if (u.debug != 0 && u.debug != 4) {
         const f3 o = debug_view(u.debug, base, ci, tri, ref.meshlet_index, normal);
@@ -321,46 +349,56 @@ __device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uin
     __stcs(out, make_float4(o.x, o.y, o.z, 1.0f));
 }
 
-constexpr uint32_t kResolveWarps = 8;   // warps per block
-constexpr uint32_t kResolveStages = 4;  // visibility rows in flight per warp
+constexpr uint32_t kResolveWarps = 8;   // warps per block = rows of a strip
+constexpr uint32_t kStripCols = 128;    // a strip: 128 x 8 pixels (4 tiles of 32 x 8)
+constexpr uint32_t kResolveStages = 2;  // strips in flight per warp
 
-// One thread per pixel, one warp per 32-pixel row segment; the grid's warps
-// stride over the segments.  With kTma each warp stages the visibility words
-// of its next kResolveStages segments in shared memory with TMA row loads
-// (box 32 x 1, one mbarrier per stage), issued by its lane 0; nothing
-// synchronises beyond the warp.  Without (rows not 16-byte aligned) each
-// thread loads its own word.
+// One thread per pixel over 128 x 8-pixel strips, one warp per strip row
+// (four 32-pixel steps); a grid of resident blocks strides over the strips,
+// so a block's warps shade the 8 rows of one strip together and their
+// gathers stay close in 2D.  With kTma each warp stages the visibility words
+// of its row of its next kResolveStages strips in shared memory with TMA row
+// loads (box 128 x 1 = 1 KB, one mbarrier per stage) issued by its lane 0;
+// nothing synchronises beyond the warp.  Without (rows not 16-byte aligned)
+// each thread loads its own words.
 template <bool kTma>
 __global__ void __launch_bounds__(kResolveWarps * 32, 3)
-    k_resolve(FrameDev f, const __grid_constant__ CUtensorMap vis_map, uint32_t segs_x, uint32_t n_segs) {
-    __shared__ __align__(128) unsigned long long s_vis[kResolveWarps][kResolveStages][32];
+    k_resolve(FrameDev f, const __grid_constant__ CUtensorMap vis_map, uint32_t strips_x, uint32_t n_strips) {
+    __shared__ __align__(128) unsigned long long s_vis[kResolveWarps][kResolveStages][kStripCols];
     __shared__ __align__(8) uint64_t s_bar[kResolveWarps][kResolveStages];
     __shared__ long long s_clock[kResolveWarps][32];
     const uint32_t W = f.uniforms->window_size.x, H = f.uniforms->window_size.y;
     const uint32_t lane = threadIdx.x, warp = threadIdx.y;
-    const uint32_t gwarp = blockIdx.x * kResolveWarps + warp, nwarps = gridDim.x * kResolveWarps;
-    unsigned long long(*vis_buf)[32] = s_vis[warp];
+    unsigned long long(*vis_buf)[kStripCols] = s_vis[warp];
     uint64_t* bar = s_bar[warp];
+    constexpr uint32_t kRowBytes = kStripCols * 8;
+    // the warp's row of strip `t` and whether it holds pixels
+    auto row_of = [&](uint32_t t, int32_t& x0, int32_t& y) {
+        x0 = (int32_t)((t % strips_x) * kStripCols);
+        y = (int32_t)((t / strips_x) * kResolveWarps + warp);
+        return (uint32_t)y < H;
+    };
     if (kTma) {
         if (lane == 0) {
             for (uint32_t k = 0; k < kResolveStages; k++) mbar_init(&bar[k], 1);
             mbar_init_fence();
             for (uint32_t k = 0; k < kResolveStages; k++) {
-                const uint32_t seg = gwarp + k * nwarps;
-                if (seg >= n_segs) break;
-                mbar_expect_tx(&bar[k], 32 * 8);
-                tma_load_2d(vis_buf[k], &vis_map, (int32_t)((seg % segs_x) * 32), (int32_t)(seg / segs_x), &bar[k]);
+                const uint32_t t = blockIdx.x + k * gridDim.x;
+                int32_t x0, y;
+                if (t >= n_strips) break;
+                if (!row_of(t, x0, y)) continue;
+                mbar_expect_tx(&bar[k], kRowBytes);
+                tma_load_2d(vis_buf[k], &vis_map, x0, y, &bar[k]);
             }
         }
         __syncwarp();
     }
     uint32_t k = 0;
-    for (uint32_t seg = gwarp; seg < n_segs; seg += nwarps, k++) {
-        const uint32_t x = (seg % segs_x) * 32 + lane, y = seg / segs_x;
-        const bool inside = x < W;
-        unsigned long long vis = 0;
+    for (uint32_t t = blockIdx.x; t < n_strips; t += gridDim.x, k++) {
+        int32_t x0, y;
+        if (!row_of(t, x0, y)) continue;  // below the image (last strip row): no load was issued
+        const uint32_t st = k % kResolveStages;
         if (kTma) {
-            const uint32_t st = k % kResolveStages;
             const bool ok = mbar_wait(&bar[st], (k / kResolveStages) & 1u);
             if (__any_sync(0xFFFFFFFFu, !ok)) {
                 // a copy that never landed: report it, wait (bounded) for the
@@ -368,27 +406,34 @@ __global__ void __launch_bounds__(kResolveWarps * 32, 3)
                 if (lane == 0) {
                     atomicOr(&f.status[kStFlags], LH_FLAG_TIMEOUT);
                     for (uint32_t j = 1; j < kResolveStages; j++) {
-                        const uint32_t kk = k + j;
-                        if (seg + j * nwarps >= n_segs) break;
-                        mbar_wait(&bar[kk % kResolveStages], (kk / kResolveStages) & 1u);
+                        const uint32_t kk = k + j, tt = t + j * gridDim.x;
+                        int32_t xx, yy;
+                        if (tt >= n_strips) break;
+                        if (row_of(tt, xx, yy)) mbar_wait(&bar[kk % kResolveStages], (kk / kResolveStages) & 1u);
                     }
                 }
                 break;
             }
-            vis = vis_buf[st][lane];
-            __syncwarp();  // stage st is free again
-            const uint32_t next = seg + kResolveStages * nwarps;
-            if (lane == 0 && next < n_segs) {
-                mbar_expect_tx(&bar[st], 32 * 8);
-                tma_load_2d(vis_buf[st], &vis_map, (int32_t)((next % segs_x) * 32), (int32_t)(next / segs_x),
-                            &bar[st]);
-            }
-        } else if (inside) {
-            vis = __ldcs(reinterpret_cast<const unsigned long long*>(f.visibility) + (size_t)y * W + x);
         }
-        if (inside) resolve_pixel(f, x, y, vis, &s_clock[warp][lane]);
+#pragma unroll 1
+        for (uint32_t j = 0; j < kStripCols / 32; j++) {
+            const uint32_t x = (uint32_t)x0 + 32 * j + lane;
+            if (x >= W) continue;
+            const unsigned long long vis =
+                kTma ? vis_buf[st][32 * j + lane]
+                     : __ldcs(reinterpret_cast<const unsigned long long*>(f.visibility) + (size_t)y * W + x);
+            resolve_pixel(f, x, (uint32_t)y, vis, &s_clock[warp][lane]);
+        }
+        if (kTma) {
+            __syncwarp();  // stage st is free again; the other stage's strip is already in flight
+            const uint32_t next = t + kResolveStages * gridDim.x;
+            int32_t nx0, ny;
+            if (lane == 0 && next < n_strips && row_of(next, nx0, ny)) {
+                mbar_expect_tx(&bar[st], kRowBytes);
+                tma_load_2d(vis_buf[st], &vis_map, nx0, ny, &bar[st]);
+            }
+        }
     }
-    (void)H;
 }
 
 // grid = (blocks, n_views)
@@ -423,16 +468,19 @@ cudaError_t launch_depth_reduce_fit(const FrameDev& f, cudaStream_t s, int sms) 
 
 cudaError_t launch_resolve(const FrameDev& f, uint32_t width, uint32_t height, const CUtensorMap* vis_map,
                            cudaStream_t s, int sms) {
-    const uint32_t segs_x = (width + 31) / 32;
-    const uint32_t n_segs = segs_x * height;
-    if (n_segs == 0) return cudaSuccess;
-    const uint32_t grid = std::min<uint32_t>((n_segs + kResolveWarps - 1) / kResolveWarps, (uint32_t)sms * 3u);
+    const uint32_t strips_x = (width + kStripCols - 1) / kStripCols, strips_y = (height + kResolveWarps - 1) / kResolveWarps;
+    const uint32_t n_strips = strips_x * strips_y;
+    if (n_strips == 0) return cudaSuccess;
+    const uint32_t grid = std::min<uint32_t>(n_strips, (uint32_t)sms * 3u);
+#ifdef LH_RESOLVE_NO_TMA
+    vis_map = nullptr;  // comparison builds: per-thread loads of the visibility words
+#endif
     if (vis_map) {
-        k_resolve<true><<<grid, dim3(32, kResolveWarps), 0, s>>>(f, *vis_map, segs_x, n_segs);
+        k_resolve<true><<<grid, dim3(32, kResolveWarps), 0, s>>>(f, *vis_map, strips_x, n_strips);
     } else {
         CUtensorMap none;
         std::memset(&none, 0, sizeof(none));
-        k_resolve<false><<<grid, dim3(32, kResolveWarps), 0, s>>>(f, none, segs_x, n_segs);
+        k_resolve<false><<<grid, dim3(32, kResolveWarps), 0, s>>>(f, none, strips_x, n_strips);
     }
     return cudaGetLastError();
 }
