@@ -301,7 +301,11 @@ __device__ __forceinline__ bool make_setup(SnapV v0, SnapV v1, SnapV v2, uint32_
              (top_left(v0.X, v0.Y, v1.X, v1.Y) ? 0u : 4u);
     // pixel centres of the bbox lie inside the vertex extents, so each
     // product of an edge function is at most ext_x * ext_y in magnitude
-    if ((int64_t)(maxX - minX) * (int64_t)(maxY - minY) < (1ll << 30)) t.bias |= 8u;
+    // (and, so that per-pixel steps of 256 units fit too, both extents are
+    // below 2^22)
+    if ((int64_t)(maxX - minX) * (int64_t)(maxY - minY) < (1ll << 30) && maxX - minX < (1 << 22) &&
+        maxY - minY < (1 << 22))
+        t.bias |= 8u;
     return true;
 }
 
@@ -318,6 +322,40 @@ __device__ __forceinline__ float edge_to_float(int64_t e) {
 #else
     return __ll2float_rn(e);
 #endif
+}
+
+// The three edge functions of a small triangle (bias bit 3) at the centre
+// of its bbox's first pixel and their steps per pixel in x and y: the
+// function at pixel (px0 + rx, py0 + ry) is e0 + rx * dx + ry * dy, the same
+// integer cover() forms, with every partial sum inside the 32-bit range.
+struct EdgeSteps {
+    int32_t e0[3], dx[3], dy[3];
+};
+__device__ __forceinline__ EdgeSteps edge_steps(const TriSetup& t) {
+    const int32_t Px = t.px0 * 256 + 128, Py = t.py0 * 256 + 128;
+    EdgeSteps s;
+    s.e0[0] = (t.Y2 - t.Y1) * (Px - t.X1) - (t.X2 - t.X1) * (Py - t.Y1);
+    s.e0[1] = (t.Y0 - t.Y2) * (Px - t.X2) - (t.X0 - t.X2) * (Py - t.Y2);
+    s.e0[2] = (t.Y1 - t.Y0) * (Px - t.X0) - (t.X1 - t.X0) * (Py - t.Y0);
+    s.dx[0] = (t.Y2 - t.Y1) * 256;
+    s.dx[1] = (t.Y0 - t.Y2) * 256;
+    s.dx[2] = (t.Y1 - t.Y0) * 256;
+    s.dy[0] = -(t.X2 - t.X1) * 256;
+    s.dy[1] = -(t.X0 - t.X2) * 256;
+    s.dy[2] = -(t.X1 - t.X0) * 256;
+    return s;
+}
+__device__ __forceinline__ bool cover_step(const TriSetup& t, const EdgeSteps& s, int32_t rx, int32_t ry,
+                                           float& depth) {
+    const int32_t e12 = s.e0[0] + rx * s.dx[0] + ry * s.dy[0];
+    const int32_t e20 = s.e0[1] + rx * s.dx[1] + ry * s.dy[1];
+    const int32_t e01 = s.e0[2] + rx * s.dx[2] + ry * s.dy[2];
+    if (e12 < (int32_t)(t.bias & 1u) || e20 < (int32_t)((t.bias >> 1) & 1u) || e01 < (int32_t)((t.bias >> 2) & 1u))
+        return false;
+    float d = (t.z0 + i32_to_f32_rn(e20) * t.s1) + i32_to_f32_rn(e01) * t.s2;
+    d = d > 0.0f ? d : 0.0f;
+    depth = d < 1.0f ? d : 1.0f;
+    return true;
 }
 
 // Coverage + depth of pixel (px, py); returns false when not covered.

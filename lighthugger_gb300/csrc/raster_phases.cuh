@@ -240,6 +240,15 @@ __device__ __forceinline__ AlphaTri alpha_of(const TriSetup& t, const AlphaSrc& 
 
 template <int KIND>
 __device__ __forceinline__ void raster_lane(const TriSetup& t, void* target, uint32_t W) {
+    if (t.bias & 8u) {
+        const EdgeSteps es = edge_steps(t);
+        for (int32_t ry = 0; ry <= t.py1 - t.py0; ry++)
+            for (int32_t rx = 0; rx <= t.px1 - t.px0; rx++) {
+                float d;
+                if (cover_step(t, es, rx, ry, d)) write_fragment<KIND>(target, W, t.px0 + rx, t.py0 + ry, d, t.id);
+            }
+        return;
+    }
     for (int32_t py = t.py0; py <= t.py1; py++)
         for (int32_t px = t.px0; px <= t.px1; px++) {
             float d;
