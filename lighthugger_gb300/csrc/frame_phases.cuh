@@ -125,6 +125,7 @@ __device__ void phase_depth_reduce(const FrameDev& f, uint64_t tid, uint64_t str
     uint32_t mn = 0xFFFFFFFFu, mx = 0u;
     const uint4* p = reinterpret_cast<const uint4*>(f.visibility);
     const uint64_t n2 = npx / 2;
+#pragma unroll 4
     for (uint64_t i = tid; i < n2; i += stride) {
         uint4 v = __ldcs(p + i);  // streaming: each pixel is read once
         uint32_t d0 = v.y, d1 = v.w;
@@ -139,9 +140,23 @@ __device__ void phase_depth_reduce(const FrameDev& f, uint64_t tid, uint64_t str
     }
     mn = __reduce_min_sync(0xFFFFFFFFu, mn);
     mx = __reduce_max_sync(0xFFFFFFFFu, mx);
+    // then across the block's warps: one pair of atomics per block
+    __shared__ uint32_t s_mn[32], s_mx[32];
+    const uint32_t warp = threadIdx.x >> 5, nwarps = (blockDim.x + 31) >> 5;
     if ((threadIdx.x & 31) == 0) {
-        if (mn != 0xFFFFFFFFu) atomicMin(&f.misc->min_depth, mn);
-        atomicMax(&f.misc->max_depth, mx);
+        s_mn[warp] = mn;
+        s_mx[warp] = mx;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        mn = threadIdx.x < nwarps ? s_mn[threadIdx.x] : 0xFFFFFFFFu;
+        mx = threadIdx.x < nwarps ? s_mx[threadIdx.x] : 0u;
+        mn = __reduce_min_sync(0xFFFFFFFFu, mn);
+        mx = __reduce_max_sync(0xFFFFFFFFu, mx);
+        if (threadIdx.x == 0) {
+            if (mn != 0xFFFFFFFFu) atomicMin(&f.misc->min_depth, mn);
+            atomicMax(&f.misc->max_depth, mx);
+        }
     }
 }
 

@@ -720,7 +720,28 @@ __device__ void phase_raster_big(const FrameDev& f) {
             continue;
         }
         // edge functions at the top of the lane's column, then one add per
-        // row (the same integers cover() forms, so the same coverage/depth)
+        // row (the same integers cover() forms, so the same coverage/depth);
+        // 32-bit when the triangle's edge products fit (bias bit 3: every
+        // value in its bbox, and one row step beyond, stays below 2^31)
+        if (b.bias & 8u) {
+            const int32_t d12 = -(b.X2 - b.X1) * 256, d20 = -(b.X0 - b.X2) * 256, d01 = -(b.X1 - b.X0) * 256;
+            const int32_t b12 = b.bias & 1u, b20 = (b.bias >> 1) & 1u, b01 = (b.bias >> 2) & 1u;
+            const int32_t Py0 = y0 * 256 + 128;
+            for (int32_t px = x0 + (int32_t)lane; px <= x1; px += 32) {
+                const int32_t Px = px * 256 + 128;
+                int32_t e12 = (b.Y2 - b.Y1) * (Px - b.X1) - (b.X2 - b.X1) * (Py0 - b.Y1);
+                int32_t e20 = (b.Y0 - b.Y2) * (Px - b.X2) - (b.X0 - b.X2) * (Py0 - b.Y2);
+                int32_t e01 = (b.Y1 - b.Y0) * (Px - b.X0) - (b.X1 - b.X0) * (Py0 - b.Y0);
+                for (int32_t py = y0; py <= y1; py++, e12 += d12, e20 += d20, e01 += d01) {
+                    if (e12 < b12 || e20 < b20 || e01 < b01) continue;
+                    float d = (b.z0 + i32_to_f32_rn(e20) * b.s1) + i32_to_f32_rn(e01) * b.s2;
+                    d = d > 0.0f ? d : 0.0f;
+                    d = d < 1.0f ? d : 1.0f;
+                    write_fragment<KIND>(target, W, px, py, d, b.id);
+                }
+            }
+            continue;
+        }
         const int64_t d12 = -(int64_t)(b.X2 - b.X1) * 256, d20 = -(int64_t)(b.X0 - b.X2) * 256,
                       d01 = -(int64_t)(b.X1 - b.X0) * 256;
         const int64_t b12 = b.bias & 1u, b20 = (b.bias >> 1) & 1u, b01 = (b.bias >> 2) & 1u;
