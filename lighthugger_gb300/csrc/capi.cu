@@ -414,7 +414,7 @@ lh_status lh_create(const lh_config* config, lh_ctx** out) {
     if (!c) return LH_ERR_OUT_OF_MEMORY;
     c->cfg = cfg;
     c->device = cfg.device;
-    c->tuning = lh_tuning{8u, 256u, 2.0f, LH_SCHEDULE_DEFAULT, 0u};
+    c->tuning = lh_tuning{32u, 128u, 2.0f, LH_SCHEDULE_DEFAULT, 0u};
     cudaError_t e = cudaSetDevice(c->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device);
     c->max_views = 5 + cfg.max_probes;

@@ -320,9 +320,35 @@ LH_HD void decide_at(F& fx, const PixelParams<T>& p, v3<T> world, const Sampler&
     fx.flip = dot(gn, V) < T(0) ? -1.0f : 1.0f;
     v3<T> sc = xform_uvs(fx, world, T(1));
     T scw = xform_uvs_w(fx, world, T(1));
-    sc = {sc.x / scw, sc.y / scw, sc.z / scw};
+    if (scw != T(1)) sc = {sc.x / scw, sc.y / scw, sc.z / scw};  // x / 1 = x
     fx.shadow_const = sc.z > T(1) ? 1u : 0u;
     const uint32_t layer = fx.cascade > 3 ? 3u : fx.cascade;
+    const T S = T(fx.shadow_size), ref = sc.z - T(fx.bias);
+    // The taps' texel columns / rows: when consecutive (one texel apart, a
+    // 1024-texel cascade) the 4 x 4 texels they share are compared once and
+    // the 36 results picked from them; otherwise tap by tap.
+    int32_t ix[3], iy[3];
+    for (int k = 0; k < 3; k++) {
+        T uu = (sc.x + T(k - 1) / T(1024)) * S - T(0.5), vv = (sc.y + T(k - 1) / T(1024)) * S - T(0.5);
+        if (!(tabs(uu) < T(1e9))) uu = T(0);
+        if (!(tabs(vv) < T(1e9))) vv = T(0);
+        ix[k] = (int32_t)tfloor(uu);
+        iy[k] = (int32_t)tfloor(vv);
+    }
+    if (ix[1] == ix[0] + 1 && ix[2] == ix[1] + 1 && iy[1] == iy[0] + 1 && iy[2] == iy[1] + 1) {
+        uint32_t win = 0;  // bit 4 * row + column of the window at (ix[0], iy[0])
+        for (int r = 0; r < 4; r++)
+            for (int c = 0; c < 4; c++)
+                win |= (smp.shadow_cmp(layer, ix[0] + c, iy[0] + r, ref) != T(0) ? 1u : 0u) << (4 * r + c);
+        uint64_t bits = 0;
+        for (int ox = 0; ox < 3; ox++)
+            for (int oy = 0; oy < 3; oy++) {
+                const uint32_t q = win >> (4 * oy + ox);
+                bits |= (uint64_t)((q & 3u) | ((q >> 2) & 12u)) << (4 * (ox * 3 + oy));
+            }
+        fx.cmp = bits;
+        return;
+    }
     uint64_t bits = 0;
     for (int ox = -1; ox <= 1; ox++)
         for (int oy = -1; oy <= 1; oy++) {
