@@ -148,8 +148,12 @@ __device__ __forceinline__ void cache_add(HotCache& c, float* addr, float v) {
 // Runs of equal keys along the warp (a warp is one row of 32 pixels, so a
 // triangle or a texel covers contiguous lanes): `end` is one past the last
 // lane of this lane's run, `head` marks its first lane.
+#ifndef LH_RUN_SPAN
+#define LH_RUN_SPAN 1
+#endif
 struct Run {
-    uint32_t end;
+    uint32_t end;   // first lane after this lane's run
+    uint32_t span;  // longest run of the warp (warp uniform)
     bool head;
 };
 
@@ -159,18 +163,29 @@ __device__ __forceinline__ Run run_of(unsigned long long key) {
     const bool head = lane == 0 || prev != key;
     const uint32_t heads = __ballot_sync(kFull, head);
     const uint32_t later = heads & ~((2u << lane) - 1u);
-    return {later ? (uint32_t)__ffs(later) - 1u : 32u, head};
+    const uint32_t end = later ? (uint32_t)__ffs(later) - 1u : 32u;
+    return {end, __reduce_max_sync(kFull, end - lane), head};
 }
 
-// Sum of v over the lanes [lane, end) of the run: the full run sum at its head.
-__device__ __forceinline__ float run_sum(float v, const Run& r) {
+// Sums of v[i] over the lanes [lane, end) of the run: the full run sums at
+// its head.  Doubling steps stop at the warp's longest run: a step of
+// o >= span adds nothing for any lane (end - lane <= span), so the sums are
+// those of the full five steps; the N values share each step's shuffles.
+template <int N>
+__device__ __forceinline__ void run_sums(float (&v)[N], const Run& r) {
     const uint32_t lane = threadIdx.x;
+#if LH_RUN_SPAN
+    for (uint32_t o = 1; o < r.span; o <<= 1) {
+#else
 #pragma unroll
     for (uint32_t o = 1; o < 32; o <<= 1) {
-        const float w = __shfl_down_sync(kFull, v, o);
-        if (lane + o < r.end) v += w;
+#endif
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            const float w = __shfl_down_sync(kFull, v[i], o);
+            if (lane + o < r.end) v[i] += w;
+        }
     }
-    return v;
 }
 
 // What the scatter needs of a differentiated pixel besides its gradients.
@@ -307,12 +322,15 @@ __device__ __forceinline__ void scatter_texels(HotCache& cache, float* const bas
     for (int q = 0; q < 4; q++) {
         if (!__any_sync(kFull, a[q] != nullptr)) continue;
         const Run r = run_of((unsigned long long)a[q]);
+        float s[NC];
 #pragma unroll
-        for (int c = 0; c < NC; c++) {
-            const float s = run_sum(v[q][c], r);
-            if (r.head && a[q]) {
-                if (small) cache_add(cache, a[q] + c0 + c, s);
-                else atomicAdd(a[q] + c0 + c, s);
+        for (int c = 0; c < NC; c++) s[c] = v[q][c];
+        run_sums(s, r);
+        if (r.head && a[q]) {
+#pragma unroll
+            for (int c = 0; c < NC; c++) {
+                if (small) cache_add(cache, a[q] + c0 + c, s[c]);
+                else atomicAdd(a[q] + c0 + c, s[c]);
             }
         }
     }
@@ -376,13 +394,12 @@ __global__ void __launch_bounds__(kBwdThreads, LH_BWD_MIN_BLOCKS)
         float* bcf_dst = mg ? reinterpret_cast<float*>(mg->base_color_factor) : nullptr;
         if (__any_sync(kFull, bcf_dst != nullptr)) {
             const Run r = run_of((unsigned long long)bcf_dst);
-            const float bx = run_sum(bcf_dst ? g.bcf.x : 0.0f, r);
-            const float by = run_sum(bcf_dst ? g.bcf.y : 0.0f, r);
-            const float bz = run_sum(bcf_dst ? g.bcf.z : 0.0f, r);
+            float b[3] = {bcf_dst ? g.bcf.x : 0.0f, bcf_dst ? g.bcf.y : 0.0f, bcf_dst ? g.bcf.z : 0.0f};
+            run_sums(b, r);
             if (r.head && bcf_dst) {
-                cache_add(cache, bcf_dst, bx);
-                cache_add(cache, bcf_dst + 1, by);
-                cache_add(cache, bcf_dst + 2, bz);
+                cache_add(cache, bcf_dst, b[0]);
+                cache_add(cache, bcf_dst + 1, b[1]);
+                cache_add(cache, bcf_dst + 2, b[2]);
             }
         }
         if (tex_targets) {
@@ -426,8 +443,7 @@ __global__ void __launch_bounds__(kBwdThreads, LH_BWD_MIN_BLOCKS)
                 v[k * 8 + 6] = g.UV[k].x;
                 v[k * 8 + 7] = g.UV[k].y;
             }
-#pragma unroll
-            for (int i = 0; i < 24; i++) v[i] = run_sum(v[i], r);
+            run_sums(v, r);
             if (r.head && mg) {
                 const lh_mesh_grads d = *mg;
                 const lh_mat4& T = o.inst->transform;

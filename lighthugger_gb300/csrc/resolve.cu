@@ -403,6 +403,9 @@ __device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uin
     __stcs(out, make_float4(o.x, o.y, o.z, 1.0f));
 }
 
+#ifndef LH_RESOLVE_MIN_BLOCKS
+#define LH_RESOLVE_MIN_BLOCKS 3
+#endif
 constexpr uint32_t kResolveWarps = 8;   // warps per block = rows of a strip
 constexpr uint32_t kStripCols = 128;    // a strip: 128 x 8 pixels (4 tiles of 32 x 8)
 constexpr uint32_t kResolveStages = 2;  // strips in flight per warp
@@ -416,7 +419,7 @@ constexpr uint32_t kResolveStages = 2;  // strips in flight per warp
 // nothing synchronises beyond the warp.  Without (rows not 16-byte aligned)
 // each thread loads its own words.
 template <bool kTma>
-__global__ void __launch_bounds__(kResolveWarps * 32, 3)
+__global__ void __launch_bounds__(kResolveWarps * 32, LH_RESOLVE_MIN_BLOCKS)
     k_resolve(FrameDev f, const __grid_constant__ CUtensorMap vis_map, uint32_t strips_x, uint32_t n_strips) {
     __shared__ __align__(128) unsigned long long s_vis[kResolveWarps][kResolveStages][kStripCols];
     __shared__ __align__(8) uint64_t s_bar[kResolveWarps][kResolveStages];
@@ -525,7 +528,7 @@ cudaError_t launch_resolve(const FrameDev& f, uint32_t width, uint32_t height, c
     const uint32_t strips_x = (width + kStripCols - 1) / kStripCols, strips_y = (height + kResolveWarps - 1) / kResolveWarps;
     const uint32_t n_strips = strips_x * strips_y;
     if (n_strips == 0) return cudaSuccess;
-    const uint32_t grid = std::min<uint32_t>(n_strips, (uint32_t)sms * 3u);
+    const uint32_t grid = std::min<uint32_t>(n_strips, (uint32_t)sms * LH_RESOLVE_MIN_BLOCKS);
 #ifdef LH_RESOLVE_NO_TMA
     vis_map = nullptr;  // comparison builds: per-thread loads of the visibility words
 #endif
