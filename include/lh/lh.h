@@ -250,6 +250,18 @@ lh_status lh_cull_instances_noalloc(const Instance* d_instances, uint32_t n_inst
                                     const Uniforms* host_uniforms, uint8_t* d_sector, uint32_t capacity,
                                     uint32_t* d_flags, void* stream);
 
+/* lh_frame followed by a copy of the HDR image (float4[height][width]) to
+ * `host_hdr`, pipelined: the copy runs on a stream of the context after the
+ * frame's resolve, and the next frame's culling and rasterisation run while
+ * it lands (that frame's resolve waits for it).  Returns once both are
+ * enqueued and the PREVIOUS call's copy has landed, so callers alternate two
+ * host buffers (pinned for an asynchronous copy): after call i returns, the
+ * buffer of call i - 1 holds its frame.  lh_readback_wait waits for the last
+ * copy.  The reference presents its frame instead; no counterpart there. */
+lh_status lh_frame_readback(lh_ctx* ctx, const Uniforms* host_uniforms, void* host_hdr, void* stream,
+                            lh_frame_out* out);
+lh_status lh_readback_wait(lh_ctx* ctx);
+
 /* Synchronise the context's last stream and copy `bytes` from a device
  * address (e.g. a field of lh_frame_out) to host memory. */
 lh_status lh_download(lh_ctx* ctx, void* host_dst, uint64_t device_src, size_t bytes);

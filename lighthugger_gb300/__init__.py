@@ -135,6 +135,8 @@ def lib():
     L.lh_frame.argtypes = [P, P, P, C.POINTER(FrameOut)]
     L.lh_frame_batched.argtypes = [P, P, P, C.c_uint32, P, C.POINTER(FrameOut)]
     L.lh_frame_graph.argtypes = [P, P, P, C.c_uint32, P, C.POINTER(FrameOut)]
+    L.lh_frame_readback.argtypes = [P, P, P, P, C.POINTER(FrameOut)]
+    L.lh_readback_wait.argtypes = [P]
     L.lh_get_outputs.argtypes = [P, C.POINTER(FrameOut)]
     L.lh_read_status.argtypes = [P, C.POINTER(DeviceStatus)]
     L.lh_download.argtypes = [P, P, C.c_uint64, C.c_size_t]
@@ -311,6 +313,18 @@ class Renderer:
         s = stream if stream is not None else self.stream
         _check(lib().lh_frame(self.ctx, C.byref(uniforms), s, C.byref(self.out)), "lh_frame", self.ctx)
         return self.out
+
+    def frame_readback(self, uniforms, host_hdr_ptr, stream=None):
+        """lh_frame with the HDR image copied to host memory at host_hdr_ptr,
+        pipelined with the next frame: when this returns, the buffer given to
+        the previous call holds that frame (readback_wait() for the last)."""
+        s = stream if stream is not None else self.stream
+        _check(lib().lh_frame_readback(self.ctx, C.byref(uniforms), host_hdr_ptr, s, C.byref(self.out)),
+               "lh_frame_readback", self.ctx)
+        return self.out
+
+    def readback_wait(self):
+        _check(lib().lh_readback_wait(self.ctx), "lh_readback_wait", self.ctx)
 
     def frame_batched(self, uniforms, probes, n_probes, stream=None):
         s = stream if stream is not None else self.stream

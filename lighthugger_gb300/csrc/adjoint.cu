@@ -327,10 +327,19 @@ __device__ __forceinline__ void scatter_texels(HotCache& cache, float* const bas
         for (int c = 0; c < NC; c++) s[c] = v[q][c];
         run_sums(s, r);
         if (r.head && a[q]) {
+            if (!small && ((uintptr_t)a[q] & 15u) == 0) {
+                // one vector reduction per texel (the other channels add 0)
+                float4 t = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                float* tc = &t.x;
 #pragma unroll
-            for (int c = 0; c < NC; c++) {
-                if (small) cache_add(cache, a[q] + c0 + c, s[c]);
-                else atomicAdd(a[q] + c0 + c, s[c]);
+                for (int c = 0; c < NC; c++) tc[c0 + c] = s[c];
+                atomicAdd(reinterpret_cast<float4*>(a[q]), t);
+            } else {
+#pragma unroll
+                for (int c = 0; c < NC; c++) {
+                    if (small) cache_add(cache, a[q] + c0 + c, s[c]);
+                    else atomicAdd(a[q] + c0 + c, s[c]);
+                }
             }
         }
     }
@@ -468,8 +477,12 @@ __global__ void __launch_bounds__(kBwdThreads, LH_BWD_MIN_BLOCKS)
                     }
                     if (d.uvs) {
                         float* p = reinterpret_cast<float*>(d.uvs) + (size_t)o.idx[k] * 2;
-                        atomicAdd(p, vk[6]);
-                        atomicAdd(p + 1, vk[7]);
+                        if (((uintptr_t)p & 7u) == 0) {
+                            atomicAdd(reinterpret_cast<float2*>(p), make_float2(vk[6], vk[7]));
+                        } else {
+                            atomicAdd(p, vk[6]);
+                            atomicAdd(p + 1, vk[7]);
+                        }
                     }
                 }
             }

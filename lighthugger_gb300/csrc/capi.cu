@@ -94,6 +94,12 @@ struct lh_ctx {
     // 16-byte aligned or the driver lacks the encoder)
     alignas(64) CUtensorMap vis_map;
     bool vis_map_ok = false;
+    // pipelined HDR readback (lh_frame_readback): copies on their own
+    // stream; a frame's resolve waits for the previous copy of d_hdr
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t resolved = nullptr;
+    cudaEvent_t readback_done[2] = {nullptr, nullptr};
+    uint32_t readbacks = 0;
 };
 
 namespace {
@@ -155,9 +161,21 @@ void free_all(lh_ctx* c) {
     for (int i = 0; i < 2; i++) {
         if (c->h_staging[i]) cudaFreeHost(c->h_staging[i]);
         if (c->staging_done[i]) cudaEventDestroy(c->staging_done[i]);
+        if (c->readback_done[i]) cudaEventDestroy(c->readback_done[i]);
         c->h_staging[i] = nullptr;
         c->staging_done[i] = nullptr;
+        c->readback_done[i] = nullptr;
     }
+    if (c->resolved) cudaEventDestroy(c->resolved);
+    c->resolved = nullptr;
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+    c->copy_stream = nullptr;
+}
+
+// Work that writes d_hdr waits for the last pipelined readback of it.
+cudaError_t wait_readback(const lh_ctx* c, cudaStream_t s) {
+    if (!c->readbacks) return cudaSuccess;
+    return cudaStreamWaitEvent(s, c->readback_done[(c->readbacks - 1) & 1u], 0);
 }
 
 // View order: 0 main, 1..n_probes probes, then cascades 0..3.
@@ -340,7 +358,9 @@ lh_status enqueue_frame(lh_ctx* c, uint32_t n_probes, uint32_t n_instances, bool
         if (e == cudaSuccess)
             e = mark(launch_raster_kind(f, n_persp, 4, kViewShadow, t.small_px, t.medium_px, t.raster_batch, s, c->sms));
     }
-    // lighting resolve of the main view
+    // lighting resolve of the main view (after the last pipelined readback
+    // of the image it overwrites; a captured graph waits as a whole instead)
+    if (e == cudaSuccess && !c->capturing) e = wait_readback(c, s);
     if (e == cudaSuccess)
         e = mark(launch_resolve(f, c->cfg.width, c->cfg.height, c->vis_map_ok ? &c->vis_map : nullptr, s, c->sms));
     if (e != cudaSuccess) return cuda_fail(c, e, "frame launch");
@@ -450,7 +470,10 @@ lh_status lh_create(const lh_config* config, lh_ctx** out) {
     for (int i = 0; i < 2 && e == cudaSuccess; i++) {
         e = cudaMallocHost(reinterpret_cast<void**>(&c->h_staging[i]), c->staging_bytes);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->staging_done[i], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->readback_done[i], cudaEventDisableTiming);
     }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->resolved, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         lh_status st = e == cudaErrorMemoryAllocation ? LH_ERR_OUT_OF_MEMORY : LH_ERR_CUDA;
         free_all(c);
@@ -514,6 +537,34 @@ static lh_status frame_impl(lh_ctx* c, const Uniforms* u, const Uniforms* probes
 
 lh_status lh_frame(lh_ctx* c, const Uniforms* u, void* stream, lh_frame_out* out) {
     return frame_impl(c, u, nullptr, 0, stream, out, false);
+}
+
+lh_status lh_frame_readback(lh_ctx* c, const Uniforms* u, void* host_hdr, void* stream, lh_frame_out* out) {
+    lh_status st = check_ctx(c);
+    if (st != LH_OK) return st;
+    if (!host_hdr) return fail(c, LH_ERR_INVALID_ARGUMENT, "host_hdr is NULL");
+    if ((st = frame_impl(c, u, nullptr, 0, stream, out, false)) != LH_OK) return st;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const uint32_t k = c->readbacks & 1u;
+    const size_t bytes = (size_t)c->cfg.width * c->cfg.height * sizeof(float4);
+    cudaError_t e = cudaEventRecord(c->resolved, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->copy_stream, c->resolved, 0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(host_hdr, c->d_hdr, bytes, cudaMemcpyDeviceToHost, c->copy_stream);
+    if (e == cudaSuccess) e = cudaEventRecord(c->readback_done[k], c->copy_stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "readback");
+    c->readbacks++;
+    // the previous call's image has landed once this returns
+    if (c->readbacks > 1 && (e = cudaEventSynchronize(c->readback_done[k ^ 1u])) != cudaSuccess)
+        return cuda_fail(c, e, "readback wait");
+    return LH_OK;
+}
+
+lh_status lh_readback_wait(lh_ctx* c) {
+    lh_status st = check_ctx(c);
+    if (st != LH_OK) return st;
+    if (!c->readbacks) return LH_OK;
+    cudaError_t e = cudaEventSynchronize(c->readback_done[(c->readbacks - 1) & 1u]);
+    return e == cudaSuccess ? LH_OK : cuda_fail(c, e, "readback wait");
 }
 
 lh_status lh_frame_batched(lh_ctx* c, const Uniforms* u, const Uniforms* probes, uint32_t n_probes, void* stream,
@@ -621,7 +672,8 @@ lh_status frame_graph_impl(lh_ctx* c, const Uniforms* u, const Uniforms* probes,
         c->graph_backward = want;
     }
     if ((st = upload_frame_constants(c, u, probes, n_probes, s)) != LH_OK) return st;
-    e = cudaGraphLaunch(c->graph_exec, s);
+    e = wait_readback(c, s);
+    if (e == cudaSuccess) e = cudaGraphLaunch(c->graph_exec, s);
     if (e != cudaSuccess) return cuda_fail(c, e, "graph launch");
     c->last_stream = s;
     if (out) fill_out(c, out);
@@ -770,6 +822,7 @@ void lh_destroy(lh_ctx* c) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->last_stream) cudaStreamSynchronize(c->last_stream);
+    if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
     free_all(c);
     delete c;
 }
