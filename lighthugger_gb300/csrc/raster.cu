@@ -2,11 +2,15 @@
 // (shared with the persistent multi-view kernel).
 #include "raster_phases.cuh"
 
+#ifndef LH_RASTER_MIN_BLOCKS
+#define LH_RASTER_MIN_BLOCKS 3  // resident blocks of k_raster per SM (registers: 65536 / 256 / this)
+#endif
+
 namespace lh {
 namespace {
 
 template <int KIND>
-__global__ void __launch_bounds__(kRasterWarps * 32, 3) k_raster(FrameDev f, uint32_t view_begin, uint32_t n_views,
+__global__ void __launch_bounds__(kRasterWarps * 32, LH_RASTER_MIN_BLOCKS) k_raster(FrameDev f, uint32_t view_begin, uint32_t n_views,
                                                                  RasterTune tune) {
     __shared__ RasterSmem sm;
     phase_raster<KIND, false>(f, view_begin, n_views, tune, &f.status[kStRasterClaim], sm, nullptr);
@@ -42,12 +46,12 @@ cudaError_t launch_raster_kind(const FrameDev& f, uint32_t view_begin, uint32_t 
         cudaMemsetAsync(f.status + kStClipCount, 0, sizeof(uint32_t) * (kStRasterClaimAlpha + 1 - kStClipCount), s);
     if (e != cudaSuccess) return e;
     if (kind == kViewVisibility) {
-        k_raster<0><<<sms * 3, kRasterWarps * 32, 0, s>>>(f, view_begin, n_views, tune);
+        k_raster<0><<<sms * LH_RASTER_MIN_BLOCKS, kRasterWarps * 32, 0, s>>>(f, view_begin, n_views, tune);
         k_raster_alpha<0><<<sms * 3, kRasterWarps * 32, 0, s>>>(f, view_begin, n_views, tune);
         k_raster_clip<0><<<sms, 128, 0, s>>>(f);
         k_raster_big<0><<<sms * 4, 256, 0, s>>>(f);
     } else {
-        k_raster<1><<<sms * 3, kRasterWarps * 32, 0, s>>>(f, view_begin, n_views, tune);
+        k_raster<1><<<sms * LH_RASTER_MIN_BLOCKS, kRasterWarps * 32, 0, s>>>(f, view_begin, n_views, tune);
         k_raster_alpha<1><<<sms * 3, kRasterWarps * 32, 0, s>>>(f, view_begin, n_views, tune);
         k_raster_clip<1><<<sms, 128, 0, s>>>(f);
         k_raster_big<1><<<sms * 4, 256, 0, s>>>(f);
