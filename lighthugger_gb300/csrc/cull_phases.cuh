@@ -186,6 +186,26 @@ __device__ __forceinline__ uint32_t upper_bound(const PrefixSumValue* v, uint32_
     return first;
 }
 
+// upper_bound by one warp: 32 probes per step (log32 of the count dependent
+// loads instead of log2).  The entries' sums do not decrease, so the probes
+// with sum <= target form a prefix of the lanes.
+__device__ __forceinline__ uint32_t upper_bound_warp(const PrefixSumValue* v, uint32_t count, uint32_t target,
+                                                     uint32_t lane) {
+    uint32_t lo = 0, hi = count;  // the answer lies in [lo, hi]
+    for (;;) {
+        const uint32_t span = hi - lo;
+        const uint32_t step = span <= 32u ? 1u : (span + 31u) / 32u;
+        const uint32_t p = lo + lane * step;
+        const bool le = p < hi && v[p].sum <= target;
+        const uint32_t k = __popc(__ballot_sync(0xFFFFFFFFu, le));
+        if (step == 1u) return lo + k;
+        const uint32_t nlo = k ? lo + (k - 1u) * step + 1u : lo;
+        const uint32_t nhi = (k < 32u && lo + k * step < hi) ? lo + k * step : hi;
+        lo = nlo;
+        hi = nhi;
+    }
+}
+
 // Candidate count of a view's sector (an overflowing sector holds only its
 // first max_instances entries).
 __device__ __forceinline__ void sector_extent(const FrameDev& f, const ViewDev* vw, uint32_t& count, uint32_t& total) {
@@ -208,7 +228,7 @@ __device__ void phase_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint
     __shared__ __align__(16) MiscStorage s_m;
     __shared__ PrefixSumValue s_entries[kMlTile];
     __shared__ uint32_t s_cnt[2][kMlItems * (kMlThreads / 32)];
-    __shared__ uint32_t s_tile, s_view, s_ea, s_ne, s_tot[2], s_loaded_view;
+    __shared__ uint32_t s_tile, s_view, s_eab[2], s_tot[2], s_loaded_view;
     __shared__ uint32_t s_tile_off[kMaxViews + 1];
     __shared__ uint64_t s_excl;
     const uint32_t md = f.max_draws;
@@ -256,17 +276,19 @@ __device__ void phase_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint
         sector_extent(f, vw, count, total);
         const uint32_t n_tiles = s_tile_off[v + 1] - s_tile_off[v];
         const uint32_t t0 = tile * kMlTile, t1 = min(total, t0 + kMlTile);
-        if (threadIdx.x == 0) {
-            uint32_t ea = upper_bound(values, count, t0), eb = upper_bound(values, count, t1 - 1);
-            s_ea = ea;
-            s_ne = eb - ea + 1;
-            s_loaded_view = v;
+        // the tile's first and last entries, one warp each
+        if (warp < 2) {
+            const uint32_t e = upper_bound_warp(values, count, warp == 0 ? t0 : t1 - 1, lane);
+            if (lane == 0) s_eab[warp] = e;
         }
         __syncthreads();
-        const uint32_t ea = s_ea, ne = s_ne;
+        const uint32_t ea = s_eab[0], ne = s_eab[1] - s_eab[0] + 1;
         const bool smem_entries = ne <= kMlTile;
         if (smem_entries)
             for (uint32_t j = threadIdx.x; j < ne; j += kMlThreads) s_entries[j] = values[ea + j];
+        // every thread has passed the s_loaded_view test above (barrier), and
+        // none reads it again before the next claim's barrier
+        if (threadIdx.x == 0) s_loaded_view = v;
         __syncthreads();
 
         uint32_t cls_bits = 0;  // 2 bits per item: 1 opaque, 2 alpha clip

@@ -5,6 +5,9 @@
 #ifndef LH_RASTER_MIN_BLOCKS
 #define LH_RASTER_MIN_BLOCKS 3  // resident blocks of k_raster per SM (registers: 65536 / 256 / this)
 #endif
+#ifndef LH_RASTER_BIG_MIN_BLOCKS
+#define LH_RASTER_BIG_MIN_BLOCKS 4  // the same for the chunk kernel k_raster_big
+#endif
 
 namespace lh {
 namespace {
@@ -30,7 +33,7 @@ __global__ void __launch_bounds__(128) k_raster_clip(FrameDev f) {
 }
 
 template <int KIND>
-__global__ void __launch_bounds__(256, 4) k_raster_big(FrameDev f) {
+__global__ void __launch_bounds__(256, LH_RASTER_BIG_MIN_BLOCKS) k_raster_big(FrameDev f) {
     phase_raster_big<KIND>(f);
 }
 
@@ -49,12 +52,12 @@ cudaError_t launch_raster_kind(const FrameDev& f, uint32_t view_begin, uint32_t 
         k_raster<0><<<sms * LH_RASTER_MIN_BLOCKS, kRasterWarps * 32, 0, s>>>(f, view_begin, n_views, tune);
         k_raster_alpha<0><<<sms * 3, kRasterWarps * 32, 0, s>>>(f, view_begin, n_views, tune);
         k_raster_clip<0><<<sms, 128, 0, s>>>(f);
-        k_raster_big<0><<<sms * 4, 256, 0, s>>>(f);
+        k_raster_big<0><<<sms * LH_RASTER_BIG_MIN_BLOCKS, 256, 0, s>>>(f);
     } else {
         k_raster<1><<<sms * LH_RASTER_MIN_BLOCKS, kRasterWarps * 32, 0, s>>>(f, view_begin, n_views, tune);
         k_raster_alpha<1><<<sms * 3, kRasterWarps * 32, 0, s>>>(f, view_begin, n_views, tune);
         k_raster_clip<1><<<sms, 128, 0, s>>>(f);
-        k_raster_big<1><<<sms * 4, 256, 0, s>>>(f);
+        k_raster_big<1><<<sms * LH_RASTER_BIG_MIN_BLOCKS, 256, 0, s>>>(f);
     }
     return cudaGetLastError();
 }

@@ -196,16 +196,19 @@ __device__ __forceinline__ void load_transform(const Instance* inst, lh_mat4& m)
     for (int i = 0; i < 4; i++) d[i] = __ldg(s + i);
 }
 
-// Append a big triangle with one 64-bit atomic of {triangles:hi24, chunks:lo40}
+// Append big triangles with 64-bit atomics of {triangles:hi24, chunks:lo40}
 // (the packed single-pass append of prefix_sum.glsl:17-30): the triangle's
 // index and its first chunk come from the same word, so chunk bases ascend
 // with the index and the band kernel finds a chunk's triangle by binary search.
-__device__ void push_big(const FrameDev& f, const TriSetup& t, uint32_t view) {
+__device__ __forceinline__ unsigned long long big_chunks(const TriSetup& t) {
     const uint32_t nbx = (uint32_t)(t.px1 - t.px0) / kChunkCols + 1;
     const uint32_t nby = (uint32_t)(t.py1 - t.py0) / kChunkRows + 1;
-    const unsigned long long n = (unsigned long long)nbx * nby;
-    const unsigned long long old =
-        atomicAdd(reinterpret_cast<unsigned long long*>(f.status + kStBigPacked), (1ull << 40) | n);
+    return (unsigned long long)nbx * nby;
+}
+// Store the queue entry of a triangle of n chunks whose packed word (before
+// its own addition) is `old`.
+__device__ void store_big(const FrameDev& f, const TriSetup& t, uint32_t view, unsigned long long old,
+                          unsigned long long n) {
     const uint64_t idx = old >> 40, base = old & ((1ull << 40) - 1);
     if (idx >= f.big_cap || base + n > 0xFFFFFFFFull) {
         atomicOr(&f.status[kStFlags], LH_FLAG_QUEUE_OVERFLOW);
@@ -223,6 +226,31 @@ __device__ void push_big(const FrameDev& f, const TriSetup& t, uint32_t view) {
     e.py1 = t.py1;
     f.big[idx] = e;
     f.big_base[idx] = (uint32_t)base;
+}
+// One thread's triangle.
+__device__ void push_big(const FrameDev& f, const TriSetup& t, uint32_t view) {
+    const unsigned long long n = big_chunks(t);
+    const unsigned long long old =
+        atomicAdd(reinterpret_cast<unsigned long long*>(f.status + kStBigPacked), (1ull << 40) | n);
+    store_big(f, t, view, old, n);
+}
+// Called by the whole warp: lanes with `big` set append their triangle with
+// one atomic per warp (a warp scan of the lanes' {1, chunks} words gives each
+// lane the running total below it).  The word's low 40 bits cannot carry into
+// the count: a sum reaching 2^32 chunks is flagged and dropped.
+__device__ void push_big_warp(const FrameDev& f, const TriSetup& t, uint32_t view, bool big, uint32_t lane) {
+    const unsigned long long n = big ? big_chunks(t) : 0ull;
+    const unsigned long long mine = big ? (1ull << 40) | n : 0ull;
+    unsigned long long incl = mine;
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        const unsigned long long v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    unsigned long long old = 0;
+    if (lane == 31) old = atomicAdd(reinterpret_cast<unsigned long long*>(f.status + kStBigPacked), incl);
+    old = __shfl_sync(0xFFFFFFFFu, old, 31) + (incl - mine);
+    if (big) store_big(f, t, view, old, n);
 }
 
 // Where a warp's alpha-tested triangles find their vertices: the warp's
@@ -356,11 +384,30 @@ __device__ __forceinline__ void raster_meshlet(const FrameDev& f, const MeshletW
         ma = load_mesh_info_alpha(mesh_info_of(w.inst));
         as.tex = ma.tex;
     }
+    // All of the meshlet's global loads are issued before any is used: the
+    // micro-index words (at most 3 per lane; 4-byte aligned offsets, as the
+    // meshletiser pads them), then both vertex indices of the lane, then both
+    // positions -- two dependent round trips instead of seven.
+    const uint64_t mbase = mi.micro_indices + w.triangle_offset;
+    const uint32_t nbytes = nt * 3, nwords = (nbytes + 3) / 4;
+    const bool micro_aligned = (mbase & 3) == 0;
+    uint32_t mw[3] = {0u, 0u, 0u};
+    if (micro_aligned) {
+#pragma unroll
+        for (uint32_t k = 0; k < 3; k++) {
+            const uint32_t j = lane + 32u * k;
+            if (j < nwords) mw[k] = __ldg(reinterpret_cast<const uint32_t*>(mbase) + j);
+        }
+    }
+    const bool v0 = lane < nv, v1 = lane + 32u < nv;
+    const uint32_t idx0 = v0 ? load_index_raw(mi.indices, mi.flags, w.index_offset + lane) : 0u;
+    const uint32_t idx1 = v1 ? load_index_raw(mi.indices, mi.flags, w.index_offset + lane + 32u) : 0u;
+    const f3 pos0 = v0 ? load_position(mi.positions, mi.flags, idx0) : f3{0.0f, 0.0f, 0.0f};
+    const f3 pos1 = v1 ? load_position(mi.positions, mi.flags, idx1) : f3{0.0f, 0.0f, 0.0f};
     int32_t min_x = INT32_MAX, max_x = INT32_MIN, min_y = INT32_MAX, max_y = INT32_MIN;
     uint32_t any_oc = 0;
-    for (uint32_t j = lane; j < nv; j += 32) {
-        uint32_t idx = load_index_raw(mi.indices, mi.flags, w.index_offset + j);
-        f3 wp = world_pos(w.transform, load_position(mi.positions, mi.flags, idx));
+    auto vertex = [&](uint32_t j, uint32_t idx, f3 pos) {
+        f3 wp = world_pos(w.transform, pos);
         f4 c = mul(*w.vp, f4{wp.x, wp.y, wp.z, 1.0f});
         uint32_t oc = outcode(c);
         SnapV s{0, 0, 0.0f};
@@ -373,7 +420,9 @@ __device__ __forceinline__ void raster_meshlet(const FrameDev& f, const MeshletW
         min_y = min(min_y, s.Y);
         max_y = max(max_y, s.Y);
         if (ALPHA) av[j] = alpha_vert(c, ma, mi.flags, idx);
-    }
+    };
+    if (v0) vertex(lane, idx0, pos0);
+    if (v1) vertex(lane + 32u, idx1, pos1);
     // A meshlet whose snapped vertices (all inside the guard band) span no
     // pixel centre produces no fragment: every triangle's bbox lies inside
     // the vertices' bbox.  Common for far meshlets in small views.
@@ -386,11 +435,12 @@ __device__ __forceinline__ void raster_meshlet(const FrameDev& f, const MeshletW
             max((min_y + 127) >> 8, 0) > min((max_y - 128) >> 8, (int32_t)H - 1))
             return;
     }
-    const uint64_t mbase = mi.micro_indices + w.triangle_offset;
-    const uint32_t nbytes = nt * 3;
-    if ((mbase & 3) == 0) {
-        for (uint32_t j = lane; j < (nbytes + 3) / 4; j += 32)
-            micro_words[j] = __ldg(reinterpret_cast<const uint32_t*>(mbase) + j);
+    if (micro_aligned) {
+#pragma unroll
+        for (uint32_t k = 0; k < 3; k++) {
+            const uint32_t j = lane + 32u * k;
+            if (j < nwords) micro_words[j] = mw[k];
+        }
     } else {
         uint8_t* d = reinterpret_cast<uint8_t*>(micro_words);
         for (uint32_t j = lane; j < nbytes; j += 32) d[j] = __ldg(reinterpret_cast<const uint8_t*>(mbase) + j);
@@ -399,7 +449,7 @@ __device__ __forceinline__ void raster_meshlet(const FrameDev& f, const MeshletW
     const uint8_t* mic = reinterpret_cast<const uint8_t*>(micro_words);
     for (uint32_t base = w.part * 32u; base < nt; base += 32u * w.split) {
         const uint32_t t = base + lane;
-        bool medium = false;
+        bool medium = false, big = false;
         TriSetup st;
         if (t < nt) {
             const uint32_t m0 = mic[3 * t], m1 = mic[3 * t + 1], m2 = mic[3 * t + 2];
@@ -433,6 +483,8 @@ __device__ __forceinline__ void raster_meshlet(const FrameDev& f, const MeshletW
                                 else raster_lane<KIND>(st, w.target, W);
                             } else if (npx <= tune.medium_px) {
                                 medium = true;
+                            } else if (KIND == 1) {
+                                big = true;  // appended below, one atomic per warp
                             } else {
                                 push_big(f, st, w.view);
                             }
@@ -441,6 +493,9 @@ __device__ __forceinline__ void raster_meshlet(const FrameDev& f, const MeshletW
                 }
             }
         }
+        // shadow views: few meshlets with many big triangles each, whose
+        // appends would queue on the one counter word
+        if (KIND == 1 && __any_sync(0xFFFFFFFFu, big)) push_big_warp(f, st, w.view, big, lane);
         uint32_t mask = __ballot_sync(0xFFFFFFFFu, medium);
         while (mask) {
             int src = __ffs(mask) - 1;
@@ -495,11 +550,19 @@ __device__ void phase_raster(const FrameDev& f, uint32_t view_begin, uint32_t n_
     const uint32_t split = total < 2u * warps_total ? 4u : 1u;
     const uint32_t units = total * split;
     const uint32_t batch = tune.batch ? tune.batch : (units > 256u * warps_total ? 4u : 1u);
-    uint32_t unit = 0, unit_end = 0;
+    // The first window of every warp is static (warp g takes units
+    // [g * batch, (g + 1) * batch)); the claim word hands out the rest from
+    // warps_total * batch on.  Launches with fewer units than warps (shadow
+    // cascades) then touch the claim word not at all, and none start with
+    // every warp queueing on it.
+    const uint32_t gwarp = blockIdx.x * (blockDim.x >> 5) + warp;
+    const uint32_t dyn_base = warps_total * batch;
+    uint32_t unit = min(gwarp * batch, units), unit_end = min(gwarp * batch + batch, units);
     for (;;) {
-        if (unit == unit_end) {
+        if (unit >= unit_end) {
+            if (dyn_base >= units) break;
             uint32_t first = 0;
-            if (lane == 0) first = atomicAdd(claim_word, batch);
+            if (lane == 0) first = dyn_base + atomicAdd(claim_word, batch);
             first = __shfl_sync(0xFFFFFFFFu, first, 0);
             if (first >= units) break;
             unit = first;
@@ -654,10 +717,13 @@ __device__ __forceinline__ uint32_t upper_bound_warp(const uint32_t* base, uint3
 }
 
 // The pixels [x0, x1] x [y0, y1] of an alpha-tested big triangle, one
-// column per lane (not inlined, as the other alpha paths).
+// column per lane (not inlined, as the other alpha paths).  The triangle is
+// passed as its queue entry: a reference to the caller's copy would keep
+// that copy in local memory on the opaque path too.
 template <int KIND>
-__device__ __noinline__ void raster_chunk_alpha(const FrameDev& f, const BigTri& b, int32_t x0, int32_t x1, int32_t y0,
-                                                int32_t y1, uint32_t lane) {
+__device__ __noinline__ void raster_chunk_alpha(const FrameDev& f, const BigTri* entry, int32_t x0, int32_t x1,
+                                                int32_t y0, int32_t y1, uint32_t lane) {
+    const BigTri b = *entry;
     const ViewDev* vw = f.views + b.view;
     void* target = vw->target;
     const uint32_t W = vw->width, H = vw->height;
@@ -686,15 +752,22 @@ __device__ void phase_raster_big(const FrameDev& f) {
     constexpr uint32_t kChunkBatch = 4;  // chunks claimed per atomic
     // chunk numbers fit 32 bits (push_big drops triangles beyond)
     const uint32_t total32 = (uint32_t)min(total, 0xFFFFFFFFull);
-    uint32_t c = 0, c_end = 0;
+    // static first batch per warp, then claims from warps * kChunkBatch on
+    const uint32_t warps_total = gridDim.x * (blockDim.x >> 5);
+    const uint32_t gwarp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const uint64_t dyn_base = (uint64_t)warps_total * kChunkBatch;
+    uint32_t c = (uint32_t)min((uint64_t)gwarp * kChunkBatch, (uint64_t)total32);
+    uint32_t c_end = (uint32_t)min((uint64_t)gwarp * kChunkBatch + kChunkBatch, (uint64_t)total32);
     for (;;) {
-        if (c == c_end) {
+        if (c >= c_end) {
+            if (dyn_base >= total32) break;
             uint32_t first_c = 0;
             if (lane == 0) first_c = atomicAdd(&f.status[kStBigClaim], kChunkBatch);
             first_c = __shfl_sync(0xFFFFFFFFu, first_c, 0);
-            if (first_c >= total32) break;
-            c = first_c;
-            c_end = first_c + min(kChunkBatch, total32 - first_c);
+            const uint64_t first = dyn_base + first_c;
+            if (first >= total32) break;
+            c = (uint32_t)first;
+            c_end = (uint32_t)min(first + kChunkBatch, (uint64_t)total32);
         }
         const uint32_t first = upper_bound_warp(f.big_base, ntri, c, lane);
         c++;
@@ -716,7 +789,7 @@ __device__ void phase_raster_big(const FrameDev& f) {
         void* target = vw->target;
         const uint32_t W = vw->width;
         if (b.bias & kBiasAlpha) {
-            raster_chunk_alpha<KIND>(f, b, x0, x1, y0, y1, lane);
+            raster_chunk_alpha<KIND>(f, f.big + i, x0, x1, y0, y1, lane);
             continue;
         }
         // edge functions at the top of the lane's column, then one add per
