@@ -344,21 +344,30 @@ __device__ void phase_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint
         }
         __syncthreads();
         if (warp == 0) {
-            // exclusive scan of 64 counts per class: 2 per lane
+            // exclusive scan of N counts per class: PER consecutive ones per lane
             constexpr uint32_t N = kMlItems * (kMlThreads / 32);
-            static_assert(N == 64, "scan layout");
+            constexpr uint32_t PER = N / 32;
+            static_assert(N % 32 == 0 && PER >= 1 && PER <= 4, "scan layout");
 #pragma unroll
             for (int cl = 0; cl < 2; cl++) {
-                uint32_t a = s_cnt[cl][2 * lane], b = s_cnt[cl][2 * lane + 1];
-                uint32_t s = a + b, incl = s;
+                uint32_t c[PER], s = 0;
+#pragma unroll
+                for (uint32_t i = 0; i < PER; i++) {
+                    c[i] = s_cnt[cl][PER * lane + i];
+                    s += c[i];
+                }
+                uint32_t incl = s;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
                     uint32_t n = __shfl_up_sync(0xFFFFFFFFu, incl, o);
                     if (lane >= (uint32_t)o) incl += n;
                 }
                 uint32_t ex = incl - s;
-                s_cnt[cl][2 * lane] = ex;
-                s_cnt[cl][2 * lane + 1] = ex + a;
+#pragma unroll
+                for (uint32_t i = 0; i < PER; i++) {
+                    s_cnt[cl][PER * lane + i] = ex;
+                    ex += c[i];
+                }
                 if (lane == 31) s_tot[cl] = incl;
             }
             __syncwarp();

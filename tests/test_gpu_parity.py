@@ -206,3 +206,23 @@ def test_debug_views(native, oracle, mode):
     lit = oracle.run_scene(scene, shadow_size=d.shadow_size, max_instances=1024, max_draws=200000)
     covered = (r.visibility() >> np.uint64(32)) != 0
     assert not np.array_equal(hdr[covered], lit.hdr[covered])  # the view replaced the lighting
+
+
+@pytest.mark.parametrize("shadow_size,width,height", [(2048, 1280, 720), (1000, 1001, 601)])
+def test_shadow_sizes_and_odd_widths(native, oracle, shadow_size, width, height):
+    """Cascades whose PCF taps are not one texel apart (2048: two texels,
+    1000: 0.98) take the per-tap path; an odd width (rows of the visibility
+    buffer not 16-byte aligned) takes the resolve without TMA staging."""
+    lh = native
+    scene = lh.Scene(1, width=width, height=height).upload(0)
+    d = scene.desc
+    cfg = lh.Config(width=d.width, height=d.height, shadow_size=shadow_size, max_instances=1024, max_draws=200000)
+    r = lh.Renderer(cfg)
+    r.set_scene(scene)
+    r.frame(scene.uniforms)
+    st = r.status()
+    fr = oracle.run_scene(scene, shadow_size=shadow_size, max_instances=1024, max_draws=200000)
+    errors, stats = compare_frame(r, fr, 200000, 1024)
+    assert not errors, "\n".join(errors) + " %s" % stats
+    assert st.flags == fr.flags
+    assert stats["covered"] > 1000
