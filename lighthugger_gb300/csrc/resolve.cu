@@ -103,6 +103,9 @@ __device__ float pcf9(const FrameDev& f, float sx, float sy, float layer_f, floa
 #pragma unroll
             for (int c = 0; c < 4; c++) bits |= (ref < __ldg(row + cl(ix[0] + c)) ? 1u : 0u) << (4 * r + c);
         }
+        // no texel passes: every tap is 0 * (finite, non-negative weights)
+        // summed, exactly +0
+        if (bits == 0u) return 0.0f;
         float sum = 0.0f;
 #pragma unroll
         for (int ox = 0; ox < 3; ox++)

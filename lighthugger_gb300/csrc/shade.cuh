@@ -454,15 +454,18 @@ template <class T, class F> LH_HD ShadowTerm<T> shadow_term(const F& fx, v3<T> w
     sc = {sc.x * inv_w, sc.y * inv_w, sc.z * inv_w};
     T shadow = T(0), dsx = T(0), dsy = T(0);
     const T S = T(fx.shadow_size);
-    for (int ox = -1; ox <= 1; ox++)
-        for (int oy = -1; oy <= 1; oy++) {
-            T da, db;
-            const uint32_t tap = (uint32_t)((ox + 1) * 3 + (oy + 1));
-            shadow += pcf_tap((uint32_t)(fx.cmp >> (4 * tap)) & 15u, sc.x + T(ox) / T(1024), sc.y + T(oy) / T(1024), S,
-                              da, db);
-            dsx += da * S;
-            dsy += db * S;
-        }
+    // with every compare 0 each tap's value and derivatives are exactly 0
+    if (fx.cmp != 0) {
+        for (int ox = -1; ox <= 1; ox++)
+            for (int oy = -1; oy <= 1; oy++) {
+                T da, db;
+                const uint32_t tap = (uint32_t)((ox + 1) * 3 + (oy + 1));
+                shadow += pcf_tap((uint32_t)(fx.cmp >> (4 * tap)) & 15u, sc.x + T(ox) / T(1024),
+                                  sc.y + T(oy) / T(1024), S, da, db);
+                dsx += da * S;
+                dsy += db * S;
+            }
+    }
     const T ninth = T(1) / T(9);
     ShadowTerm<T> r;
     r.value = fx.shadow_const ? T(1) : shadow * ninth;
