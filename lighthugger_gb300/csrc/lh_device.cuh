@@ -249,16 +249,6 @@ __device__ __forceinline__ int64_t cross_rel(const SnapV& a, const SnapV& b, con
     return (int64_t)ux * vy - (int64_t)vx * uy;
 }
 
-// Whether the triangle's bounding box holds a pixel centre of the W x H
-// target (the bbox rule of make_setup); false means no coverage at all.
-__device__ __forceinline__ bool covers_centre(const SnapV& v0, const SnapV& v1, const SnapV& v2, uint32_t W,
-                                              uint32_t H) {
-    const int32_t minX = min(v0.X, min(v1.X, v2.X)), maxX = max(v0.X, max(v1.X, v2.X));
-    const int32_t minY = min(v0.Y, min(v1.Y, v2.Y)), maxY = max(v0.Y, max(v1.Y, v2.Y));
-    return max((minX + 127) >> 8, 0) <= min((maxX - 128) >> 8, (int32_t)W - 1) &&
-           max((minY + 127) >> 8, 0) <= min((maxY - 128) >> 8, (int32_t)H - 1);
-}
-
 // Triangle ready for coverage: orientation normalised (interior has every
 // edge function >= 0), bias 1 for edges that are not top-left.
 struct TriSetup {
@@ -278,19 +268,34 @@ __device__ __forceinline__ bool top_left(int32_t ax, int32_t ay, int32_t bx, int
     return dy > 0 || (dy == 0 && dx < 0);
 }
 
-// Build the setup of a normalised triangle; returns false when no pixel
-// centre of the (W x H) target can be covered.
-__device__ __forceinline__ bool make_setup(SnapV v0, SnapV v1, SnapV v2, uint32_t id, uint32_t W, uint32_t H,
-                                           TriSetup& t) {
-    int64_t A = (int64_t)(v2.Y - v1.Y) * (v0.X - v1.X) - (int64_t)(v2.X - v1.X) * (v0.Y - v1.Y);
-    if (A <= 0) return false;
-    int32_t minX = min(v0.X, min(v1.X, v2.X)), maxX = max(v0.X, max(v1.X, v2.X));
-    int32_t minY = min(v0.Y, min(v1.Y, v2.Y)), maxY = max(v0.Y, max(v1.Y, v2.Y));
-    t.px0 = max((minX + 127) >> 8, 0);
-    t.px1 = min((maxX - 128) >> 8, (int32_t)W - 1);
-    t.py0 = max((minY + 127) >> 8, 0);
-    t.py1 = min((maxY - 128) >> 8, (int32_t)H - 1);
-    if (t.px0 > t.px1 || t.py0 > t.py1) return false;
+// Pixel bbox of a triangle in a W x H target (the pixel centres its snapped
+// vertex extents can hold) and the extents themselves.
+struct TriBox {
+    int32_t px0, px1, py0, py1;
+    int32_t ext_x, ext_y;  // snapped vertex extents (1/256 pixel)
+};
+__device__ __forceinline__ TriBox tri_box(const SnapV& v0, const SnapV& v1, const SnapV& v2, uint32_t W, uint32_t H) {
+    const int32_t minX = min(v0.X, min(v1.X, v2.X)), maxX = max(v0.X, max(v1.X, v2.X));
+    const int32_t minY = min(v0.Y, min(v1.Y, v2.Y)), maxY = max(v0.Y, max(v1.Y, v2.Y));
+    TriBox b;
+    b.px0 = max((minX + 127) >> 8, 0);
+    b.px1 = min((maxX - 128) >> 8, (int32_t)W - 1);
+    b.py0 = max((minY + 127) >> 8, 0);
+    b.py1 = min((maxY - 128) >> 8, (int32_t)H - 1);
+    b.ext_x = maxX - minX;
+    b.ext_y = maxY - minY;
+    return b;
+}
+__device__ __forceinline__ bool box_empty(const TriBox& b) { return b.px0 > b.px1 || b.py0 > b.py1; }
+
+// The rest of the setup once the orientation is normalised and the doubled
+// area A > 0 and the (non-empty) box are known.
+__device__ __forceinline__ void finish_setup(SnapV v0, SnapV v1, SnapV v2, int64_t A, const TriBox& b, uint32_t id,
+                                             TriSetup& t) {
+    t.px0 = b.px0;
+    t.px1 = b.px1;
+    t.py0 = b.py0;
+    t.py1 = b.py1;
     t.X0 = v0.X; t.Y0 = v0.Y; t.X1 = v1.X; t.Y1 = v1.Y; t.X2 = v2.X; t.Y2 = v2.Y;
     float fA = __ll2float_rn(A);
     t.z0 = v0.z;
@@ -303,9 +308,19 @@ __device__ __forceinline__ bool make_setup(SnapV v0, SnapV v1, SnapV v2, uint32_
     // product of an edge function is at most ext_x * ext_y in magnitude
     // (and, so that per-pixel steps of 256 units fit too, both extents are
     // below 2^22)
-    if ((int64_t)(maxX - minX) * (int64_t)(maxY - minY) < (1ll << 30) && maxX - minX < (1 << 22) &&
-        maxY - minY < (1 << 22))
+    if ((int64_t)b.ext_x * (int64_t)b.ext_y < (1ll << 30) && b.ext_x < (1 << 22) && b.ext_y < (1 << 22))
         t.bias |= 8u;
+}
+
+// Build the setup of a normalised triangle; returns false when no pixel
+// centre of the (W x H) target can be covered.
+__device__ __forceinline__ bool make_setup(SnapV v0, SnapV v1, SnapV v2, uint32_t id, uint32_t W, uint32_t H,
+                                           TriSetup& t) {
+    int64_t A = (int64_t)(v2.Y - v1.Y) * (v0.X - v1.X) - (int64_t)(v2.X - v1.X) * (v0.Y - v1.Y);
+    if (A <= 0) return false;
+    const TriBox b = tri_box(v0, v1, v2, W, H);
+    if (box_empty(b)) return false;
+    finish_setup(v0, v1, v2, A, b, id, t);
     return true;
 }
 

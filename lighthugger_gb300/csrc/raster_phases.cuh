@@ -466,28 +466,30 @@ __device__ __forceinline__ void raster_meshlet(const FrameDev& f, const MeshletW
                 } else {
                     SnapV a = sv[m0], b = sv[m1], c = sv[m2];
                     // most visible triangles hold no pixel centre: the 32-bit
-                    // bbox test rejects them before the area
-                    int64_t cr = covers_centre(a, b, c, W, H) ? cross_rel(a, b, c) : 0;
+                    // bbox test rejects them before the area.  The box and the
+                    // area do not depend on the vertex order, so the set-up
+                    // reuses both (make_setup's A is |cr| once oriented).
+                    const TriBox box = tri_box(a, b, c, W, H);
+                    int64_t cr = box_empty(box) ? 0 : cross_rel(a, b, c);
                     // alpha clip is double sided
                     bool keep = ALPHA ? cr != 0 : (KIND == 0 ? cr < 0 : cr > 0);
                     if (keep) {
                         if (cr > 0) { SnapV tmp = b; b = c; c = tmp; }
-                        if (make_setup(a, b, c, LH_PACK_ID(t, w.slot), W, H, st)) {
-                            if (ALPHA) {
-                                st.bias |= kBiasAlpha;
-                                st.verts = m0 | (m1 << 8) | (m2 << 16);
-                            }
-                            uint32_t npx = (uint32_t)(st.px1 - st.px0 + 1) * (uint32_t)(st.py1 - st.py0 + 1);
-                            if (npx <= tune.small_px) {
-                                if (ALPHA) raster_lane_alpha<KIND>(f, st, w.target, W, as);
-                                else raster_lane<KIND>(st, w.target, W);
-                            } else if (npx <= tune.medium_px) {
-                                medium = true;
-                            } else if (KIND == 1) {
-                                big = true;  // appended below, one atomic per warp
-                            } else {
-                                push_big(f, st, w.view);
-                            }
+                        finish_setup(a, b, c, cr < 0 ? -cr : cr, box, LH_PACK_ID(t, w.slot), st);
+                        if (ALPHA) {
+                            st.bias |= kBiasAlpha;
+                            st.verts = m0 | (m1 << 8) | (m2 << 16);
+                        }
+                        uint32_t npx = (uint32_t)(st.px1 - st.px0 + 1) * (uint32_t)(st.py1 - st.py0 + 1);
+                        if (npx <= tune.small_px) {
+                            if (ALPHA) raster_lane_alpha<KIND>(f, st, w.target, W, as);
+                            else raster_lane<KIND>(st, w.target, W);
+                        } else if (npx <= tune.medium_px) {
+                            medium = true;
+                        } else if (KIND == 1) {
+                            big = true;  // appended below, one atomic per warp
+                        } else {
+                            push_big(f, st, w.view);
                         }
                     }
                 }
