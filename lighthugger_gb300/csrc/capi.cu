@@ -265,17 +265,13 @@ lh_status check_ctx(lh_ctx* c) {
 
 // Stage per-frame constants (uniforms + host-evaluated pow terms) in pinned
 // memory and copy them to the device on `s`.
-lh_status upload_frame_constants(lh_ctx* c, const Uniforms* u, const Uniforms* probes, uint32_t n_probes,
-                                 cudaStream_t s) {
-    uint32_t slot = c->frame_index++ & 1u;
-    cudaError_t e = cudaEventSynchronize(c->staging_done[slot]);
-    if (e != cudaSuccess) return cuda_fail(c, e, "staging event");
-    uint8_t* h = c->h_staging[slot];
-    Uniforms* hu = reinterpret_cast<Uniforms*>(h);
+// The per-frame Uniforms as the kernels read them (address fields are the
+// context's own buffers) and the frame constants.
+void fill_frame_constants(const lh_ctx* c, const Uniforms* u, const Uniforms* probes, uint32_t n_probes, Uniforms* hu,
+                          float* consts) {
     hu[0] = *u;
     for (uint32_t p = 0; p < n_probes; p++) hu[1 + p] = probes[p];
     for (uint32_t v = 0; v <= n_probes; v++) {
-        // address fields are the context's own buffers
         hu[v].meshlet_references = (uint64_t)(uintptr_t)c->h_views[v].refs;
         hu[v].instances = (uint64_t)(uintptr_t)c->instances;
         hu[v].draw_calls = (uint64_t)(uintptr_t)c->h_views[v].draws;
@@ -283,12 +279,21 @@ lh_status upload_frame_constants(lh_ctx* c, const Uniforms* u, const Uniforms* p
         hu[v].num_meshlets_prefix_sum = (uint64_t)(uintptr_t)c->h_views[v].sector;
         hu[v].dispatches = 0;
     }
-    size_t ubytes = sizeof(Uniforms) * (1 + n_probes);
-    float* consts = reinterpret_cast<float*>(h + sizeof(Uniforms) * (1 + c->cfg.max_probes));
     // generate_shadow_matrices.glsl:39-48: pow(0.5|0.75, cascade_split_pow),
     // uniform-only terms, evaluated here in double and rounded to float.
     consts[0] = (float)std::pow(0.5, (double)u->cascade_split_pow);
     consts[1] = (float)std::pow(0.75, (double)u->cascade_split_pow);
+}
+
+lh_status upload_frame_constants(lh_ctx* c, const Uniforms* u, const Uniforms* probes, uint32_t n_probes,
+                                 cudaStream_t s) {
+    uint32_t slot = c->frame_index++ & 1u;
+    cudaError_t e = cudaEventSynchronize(c->staging_done[slot]);
+    if (e != cudaSuccess) return cuda_fail(c, e, "staging event");
+    uint8_t* h = c->h_staging[slot];
+    float* consts = reinterpret_cast<float*>(h + sizeof(Uniforms) * (1 + c->cfg.max_probes));
+    fill_frame_constants(c, u, probes, n_probes, reinterpret_cast<Uniforms*>(h), consts);
+    size_t ubytes = sizeof(Uniforms) * (1 + n_probes);
     e = cudaMemcpyAsync(c->d_uniforms, h, ubytes, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_consts, consts, 2 * sizeof(float), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaEventRecord(c->staging_done[slot], s);
@@ -298,13 +303,22 @@ lh_status upload_frame_constants(lh_ctx* c, const Uniforms* u, const Uniforms* p
 
 // The frame's kernels, all stream ordered (capturable).  `batched` selects
 // the default schedule of lh_frame_batched.
-lh_status enqueue_frame(lh_ctx* c, uint32_t n_probes, uint32_t n_instances, bool batched, cudaStream_t s) {
+uint32_t frame_schedule(const lh_ctx* c, bool batched) {
+    uint32_t schedule = c->tuning.schedule;
+    if (schedule == LH_SCHEDULE_DEFAULT) schedule = batched ? LH_SCHEDULE_PERSISTENT : LH_SCHEDULE_PER_STAGE;
+    if (schedule == LH_SCHEDULE_PERSISTENT && persistent_blocks_per_sm() <= 0) schedule = LH_SCHEDULE_PER_STAGE;
+    return schedule;
+}
+
+// `start` (schedules with a clear launch only): the uniforms, constants and
+// scratch reset travel with the clear kernel instead of copies and a memset.
+lh_status enqueue_frame(lh_ctx* c, uint32_t n_probes, uint32_t n_instances, bool batched, cudaStream_t s,
+                        const FrameStart* start = nullptr) {
     const uint32_t n_persp = 1 + n_probes, n_views = n_persp + 4;
     FrameDev f = frame_dev(c, n_views, n_instances);
     const lh_tuning& t = c->tuning;
-    uint32_t schedule = t.schedule;
-    if (schedule == LH_SCHEDULE_DEFAULT) schedule = batched ? LH_SCHEDULE_PERSISTENT : LH_SCHEDULE_PER_STAGE;
-    if (schedule == LH_SCHEDULE_PERSISTENT && persistent_blocks_per_sm() <= 0) schedule = LH_SCHEDULE_PER_STAGE;
+    const uint32_t schedule = frame_schedule(c, batched);
+    if (start && schedule == LH_SCHEDULE_PERSISTENT) return fail(c, LH_ERR_CUDA, "frame start without a clear launch");
     const bool prof = c->profiling && !c->capturing;
     uint32_t stage = 0;
     auto mark = [&](cudaError_t e) {
@@ -317,7 +331,7 @@ lh_status enqueue_frame(lh_ctx* c, uint32_t n_probes, uint32_t n_instances, bool
         return e;
     };
     cudaError_t e = mark(cudaSuccess);
-    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_reset, 0, c->reset_bytes, s);
+    if (e == cudaSuccess && !start) e = cudaMemsetAsync(c->d_reset, 0, c->reset_bytes, s);
     const uint32_t cull_blocks = std::max(1u, (uint32_t)(c->sms * t.cull_blocks_per_sm));
     if (schedule == LH_SCHEDULE_PERSISTENT) {
         // stages 0..7 in one launch: the time lands in stage 0 ("clear")
@@ -327,7 +341,7 @@ lh_status enqueue_frame(lh_ctx* c, uint32_t n_probes, uint32_t n_instances, bool
         e = mark(e);
         e = skip_to(8, e);
     } else if (schedule == LH_SCHEDULE_PER_VIEW) {
-        if (e == cudaSuccess) e = mark(launch_clear_targets(f, s, c->sms));
+        if (e == cudaSuccess) e = mark(launch_clear_targets(f, s, c->sms, start));
         for (uint32_t v = 0; v < n_persp && e == cudaSuccess; v++) {
             e = launch_cull_instances(f, v, 1, s);
             if (e == cudaSuccess) e = launch_cull_meshlets(f, v, 1, cull_blocks, s);
@@ -344,7 +358,7 @@ lh_status enqueue_frame(lh_ctx* c, uint32_t n_probes, uint32_t n_instances, bool
         }
         e = skip_to(8, e);
     } else {
-        if (e == cudaSuccess) e = mark(launch_clear_targets(f, s, c->sms));
+        if (e == cudaSuccess) e = mark(launch_clear_targets(f, s, c->sms, start));
         // visibility views: instance cull + prefix, meshlet cull, raster
         if (e == cudaSuccess) e = mark(launch_cull_instances(f, 0, n_persp, s));
         if (e == cudaSuccess) e = mark(launch_cull_meshlets(f, 0, n_persp, cull_blocks, s));
@@ -593,9 +607,21 @@ static lh_status frame_impl(lh_ctx* c, const Uniforms* u, const Uniforms* probes
         if (e != cudaSuccess) return cuda_fail(c, e, "stream sync");
         if ((st = prepare_views(c, probes, n_probes)) != LH_OK) return st;
     }
-    if ((st = upload_frame_constants(c, u, probes, n_probes, s)) != LH_OK) return st;
     uint32_t n_inst = std::min(u->num_instances, c->n_instances);
-    if ((st = enqueue_frame(c, n_probes, n_inst, batched, s)) != LH_OK) return st;
+    if (n_probes == 0 && frame_schedule(c, batched) != LH_SCHEDULE_PERSISTENT) {
+        // one main view: its uniforms ride on the clear launch
+        FrameStart start;
+        std::memset(&start, 0, sizeof(start));
+        fill_frame_constants(c, u, nullptr, 0, &start.u, start.consts);
+        start.d_uniforms = c->d_uniforms;
+        start.d_consts = c->d_consts;
+        start.reset = reinterpret_cast<uint4*>(c->d_reset);
+        start.reset_words = c->reset_bytes / sizeof(uint4);
+        if ((st = enqueue_frame(c, n_probes, n_inst, batched, s, &start)) != LH_OK) return st;
+    } else {
+        if ((st = upload_frame_constants(c, u, probes, n_probes, s)) != LH_OK) return st;
+        if ((st = enqueue_frame(c, n_probes, n_inst, batched, s)) != LH_OK) return st;
+    }
     c->last_stream = s;
     if (out) fill_out(c, out);
     return LH_OK;

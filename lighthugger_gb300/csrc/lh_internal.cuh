@@ -103,7 +103,19 @@ struct FrameDev {
 };
 
 // Launchers (stream ordered).  Each returns the CUDA error of its launch.
-cudaError_t launch_clear_targets(const FrameDev& f, cudaStream_t s, int sms);
+// What the first kernel of a frame writes before anything reads it, when
+// the host hands it over as a kernel parameter instead of two copies and a
+// memset: the main view's Uniforms and the two frame constants, and the
+// per-frame scratch zeroed.
+struct FrameStart {
+    Uniforms u;
+    float consts[2];
+    Uniforms* d_uniforms;
+    float* d_consts;
+    uint4* reset;          // per-frame scratch, zeroed
+    uint64_t reset_words;  // its size in uint4
+};
+cudaError_t launch_clear_targets(const FrameDev& f, cudaStream_t s, int sms, const FrameStart* start = nullptr);
 cudaError_t launch_cull_instances(const FrameDev& f, uint32_t view_begin, uint32_t n_views, cudaStream_t s);
 cudaError_t launch_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint32_t n_views, uint32_t blocks,
                                  cudaStream_t s);

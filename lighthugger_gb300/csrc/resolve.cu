@@ -496,8 +496,21 @@ __global__ void __launch_bounds__(kResolveWarps * 32, LH_RESOLVE_MIN_BLOCKS)
     }
 }
 
-// grid = (blocks, n_views)
-__global__ void __launch_bounds__(256) k_clear_targets(FrameDev f) {
+// grid = (blocks, n_views).  With `has_start`, view 0's blocks also zero the
+// frame's scratch and block (0, 0) stores the frame's uniforms and constants
+// (nothing in this kernel reads either).
+__global__ void __launch_bounds__(256) k_clear_targets(FrameDev f, const __grid_constant__ FrameStart start,
+                                                       uint32_t has_start) {
+    if (has_start && blockIdx.y == 0) {
+        const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (uint64_t)gridDim.x * blockDim.x;
+        for (uint64_t i = tid; i < start.reset_words; i += stride) start.reset[i] = make_uint4(0u, 0u, 0u, 0u);
+        if (blockIdx.x == 0) {
+            const uint32_t* src = reinterpret_cast<const uint32_t*>(&start.u);
+            uint32_t* dst = reinterpret_cast<uint32_t*>(start.d_uniforms);
+            for (uint32_t i = threadIdx.x; i < sizeof(Uniforms) / 4; i += blockDim.x) dst[i] = src[i];
+            if (threadIdx.x < 2) start.d_consts[threadIdx.x] = start.consts[threadIdx.x];
+        }
+    }
     phase_clear_view(f, blockIdx.y, (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, (uint64_t)gridDim.x * blockDim.x,
                      blockIdx.x == 0 && blockIdx.y == 0);
 }
@@ -515,9 +528,15 @@ __global__ void __launch_bounds__(256) k_depth_reduce_fit(FrameDev f) {
 
 }  // namespace
 
-cudaError_t launch_clear_targets(const FrameDev& f, cudaStream_t s, int sms) {
+cudaError_t launch_clear_targets(const FrameDev& f, cudaStream_t s, int sms, const FrameStart* start) {
     dim3 grid((unsigned)sms, f.n_views);
-    k_clear_targets<<<grid, 256, 0, s>>>(f);
+    if (start) {
+        k_clear_targets<<<grid, 256, 0, s>>>(f, *start, 1u);
+    } else {
+        FrameStart none;
+        std::memset(&none, 0, sizeof(none));
+        k_clear_targets<<<grid, 256, 0, s>>>(f, none, 0u);
+    }
     return cudaGetLastError();
 }
 
