@@ -82,13 +82,19 @@ typedef struct lh_config {
     uint32_t max_probes;      /* probe views for lh_frame_batched; 0 = none */
     uint32_t max_probe_pixels; /* total pixels over all probe views */
     int32_t device;           /* CUDA device ordinal */
-    uint32_t flags;           /* reserved, 0 */
+    uint32_t flags;           /* LH_CONFIG_* bits; others must be 0 */
 } lh_config;
+
+/* lh_config.flags: the HDR image in RGBA16F (4 x IEEE half, round to
+ * nearest even; the reference's frame_resources.h:20 format) instead of
+ * RGBA32F.  Half the bytes written and read back; the differentiable resolve
+ * needs RGBA32F. */
+#define LH_CONFIG_HDR_RGBA16F 1u
 
 /* Device pointers to the context-owned results of the last frame. */
 typedef struct lh_frame_out {
     uint64_t visibility;   /* u64[height][width]: (float bits of depth << 32) | packed ID; 0 = clear */
-    uint64_t hdr;          /* float4[height][width]: linear HDR radiance, alpha = 1 */
+    uint64_t hdr;          /* float4[height][width] (or 4 x half with LH_CONFIG_HDR_RGBA16F): linear HDR radiance, alpha = 1 */
     uint64_t shadow_maps;  /* float[4][shadow_size][shadow_size]: cascade depth, clear 1.0 */
     uint64_t misc_storage; /* MiscStorage */
     uint64_t prefix_sums;  /* n_views prefix sectors of prefix_sector_bytes each */
@@ -250,7 +256,8 @@ lh_status lh_cull_instances_noalloc(const Instance* d_instances, uint32_t n_inst
                                     const Uniforms* host_uniforms, uint8_t* d_sector, uint32_t capacity,
                                     uint32_t* d_flags, void* stream);
 
-/* lh_frame followed by a copy of the HDR image (float4[height][width]) to
+/* lh_frame followed by a copy of the HDR image (width * height pixels of 16
+ * bytes, 8 with LH_CONFIG_HDR_RGBA16F) to
  * `host_hdr`, pipelined: the copy runs on a stream of the context after the
  * frame's resolve, and the next frame's culling and rasterisation run while
  * it lands (that frame's resolve waits for it).  Returns once both are

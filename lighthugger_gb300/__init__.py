@@ -75,6 +75,7 @@ class DeviceStatus(C.Structure):
 
 
 SCHEDULE_DEFAULT, SCHEDULE_PER_STAGE, SCHEDULE_PERSISTENT, SCHEDULE_PER_VIEW = 0, 1, 2, 3
+CONFIG_HDR_RGBA16F = 1  # lh_config.flags: the HDR image in RGBA16F
 
 
 class Tuning(C.Structure):
@@ -370,7 +371,10 @@ class Renderer:
         return self.download(o.visibility, o.width * o.height * 8, np.uint64).reshape(o.height, o.width)
 
     def hdr(self):
+        """The HDR image as float32 [h, w, 4] (float16 with CONFIG_HDR_RGBA16F)."""
         o = self.out
+        if self.config.flags & CONFIG_HDR_RGBA16F:
+            return self.download(o.hdr, o.width * o.height * 8, np.float16).reshape(o.height, o.width, 4)
         return self.download(o.hdr, o.width * o.height * 16, np.float32).reshape(o.height, o.width, 4)
 
     def shadow_maps(self):

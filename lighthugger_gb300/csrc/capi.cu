@@ -51,7 +51,7 @@ struct lh_ctx {
     uint8_t* d_draws = nullptr;
     uint64_t* d_vis = nullptr;
     float* d_shadow = nullptr;
-    float4* d_hdr = nullptr;
+    void* d_hdr = nullptr;
     uint64_t* d_probe_vis = nullptr;
     BigTri* d_big = nullptr;
     uint32_t* d_big_base = nullptr;
@@ -172,6 +172,8 @@ void free_all(lh_ctx* c) {
     c->copy_stream = nullptr;
 }
 
+size_t hdr_pixel_bytes(const lh_config& cfg) { return (cfg.flags & LH_CONFIG_HDR_RGBA16F) ? 8 : 16; }
+
 // Work that writes d_hdr waits for the last pipelined readback of it.
 cudaError_t wait_readback(const lh_ctx* c, cudaStream_t s) {
     if (!c->readbacks) return cudaSuccess;
@@ -249,6 +251,7 @@ FrameDev frame_dev(const lh_ctx* c, uint32_t n_views, uint32_t n_instances) {
     f.shadow_maps = c->d_shadow;
     f.shadow_size = c->cfg.shadow_size;
     f.hdr = c->d_hdr;
+    f.hdr_half = (c->cfg.flags & LH_CONFIG_HDR_RGBA16F) ? 1u : 0u;
     f.visibility = c->d_vis;
     f.uniforms = c->d_uniforms;
     f.frame_consts = c->d_consts;
@@ -444,6 +447,7 @@ lh_status lh_create(const lh_config* config, lh_ctx** out) {
     if ((uint64_t)cfg.max_draws * 2 > (1ull << 24)) return LH_ERR_INVALID_ARGUMENT;
     if (cfg.max_big_triangles == 0) cfg.max_big_triangles = 1u << 20;
     if (cfg.max_probes > kMaxViews - 5) return LH_ERR_INVALID_ARGUMENT;
+    if (cfg.flags & ~LH_CONFIG_HDR_RGBA16F) return LH_ERR_INVALID_ARGUMENT;
     lh_ctx* c = new (std::nothrow) lh_ctx();
     if (!c) return LH_ERR_OUT_OF_MEMORY;
     c->cfg = cfg;
@@ -464,7 +468,7 @@ lh_status lh_create(const lh_config* config, lh_ctx** out) {
     if (e == cudaSuccess) e = dalloc(c, &c->d_draws, c->draw_bytes * c->max_views);
     if (e == cudaSuccess) e = dalloc(c, &c->d_vis, W * H * 8);
     if (e == cudaSuccess) e = dalloc(c, &c->d_shadow, 4 * S * S * 4);
-    if (e == cudaSuccess) e = dalloc(c, &c->d_hdr, W * H * 16);
+    if (e == cudaSuccess) e = dalloc(c, &c->d_hdr, W * H * hdr_pixel_bytes(c->cfg));
     if (e == cudaSuccess) e = dalloc(c, &c->d_probe_vis, (size_t)std::max(cfg.max_probe_pixels, 32u) * 8);
     if (e == cudaSuccess) e = dalloc(c, &c->d_big, sizeof(BigTri) * (size_t)cfg.max_big_triangles);
     if (e == cudaSuccess) e = dalloc(c, &c->d_big_base, sizeof(uint32_t) * (size_t)cfg.max_big_triangles);
@@ -560,7 +564,7 @@ lh_status lh_frame_readback(lh_ctx* c, const Uniforms* u, void* host_hdr, void* 
     if ((st = frame_impl(c, u, nullptr, 0, stream, out, false)) != LH_OK) return st;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     const uint32_t k = c->readbacks & 1u;
-    const size_t bytes = (size_t)c->cfg.width * c->cfg.height * sizeof(float4);
+    const size_t bytes = (size_t)c->cfg.width * c->cfg.height * hdr_pixel_bytes(c->cfg);
     cudaError_t e = cudaEventRecord(c->resolved, s);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(c->copy_stream, c->resolved, 0);
     if (e == cudaSuccess) e = cudaMemcpyAsync(host_hdr, c->d_hdr, bytes, cudaMemcpyDeviceToHost, c->copy_stream);

@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(256) k_display_transform(FrameDev f, const flo
     const uint32_t W = u.window_size.x, H = u.window_size.y;
     const uint32_t x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
     if (x >= W || y >= H) return;
-    const float4 hdr = __ldcs(f.hdr + (size_t)y * W + x);
+    const float4 hdr = load_hdr(f.hdr, f.hdr_half, (size_t)y * W + x);
     const f3 stimulus{hdr.x, hdr.y, hdr.z};
     // tony_mc_mapface (display_transform.comp:5-17)
     const f3 encoded{stimulus.x / (stimulus.x + 1.0f), stimulus.y / (stimulus.y + 1.0f),

@@ -9,6 +9,8 @@
 // which makes culling, visibility IDs, depth and shadow maps bit exact.
 #pragma once
 
+#include <cuda_fp16.h>
+
 #include <cstdint>
 
 #include "int_float.cuh"
@@ -419,6 +421,30 @@ __device__ __forceinline__ void write_fragment(void* target, uint32_t W, int32_t
         asm volatile("red.relaxed.gpu.global.min.u32 [%0], %1;" ::"l"(reinterpret_cast<uint32_t*>(target) + pix),
                      "r"(f2u(depth)));
     }
+}
+
+// One pixel of the HDR target: RGBA32F, or RGBA16F (round to nearest even,
+// the reference's format) when the context asks for it.  Streaming stores:
+// nothing re-reads the image in the frame.
+__device__ __forceinline__ void store_hdr(void* hdr, uint32_t half, size_t pixel, float r, float g, float b) {
+    if (half) {
+        const __half2 rg = __floats2half2_rn(r, g), ba = __floats2half2_rn(b, 1.0f);
+        uint2 v;
+        v.x = *reinterpret_cast<const uint32_t*>(&rg);
+        v.y = *reinterpret_cast<const uint32_t*>(&ba);
+        __stcs(reinterpret_cast<uint2*>(hdr) + pixel, v);
+    } else {
+        __stcs(reinterpret_cast<float4*>(hdr) + pixel, make_float4(r, g, b, 1.0f));
+    }
+}
+__device__ __forceinline__ float4 load_hdr(const void* hdr, uint32_t half, size_t pixel) {
+    if (half) {
+        const uint2 v = __ldcs(reinterpret_cast<const uint2*>(hdr) + pixel);
+        const float2 rg = __half22float2(*reinterpret_cast<const __half2*>(&v.x));
+        const float2 ba = __half22float2(*reinterpret_cast<const __half2*>(&v.y));
+        return make_float4(rg.x, rg.y, ba.x, ba.y);
+    }
+    return __ldcs(reinterpret_cast<const float4*>(hdr) + pixel);
 }
 
 }  // namespace lh

@@ -95,7 +95,8 @@ struct FrameDev {
     uint32_t n_textures;
     float* shadow_maps;
     uint32_t shadow_size;
-    float4* hdr;
+    void* hdr;               // float4[H][W], or (hdr_half) RGBA16F as 4 x half
+    uint32_t hdr_half;
     uint64_t* visibility;       // main view
     const Uniforms* uniforms;   // main view
     const float* frame_consts;  // [0] pow(0.5, split), [1] pow(0.75, split)

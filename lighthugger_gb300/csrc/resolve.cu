@@ -313,14 +313,14 @@ __device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uin
     if (u.debug == 4) *clock_slot = clock64();
     const uint32_t W = u.window_size.x, H = u.window_size.y;
     const f2 ndc{(float)x / (float)W * 2.0f - 1.0f, (float)y / (float)H * 2.0f - 1.0f};
-    float4* out = f.hdr + (size_t)y * W + x;
+    const size_t pix = (size_t)y * W + x;
     if (u2f((uint32_t)(vis >> 32)) == 0.0f) {
         f4 un = mul(u.perspective_inverse, f4{ndc.x, ndc.y, 0.0f, 1.0f});
         f3 lr = normalize(f3{un.x, un.y, un.z});
         f4 r4 = mul(u.view_inverse, f4{lr.x, lr.y, lr.z, 0.0f});
         // procedural sky in place of the missing cubemap asset
         f3 s = f3{0.25f + 0.10f * r4.y, 0.35f + 0.15f * r4.y, 0.55f + 0.25f * r4.y} * powf(2.0f, 3.0f);
-        __stcs(out, make_float4(s.x, s.y, s.z, 1.0f));
+        store_hdr(f.hdr, f.hdr_half, pix, s.x, s.y, s.z);
         return;
     }
     const uint32_t packed = (uint32_t)vis;
@@ -387,7 +387,7 @@ __device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uin
     // AMBIENT_SH (render_geometry.comp:40-57): only sh[0] = sh[2] = 0.025.
     if (u.debug != 0 && u.debug != 4) {
         const f3 o = debug_view(u.debug, base, ci, tri, ref.meshlet_index, normal);
-        __stcs(out, make_float4(o.x, o.y, o.z, 1.0f));
+        store_hdr(f.hdr, f.hdr_half, pix, o.x, o.y, o.z);
         return;
     }
     const float amb_level = 0.025f;
@@ -403,7 +403,7 @@ __device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uin
              ld3(u.sun_intensity);
     f3 o = sun + ambient;
     if (u.debug == 4) o = clock_view(*clock_slot);
-    __stcs(out, make_float4(o.x, o.y, o.z, 1.0f));
+    store_hdr(f.hdr, f.hdr_half, pix, o.x, o.y, o.z);
 }
 
 #ifndef LH_RESOLVE_MIN_BLOCKS

@@ -78,6 +78,9 @@ class DiffResolve:
         self.torch = torch
         self.renderer = renderer
         self.scene = scene
+        from . import CONFIG_HDR_RGBA16F
+        if renderer.config.flags & CONFIG_HDR_RGBA16F:
+            raise ValueError("the differentiable resolve needs the RGBA32F HDR image")
         recs, inst = _scene_records(scene)
         if not recs or not recs[0].device_info:
             raise ValueError("scene is not uploaded")

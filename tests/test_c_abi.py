@@ -76,6 +76,10 @@ def test_null_and_bad_arguments_return_status(native):
     assert L.lh_create(C.byref(cfg), C.byref(h)) == 1  # empty window
     cfg = native.Config(width=64, height=64, max_draws=1 << 24)  # 2*max_draws slots exceed the 24-bit ID
     assert L.lh_create(C.byref(cfg), C.byref(h)) == 1
+    cfg = native.Config(width=64, height=64, shadow_size=64, max_instances=16, max_draws=16, flags=2)
+    assert L.lh_create(C.byref(cfg), C.byref(h)) == 1  # unknown config flag
+    assert L.lh_frame_readback(None, None, None, None, None) == 1
+    assert L.lh_readback_wait(None) == 1
     assert L.lh_scene_create(9, 1, None, C.byref(h)) == 1
     cam = native.Camera()
     u = native.Uniforms()

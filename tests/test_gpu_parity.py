@@ -226,3 +226,32 @@ def test_shadow_sizes_and_odd_widths(native, oracle, shadow_size, width, height)
     assert not errors, "\n".join(errors) + " %s" % stats
     assert st.flags == fr.flags
     assert stats["covered"] > 1000
+
+
+def test_hdr_rgba16f_is_the_rgba32f_image_rounded(native):
+    """LH_CONFIG_HDR_RGBA16F: every channel is the RGBA32F result rounded to
+    nearest-even half (numpy's float16 conversion), alpha 1; the pipelined
+    readback copies 8 bytes per pixel."""
+    import torch
+    lh = native
+    scene = lh.Scene(1).upload(0)
+    d = scene.desc
+    out = {}
+    for flags in (0, lh.CONFIG_HDR_RGBA16F):
+        cfg = lh.Config(width=d.width, height=d.height, shadow_size=d.shadow_size, max_instances=1024,
+                        max_draws=200000, flags=flags)
+        r = lh.Renderer(cfg)
+        r.set_scene(scene)
+        r.frame(scene.uniforms)
+        out[flags] = r.hdr().copy()
+        if flags:
+            buf = torch.empty(d.width * d.height * 4, dtype=torch.float16, pin_memory=True)
+            r.frame_readback(scene.uniforms, buf.data_ptr())
+            r.readback_wait()
+            out["readback"] = buf.numpy().reshape(d.height, d.width, 4).copy()
+    h16 = out[lh.CONFIG_HDR_RGBA16F]
+    assert h16.dtype == np.float16
+    assert np.array_equal(h16.view(np.uint16), out[0].astype(np.float16).view(np.uint16))
+    assert np.all(h16[..., 3] == 1.0)
+    assert np.array_equal(out["readback"].view(np.uint16), h16.view(np.uint16))
+
