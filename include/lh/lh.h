@@ -134,7 +134,11 @@ lh_status lh_create(const lh_config* config, lh_ctx** out_ctx);
  * mesh_info_address fields are device addresses (src/main.cpp:433-440);
  * `textures` is a host array of descriptors with device texel addresses,
  * indexed by MeshInfo texture indices (replaces the bindless texture array,
- * src/shaders/common/bindings.glsl:7, src/descriptor_set.cpp:28-139). */
+ * src/shaders/common/bindings.glsl:7, src/descriptor_set.cpp:28-139).
+ * Texels are read here, once, into a linear float copy owned by the context
+ * (16 bytes per texel; sRGB decoded), as the reference uploads its images
+ * once: call lh_set_scene again after changing texel data.  Instance,
+ * MeshInfo and vertex data are read by every frame. */
 lh_status lh_set_scene(lh_ctx* ctx, const Instance* d_instances, uint32_t n,
                        const lh_texture* textures, uint32_t n_textures);
 

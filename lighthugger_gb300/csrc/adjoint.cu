@@ -33,7 +33,7 @@ struct DeviceSampler {
             return s;
         }
         const lh_texture t = f->textures[index];
-        const uchar4* tex = reinterpret_cast<const uchar4*>(t.texels);
+        const float4* tex = f->tex_linear[index];
         float u = uv.x * (float)t.width - 0.5f, v = uv.y * (float)t.height - 0.5f;
         if (!(fabsf(u) < 1e9f)) u = 0.0f;
         if (!(fabsf(v) < 1e9f)) v = 0.0f;
@@ -49,10 +49,11 @@ struct DeviceSampler {
         s.size_u = (float)t.width;
         s.size_v = (float)t.height;
         auto texel = [&](int32_t i, int32_t j, float* o) {
-            uchar4 p = __ldg(tex + ((size_t)j * W + i));
-            if (t.srgb) { o[0] = f->srgb_lut[p.x]; o[1] = f->srgb_lut[p.y]; o[2] = f->srgb_lut[p.z]; }
-            else { o[0] = (float)p.x / 255.0f; o[1] = (float)p.y / 255.0f; o[2] = (float)p.z / 255.0f; }
-            o[3] = (float)p.w / 255.0f;
+            const float4 p = __ldg(tex + ((size_t)j * W + i));
+            o[0] = p.x;
+            o[1] = p.y;
+            o[2] = p.z;
+            o[3] = p.w;
         };
         texel(s.i0, s.j0, s.t00);
         texel(s.i1, s.j0, s.t10);

@@ -59,6 +59,10 @@ struct lh_ctx {
     ViewDev* d_views = nullptr;
     lh_texture* d_textures = nullptr;
     uint32_t n_textures = 0;
+    // linear float4 copies of the textures (one buffer) and a table of
+    // device pointers into it, made by lh_set_scene
+    float4* d_tex_linear = nullptr;
+    const float4** d_tex_linear_ptrs = nullptr;
     // per-frame zeroed scratch (look-back words and tile claims)
     uint8_t* d_reset = nullptr;
     size_t reset_bytes = 0;
@@ -248,6 +252,7 @@ FrameDev frame_dev(const lh_ctx* c, uint32_t n_views, uint32_t n_instances) {
     f.clip_cap = c->cfg.max_big_triangles;
     f.textures = c->d_textures;
     f.n_textures = c->n_textures;
+    f.tex_linear = c->d_tex_linear_ptrs;
     f.shadow_maps = c->d_shadow;
     f.shadow_size = c->cfg.shadow_size;
     f.hdr = c->d_hdr;
@@ -538,6 +543,31 @@ lh_status lh_set_scene(lh_ctx* c, const Instance* d_instances, uint32_t n, const
     if (e == cudaSuccess && n_textures)
         e = cudaMemcpy(c->d_textures, textures, sizeof(lh_texture) * n_textures, cudaMemcpyHostToDevice);
     c->n_textures = n_textures;
+    // the kernels sample linear float4 texels: sRGB decoded through the LUT,
+    // channels / 255 -- decoded here once instead of per sample
+    for (void* old : {(void*)c->d_tex_linear, (void*)c->d_tex_linear_ptrs}) {
+        if (!old) continue;
+        for (auto it = c->allocs.begin(); it != c->allocs.end(); ++it)
+            if (it->p == old) { cudaFree(it->p); c->allocs.erase(it); break; }
+    }
+    c->d_tex_linear = nullptr;
+    c->d_tex_linear_ptrs = nullptr;
+    {
+        std::vector<size_t> offset(n_textures + 1, 0);
+        for (uint32_t i = 0; i < n_textures; i++)
+            offset[i + 1] = offset[i] + (size_t)textures[i].width * textures[i].height;
+        if (e == cudaSuccess) e = dalloc(c, &c->d_tex_linear, sizeof(float4) * std::max<size_t>(1, offset[n_textures]));
+        if (e == cudaSuccess) e = dalloc(c, &c->d_tex_linear_ptrs, sizeof(float4*) * std::max(1u, n_textures));
+        std::vector<const float4*> ptrs(n_textures);
+        for (uint32_t i = 0; i < n_textures && e == cudaSuccess; i++) {
+            ptrs[i] = c->d_tex_linear + offset[i];
+            e = launch_linearize_texture(reinterpret_cast<const uchar4*>(textures[i].texels), c->d_tex_linear + offset[i],
+                                         offset[i + 1] - offset[i], textures[i].srgb, c->d_srgb, 0);
+        }
+        if (e == cudaSuccess && n_textures)
+            e = cudaMemcpy(c->d_tex_linear_ptrs, ptrs.data(), sizeof(float4*) * n_textures, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    }
     // per-frame scratch
     if (c->d_reset) {
         for (auto it = c->allocs.begin(); it != c->allocs.end(); ++it)

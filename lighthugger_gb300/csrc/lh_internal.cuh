@@ -93,6 +93,7 @@ struct FrameDev {
     uint32_t clip_cap;
     const lh_texture* textures;
     uint32_t n_textures;
+    const float4* const* tex_linear;  // per texture: its texels as linear float4 (see launch_linearize_texture)
     float* shadow_maps;
     uint32_t shadow_size;
     void* hdr;               // float4[H][W], or (hdr_half) RGBA16F as 4 x half
@@ -116,6 +117,11 @@ struct FrameStart {
     uint4* reset;          // per-frame scratch, zeroed
     uint64_t reset_words;  // its size in uint4
 };
+// dst[i] = texel i of an RGBA8 texture as linear floats: RGB through the
+// sRGB decode table when `srgb`, else / 255; alpha / 255 (correctly rounded
+// divisions, the oracle's definition).
+cudaError_t launch_linearize_texture(const uchar4* src, float4* dst, size_t n, uint32_t srgb, const float* lut,
+                                     cudaStream_t s);
 cudaError_t launch_clear_targets(const FrameDev& f, cudaStream_t s, int sms, const FrameStart* start = nullptr);
 cudaError_t launch_cull_instances(const FrameDev& f, uint32_t view_begin, uint32_t n_views, cudaStream_t s);
 cudaError_t launch_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint32_t n_views, uint32_t blocks,

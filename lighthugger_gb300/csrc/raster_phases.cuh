@@ -127,7 +127,7 @@ __device__ __forceinline__ AlphaTri alpha_setup(const AlphaVert& v0, const Alpha
 __device__ __forceinline__ float sample_alpha(const FrameDev& f, uint32_t index, float uvx, float uvy) {
     if (index >= f.n_textures) return 0.0f;
     const lh_texture t = f.textures[index];
-    const uchar4* tex = reinterpret_cast<const uchar4*>(t.texels);
+    const float4* tex = f.tex_linear[index];
     float u = uvx * (float)t.width - 0.5f, v = uvy * (float)t.height - 0.5f;
     if (!(fabsf(u) < 1e9f)) u = 0.0f;
     if (!(fabsf(v) < 1e9f)) v = 0.0f;
@@ -135,7 +135,7 @@ __device__ __forceinline__ float sample_alpha(const FrameDev& f, uint32_t index,
     const float a = u - fu, b = v - fv;
     const int32_t i0 = (int32_t)fu, j0 = (int32_t)fv, W = (int32_t)t.width, H = (int32_t)t.height;
     const int32_t ia = wrap_texel(i0, W), ib = wrap_texel(i0 + 1, W), ja = wrap_texel(j0, H), jb = wrap_texel(j0 + 1, H);
-    auto al = [&](int32_t i, int32_t j) { return (float)__ldg(tex + ((size_t)j * W + i)).w / 255.0f; };
+    auto al = [&](int32_t i, int32_t j) { return __ldg(&tex[(size_t)j * W + i].w); };
     const float t00 = al(ia, ja), t10 = al(ib, ja), t01 = al(ia, jb), t11 = al(ib, jb);
     const float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
     return ((t00 * w00 + t10 * w10) + t01 * w01) + t11 * w11;
@@ -758,6 +758,7 @@ __device__ void phase_raster_big(const FrameDev& f) {
     const uint32_t warps_total = gridDim.x * (blockDim.x >> 5);
     const uint32_t gwarp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const uint64_t dyn_base = (uint64_t)warps_total * kChunkBatch;
+    uint32_t t_idx = 0, t_base = 1, t_end = 0;  // chunk range [t_base, t_end) of triangle t_idx (empty at first)
     uint32_t c = (uint32_t)min((uint64_t)gwarp * kChunkBatch, (uint64_t)total32);
     uint32_t c_end = (uint32_t)min((uint64_t)gwarp * kChunkBatch + kChunkBatch, (uint64_t)total32);
     for (;;) {
@@ -771,15 +772,29 @@ __device__ void phase_raster_big(const FrameDev& f) {
             c = (uint32_t)first;
             c_end = (uint32_t)min(first + kChunkBatch, (uint64_t)total32);
         }
-        const uint32_t first = upper_bound_warp(f.big_base, ntri, c, lane);
+        // the chunk's triangle: the previous chunk's while c stays in its
+        // range (consecutive claims), else a 32-ary search of the bases
+        uint32_t i;
+        if (c >= t_base && c < t_end) {
+            i = t_idx;
+        } else {
+            const uint32_t first = upper_bound_warp(f.big_base, ntri, c, lane);
+            if (first == 0) {
+                c++;
+                continue;
+            }
+            i = first - 1;
+        }
         c++;
-        if (first == 0) continue;
-        const uint32_t i = first - 1;
         const BigTri b = f.big[i];
         const uint32_t nbx = (uint32_t)(b.px1 - b.px0) / kChunkCols + 1;
         const uint32_t nby = (uint32_t)(b.py1 - b.py0) / kChunkRows + 1;
-        const unsigned long long local = (c - 1u) - f.big_base[i];
+        const uint32_t base = f.big_base[i];
+        const unsigned long long local = (c - 1u) - base;
         if (local >= (unsigned long long)nbx * nby) continue;  // chunk of a dropped triangle
+        t_idx = i;
+        t_base = base;
+        t_end = base + nbx * nby;
         const int32_t cx = (int32_t)(local % nbx), cy = (int32_t)(local / nbx);
         const int32_t x0 = b.px0 + cx * kChunkCols, x1 = min(b.px1, x0 + kChunkCols - 1);
         const int32_t y0 = b.py0 + cy * kChunkRows, y1 = min(b.py1, y0 + kChunkRows - 1);

@@ -17,11 +17,12 @@ namespace {
 // ---------------------------------------------------------------- resolve
 struct Tex4 { float r, g, b, a; };
 
-// Bilinear filtering of level 0 with repeat addressing.
+// Bilinear filtering of level 0 with repeat addressing, over the texture's
+// linear float4 copy.
 __device__ Tex4 sample_repeat(const FrameDev& f, uint32_t index, f2 uv) {
     if (index >= f.n_textures) return {0.0f, 0.0f, 0.0f, 0.0f};
     const lh_texture t = f.textures[index];
-    const uint8_t* tex = reinterpret_cast<const uint8_t*>(t.texels);
+    const float4* tex = f.tex_linear[index];
     float u = uv.x * (float)t.width - 0.5f, v = uv.y * (float)t.height - 0.5f;
     if (!(fabsf(u) < 1e9f)) u = 0.0f;
     if (!(fabsf(v) < 1e9f)) v = 0.0f;
@@ -32,12 +33,8 @@ __device__ Tex4 sample_repeat(const FrameDev& f, uint32_t index, f2 uv) {
     const int32_t ia = wrap_texel(i0, W), ib = wrap_texel(i0 + 1, W);
     const int32_t ja = wrap_texel(j0, H), jb = wrap_texel(j0 + 1, H);
     auto texel = [&](int32_t i, int32_t j) {
-        uchar4 p = __ldg(reinterpret_cast<const uchar4*>(tex) + ((size_t)j * W + i));
-        Tex4 r;
-        if (t.srgb) { r.r = f.srgb_lut[p.x]; r.g = f.srgb_lut[p.y]; r.b = f.srgb_lut[p.z]; }
-        else { r.r = (float)p.x * (1.0f / 255.0f); r.g = (float)p.y * (1.0f / 255.0f); r.b = (float)p.z * (1.0f / 255.0f); }
-        r.a = (float)p.w * (1.0f / 255.0f);
-        return r;
+        const float4 p = __ldg(tex + ((size_t)j * W + i));
+        return Tex4{p.x, p.y, p.z, p.w};
     };
     Tex4 t00 = texel(ia, ja), t10 = texel(ib, ja), t01 = texel(ia, jb), t11 = texel(ib, jb);
     float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
@@ -527,6 +524,35 @@ __global__ void __launch_bounds__(256) k_depth_reduce_fit(FrameDev f) {
 }
 
 }  // namespace
+
+namespace {
+__global__ void __launch_bounds__(256) k_linearize_texture(const uchar4* src, float4* dst, size_t n, uint32_t srgb,
+                                                           const float* lut) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const uchar4 p = src[i];
+        float4 o;
+        if (srgb) {
+            o.x = lut[p.x];
+            o.y = lut[p.y];
+            o.z = lut[p.z];
+        } else {
+            o.x = (float)p.x / 255.0f;
+            o.y = (float)p.y / 255.0f;
+            o.z = (float)p.z / 255.0f;
+        }
+        o.w = (float)p.w / 255.0f;
+        dst[i] = o;
+    }
+}
+}  // namespace
+
+cudaError_t launch_linearize_texture(const uchar4* src, float4* dst, size_t n, uint32_t srgb, const float* lut,
+                                     cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    const size_t blocks = std::min<size_t>((n + 255) / 256, 4096);
+    k_linearize_texture<<<(unsigned)blocks, 256, 0, s>>>(src, dst, n, srgb, lut);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_clear_targets(const FrameDev& f, cudaStream_t s, int sms, const FrameStart* start) {
     dim3 grid((unsigned)sms, f.n_views);
