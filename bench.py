@@ -192,32 +192,53 @@ def run_gpu(args):
         r.frame(u, stream=sptr)
     torch.cuda.synchronize()
     st = r.status()
-    # per-stage times (device events on the frame stream), one profiled frame per step
-    r.set_profiling(True)
-    stage_acc = {k: 0.0 for k in lh.STAGES}
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    def timed_frames(run, steps):
+        """Device ms of each frame (events on the frame stream), the 256 MiB
+        flush written before each, outside the events."""
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for i in range(steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(i))
+                evs[i][0].record(stream)
+            run()
+            with torch.cuda.stream(stream):
+                evs[i][1].record(stream)
+        torch.cuda.synchronize()
+        return [a.elapsed_time(b) for a, b in evs]
+
     clocks = _clock_sampler()
     time.sleep(0.3)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    for i in range(args.steps):
-        with torch.cuda.stream(stream):
-            flush.fill_(float(i))
-            ev[i][0].record(stream)
-        r.frame(u, stream=sptr)
-        with torch.cuda.stream(stream):
-            ev[i][1].record(stream)
-        for k, v in r.stage_times().items():
-            stage_acc[k] += v
+    # the timed frames (no stage events inside them)
+    ms_steps = timed_frames(lambda: r.frame(u, stream=sptr), args.steps)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
     clk = _clock_summary(clocks, local_rank)
-    ms_steps = [a.elapsed_time(b) for a, b in ev]
     ms = sum(ms_steps) / len(ms_steps)
+    # per-stage split: the same frames again with an event between stages
+    r.set_profiling(True)
+    stage_acc = {k: 0.0 for k in lh.STAGES}
+    for i in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(i))
+        r.frame(u, stream=sptr)
+        for k, v in r.stage_times().items():
+            stage_acc[k] += v
     stage_ms = {k: v / args.steps for k, v in stage_acc.items()}
     r.set_profiling(False)
+    # the same frame replayed from its CUDA graph (lh_frame_graph, no probes,
+    # the per-stage schedule of lh_frame)
+    tuning = r.tuning()
+    r.set_tuning(schedule=lh.SCHEDULE_PER_STAGE)
+    for _ in range(2):
+        r.frame_graph(u, None, 0, stream=sptr)
+    torch.cuda.synchronize()
+    graph_steps = timed_frames(lambda: r.frame_graph(u, None, 0, stream=sptr), args.steps)
+    graph_ms = sum(graph_steps) / len(graph_steps)
+    r.set_tuning(schedule=tuning.schedule)
     ms = reduce_max_over_ranks(ms, device="cuda")
 
     # e2e through the C ABI with host buffers.  Pipelined (lh_frame_readback):
@@ -285,6 +306,7 @@ def run_gpu(args):
         "shadow_visible_meshlets": [int(st.visible_opaque[k]) for k in range(1, 5)],
         "big_triangles_last_pass": int(st.big_triangles), "clipped_triangles_last_pass": int(st.clipped_triangles),
         "stage_ms": {k: round(v, 4) for k, v in stage_ms.items()},
+        "graph_ms": graph_ms,
         "raster": {"visible_triangles": tri_main, "shadow_triangles": tri_shadow,
                    "gtri_per_s": tri_main / (stage_ms["raster"] * 1e-3) / 1e9,
                    "shadow_gtri_per_s": tri_shadow / (stage_ms["shadow_raster"] * 1e-3) / 1e9},
