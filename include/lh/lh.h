@@ -160,7 +160,8 @@ lh_status lh_frame_batched(lh_ctx* ctx, const Uniforms* host_uniforms,
 /* Same frame as lh_frame_batched, replayed from a CUDA graph: the first call
  * (or a call with different probe sizes, tuning or scene) captures the
  * frame's launches into a graph on a private stream; every call copies the
- * per-frame uniforms on `stream` and launches the graph there. */
+ * per-frame uniforms on `stream` and launches the graph there.  With no
+ * probes the default schedule is the per-stage one of lh_frame. */
 lh_status lh_frame_graph(lh_ctx* ctx, const Uniforms* host_uniforms,
                          const Uniforms* probe_uniforms, uint32_t n_probes,
                          void* stream, lh_frame_out* out);
@@ -216,7 +217,7 @@ lh_status lh_read_status(lh_ctx* ctx, lh_device_status* out);
 /* Launch-shape knobs of the raster and cull kernels (set by the autotuner,
  * lighthugger_gb300/autotune.py) and the launch schedule.  Results never
  * depend on them. */
-#define LH_SCHEDULE_DEFAULT 0    /* lh_frame: per stage; lh_frame_batched: persistent */
+#define LH_SCHEDULE_DEFAULT 0    /* per stage; persistent for frames with probe views */
 #define LH_SCHEDULE_PER_STAGE 1  /* one launch per stage, each over all views of a kind */
 #define LH_SCHEDULE_PERSISTENT 2 /* cull + raster of all views in one cooperative launch */
 #define LH_SCHEDULE_PER_VIEW 3   /* each view's cull and raster launched on its own (the reference's per-cascade loop) */
@@ -260,11 +261,12 @@ lh_status lh_cull_instances_noalloc(const Instance* d_instances, uint32_t n_inst
                                     const Uniforms* host_uniforms, uint8_t* d_sector, uint32_t capacity,
                                     uint32_t* d_flags, void* stream);
 
-/* lh_frame followed by a copy of the HDR image (width * height pixels of 16
- * bytes, 8 with LH_CONFIG_HDR_RGBA16F) to
- * `host_hdr`, pipelined: the copy runs on a stream of the context after the
- * frame's resolve, and the next frame's culling and rasterisation run while
- * it lands (that frame's resolve waits for it).  Returns once both are
+/* The plain frame (as lh_frame) followed by a copy of the HDR image (width *
+ * height pixels of 16 bytes, 8 with LH_CONFIG_HDR_RGBA16F) to `host_hdr`,
+ * pipelined: the frame up to the resolve is replayed from the context's CUDA
+ * graph, the resolve is launched once the previous call's copy has landed,
+ * and the copy runs on a stream of the context after it -- so the next
+ * frame's culling and rasterisation run while it lands.  Returns once both are
  * enqueued and the PREVIOUS call's copy has landed, so callers alternate two
  * host buffers (pinned for an asynchronous copy): after call i returns, the
  * buffer of call i - 1 holds its frame.  lh_readback_wait waits for the last

@@ -93,10 +93,11 @@ struct lh_ctx {
     cudaStream_t capture_stream = nullptr;
     bool capturing = false;
     GraphBackward graph_backward{};
+    bool graph_until_resolve = false;
     float4* d_lut_standin = nullptr;  // identity 48^3 LUT for lh_display_transform
     // 2D tensor map of d_vis for the TMA-staged resolve (false: rows are not
     // 16-byte aligned or the driver lacks the encoder)
-    alignas(64) CUtensorMap vis_map;
+    CUtensorMap vis_map;  // the type carries its own (TMA) alignment
     bool vis_map_ok = false;
     // pipelined HDR readback (lh_frame_readback): copies on their own
     // stream; a frame's resolve waits for the previous copy of d_hdr
@@ -311,6 +312,8 @@ lh_status upload_frame_constants(lh_ctx* c, const Uniforms* u, const Uniforms* p
 
 // The frame's kernels, all stream ordered (capturable).  `batched` selects
 // the default schedule of lh_frame_batched.
+// `batched`: a frame with probe views (a plain frame takes the per-stage
+// default even through the batched entry points).
 uint32_t frame_schedule(const lh_ctx* c, bool batched) {
     uint32_t schedule = c->tuning.schedule;
     if (schedule == LH_SCHEDULE_DEFAULT) schedule = batched ? LH_SCHEDULE_PERSISTENT : LH_SCHEDULE_PER_STAGE;
@@ -320,12 +323,13 @@ uint32_t frame_schedule(const lh_ctx* c, bool batched) {
 
 // `start` (schedules with a clear launch only): the uniforms, constants and
 // scratch reset travel with the clear kernel instead of copies and a memset.
+// `with_resolve` false: everything up to the resolve (the caller launches it).
 lh_status enqueue_frame(lh_ctx* c, uint32_t n_probes, uint32_t n_instances, bool batched, cudaStream_t s,
-                        const FrameStart* start = nullptr) {
+                        const FrameStart* start = nullptr, bool with_resolve = true) {
     const uint32_t n_persp = 1 + n_probes, n_views = n_persp + 4;
     FrameDev f = frame_dev(c, n_views, n_instances);
     const lh_tuning& t = c->tuning;
-    const uint32_t schedule = frame_schedule(c, batched);
+    const uint32_t schedule = frame_schedule(c, batched && n_probes > 0);
     if (start && schedule == LH_SCHEDULE_PERSISTENT) return fail(c, LH_ERR_CUDA, "frame start without a clear launch");
     const bool prof = c->profiling && !c->capturing;
     uint32_t stage = 0;
@@ -382,9 +386,11 @@ lh_status enqueue_frame(lh_ctx* c, uint32_t n_probes, uint32_t n_instances, bool
     }
     // lighting resolve of the main view (after the last pipelined readback
     // of the image it overwrites; a captured graph waits as a whole instead)
-    if (e == cudaSuccess && !c->capturing) e = wait_readback(c, s);
-    if (e == cudaSuccess)
-        e = mark(launch_resolve(f, c->cfg.width, c->cfg.height, c->vis_map_ok ? &c->vis_map : nullptr, s, c->sms));
+    if (with_resolve) {
+        if (e == cudaSuccess && !c->capturing) e = wait_readback(c, s);
+        if (e == cudaSuccess)
+            e = mark(launch_resolve(f, c->cfg.width, c->cfg.height, c->vis_map_ok ? &c->vis_map : nullptr, s, c->sms));
+    }
     if (e != cudaSuccess) return cuda_fail(c, e, "frame launch");
     return LH_OK;
 }
@@ -582,6 +588,10 @@ lh_status lh_set_scene(lh_ctx* c, const Instance* d_instances, uint32_t n, const
 
 static lh_status frame_impl(lh_ctx* c, const Uniforms* u, const Uniforms* probes, uint32_t n_probes, void* stream,
                             lh_frame_out* out, bool batched);
+namespace {
+lh_status frame_graph_impl(lh_ctx* c, const Uniforms* u, const Uniforms* probes, uint32_t n_probes,
+                           const GraphBackward* bw, void* stream, lh_frame_out* out, bool until_resolve = false);
+}  // namespace
 
 lh_status lh_frame(lh_ctx* c, const Uniforms* u, void* stream, lh_frame_out* out) {
     return frame_impl(c, u, nullptr, 0, stream, out, false);
@@ -591,7 +601,11 @@ lh_status lh_frame_readback(lh_ctx* c, const Uniforms* u, void* host_hdr, void* 
     lh_status st = check_ctx(c);
     if (st != LH_OK) return st;
     if (!host_hdr) return fail(c, LH_ERR_INVALID_ARGUMENT, "host_hdr is NULL");
-    if ((st = frame_impl(c, u, nullptr, 0, stream, out, false)) != LH_OK) return st;
+    // replayed from the context's graph (up to the resolve) unless stage
+    // timing is on, which needs the launches
+    st = c->profiling ? frame_impl(c, u, nullptr, 0, stream, out, false)
+                      : frame_graph_impl(c, u, nullptr, 0, nullptr, stream, out, true);
+    if (st != LH_OK) return st;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     const uint32_t k = c->readbacks & 1u;
     const size_t bytes = (size_t)c->cfg.width * c->cfg.height * hdr_pixel_bytes(c->cfg);
@@ -642,7 +656,7 @@ static lh_status frame_impl(lh_ctx* c, const Uniforms* u, const Uniforms* probes
         if ((st = prepare_views(c, probes, n_probes)) != LH_OK) return st;
     }
     uint32_t n_inst = std::min(u->num_instances, c->n_instances);
-    if (n_probes == 0 && frame_schedule(c, batched) != LH_SCHEDULE_PERSISTENT) {
+    if (n_probes == 0 && frame_schedule(c, false) != LH_SCHEDULE_PERSISTENT) {
         // one main view: its uniforms ride on the clear launch
         FrameStart start;
         std::memset(&start, 0, sizeof(start));
@@ -665,8 +679,12 @@ namespace {
 
 // Batched frame replayed from a captured CUDA graph; with `bw` the resolve
 // adjoint is captured into the same graph after the frame.
+// `until_resolve` (plain frames only): the graph holds the frame up to the
+// resolve, which is launched after it once the last pipelined readback of
+// the image has landed -- so that readback overlaps the graph's culls and
+// rasterisation instead of holding the whole graph back.
 lh_status frame_graph_impl(lh_ctx* c, const Uniforms* u, const Uniforms* probes, uint32_t n_probes,
-                           const GraphBackward* bw, void* stream, lh_frame_out* out) {
+                           const GraphBackward* bw, void* stream, lh_frame_out* out, bool until_resolve) {
     lh_status st = check_ctx(c);
     if (st != LH_OK) return st;
     if (!u) return fail(c, LH_ERR_INVALID_ARGUMENT, "uniforms is NULL");
@@ -694,8 +712,9 @@ lh_status frame_graph_impl(lh_ctx* c, const Uniforms* u, const Uniforms* probes,
     const GraphBackward none{};
     const GraphBackward& want = bw ? *bw : none;
     const bool backward_changed = std::memcmp(&c->graph_backward, &want, sizeof(GraphBackward)) != 0;
+    if (until_resolve && (n_probes || bw)) return fail(c, LH_ERR_INVALID_ARGUMENT, "readback graph of a plain frame only");
     if (!c->graph_exec || c->graph_probes != n_probes || c->graph_instances != n_inst || tuning_changed ||
-        backward_changed) {
+        backward_changed || c->graph_until_resolve != until_resolve) {
         if (c->graph_exec) {
             cudaGraphExecDestroy(c->graph_exec);
             c->graph_exec = nullptr;
@@ -707,7 +726,7 @@ lh_status frame_graph_impl(lh_ctx* c, const Uniforms* u, const Uniforms* probes,
         e = cudaStreamBeginCapture(c->capture_stream, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) return cuda_fail(c, e, "begin capture");
         c->capturing = true;
-        st = enqueue_frame(c, n_probes, n_inst, true, c->capture_stream);
+        st = enqueue_frame(c, n_probes, n_inst, true, c->capture_stream, nullptr, !until_resolve);
         if (st == LH_OK && bw) {
             const FrameDev f = frame_dev(c, 5 + n_probes, n_inst);
             cudaError_t eb = launch_resolve_backward(f, c->cfg.width, c->cfg.height,
@@ -730,10 +749,20 @@ lh_status frame_graph_impl(lh_ctx* c, const Uniforms* u, const Uniforms* probes,
         c->graph_instances = n_inst;
         c->graph_tuning = c->tuning;
         c->graph_backward = want;
+        c->graph_until_resolve = until_resolve;
     }
     if ((st = upload_frame_constants(c, u, probes, n_probes, s)) != LH_OK) return st;
-    e = wait_readback(c, s);
-    if (e == cudaSuccess) e = cudaGraphLaunch(c->graph_exec, s);
+    if (until_resolve) {
+        e = cudaGraphLaunch(c->graph_exec, s);
+        if (e == cudaSuccess) e = wait_readback(c, s);
+        if (e == cudaSuccess) {
+            const FrameDev f = frame_dev(c, 5, n_inst);
+            e = launch_resolve(f, c->cfg.width, c->cfg.height, c->vis_map_ok ? &c->vis_map : nullptr, s, c->sms);
+        }
+    } else {
+        e = wait_readback(c, s);
+        if (e == cudaSuccess) e = cudaGraphLaunch(c->graph_exec, s);
+    }
     if (e != cudaSuccess) return cuda_fail(c, e, "graph launch");
     c->last_stream = s;
     if (out) fill_out(c, out);

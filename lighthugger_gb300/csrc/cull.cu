@@ -6,13 +6,22 @@
 namespace lh {
 namespace {
 
-// grid = (tiles per view, n_views)
+// grid = (tiles per view, n_views).  Also zeroes the claim word of the
+// meshlet cull that follows in the stream (nothing here reads it).
 __global__ void __launch_bounds__(kInstTile) k_cull_instances(FrameDev f, uint32_t view_begin) {
+    if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) f.status[kStMlClaim] = 0u;
     phase_cull_instances_tile(f, view_begin + blockIdx.y, gridDim.x);
 }
 
-// persistent over (view, tile) claims of views [view_begin, view_begin + n_views)
+// persistent over (view, tile) claims of views [view_begin, view_begin + n_views).
+// Also zeroes the raster words of the raster launches that follow (clip
+// count, claims, reduce counter, big-triangle counter; nothing here reads
+// them).
 __global__ void __launch_bounds__(kMlThreads) k_cull_meshlets(FrameDev f, uint32_t view_begin, uint32_t n_views) {
+    if (blockIdx.x == 0 && threadIdx.x < kStWords) {
+        const uint32_t w = threadIdx.x;
+        if (w >= kStClipCount && w <= kStRasterClaimAlpha && w != kStMlClaim && w != kStBarrier) f.status[w] = 0u;
+    }
     phase_cull_meshlets(f, view_begin, n_views, &f.status[kStMlClaim]);
 }
 
@@ -36,8 +45,7 @@ cudaError_t launch_cull_instances(const FrameDev& f, uint32_t view_begin, uint32
 cudaError_t launch_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint32_t n_views, uint32_t blocks,
                                  cudaStream_t s) {
     if (n_views == 0) return cudaSuccess;
-    cudaError_t e = cudaMemsetAsync(&f.status[kStMlClaim], 0, sizeof(uint32_t), s);
-    if (e != cudaSuccess) return e;
+    // the claim word was zeroed by the frame start or the instance cull
     k_cull_meshlets<<<blocks, kMlThreads, 0, s>>>(f, view_begin, n_views);
     return cudaGetLastError();
 }

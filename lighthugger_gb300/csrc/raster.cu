@@ -44,10 +44,8 @@ cudaError_t launch_raster_kind(const FrameDev& f, uint32_t view_begin, uint32_t 
     if (n_views == 0) return cudaSuccess;
     if (n_views > kMaxViews) return cudaErrorInvalidValue;
     RasterTune tune{small_px, medium_px, raster_batch};
-    // raster words: clip count, claims, reduce counter, packed big-triangle word
-    cudaError_t e =
-        cudaMemsetAsync(f.status + kStClipCount, 0, sizeof(uint32_t) * (kStRasterClaimAlpha + 1 - kStClipCount), s);
-    if (e != cudaSuccess) return e;
+    // the raster words (clip count, claims, reduce counter, packed
+    // big-triangle word) were zeroed by the meshlet cull launched before
     if (kind == kViewVisibility) {
         k_raster<0><<<sms * LH_RASTER_MIN_BLOCKS, kRasterWarps * 32, 0, s>>>(f, view_begin, n_views, tune);
         k_raster_alpha<0><<<sms * 3, kRasterWarps * 32, 0, s>>>(f, view_begin, n_views, tune);
