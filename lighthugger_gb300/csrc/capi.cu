@@ -32,6 +32,8 @@ struct Alloc {
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+constexpr size_t kConstBytes = 64;  // frame constants ahead of the Uniforms (device and staging)
+
 }  // namespace
 
 struct lh_ctx {
@@ -299,12 +301,13 @@ lh_status upload_frame_constants(lh_ctx* c, const Uniforms* u, const Uniforms* p
     uint32_t slot = c->frame_index++ & 1u;
     cudaError_t e = cudaEventSynchronize(c->staging_done[slot]);
     if (e != cudaSuccess) return cuda_fail(c, e, "staging event");
+    // staging and device share one layout: 64 bytes of frame constants, then
+    // the views' Uniforms -- one copy per frame
     uint8_t* h = c->h_staging[slot];
-    float* consts = reinterpret_cast<float*>(h + sizeof(Uniforms) * (1 + c->cfg.max_probes));
-    fill_frame_constants(c, u, probes, n_probes, reinterpret_cast<Uniforms*>(h), consts);
-    size_t ubytes = sizeof(Uniforms) * (1 + n_probes);
-    e = cudaMemcpyAsync(c->d_uniforms, h, ubytes, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_consts, consts, 2 * sizeof(float), cudaMemcpyHostToDevice, s);
+    fill_frame_constants(c, u, probes, n_probes, reinterpret_cast<Uniforms*>(h + kConstBytes),
+                         reinterpret_cast<float*>(h));
+    const size_t bytes = kConstBytes + sizeof(Uniforms) * (1 + n_probes);
+    e = cudaMemcpyAsync(c->d_consts, h, bytes, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaEventRecord(c->staging_done[slot], s);
     if (e != cudaSuccess) return cuda_fail(c, e, "upload uniforms");
     return LH_OK;
@@ -470,8 +473,12 @@ lh_status lh_create(const lh_config* config, lh_ctx** out) {
     c->sector_bytes = align_up(8 + 8 * (size_t)cfg.max_instances, 16);
     c->draw_bytes = align_up(8 + 16 * 2 * (size_t)cfg.max_draws, 16);
     const size_t W = cfg.width, H = cfg.height, S = cfg.shadow_size;
-    if (e == cudaSuccess) e = dalloc(c, &c->d_uniforms, sizeof(Uniforms) * (1 + cfg.max_probes));
-    if (e == cudaSuccess) e = dalloc(c, &c->d_consts, 64);
+    uint8_t* frame_block = nullptr;  // kConstBytes of constants, then the Uniforms
+    if (e == cudaSuccess) e = dalloc(c, &frame_block, kConstBytes + sizeof(Uniforms) * (1 + cfg.max_probes));
+    if (e == cudaSuccess) {
+        c->d_consts = reinterpret_cast<float*>(frame_block);
+        c->d_uniforms = reinterpret_cast<Uniforms*>(frame_block + kConstBytes);
+    }
     if (e == cudaSuccess) e = dalloc(c, &c->d_srgb, 256 * sizeof(float));
     if (e == cudaSuccess) e = dalloc(c, &c->d_misc, sizeof(MiscStorage));
     if (e == cudaSuccess) e = dalloc(c, &c->d_sectors, c->sector_bytes * c->max_views);
@@ -495,7 +502,7 @@ lh_status lh_create(const lh_config* config, lh_ctx** out) {
     }
     if (e == cudaSuccess) e = cudaMemset(c->d_misc, 0, sizeof(MiscStorage));
     if (e == cudaSuccess) c->vis_map_ok = encode_vis_map(c);
-    c->staging_bytes = sizeof(Uniforms) * (1 + cfg.max_probes) + 64;
+    c->staging_bytes = kConstBytes + sizeof(Uniforms) * (1 + cfg.max_probes);
     for (int i = 0; i < 2 && e == cudaSuccess; i++) {
         e = cudaMallocHost(reinterpret_cast<void**>(&c->h_staging[i]), c->staging_bytes);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->staging_done[i], cudaEventDisableTiming);
