@@ -61,6 +61,16 @@ typedef struct lh_scene_desc {
 /* Build config `config_id` (1..5) with `seed`; params may be NULL. */
 lh_status lh_scene_create(uint32_t config_id, uint64_t seed, const lh_scene_params* params,
                           lh_scene** out);
+/* A scene of one caller mesh (a triangle list) drawn by n_instances
+ * instances: meshletised like the synthetic meshes (fp32 attributes, 32-bit
+ * indices), one untextured material, the camera `uniforms` (address fields
+ * ignored; num_instances set).  positions: float[3] per vertex, finite;
+ * normals: float[3] per vertex or NULL (area-weighted vertex normals); uvs:
+ * float[2] per vertex or NULL (zero); indices: 3 per triangle, each below
+ * n_vertices; transforms: one lh_mat4 (column major) per instance. */
+lh_status lh_scene_from_mesh(const float* positions, const float* normals, const float* uvs, uint32_t n_vertices,
+                             const uint32_t* indices, uint32_t n_triangles, const lh_mat4* transforms,
+                             uint32_t n_instances, const Uniforms* uniforms, lh_scene** out);
 lh_status lh_scene_describe(const lh_scene* scene, lh_scene_desc* out);
 /* Copy meshes, instances and textures to `device`; patch device addresses. */
 lh_status lh_scene_upload(lh_scene* scene, int device);

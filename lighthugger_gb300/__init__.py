@@ -137,6 +137,7 @@ def lib():
     L.lh_frame_batched.argtypes = [P, P, P, C.c_uint32, P, C.POINTER(FrameOut)]
     L.lh_frame_graph.argtypes = [P, P, P, C.c_uint32, P, C.POINTER(FrameOut)]
     L.lh_frame_readback.argtypes = [P, P, P, P, C.POINTER(FrameOut)]
+    L.lh_scene_from_mesh.argtypes = [P, P, P, C.c_uint32, P, C.c_uint32, P, C.c_uint32, P, C.POINTER(P)]
     L.lh_readback_wait.argtypes = [P]
     L.lh_get_outputs.argtypes = [P, C.POINTER(FrameOut)]
     L.lh_read_status.argtypes = [P, C.POINTER(DeviceStatus)]
@@ -195,6 +196,29 @@ class Scene:
         self.handle = h
         self.params = params
         self._describe()
+
+    @classmethod
+    def from_mesh(cls, positions, indices, transforms, uniforms, normals=None, uvs=None):
+        """A scene of one caller mesh (lh_scene_from_mesh): positions float
+        [n, 3], indices [m, 3], transforms [k, 4, 4] (row-major numpy, applied
+        to column vectors), camera Uniforms."""
+        pos = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 3)
+        idx = np.ascontiguousarray(indices, dtype=np.uint32).reshape(-1, 3)
+        # lh_mat4 is column major: the transpose of the row-major matrix
+        tr = np.ascontiguousarray(np.transpose(np.asarray(transforms, dtype=np.float32).reshape(-1, 4, 4), (0, 2, 1)))
+        nrm = None if normals is None else np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3)
+        uv = None if uvs is None else np.ascontiguousarray(uvs, dtype=np.float32).reshape(-1, 2)
+        ptr = lambda a: None if a is None else a.ctypes.data
+        h = C.c_void_p()
+        _check(lib().lh_scene_from_mesh(ptr(pos), ptr(nrm), ptr(uv), len(pos), ptr(idx), len(idx), ptr(tr), len(tr),
+                                        C.byref(uniforms), C.byref(h)), "lh_scene_from_mesh")
+        self = cls.__new__(cls)
+        self.config_id = 0
+        self.seed = 0
+        self.handle = h
+        self.params = {}
+        self._describe()
+        return self
 
     def _describe(self):
         d = SceneDesc()

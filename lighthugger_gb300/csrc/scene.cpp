@@ -942,6 +942,80 @@ lh_status lh_scene_create(uint32_t config_id, uint64_t seed, const lh_scene_para
     return LH_OK;
 }
 
+lh_status lh_scene_from_mesh(const float* positions, const float* normals, const float* uvs, uint32_t n_vertices,
+                             const uint32_t* indices, uint32_t n_triangles, const lh_mat4* transforms,
+                             uint32_t n_instances, const Uniforms* uniforms, lh_scene** out) {
+    if (!out || !positions || !indices || !transforms || !uniforms || n_vertices == 0 || n_triangles == 0 ||
+        n_instances == 0 || uniforms->window_size.x == 0 || uniforms->window_size.y == 0)
+        return LH_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    for (uint64_t i = 0; i < (uint64_t)n_triangles * 3; i++)
+        if (indices[i] >= n_vertices) return LH_ERR_INVALID_ARGUMENT;
+    for (uint64_t i = 0; i < (uint64_t)n_vertices * 3; i++)
+        if (!std::isfinite(positions[i])) return LH_ERR_INVALID_ARGUMENT;
+    lh_scene* s = new (std::nothrow) lh_scene();
+    if (!s) return LH_ERR_OUT_OF_MEMORY;
+    try {
+        RawMesh raw;
+        raw.pos.resize(n_vertices);
+        raw.u.assign(n_vertices, 0.0);
+        raw.v.assign(n_vertices, 0.0);
+        for (uint32_t i = 0; i < n_vertices; i++) {
+            raw.pos[i] = V3{positions[3 * i], positions[3 * i + 1], positions[3 * i + 2]};
+            if (uvs) {
+                raw.u[i] = uvs[2 * i];
+                raw.v[i] = uvs[2 * i + 1];
+            }
+        }
+        raw.tris.assign(indices, indices + (size_t)n_triangles * 3);
+        if (normals) {
+            raw.nrm.resize(n_vertices);
+            for (uint32_t i = 0; i < n_vertices; i++) {
+                V3 n = norm(V3{normals[3 * i], normals[3 * i + 1], normals[3 * i + 2]});
+                raw.nrm[i] = len(n) > 0 ? n : V3{0, 1, 0};
+            }
+        } else {
+            compute_vertex_normals(raw);
+        }
+        s->config_id = 0;
+        s->seed = 0;
+        s->width = uniforms->window_size.x;
+        s->height = uniforms->window_size.y;
+        s->meshes.push_back(build_mesh(raw, false));
+        if (s->meshes[0].meshlets.size() > 65535) {
+            delete s;
+            return LH_ERR_CAPACITY;  // num_meshlets is u16
+        }
+        // one untextured material: light grey base colour, roughness 0.5
+        s->textures.push_back(constant_texture(0.8, 0.8, 0.8, true));
+        s->textures.push_back(constant_texture(1.0, 0.5, 0.0, false));
+        Material m;
+        m.base_tex = 0;
+        m.mr_tex = 1;
+        m.normal_tex = (uint16_t)UNUSED_TEXTURE_INDEX;
+        m.factor[0] = m.factor[1] = m.factor[2] = 1.0f;
+        m.alpha_clip = false;
+        s->materials.push_back(m);
+        std::vector<int64_t> cache(1, -1);
+        const uint32_t info = info_for(s, 0, 0, cache);
+        for (uint32_t i = 0; i < n_instances; i++) {
+            Instance inst;
+            std::memset(&inst, 0, sizeof(inst));
+            make_instance(inst, mul(from_f(transforms[i]), s->meshes[0].dequant), false);
+            s->host_instances.push_back(inst);
+            s->instance_info.push_back(info);
+        }
+        s->uniforms = *uniforms;
+        s->uniforms.num_instances = n_instances;
+    } catch (...) {
+        delete s;
+        return LH_ERR_OUT_OF_MEMORY;
+    }
+    finish_infos(s);
+    *out = s;
+    return LH_OK;
+}
+
 lh_status lh_scene_describe(const lh_scene* s, lh_scene_desc* d) {
     if (!s || !d) return LH_ERR_INVALID_ARGUMENT;
     std::memset(d, 0, sizeof(*d));

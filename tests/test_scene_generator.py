@@ -90,3 +90,27 @@ def test_uniforms_projection(native):
     PV = f["combined_perspective_view"].T.astype(np.float64)
     inv = f["inv_perspective_view"].T.astype(np.float64)
     assert np.allclose(PV @ inv, np.eye(4), atol=1e-4)
+
+
+def test_scene_from_mesh_builds_and_validates(native):
+    """lh_scene_from_mesh: a caller mesh is meshletised (every triangle lands
+    in one meshlet, <= 64 vertices and <= 124 triangles each) and bad input
+    is refused."""
+    lh = native
+    rng = np.random.default_rng(3)
+    pos = rng.uniform(-1, 1, (500, 3)).astype(np.float32)
+    tris = rng.integers(0, 500, (700, 3)).astype(np.uint32)
+    u = lh.make_uniforms((0.0, 0.0, -3.0), 1.5707963, 0.0, 60.0, 320, 200, 2)
+    s = lh.Scene.from_mesh(pos, tris, [np.eye(4), np.eye(4)], u)
+    d = s.desc
+    assert (d.n_instances, d.n_meshes, d.width, d.height) == (2, 1, 320, 200)
+    assert d.total_triangles == 2 * 700
+    assert 700 / 124 <= d.total_meshlets / 2 <= 700
+    bad = tris.copy()
+    bad[5, 1] = 500  # index out of range
+    with pytest.raises(lh.LHError):
+        lh.Scene.from_mesh(pos, bad, [np.eye(4)], u)
+    nan = pos.copy()
+    nan[3, 0] = np.nan
+    with pytest.raises(lh.LHError):
+        lh.Scene.from_mesh(nan, tris, [np.eye(4)], u)
