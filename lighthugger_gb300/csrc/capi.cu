@@ -50,6 +50,7 @@ struct lh_ctx {
     uint32_t* d_status = nullptr;
     uint8_t* d_sectors = nullptr;
     MeshletReference* d_refs = nullptr;
+    RasterDraw* d_rdraws = nullptr;  // the raster's per-slot draw records
     uint8_t* d_draws = nullptr;
     uint64_t* d_vis = nullptr;
     float* d_shadow = nullptr;
@@ -220,6 +221,7 @@ void build_views(lh_ctx* c, uint32_t n_probes, const Uniforms* probe_uniforms) {
         }
         vw.sector = c->d_sectors + v * c->sector_bytes;
         vw.refs = c->d_refs + (size_t)v * 2 * cfg.max_draws;
+        vw.rdraws = c->d_rdraws + (size_t)v * 2 * cfg.max_draws;
         vw.draws = c->d_draws + v * c->draw_bytes;
         vw.section_base = v * 2 * cfg.max_draws;
         uint8_t* r = c->d_reset + kStWords * 4 + v * per_view;
@@ -483,6 +485,7 @@ lh_status lh_create(const lh_config* config, lh_ctx** out) {
     if (e == cudaSuccess) e = dalloc(c, &c->d_misc, sizeof(MiscStorage));
     if (e == cudaSuccess) e = dalloc(c, &c->d_sectors, c->sector_bytes * c->max_views);
     if (e == cudaSuccess) e = dalloc(c, &c->d_refs, sizeof(MeshletReference) * 2 * (size_t)cfg.max_draws * c->max_views);
+    if (e == cudaSuccess) e = dalloc(c, &c->d_rdraws, sizeof(RasterDraw) * 2 * (size_t)cfg.max_draws * c->max_views);
     if (e == cudaSuccess) e = dalloc(c, &c->d_draws, c->draw_bytes * c->max_views);
     if (e == cudaSuccess) e = dalloc(c, &c->d_vis, W * H * 8);
     if (e == cudaSuccess) e = dalloc(c, &c->d_shadow, 4 * S * S * 4);

@@ -67,6 +67,26 @@ __device__ __noinline__ uint64_t lookback(uint64_t* status, uint32_t tile, uint6
 }
 
 
+// The raster's record of a visible meshlet (the scene records it reads were
+// loaded moments earlier by the same thread, so these loads mostly hit).
+__device__ __forceinline__ RasterDraw raster_draw_of(const FrameDev& f, MeshletReference ref) {
+    const Instance* inst = f.instances + ref.instance_index;
+    const unsigned long long* mw = reinterpret_cast<const unsigned long long*>(__ldg(&inst->mesh_info_address));
+    const uint64_t positions = __ldg(mw + 0), indices = __ldg(mw + 1), micro = __ldg(mw + 4), meshlets = __ldg(mw + 5);
+    const uint32_t mflags = (uint32_t)((__ldg(mw + 6) >> 16) & 0xFFu);
+    // Meshlet words at byte 44: triangle_offset, index_offset, counts
+    const uint32_t* ml = reinterpret_cast<const uint32_t*>(reinterpret_cast<const Meshlet*>(meshlets) + ref.meshlet_index);
+    const uint32_t tri_off = __ldg(ml + 11), idx_off = __ldg(ml + 12), counts = __ldg(ml + 13);
+    RasterDraw r;
+    r.positions = positions;
+    r.indices = indices + (uint64_t)idx_off * ((mflags & MESH_INFO_FLAGS_32_BIT_INDICES) ? 4u : 2u);
+    r.micro = micro + tri_off;
+    r.instance = ref.instance_index;
+    // counts = triangle_count | index_count << 8
+    r.bits = ((counts >> 8) & 0xFFu) | ((counts & 0xFFu) << 8) | (mflags << 16);
+    return r;
+}
+
 // Fields of a MeshInfo the cull needs (loaded as aligned 8-byte words).
 struct MeshInfoCull {
     uint64_t meshlets;
@@ -410,6 +430,7 @@ __device__ void phase_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint
             dc.firstInstance = vw->section_base + slot;
             draws[slot] = dc;
             out_refs[slot] = refs[k];
+            vw->rdraws[slot] = raster_draw_of(f, refs[k]);
         }
         __syncthreads();
     }

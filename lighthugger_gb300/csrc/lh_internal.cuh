@@ -28,6 +28,22 @@ constexpr uint64_t kPayloadMask = (1ull << 62) - 1;
 
 enum ViewKind : uint32_t { kViewVisibility = 0, kViewShadow = 1 };
 
+// What the raster needs of one visible meshlet, with the address arithmetic
+// done: written by the meshlet cull at the meshlet's draw slot, beside its
+// MeshletReference.  The raster then reaches the vertices in three dependent
+// loads (this record -> index words -> positions) where the reference chain
+// takes six (MeshletReference -> Instance -> MeshInfo -> Meshlet -> index
+// words -> positions; src/shaders/rasterization.glsl:12-37 and
+// util.glsl:3-20 walk that chain per vertex).
+struct __align__(16) RasterDraw {
+    uint64_t positions;  // MeshInfo.positions
+    uint64_t indices;    // MeshInfo.indices + Meshlet.index_offset elements
+    uint64_t micro;      // MeshInfo.micro_indices + Meshlet.triangle_offset
+    uint32_t instance;   // MeshletReference.instance_index
+    uint32_t bits;       // index_count | triangle_count << 8 | MeshInfo.flags << 16
+};
+static_assert(sizeof(RasterDraw) == 32, "RasterDraw layout");
+
 struct ViewDev {
     uint32_t kind;
     uint32_t cascade;
@@ -35,6 +51,7 @@ struct ViewDev {
     const Uniforms* uniforms;   // perspective views: their own; cascades: the main view's
     uint8_t* sector;            // prefix sector: u64 counter + PrefixSumValue[max_instances]
     MeshletReference* refs;     // 2*max_draws
+    RasterDraw* rdraws;         // 2*max_draws, at the same slots as refs
     uint8_t* draws;             // u32 num_opaque, u32 num_alpha_clip, DrawIndirectCommand[2*max_draws]
     void* target;               // u64 visibility or u32 depth
     uint64_t* inst_status;      // per-frame zeroed look-back words, instance cull

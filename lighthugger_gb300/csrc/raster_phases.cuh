@@ -560,15 +560,20 @@ __device__ void phase_raster(const FrameDev& f, uint32_t view_begin, uint32_t n_
     const uint32_t gwarp = blockIdx.x * (blockDim.x >> 5) + warp;
     const uint32_t dyn_base = warps_total * batch;
     uint32_t unit = min(gwarp * batch, units), unit_end = min(gwarp * batch + batch, units);
+    // Each claim is issued when the window before it starts, so the atomic's
+    // round trip overlaps that window's work (a warp holds at most one
+    // window it has not started).
+    const bool dynamic = dyn_base < units;
+    uint32_t pending = 0;
+    if (dynamic && lane == 0) pending = atomicAdd(claim_word, batch);
     for (;;) {
         if (unit >= unit_end) {
-            if (dyn_base >= units) break;
-            uint32_t first = 0;
-            if (lane == 0) first = dyn_base + atomicAdd(claim_word, batch);
-            first = __shfl_sync(0xFFFFFFFFu, first, 0);
+            if (!dynamic) break;
+            const uint32_t first = dyn_base + __shfl_sync(0xFFFFFFFFu, pending, 0);
             if (first >= units) break;
             unit = first;
             unit_end = min(first + batch, units);
+            if (lane == 0) pending = atomicAdd(claim_word, batch);
         }
         const uint32_t item = unit / split, part = unit % split;
         unit++;
@@ -578,25 +583,29 @@ __device__ void phase_raster(const FrameDev& f, uint32_t view_begin, uint32_t n_
         const ViewDev* vw = f.views + view;
         const uint32_t local = item - s_prefix[v];
         const uint32_t slot = ALPHA ? md + local : local;
-        const MeshletReference ref = vw->refs[slot];
-        const Instance* inst = f.instances + ref.instance_index;
+        // the slot's draw record (written by the meshlet cull): the index and
+        // micro-index addresses come offset to the meshlet already
+        const RasterDraw rd = vw->rdraws[slot];
+        const Instance* inst = f.instances + rd.instance;
         lh_mat4 transform;
         load_transform(inst, transform);
-        const MeshInfoRaster mi = load_mesh_info_raster(mesh_info_of(inst));
-        MeshletBits mb;
-        load_meshlet(reinterpret_cast<const Meshlet*>(mi.meshlets) + ref.meshlet_index, mb);
+        MeshInfoRaster mi;
+        mi.positions = rd.positions;
+        mi.indices = rd.indices;
+        mi.micro_indices = rd.micro;
+        mi.meshlets = 0;
+        mi.flags = rd.bits >> 16;
         const uint32_t W = vw->width, H = vw->height;
         void* target = vw->target;
         const float hw = (float)W * 0.5f, hh = (float)H * 0.5f;
-        const uint32_t nv = mb.m.index_count, nt = mb.m.triangle_count;
+        const uint32_t nv = rd.bits & 0xFFu, nt = (rd.bits >> 8) & 0xFFu;
         if (nv > MAX_MESHLET_UNIQUE_VERTICES || nt > MAX_MESHLET_TRIANGLES) {
             // beyond the meshletiser limits: malformed, skipped and flagged
             if (lane == 0 && part == 0) atomicOr(&f.status[kStFlags], LH_FLAG_BAD_MESHLET);
             continue;
         }
         if (part * 32u >= nt) continue;  // this quarter holds no triangles
-        const MeshletWork w{view,   slot, part, split, nv,        nt, W, H, target, hw, hh, &s_vp[v],
-                            transform, mi, mb.m.index_offset, mb.m.triangle_offset, inst};
+        const MeshletWork w{view, slot, part, split, nv, nt, W, H, target, hw, hh, &s_vp[v], transform, mi, 0u, 0u, inst};
         raster_meshlet<KIND, ALPHA>(f, w, tune, sv, so, s_micro[warp], ALPHA ? s_av[warp] : nullptr, lane);
     }
 }
