@@ -371,6 +371,7 @@ __global__ void __launch_bounds__(kBwdThreads, LH_BWD_MIN_BLOCKS)
     k_resolve_backward(FrameDev f, const float4* grad, lh_grad_targets t, uint32_t tiles_x, uint32_t n_tiles) {
     __shared__ HotCache cache;
     __shared__ float s_light[kBwdThreads / 32][6];
+    pdl_enter();
     __shared__ __align__(16) FrameMats s_mats;
     const uint32_t tid = threadIdx.y * 32 + threadIdx.x;
     for (uint32_t s = tid; s < kCacheSlots; s += kBwdThreads) {
@@ -525,8 +526,7 @@ cudaError_t launch_resolve_backward(const FrameDev& f, uint32_t width, uint32_t 
     const uint32_t n_tiles = tiles_x * tiles_y;
     if (n_tiles == 0) return cudaSuccess;
     const uint32_t grid = std::min<uint32_t>(n_tiles, (uint32_t)(sms * g_backward_blocks_per_sm));
-    k_resolve_backward<<<grid, dim3(32, kBwdRows), 0, s>>>(f, grad, t, tiles_x, n_tiles);
-    return cudaGetLastError();
+    return launch_pdl(k_resolve_backward, dim3(grid), dim3(32, kBwdRows), s, f, grad, t, tiles_x, n_tiles);
 }
 
 }  // namespace lh

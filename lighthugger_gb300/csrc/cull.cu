@@ -9,6 +9,7 @@ namespace {
 // grid = (tiles per view, n_views).  Also zeroes the claim word of the
 // meshlet cull that follows in the stream (nothing here reads it).
 __global__ void __launch_bounds__(kInstTile) k_cull_instances(FrameDev f, uint32_t view_begin) {
+    pdl_enter();
     if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) f.status[kStMlClaim] = 0u;
     phase_cull_instances_tile(f, view_begin + blockIdx.y, gridDim.x);
 }
@@ -18,6 +19,7 @@ __global__ void __launch_bounds__(kInstTile) k_cull_instances(FrameDev f, uint32
 // count, claims, reduce counter, big-triangle counter; nothing here reads
 // them).
 __global__ void __launch_bounds__(kMlThreads) k_cull_meshlets(FrameDev f, uint32_t view_begin, uint32_t n_views) {
+    pdl_enter();
     if (blockIdx.x == 0 && threadIdx.x < kStWords) {
         const uint32_t w = threadIdx.x;
         if (w >= kStClipCount && w <= kStRasterClaimAlpha && w != kStMlClaim && w != kStBarrier) f.status[w] = 0u;
@@ -38,16 +40,14 @@ __global__ void k_sum_meshlets(const Instance* inst, uint32_t n, unsigned long l
 cudaError_t launch_cull_instances(const FrameDev& f, uint32_t view_begin, uint32_t n_views, cudaStream_t s) {
     if (f.n_instances == 0 || n_views == 0) return cudaSuccess;
     dim3 grid((f.n_instances + kInstTile - 1) / kInstTile, n_views);
-    k_cull_instances<<<grid, kInstTile, 0, s>>>(f, view_begin);
-    return cudaGetLastError();
+    return launch_pdl(k_cull_instances, grid, dim3(kInstTile), s, f, view_begin);
 }
 
 cudaError_t launch_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint32_t n_views, uint32_t blocks,
                                  cudaStream_t s) {
     if (n_views == 0) return cudaSuccess;
     // the claim word was zeroed by the frame start or the instance cull
-    k_cull_meshlets<<<blocks, kMlThreads, 0, s>>>(f, view_begin, n_views);
-    return cudaGetLastError();
+    return launch_pdl(k_cull_meshlets, dim3(blocks), dim3(kMlThreads), s, f, view_begin, n_views);
 }
 
 cudaError_t launch_sum_meshlets(const Instance* instances, uint32_t n, unsigned long long* out, cudaStream_t s) {

@@ -58,6 +58,7 @@ __device__ __forceinline__ uint32_t unorm8(float v) {
 
 // One thread per pixel (blocks of 32 x 8).
 __global__ void __launch_bounds__(256) k_display_transform(FrameDev f, const float4* lut, uchar4* out) {
+    pdl_enter();
     const Uniforms& u = *f.uniforms;
     const uint32_t W = u.window_size.x, H = u.window_size.y;
     const uint32_t x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
@@ -90,8 +91,7 @@ __global__ void __launch_bounds__(256) k_display_transform(FrameDev f, const flo
 cudaError_t launch_display_transform(const FrameDev& f, uint32_t width, uint32_t height, const float4* lut, uchar4* out,
                                      cudaStream_t s) {
     dim3 grid((width + 31) / 32, (height + 7) / 8);
-    k_display_transform<<<grid, dim3(32, 8), 0, s>>>(f, lut, out);
-    return cudaGetLastError();
+    return launch_pdl(k_display_transform, grid, dim3(32, 8), s, f, lut, out);
 }
 
 }  // namespace lh

@@ -18,6 +18,17 @@
 
 namespace lh {
 
+// Programmatic dependent launch.  A frame kernel launched by launch_pdl may
+// be scheduled while the kernel before it in the stream is still finishing;
+// its first statement waits (griddepcontrol.wait) until that kernel has
+// completed and its writes are visible, so nothing is read or written
+// early, and then lets the next kernel of the stream begin launching.  In a
+// kernel launched without the attribute both instructions return at once.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // ------------------------------------------------------------------ vectors
 struct f2 { float x, y; };
 struct f3 { float x, y, z; };

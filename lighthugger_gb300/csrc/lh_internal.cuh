@@ -121,6 +121,28 @@ struct FrameDev {
     const float* srgb_lut;      // 256 entries
 };
 
+// Launch `kernel` with programmatic stream serialisation: its blocks may
+// become resident while the previous kernel of the stream drains, hiding the
+// launch gap between the frame's kernels (the kernel must begin with
+// pdl_enter()).  Build with LH_PDL=0 for plain launches.
+#ifndef LH_PDL
+#define LH_PDL 1
+#endif
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = LH_PDL ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 // Launchers (stream ordered).  Each returns the CUDA error of its launch.
 // What the first kernel of a frame writes before anything reads it, when
 // the host hands it over as a kernel parameter instead of two copies and a

@@ -16,6 +16,7 @@ template <int KIND>
 __global__ void __launch_bounds__(kRasterWarps * 32, LH_RASTER_MIN_BLOCKS) k_raster(FrameDev f, uint32_t view_begin, uint32_t n_views,
                                                                  RasterTune tune) {
     __shared__ RasterSmem sm;
+    pdl_enter();
     phase_raster<KIND, false>(f, view_begin, n_views, tune, &f.status[kStRasterClaim], sm, nullptr);
 }
 
@@ -24,16 +25,19 @@ template <int KIND>
 __global__ void __launch_bounds__(kRasterWarps * 32, 3) k_raster_alpha(FrameDev f, uint32_t view_begin,
                                                                        uint32_t n_views, RasterTune tune) {
     __shared__ RasterSmemAlpha sm;
+    pdl_enter();
     phase_raster<KIND, true>(f, view_begin, n_views, tune, &f.status[kStRasterClaimAlpha], sm, sm.av);
 }
 
 template <int KIND>
 __global__ void __launch_bounds__(128) k_raster_clip(FrameDev f) {
+    pdl_enter();
     phase_raster_clip<KIND>(f, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
 template <int KIND>
 __global__ void __launch_bounds__(256, LH_RASTER_BIG_MIN_BLOCKS) k_raster_big(FrameDev f) {
+    pdl_enter();
     phase_raster_big<KIND>(f);
 }
 
@@ -46,18 +50,20 @@ cudaError_t launch_raster_kind(const FrameDev& f, uint32_t view_begin, uint32_t 
     RasterTune tune{small_px, medium_px, raster_batch};
     // the raster words (clip count, claims, reduce counter, packed
     // big-triangle word) were zeroed by the meshlet cull launched before
+    const dim3 rb(kRasterWarps * 32);
+    cudaError_t e;
     if (kind == kViewVisibility) {
-        k_raster<0><<<sms * LH_RASTER_MIN_BLOCKS, kRasterWarps * 32, 0, s>>>(f, view_begin, n_views, tune);
-        k_raster_alpha<0><<<sms * 3, kRasterWarps * 32, 0, s>>>(f, view_begin, n_views, tune);
-        k_raster_clip<0><<<sms, 128, 0, s>>>(f);
-        k_raster_big<0><<<sms * LH_RASTER_BIG_MIN_BLOCKS, 256, 0, s>>>(f);
+        e = launch_pdl(k_raster<0>, dim3(sms * LH_RASTER_MIN_BLOCKS), rb, s, f, view_begin, n_views, tune);
+        if (e == cudaSuccess) e = launch_pdl(k_raster_alpha<0>, dim3(sms * 3), rb, s, f, view_begin, n_views, tune);
+        if (e == cudaSuccess) e = launch_pdl(k_raster_clip<0>, dim3(sms), dim3(128), s, f);
+        if (e == cudaSuccess) e = launch_pdl(k_raster_big<0>, dim3(sms * LH_RASTER_BIG_MIN_BLOCKS), dim3(256), s, f);
     } else {
-        k_raster<1><<<sms * LH_RASTER_MIN_BLOCKS, kRasterWarps * 32, 0, s>>>(f, view_begin, n_views, tune);
-        k_raster_alpha<1><<<sms * 3, kRasterWarps * 32, 0, s>>>(f, view_begin, n_views, tune);
-        k_raster_clip<1><<<sms, 128, 0, s>>>(f);
-        k_raster_big<1><<<sms * LH_RASTER_BIG_MIN_BLOCKS, 256, 0, s>>>(f);
+        e = launch_pdl(k_raster<1>, dim3(sms * LH_RASTER_MIN_BLOCKS), rb, s, f, view_begin, n_views, tune);
+        if (e == cudaSuccess) e = launch_pdl(k_raster_alpha<1>, dim3(sms * 3), rb, s, f, view_begin, n_views, tune);
+        if (e == cudaSuccess) e = launch_pdl(k_raster_clip<1>, dim3(sms), dim3(128), s, f);
+        if (e == cudaSuccess) e = launch_pdl(k_raster_big<1>, dim3(sms * LH_RASTER_BIG_MIN_BLOCKS), dim3(256), s, f);
     }
-    return cudaGetLastError();
+    return e;
 }
 
 }  // namespace lh

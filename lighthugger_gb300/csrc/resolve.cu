@@ -423,6 +423,7 @@ __global__ void __launch_bounds__(kResolveWarps * 32, LH_RESOLVE_MIN_BLOCKS)
     k_resolve(FrameDev f, const __grid_constant__ CUtensorMap vis_map, uint32_t strips_x, uint32_t n_strips) {
     __shared__ __align__(128) unsigned long long s_vis[kResolveWarps][kResolveStages][kStripCols];
     __shared__ __align__(8) uint64_t s_bar[kResolveWarps][kResolveStages];
+    pdl_enter();
     __shared__ long long s_clock[kResolveWarps][32];
     const uint32_t W = f.uniforms->window_size.x, H = f.uniforms->window_size.y;
     const uint32_t lane = threadIdx.x, warp = threadIdx.y;
@@ -498,6 +499,7 @@ __global__ void __launch_bounds__(kResolveWarps * 32, LH_RESOLVE_MIN_BLOCKS)
 // (nothing in this kernel reads either).
 __global__ void __launch_bounds__(256) k_clear_targets(FrameDev f, const __grid_constant__ FrameStart start,
                                                        uint32_t has_start) {
+    pdl_enter();
     if (has_start && blockIdx.y == 0) {
         const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (uint64_t)gridDim.x * blockDim.x;
         for (uint64_t i = tid; i < start.reset_words; i += stride) start.reset[i] = make_uint4(0u, 0u, 0u, 0u);
@@ -514,6 +516,7 @@ __global__ void __launch_bounds__(256) k_clear_targets(FrameDev f, const __grid_
 
 // Depth reduction; the last block to finish fits the cascades.
 __global__ void __launch_bounds__(256) k_depth_reduce_fit(FrameDev f) {
+    pdl_enter();
     phase_depth_reduce(f, (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, (uint64_t)gridDim.x * blockDim.x);
     __shared__ bool s_last;
     __threadfence();
@@ -556,19 +559,14 @@ cudaError_t launch_linearize_texture(const uchar4* src, float4* dst, size_t n, u
 
 cudaError_t launch_clear_targets(const FrameDev& f, cudaStream_t s, int sms, const FrameStart* start) {
     dim3 grid((unsigned)sms, f.n_views);
-    if (start) {
-        k_clear_targets<<<grid, 256, 0, s>>>(f, *start, 1u);
-    } else {
-        FrameStart none;
-        std::memset(&none, 0, sizeof(none));
-        k_clear_targets<<<grid, 256, 0, s>>>(f, none, 0u);
-    }
-    return cudaGetLastError();
+    if (start) return launch_pdl(k_clear_targets, grid, dim3(256), s, f, *start, 1u);
+    FrameStart none;
+    std::memset(&none, 0, sizeof(none));
+    return launch_pdl(k_clear_targets, grid, dim3(256), s, f, none, 0u);
 }
 
 cudaError_t launch_depth_reduce_fit(const FrameDev& f, cudaStream_t s, int sms) {
-    k_depth_reduce_fit<<<(unsigned)sms * 2, 256, 0, s>>>(f);
-    return cudaGetLastError();
+    return launch_pdl(k_depth_reduce_fit, dim3((unsigned)sms * 2), dim3(256), s, f);
 }
 
 cudaError_t launch_resolve(const FrameDev& f, uint32_t width, uint32_t height, const CUtensorMap* vis_map,
@@ -580,14 +578,10 @@ cudaError_t launch_resolve(const FrameDev& f, uint32_t width, uint32_t height, c
 #ifdef LH_RESOLVE_NO_TMA
     vis_map = nullptr;  // comparison builds: per-thread loads of the visibility words
 #endif
-    if (vis_map) {
-        k_resolve<true><<<grid, dim3(32, kResolveWarps), 0, s>>>(f, *vis_map, strips_x, n_strips);
-    } else {
-        CUtensorMap none;
-        std::memset(&none, 0, sizeof(none));
-        k_resolve<false><<<grid, dim3(32, kResolveWarps), 0, s>>>(f, none, strips_x, n_strips);
-    }
-    return cudaGetLastError();
+    if (vis_map) return launch_pdl(k_resolve<true>, dim3(grid), dim3(32, kResolveWarps), s, f, *vis_map, strips_x, n_strips);
+    CUtensorMap none;
+    std::memset(&none, 0, sizeof(none));
+    return launch_pdl(k_resolve<false>, dim3(grid), dim3(32, kResolveWarps), s, f, none, strips_x, n_strips);
 }
 
 }  // namespace lh
