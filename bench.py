@@ -314,8 +314,8 @@ def run_gpu(args):
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": 560 + 8, "d2h_bytes_per_step": npx * 16,
                 "pipelined": True, "serial_value": e2e_serial_ms},
         # per frame: clear; 2 x (cull instances, cull meshlets, raster opaque,
-        # raster alpha clip, clip, chunks); depth + fit; resolve
-        "gpu_launches": 15 * args.steps,
+        # raster alpha clip, chunks); depth + fit; resolve
+        "gpu_launches": 13 * args.steps,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": RESOLVE_TRAFFIC_C2 if (dom == "resolve" and args.config == 2) else None,

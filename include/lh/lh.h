@@ -117,7 +117,7 @@ typedef struct lh_device_status {
     uint32_t visible_opaque[40];     /* per view: num_opaque */
     uint32_t visible_alpha_clip[40]; /* per view: num_alpha_clip */
     uint32_t big_triangles;          /* triangles sent to the tiled raster path */
-    uint32_t clipped_triangles;      /* triangles sent to the clipper */
+    uint32_t clipped_triangles;      /* triangles clipped (last raster pass) */
 } lh_device_status;
 
 typedef struct lh_ctx lh_ctx;

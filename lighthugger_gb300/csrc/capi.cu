@@ -58,7 +58,6 @@ struct lh_ctx {
     uint64_t* d_probe_vis = nullptr;
     BigTri* d_big = nullptr;
     uint32_t* d_big_base = nullptr;
-    ClipItem* d_clip = nullptr;
     ViewDev* d_views = nullptr;
     lh_texture* d_textures = nullptr;
     uint32_t n_textures = 0;
@@ -253,8 +252,6 @@ FrameDev frame_dev(const lh_ctx* c, uint32_t n_views, uint32_t n_instances) {
     f.big = c->d_big;
     f.big_base = c->d_big_base;
     f.big_cap = c->cfg.max_big_triangles;
-    f.clip = c->d_clip;
-    f.clip_cap = c->cfg.max_big_triangles;
     f.textures = c->d_textures;
     f.n_textures = c->n_textures;
     f.tex_linear = c->d_tex_linear_ptrs;
@@ -493,7 +490,6 @@ lh_status lh_create(const lh_config* config, lh_ctx** out) {
     if (e == cudaSuccess) e = dalloc(c, &c->d_probe_vis, (size_t)std::max(cfg.max_probe_pixels, 32u) * 8);
     if (e == cudaSuccess) e = dalloc(c, &c->d_big, sizeof(BigTri) * (size_t)cfg.max_big_triangles);
     if (e == cudaSuccess) e = dalloc(c, &c->d_big_base, sizeof(uint32_t) * (size_t)cfg.max_big_triangles);
-    if (e == cudaSuccess) e = dalloc(c, &c->d_clip, sizeof(ClipItem) * (size_t)cfg.max_big_triangles);
     if (e == cudaSuccess) e = dalloc(c, &c->d_views, sizeof(ViewDev) * c->max_views);
     if (e == cudaSuccess) {
         float lut[256];

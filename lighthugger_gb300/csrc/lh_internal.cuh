@@ -74,10 +74,6 @@ struct BigTri {
 constexpr int32_t kChunkRows = 16;
 constexpr int32_t kChunkCols = 64;
 
-struct ClipItem {
-    uint32_t view, slot, tri, pad;
-};
-
 // Per-frame scratch words (zeroed at frame start; the raster words again
 // before each raster pass).
 enum StatusWord : uint32_t {
@@ -106,8 +102,6 @@ struct FrameDev {
     BigTri* big;
     uint32_t* big_base;         // first chunk of each big triangle (ascending)
     uint32_t big_cap;
-    ClipItem* clip;
-    uint32_t clip_cap;
     const lh_texture* textures;
     uint32_t n_textures;
     const float4* const* tex_linear;  // per texture: its texels as linear float4 (see launch_linearize_texture)
@@ -166,7 +160,8 @@ cudaError_t launch_cull_instances(const FrameDev& f, uint32_t view_begin, uint32
 cudaError_t launch_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint32_t n_views, uint32_t blocks,
                                  cudaStream_t s);
 // Raster all views [view_begin, view_begin + n_views) of one kind (kViewVisibility
-// or kViewShadow): main kernel, clipper, band kernel.
+// or kViewShadow): the opaque and alpha-clip classes (clipping inline), then
+// the band kernel.
 cudaError_t launch_raster_kind(const FrameDev& f, uint32_t view_begin, uint32_t n_views, int kind, uint32_t small_px,
                                uint32_t medium_px, uint32_t raster_batch, cudaStream_t s, int sms);
 cudaError_t launch_depth_reduce_fit(const FrameDev& f, cudaStream_t s, int sms);

@@ -75,8 +75,6 @@ __global__ void __launch_bounds__(kPersistentThreads, 3) k_frame_persistent(Fram
     phase_raster<0, false>(f, 0, n_persp, tune, &f.status[kStRasterClaim], s_raster, nullptr);
     phase_raster<0, true>(f, 0, n_persp, tune, &f.status[kStRasterClaimAlpha], s_raster, s_raster.av);
     grid_barrier(f, epoch);
-    phase_raster_clip<0>(f, (uint32_t)gtid, (uint32_t)gstride);
-    grid_barrier(f, epoch);
     phase_raster_big<0>(f);
     grid_barrier(f, epoch);
     // depth range of the main view, then the cascade fit
@@ -95,8 +93,6 @@ __global__ void __launch_bounds__(kPersistentThreads, 3) k_frame_persistent(Fram
     grid_barrier(f, epoch);
     phase_raster<1, false>(f, n_persp, 4, tune, &f.status[kStRasterClaim], s_raster, nullptr);
     phase_raster<1, true>(f, n_persp, 4, tune, &f.status[kStRasterClaimAlpha], s_raster, s_raster.av);
-    grid_barrier(f, epoch);
-    phase_raster_clip<1>(f, (uint32_t)gtid, (uint32_t)gstride);
     grid_barrier(f, epoch);
     phase_raster_big<1>(f);
 }

@@ -30,12 +30,6 @@ __global__ void __launch_bounds__(kRasterWarps * 32, 3) k_raster_alpha(FrameDev 
 }
 
 template <int KIND>
-__global__ void __launch_bounds__(128) k_raster_clip(FrameDev f) {
-    pdl_enter();
-    phase_raster_clip<KIND>(f, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
-}
-
-template <int KIND>
 __global__ void __launch_bounds__(256, LH_RASTER_BIG_MIN_BLOCKS) k_raster_big(FrameDev f) {
     pdl_enter();
     phase_raster_big<KIND>(f);
@@ -55,12 +49,10 @@ cudaError_t launch_raster_kind(const FrameDev& f, uint32_t view_begin, uint32_t 
     if (kind == kViewVisibility) {
         e = launch_pdl(k_raster<0>, dim3(sms * LH_RASTER_MIN_BLOCKS), rb, s, f, view_begin, n_views, tune);
         if (e == cudaSuccess) e = launch_pdl(k_raster_alpha<0>, dim3(sms * 3), rb, s, f, view_begin, n_views, tune);
-        if (e == cudaSuccess) e = launch_pdl(k_raster_clip<0>, dim3(sms), dim3(128), s, f);
         if (e == cudaSuccess) e = launch_pdl(k_raster_big<0>, dim3(sms * LH_RASTER_BIG_MIN_BLOCKS), dim3(256), s, f);
     } else {
         e = launch_pdl(k_raster<1>, dim3(sms * LH_RASTER_MIN_BLOCKS), rb, s, f, view_begin, n_views, tune);
         if (e == cudaSuccess) e = launch_pdl(k_raster_alpha<1>, dim3(sms * 3), rb, s, f, view_begin, n_views, tune);
-        if (e == cudaSuccess) e = launch_pdl(k_raster_clip<1>, dim3(sms), dim3(128), s, f);
         if (e == cudaSuccess) e = launch_pdl(k_raster_big<1>, dim3(sms * LH_RASTER_BIG_MIN_BLOCKS), dim3(256), s, f);
     }
     return e;

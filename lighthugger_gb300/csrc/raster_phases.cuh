@@ -19,11 +19,10 @@
 //                 memory; then one lane per triangle does set-up and face
 //                 culling.  Triangles covering <= `small` pixel centres are
 //                 rasterised by their lane, up to `medium` by the whole warp,
-//                 larger ones go to a queue of 16-row bands; triangles that
-//                 need clipping go to the clip queue.
-//  k_raster_clip  one thread per clipped triangle: Sutherland-Hodgman in
-//                 clip space against 0 <= z <= w and the guard band, fan
-//                 triangulation, band queue.
+//                 larger ones go to a queue of 16-row bands.  A triangle
+//                 that needs clipping is clipped by its lane
+//                 (Sutherland-Hodgman in clip space against 0 <= z <= w and
+//                 the guard band, fan triangulation) into the band queue.
 //  k_raster_big   one warp per band.
 // The depth test is an atomicMax of (depth bits << 32 | packed ID) for the
 // visibility buffer and an atomicMin of depth bits for shadow maps, so the
@@ -253,6 +252,93 @@ __device__ void push_big_warp(const FrameDev& f, const TriSetup& t, uint32_t vie
     if (big) store_big(f, t, view, old, n);
 }
 
+// Sutherland-Hodgman against w-z, z, g*w-x, g*w+x, g*w-y, g*w+y >= 0.
+__device__ int clip_polygon(f4* poly, int n) {
+    f4 out[9];
+    for (int plane = 0; plane < 6 && n >= 3; plane++) {
+        int m = 0;
+        for (int i = 0; i < n; i++) {
+            f4 a = poly[i], b = poly[i + 1 < n ? i + 1 : 0];
+            float ga = LH_GUARD_BAND * a.w, gb = LH_GUARD_BAND * b.w;
+            float da, db;
+            switch (plane) {
+                case 0: da = a.w - a.z; db = b.w - b.z; break;
+                case 1: da = a.z; db = b.z; break;
+                case 2: da = ga - a.x; db = gb - b.x; break;
+                case 3: da = ga + a.x; db = gb + b.x; break;
+                case 4: da = ga - a.y; db = gb - b.y; break;
+                default: da = ga + a.y; db = gb + b.y; break;
+            }
+            if (da >= 0.0f) out[m++] = a;
+            if ((da >= 0.0f) != (db >= 0.0f)) {
+                float tt = da / (da - db);
+                out[m++] = f4{a.x + tt * (b.x - a.x), a.y + tt * (b.y - a.y), a.z + tt * (b.z - a.z), a.w + tt * (b.w - a.w)};
+            }
+        }
+        n = m;
+        for (int i = 0; i < n; i++) poly[i] = out[i];
+    }
+    return n;
+}
+
+// Triangle `tri` of the meshlet at draw slot `slot` of view `view`, one of
+// whose vertices lies outside 0 <= z <= w, w > 0 or the guard band: clipped
+// in clip space, fan-triangulated, the pieces appended to the chunk queue.
+// Called by the lane that found it during the raster (rare, so the
+// polygon's stack arrays stay out of the raster's register allocation).
+template <int KIND>
+__device__ __noinline__ void clip_triangle(const FrameDev& f, uint32_t view, uint32_t slot, uint32_t tri) {
+    {
+        const struct { uint32_t view, slot, tri; } it{view, slot, tri};
+        const ViewDev* vw = f.views + it.view;
+        const MeshletReference ref = vw->refs[it.slot];
+        const Instance* inst = f.instances + ref.instance_index;
+        lh_mat4 transform;
+        load_transform(inst, transform);
+        const MeshInfoRaster mi = load_mesh_info_raster(mesh_info_of(inst));
+        MeshletBits mb;
+        load_meshlet(reinterpret_cast<const Meshlet*>(mi.meshlets) + ref.meshlet_index, mb);
+        const lh_mat4& vp = view_matrix(f, vw);
+        const uint8_t* micro = reinterpret_cast<const uint8_t*>(mi.micro_indices) + mb.m.triangle_offset + it.tri * 3;
+        const bool alpha = it.slot >= f.max_draws;  // alpha clip: double sided, alpha tested
+        f4 poly[9];
+        for (int k = 0; k < 3; k++) {
+            uint32_t idx = load_index_raw(mi.indices, mi.flags, mb.m.index_offset + micro[k]);
+            f3 w = world_pos(transform, load_position(mi.positions, mi.flags, idx));
+            poly[k] = mul(vp, f4{w.x, w.y, w.z, 1.0f});
+        }
+        int np = clip_polygon(poly, 3);
+        if (np < 3) return;
+        bool projectable = true;  // false only for a triangle through the eye point
+        for (int k = 0; k < np; k++) projectable = projectable && poly[k].w > 0.0f;
+        if (!projectable) return;
+        const uint32_t W = vw->width, H = vw->height;
+        const float hw = (float)W * 0.5f, hh = (float)H * 0.5f;
+        SnapV s[9];
+        for (int k = 0; k < np; k++) s[k] = snap(poly[k], hw, hh);
+        int64_t pc = 0;
+        for (int k = 0; k < np; k++) {
+            const SnapV &a = s[k], &b = s[k + 1 < np ? k + 1 : 0];
+            pc += (int64_t)a.X * b.Y - (int64_t)b.X * a.Y;
+        }
+        if (pc == 0) return;
+        if (!alpha && KIND == 0 && pc > 0) return;
+        if (!alpha && KIND == 1 && pc < 0) return;
+        const uint32_t id = LH_PACK_ID(it.tri, it.slot);
+        for (int k = 1; k + 1 < np; k++) {
+            SnapV a = s[0], b = s[k], c = s[k + 1];
+            int64_t tc = cross3(a, b, c);
+            if (tc == 0 || ((tc < 0) != (pc < 0))) continue;
+            if (tc > 0) { SnapV tmp = b; b = c; c = tmp; }
+            TriSetup st;
+            if (make_setup(a, b, c, id, W, H, st)) {
+                if (alpha) st.bias |= kBiasAlpha;
+                push_big(f, st, it.view);
+            }
+        }
+    }
+}
+
 // Where a warp's alpha-tested triangles find their vertices: the warp's
 // shared AlphaVert array (indexed by TriSetup::verts) and the meshlet's
 // base texture.
@@ -460,9 +546,8 @@ __device__ __forceinline__ void raster_meshlet(const FrameDev& f, const MeshletW
                 if (((o0 | o1 | o2) & 64u) || (o0 & o1 & o2)) {
                     // non-finite / w <= 0, or entirely outside one plane
                 } else if (o0 | o1 | o2) {
-                    uint32_t pos = atomicAdd(&f.status[kStClipCount], 1u);
-                    if (pos < f.clip_cap) f.clip[pos] = ClipItem{w.view, w.slot, t, 0u};
-                    else atomicOr(&f.status[kStFlags], LH_FLAG_QUEUE_OVERFLOW);
+                    atomicAdd(&f.status[kStClipCount], 1u);  // statistics only
+                    clip_triangle<KIND>(f, w.view, w.slot, t);
                 } else {
                     SnapV a = sv[m0], b = sv[m1], c = sv[m2];
                     // most visible triangles hold no pixel centre: the 32-bit
@@ -607,90 +692,6 @@ __device__ void phase_raster(const FrameDev& f, uint32_t view_begin, uint32_t n_
         if (part * 32u >= nt) continue;  // this quarter holds no triangles
         const MeshletWork w{view, slot, part, split, nv, nt, W, H, target, hw, hh, &s_vp[v], transform, mi, 0u, 0u, inst};
         raster_meshlet<KIND, ALPHA>(f, w, tune, sv, so, s_micro[warp], ALPHA ? s_av[warp] : nullptr, lane);
-    }
-}
-
-// Sutherland-Hodgman against w-z, z, g*w-x, g*w+x, g*w-y, g*w+y >= 0.
-__device__ int clip_polygon(f4* poly, int n) {
-    f4 out[9];
-    for (int plane = 0; plane < 6 && n >= 3; plane++) {
-        int m = 0;
-        for (int i = 0; i < n; i++) {
-            f4 a = poly[i], b = poly[i + 1 < n ? i + 1 : 0];
-            float ga = LH_GUARD_BAND * a.w, gb = LH_GUARD_BAND * b.w;
-            float da, db;
-            switch (plane) {
-                case 0: da = a.w - a.z; db = b.w - b.z; break;
-                case 1: da = a.z; db = b.z; break;
-                case 2: da = ga - a.x; db = gb - b.x; break;
-                case 3: da = ga + a.x; db = gb + b.x; break;
-                case 4: da = ga - a.y; db = gb - b.y; break;
-                default: da = ga + a.y; db = gb + b.y; break;
-            }
-            if (da >= 0.0f) out[m++] = a;
-            if ((da >= 0.0f) != (db >= 0.0f)) {
-                float tt = da / (da - db);
-                out[m++] = f4{a.x + tt * (b.x - a.x), a.y + tt * (b.y - a.y), a.z + tt * (b.z - a.z), a.w + tt * (b.w - a.w)};
-            }
-        }
-        n = m;
-        for (int i = 0; i < n; i++) poly[i] = out[i];
-    }
-    return n;
-}
-
-// One thread per clipped triangle; thread `gtid` of `gstride`.
-template <int KIND>
-__device__ void phase_raster_clip(const FrameDev& f, uint32_t gtid, uint32_t gstride) {
-    const uint32_t n = min(*reinterpret_cast<volatile uint32_t*>(&f.status[kStClipCount]), f.clip_cap);
-    for (uint32_t i = gtid; i < n; i += gstride) {
-        const ClipItem it = f.clip[i];
-        const ViewDev* vw = f.views + it.view;
-        const MeshletReference ref = vw->refs[it.slot];
-        const Instance* inst = f.instances + ref.instance_index;
-        lh_mat4 transform;
-        load_transform(inst, transform);
-        const MeshInfoRaster mi = load_mesh_info_raster(mesh_info_of(inst));
-        MeshletBits mb;
-        load_meshlet(reinterpret_cast<const Meshlet*>(mi.meshlets) + ref.meshlet_index, mb);
-        const lh_mat4& vp = view_matrix(f, vw);
-        const uint8_t* micro = reinterpret_cast<const uint8_t*>(mi.micro_indices) + mb.m.triangle_offset + it.tri * 3;
-        const bool alpha = it.slot >= f.max_draws;  // alpha clip: double sided, alpha tested
-        f4 poly[9];
-        for (int k = 0; k < 3; k++) {
-            uint32_t idx = load_index_raw(mi.indices, mi.flags, mb.m.index_offset + micro[k]);
-            f3 w = world_pos(transform, load_position(mi.positions, mi.flags, idx));
-            poly[k] = mul(vp, f4{w.x, w.y, w.z, 1.0f});
-        }
-        int np = clip_polygon(poly, 3);
-        if (np < 3) continue;
-        bool projectable = true;  // false only for a triangle through the eye point
-        for (int k = 0; k < np; k++) projectable = projectable && poly[k].w > 0.0f;
-        if (!projectable) continue;
-        const uint32_t W = vw->width, H = vw->height;
-        const float hw = (float)W * 0.5f, hh = (float)H * 0.5f;
-        SnapV s[9];
-        for (int k = 0; k < np; k++) s[k] = snap(poly[k], hw, hh);
-        int64_t pc = 0;
-        for (int k = 0; k < np; k++) {
-            const SnapV &a = s[k], &b = s[k + 1 < np ? k + 1 : 0];
-            pc += (int64_t)a.X * b.Y - (int64_t)b.X * a.Y;
-        }
-        if (pc == 0) continue;
-        if (!alpha && KIND == 0 && pc > 0) continue;
-        if (!alpha && KIND == 1 && pc < 0) continue;
-        const uint32_t id = LH_PACK_ID(it.tri, it.slot);
-        for (int k = 1; k + 1 < np; k++) {
-            SnapV a = s[0], b = s[k], c = s[k + 1];
-            int64_t tc = cross3(a, b, c);
-            if (tc == 0 || ((tc < 0) != (pc < 0))) continue;
-            if (tc > 0) { SnapV tmp = b; b = c; c = tmp; }
-            TriSetup st;
-            if (make_setup(a, b, c, id, W, H, st)) {
-                if (alpha) st.bias |= kBiasAlpha;
-                push_big(f, st, it.view);
-            }
-        }
     }
 }
 

@@ -322,23 +322,24 @@ __device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uin
     }
     const uint32_t packed = (uint32_t)vis;
     const uint32_t slot = packed & ((1u << 24) - 1u), tri = packed >> 24;
-    const MeshletReference ref = f.views[0].refs[slot];
-    const Instance* inst = f.instances + ref.instance_index;
+    // the slot's draw record (written by the meshlet cull) carries the index
+    // and micro-index addresses of the meshlet: the micro indices load in
+    // parallel with the instance and its MeshInfo instead of after them
+    const RasterDraw rd = f.views[0].rdraws[slot];
+    const Instance* inst = f.instances + rd.instance;
     const MeshInfoResolve mi = load_mesh_info_resolve(mesh_info_of(inst));
-    const Meshlet* ml = reinterpret_cast<const Meshlet*>(mi.meshlets) + ref.meshlet_index;
-    const uint32_t tri_off = __ldg(&ml->triangle_offset), idx_off = __ldg(&ml->index_offset);
-    const uint8_t* micro = reinterpret_cast<const uint8_t*>(mi.micro_indices) + tri_off + tri * 3;
-    const uint32_t flags = mi.flags;
+    const uint8_t* micro = reinterpret_cast<const uint8_t*>(rd.micro) + tri * 3;
+    const uint32_t flags = rd.bits >> 16;
     uint32_t idx[3];
     for (int k = 0; k < 3; k++) {
-        uint32_t vi = idx_off + __ldg(micro + k);
-        idx[k] = (flags & MESH_INFO_FLAGS_32_BIT_INDICES) ? __ldg(reinterpret_cast<const uint32_t*>(mi.indices) + vi)
-                                                          : __ldg(reinterpret_cast<const uint16_t*>(mi.indices) + vi);
+        const uint32_t vi = __ldg(micro + k);
+        idx[k] = (flags & MESH_INFO_FLAGS_32_BIT_INDICES) ? __ldg(reinterpret_cast<const uint32_t*>(rd.indices) + vi)
+                                                          : __ldg(reinterpret_cast<const uint16_t*>(rd.indices) + vi);
     }
     const lh_mat4& T = inst->transform;
-    f3 pa = world_pos(T, load_position(mi.positions, flags, idx[0]));
-    f3 pb = world_pos(T, load_position(mi.positions, flags, idx[1]));
-    f3 pc = world_pos(T, load_position(mi.positions, flags, idx[2]));
+    f3 pa = world_pos(T, load_position(rd.positions, flags, idx[0]));
+    f3 pb = world_pos(T, load_position(rd.positions, flags, idx[1]));
+    f3 pc = world_pos(T, load_position(rd.positions, flags, idx[2]));
     const lh_mat4& PV = u.combined_perspective_view;
     const Bary bary = calc_full_bary<false>(mul(PV, f4{pa.x, pa.y, pa.z, 1.0f}), mul(PV, f4{pb.x, pb.y, pb.z, 1.0f}),
                                             mul(PV, f4{pc.x, pc.y, pc.z, 1.0f}), ndc, f2{(float)W, (float)H});
@@ -383,7 +384,7 @@ __device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uin
     if (sc.z > 1.0f) shadow_sum = 1.0f;
     // AMBIENT_SH (render_geometry.comp:40-57): only sh[0] = sh[2] = 0.025.
     if (u.debug != 0 && u.debug != 4) {
-        const f3 o = debug_view(u.debug, base, ci, tri, ref.meshlet_index, normal);
+        const f3 o = debug_view(u.debug, base, ci, tri, f.views[0].refs[slot].meshlet_index, normal);
         store_hdr(f.hdr, f.hdr_half, pix, o.x, o.y, o.z);
         return;
     }
