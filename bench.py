@@ -407,6 +407,9 @@ def bench_batched(lh, torch, args, device):
     out["status_flags"] = int(st.flags)
     out["visible_meshlets_all_views"] = int(sum(st.visible_opaque[v] for v in range(5 + n)))
     out["speedup_persistent_vs_per_view_launches"] = out["per_view_launches_ms"] / out["persistent_graph_ms"]
+    best = min(("persistent_graph", "per_stage_graph", "per_stage_launches"), key=lambda k: out[k + "_ms"])
+    out["best_batched"] = best
+    out["speedup_best_batched_vs_per_view_launches"] = out["per_view_launches_ms"] / out[best + "_ms"]
     out["speedup_persistent_vs_per_view_graph"] = out["per_view_graph_ms"] / out["persistent_graph_ms"]
     return out
 

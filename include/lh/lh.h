@@ -217,7 +217,7 @@ lh_status lh_read_status(lh_ctx* ctx, lh_device_status* out);
 /* Launch-shape knobs of the raster and cull kernels (set by the autotuner,
  * lighthugger_gb300/autotune.py) and the launch schedule.  Results never
  * depend on them. */
-#define LH_SCHEDULE_DEFAULT 0    /* per stage; persistent for frames with probe views */
+#define LH_SCHEDULE_DEFAULT 0    /* per stage */
 #define LH_SCHEDULE_PER_STAGE 1  /* one launch per stage, each over all views of a kind */
 #define LH_SCHEDULE_PERSISTENT 2 /* cull + raster of all views in one cooperative launch */
 #define LH_SCHEDULE_PER_VIEW 3   /* each view's cull and raster launched on its own (the reference's per-cascade loop) */

@@ -312,13 +312,15 @@ lh_status upload_frame_constants(lh_ctx* c, const Uniforms* u, const Uniforms* p
     return LH_OK;
 }
 
-// The frame's kernels, all stream ordered (capturable).  `batched` selects
-// the default schedule of lh_frame_batched.
-// `batched`: a frame with probe views (a plain frame takes the per-stage
-// default even through the batched entry points).
+// The frame's kernels, all stream ordered (capturable).  The default is the
+// per-stage schedule for every frame: with the multi-view raster at four
+// blocks per SM it measured 3.54 ms against 3.65 ms for the persistent
+// launch on main + 32 probes + 4 cascades at 2048^2.  `batched` (a frame with
+// probe views) is kept for schedules that depend on it.
 uint32_t frame_schedule(const lh_ctx* c, bool batched) {
+    (void)batched;
     uint32_t schedule = c->tuning.schedule;
-    if (schedule == LH_SCHEDULE_DEFAULT) schedule = batched ? LH_SCHEDULE_PERSISTENT : LH_SCHEDULE_PER_STAGE;
+    if (schedule == LH_SCHEDULE_DEFAULT) schedule = LH_SCHEDULE_PER_STAGE;
     if (schedule == LH_SCHEDULE_PERSISTENT && persistent_blocks_per_sm() <= 0) schedule = LH_SCHEDULE_PER_STAGE;
     return schedule;
 }
