@@ -349,6 +349,7 @@ lh_status enqueue_frame(lh_ctx* c, uint32_t n_probes, uint32_t n_instances, bool
     cudaError_t e = mark(cudaSuccess);
     if (e == cudaSuccess && !start) e = cudaMemsetAsync(c->d_reset, 0, c->reset_bytes, s);
     const uint32_t cull_blocks = std::max(1u, (uint32_t)(c->sms * t.cull_blocks_per_sm));
+    const uint32_t clear_blocks = (uint32_t)c->sms;  // per view, beside each instance-cull launch
     if (schedule == LH_SCHEDULE_PERSISTENT) {
         // stages 0..7 in one launch: the time lands in stage 0 ("clear")
         if (e == cudaSuccess)
@@ -357,9 +358,9 @@ lh_status enqueue_frame(lh_ctx* c, uint32_t n_probes, uint32_t n_instances, bool
         e = mark(e);
         e = skip_to(8, e);
     } else if (schedule == LH_SCHEDULE_PER_VIEW) {
-        if (e == cudaSuccess) e = mark(launch_clear_targets(f, s, c->sms, start));
+        if (e == cudaSuccess) e = mark(launch_clear_targets(f, s, c->sms, start, false));
         for (uint32_t v = 0; v < n_persp && e == cudaSuccess; v++) {
-            e = launch_cull_instances(f, v, 1, s);
+            e = launch_cull_instances(f, v, 1, s, clear_blocks);
             if (e == cudaSuccess) e = launch_cull_meshlets(f, v, 1, cull_blocks, s);
             if (e == cudaSuccess)
                 e = launch_raster_kind(f, v, 1, kViewVisibility, t.small_px, t.medium_px, t.raster_batch, s, c->sms);
@@ -367,23 +368,23 @@ lh_status enqueue_frame(lh_ctx* c, uint32_t n_probes, uint32_t n_instances, bool
         e = skip_to(4, e);
         if (e == cudaSuccess) e = mark(launch_depth_reduce_fit(f, s, c->sms));
         for (uint32_t k = 0; k < 4 && e == cudaSuccess; k++) {
-            e = launch_cull_instances(f, n_persp + k, 1, s);
+            e = launch_cull_instances(f, n_persp + k, 1, s, clear_blocks);
             if (e == cudaSuccess) e = launch_cull_meshlets(f, n_persp + k, 1, cull_blocks, s);
             if (e == cudaSuccess)
                 e = launch_raster_kind(f, n_persp + k, 1, kViewShadow, t.small_px, t.medium_px, t.raster_batch, s, c->sms);
         }
         e = skip_to(8, e);
     } else {
-        if (e == cudaSuccess) e = mark(launch_clear_targets(f, s, c->sms, start));
-        // visibility views: instance cull + prefix, meshlet cull, raster
-        if (e == cudaSuccess) e = mark(launch_cull_instances(f, 0, n_persp, s));
+        if (e == cudaSuccess) e = mark(launch_clear_targets(f, s, c->sms, start, false));
+        // visibility views: instance cull + prefix (and the targets' clear), meshlet cull, raster
+        if (e == cudaSuccess) e = mark(launch_cull_instances(f, 0, n_persp, s, clear_blocks));
         if (e == cudaSuccess) e = mark(launch_cull_meshlets(f, 0, n_persp, cull_blocks, s));
         if (e == cudaSuccess)
             e = mark(launch_raster_kind(f, 0, n_persp, kViewVisibility, t.small_px, t.medium_px, t.raster_batch, s, c->sms));
         // depth range + cascade fit (main view only)
         if (e == cudaSuccess) e = mark(launch_depth_reduce_fit(f, s, c->sms));
-        // cascades
-        if (e == cudaSuccess) e = mark(launch_cull_instances(f, n_persp, 4, s));
+        // cascades (the shadow maps are cleared beside their instance cull)
+        if (e == cudaSuccess) e = mark(launch_cull_instances(f, n_persp, 4, s, clear_blocks));
         if (e == cudaSuccess) e = mark(launch_cull_meshlets(f, n_persp, 4, cull_blocks, s));
         if (e == cudaSuccess)
             e = mark(launch_raster_kind(f, n_persp, 4, kViewShadow, t.small_px, t.medium_px, t.raster_batch, s, c->sms));

@@ -2,16 +2,26 @@
 // cull; the work itself is in cull_phases.cuh (shared with the persistent
 // multi-view kernel).
 #include "cull_phases.cuh"
+#include "frame_phases.cuh"
 
 namespace lh {
 namespace {
 
-// grid = (tiles per view, n_views).  Also zeroes the claim word of the
-// meshlet cull that follows in the stream (nothing here reads it).
-__global__ void __launch_bounds__(kInstTile) k_cull_instances(FrameDev f, uint32_t view_begin) {
+// grid = (tiles per view + clear blocks, n_views).  Blocks past the view's
+// tiles clear its target (visibility 0 or shadow depth 1.0) while the tiles
+// cull: the cull occupies few SMs, and nothing reads the target before the
+// raster launched after it.  Also zeroes the claim word of the meshlet cull
+// that follows in the stream (nothing here reads it).
+__global__ void __launch_bounds__(kInstTile) k_cull_instances(FrameDev f, uint32_t view_begin, uint32_t tiles) {
     pdl_enter();
     if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) f.status[kStMlClaim] = 0u;
-    phase_cull_instances_tile(f, view_begin + blockIdx.y, gridDim.x);
+    if (blockIdx.x >= tiles) {
+        const uint32_t clear_blocks = gridDim.x - tiles;
+        phase_clear_view(f, view_begin + blockIdx.y, (uint64_t)(blockIdx.x - tiles) * blockDim.x + threadIdx.x,
+                         (uint64_t)clear_blocks * blockDim.x, false);
+        return;
+    }
+    phase_cull_instances_tile(f, view_begin + blockIdx.y, tiles);
 }
 
 // persistent over (view, tile) claims of views [view_begin, view_begin + n_views).
@@ -37,10 +47,13 @@ __global__ void k_sum_meshlets(const Instance* inst, uint32_t n, unsigned long l
 
 }  // namespace
 
-cudaError_t launch_cull_instances(const FrameDev& f, uint32_t view_begin, uint32_t n_views, cudaStream_t s) {
-    if (f.n_instances == 0 || n_views == 0) return cudaSuccess;
-    dim3 grid((f.n_instances + kInstTile - 1) / kInstTile, n_views);
-    return launch_pdl(k_cull_instances, grid, dim3(kInstTile), s, f, view_begin);
+cudaError_t launch_cull_instances(const FrameDev& f, uint32_t view_begin, uint32_t n_views, cudaStream_t s,
+                                  uint32_t clear_blocks) {
+    if (n_views == 0) return cudaSuccess;
+    const uint32_t tiles = (f.n_instances + kInstTile - 1) / kInstTile;
+    if (tiles + clear_blocks == 0) return cudaSuccess;
+    dim3 grid(tiles + clear_blocks, n_views);
+    return launch_pdl(k_cull_instances, grid, dim3(kInstTile), s, f, view_begin, tiles);
 }
 
 cudaError_t launch_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint32_t n_views, uint32_t blocks,

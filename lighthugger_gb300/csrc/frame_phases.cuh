@@ -18,6 +18,18 @@ namespace {
 // counters and the depth range (reset_buffers.glsl:9-29, util.glsl:61-70).
 // Clear the target of view `view` with threads gtid of gstride; the thread
 // with `reset_counters` also resets the per-view counters and depth range.
+// Per-view counters and the depth range (one block).
+__device__ void reset_view_counters(const FrameDev& f) {
+    for (uint32_t v = threadIdx.x; v < f.n_views; v += blockDim.x) {
+        *reinterpret_cast<unsigned long long*>(f.views[v].sector) = 0ull;
+        *reinterpret_cast<unsigned long long*>(f.views[v].draws) = 0ull;
+    }
+    if (threadIdx.x == 0) {
+        f.misc->min_depth = 0xFFFFFFFFu;
+        f.misc->max_depth = 0u;
+    }
+}
+
 __device__ void phase_clear_view(const FrameDev& f, uint32_t view, uint64_t tid, uint64_t stride, bool reset_counters) {
     const ViewDev* vw = f.views + view;
     const uint64_t npx = (uint64_t)vw->width * vw->height;
@@ -33,16 +45,7 @@ __device__ void phase_clear_view(const FrameDev& f, uint32_t view, uint64_t tid,
         for (uint64_t i = tid; i < n; i += stride) p[i] = make_uint4(one, one, one, one);
         for (uint64_t i = n * 4 + tid; i < npx; i += stride) reinterpret_cast<uint32_t*>(vw->target)[i] = one;
     }
-    if (reset_counters) {
-        for (uint32_t v = threadIdx.x; v < f.n_views; v += blockDim.x) {
-            *reinterpret_cast<unsigned long long*>(f.views[v].sector) = 0ull;
-            *reinterpret_cast<unsigned long long*>(f.views[v].draws) = 0ull;
-        }
-        if (threadIdx.x == 0) {
-            f.misc->min_depth = 0xFFFFFFFFu;
-            f.misc->max_depth = 0u;
-        }
-    }
+    if (reset_counters) reset_view_counters(f);
 }
 
 // ---------------------------------------------------------------- cascade fit

@@ -155,8 +155,12 @@ struct FrameStart {
 // divisions, the oracle's definition).
 cudaError_t launch_linearize_texture(const uchar4* src, float4* dst, size_t n, uint32_t srgb, const float* lut,
                                      cudaStream_t s);
-cudaError_t launch_clear_targets(const FrameDev& f, cudaStream_t s, int sms, const FrameStart* start = nullptr);
-cudaError_t launch_cull_instances(const FrameDev& f, uint32_t view_begin, uint32_t n_views, cudaStream_t s);
+// `targets` false: only the frame start and the counters (the instance-cull
+// launches clear the targets, each with `clear_blocks` blocks per view).
+cudaError_t launch_clear_targets(const FrameDev& f, cudaStream_t s, int sms, const FrameStart* start = nullptr,
+                                 bool targets = true);
+cudaError_t launch_cull_instances(const FrameDev& f, uint32_t view_begin, uint32_t n_views, cudaStream_t s,
+                                  uint32_t clear_blocks = 0);
 cudaError_t launch_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint32_t n_views, uint32_t blocks,
                                  cudaStream_t s);
 // Raster all views [view_begin, view_begin + n_views) of one kind (kViewVisibility

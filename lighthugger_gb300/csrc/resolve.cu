@@ -495,11 +495,14 @@ __global__ void __launch_bounds__(kResolveWarps * 32, LH_RESOLVE_MIN_BLOCKS)
     }
 }
 
-// grid = (blocks, n_views).  With `has_start`, view 0's blocks also zero the
-// frame's scratch and block (0, 0) stores the frame's uniforms and constants
-// (nothing in this kernel reads either).
+// grid = (blocks, n_views), or (blocks, 1) without `targets`.  With
+// `has_start`, view 0's blocks also zero the frame's scratch and block (0, 0)
+// stores the frame's uniforms and constants (nothing in this kernel reads
+// either).  Without `targets` only block (0, 0) resets the per-view counters
+// and the depth range: the targets are cleared by the instance-cull launches
+// (launch_cull_instances with `clear`), beside the cull.
 __global__ void __launch_bounds__(256) k_clear_targets(FrameDev f, const __grid_constant__ FrameStart start,
-                                                       uint32_t has_start) {
+                                                       uint32_t has_start, uint32_t targets) {
     pdl_enter();
     if (has_start && blockIdx.y == 0) {
         const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (uint64_t)gridDim.x * blockDim.x;
@@ -511,8 +514,11 @@ __global__ void __launch_bounds__(256) k_clear_targets(FrameDev f, const __grid_
             if (threadIdx.x < 2) start.d_consts[threadIdx.x] = start.consts[threadIdx.x];
         }
     }
-    phase_clear_view(f, blockIdx.y, (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, (uint64_t)gridDim.x * blockDim.x,
-                     blockIdx.x == 0 && blockIdx.y == 0);
+    if (targets)
+        phase_clear_view(f, blockIdx.y, (uint64_t)blockIdx.x * blockDim.x + threadIdx.x,
+                         (uint64_t)gridDim.x * blockDim.x, blockIdx.x == 0 && blockIdx.y == 0);
+    else if (blockIdx.x == 0)
+        reset_view_counters(f);
 }
 
 // Depth reduction; the last block to finish fits the cascades.
@@ -558,12 +564,12 @@ cudaError_t launch_linearize_texture(const uchar4* src, float4* dst, size_t n, u
     return cudaGetLastError();
 }
 
-cudaError_t launch_clear_targets(const FrameDev& f, cudaStream_t s, int sms, const FrameStart* start) {
-    dim3 grid((unsigned)sms, f.n_views);
-    if (start) return launch_pdl(k_clear_targets, grid, dim3(256), s, f, *start, 1u);
+cudaError_t launch_clear_targets(const FrameDev& f, cudaStream_t s, int sms, const FrameStart* start, bool targets) {
+    const dim3 grid((unsigned)sms, targets ? f.n_views : 1u);
+    if (start) return launch_pdl(k_clear_targets, grid, dim3(256), s, f, *start, 1u, targets ? 1u : 0u);
     FrameStart none;
     std::memset(&none, 0, sizeof(none));
-    return launch_pdl(k_clear_targets, grid, dim3(256), s, f, none, 0u);
+    return launch_pdl(k_clear_targets, grid, dim3(256), s, f, none, 0u, targets ? 1u : 0u);
 }
 
 cudaError_t launch_depth_reduce_fit(const FrameDev& f, cudaStream_t s, int sms) {
