@@ -78,11 +78,11 @@ constexpr int32_t kChunkCols = 64;
 // before each raster pass).
 enum StatusWord : uint32_t {
     kStFlags = 0,
-    kStClipCount = 1,
+    kStClipCount = 1,  // triangles clipped in the last raster pass (statistics)
     kStRasterClaim = 2,
     kStBigClaim = 3,
     kStReduceDone = 4,
-    kStClipClaim = 5,
+    // word 5 is unused
     kStMlClaim = 6,    // meshlet-cull (view, tile) claims
     kStBarrier = 7,    // grid barrier of the persistent kernel
     kStBigPacked = 8,  // u64 (words 8-9): big-triangle count << 40 | chunk count

@@ -121,14 +121,23 @@ def test_empty_view(native, oracle):
     assert not errors, errors
 
 
-def test_zero_instances(native):
+@pytest.mark.parametrize("schedule", ["per_stage", "per_view", "persistent"])
+def test_zero_instances(native, schedule):
+    """A frame with no instances after one with many: every target is cleared
+    (visibility 0, shadow depth 1.0) although no instance is culled or drawn
+    (the targets are cleared beside the instance cull, which then has no
+    tiles)."""
     lh = native
-    scene = lh.Scene(1, n_instances=1).upload(0)
+    scene = lh.Scene(1).upload(0)
     d = scene.desc
     u = scene.uniforms
-    cfg = lh.Config(width=d.width, height=d.height, shadow_size=256, max_instances=1024, max_draws=1000)
+    cfg = lh.Config(width=d.width, height=d.height, shadow_size=256, max_instances=1024, max_draws=100000)
     r = lh.Renderer(cfg)
     r.set_scene(scene)
+    r.set_tuning(schedule={"per_stage": lh.SCHEDULE_PER_STAGE, "per_view": lh.SCHEDULE_PER_VIEW,
+                           "persistent": lh.SCHEDULE_PERSISTENT}[schedule])
+    r.frame(u)
+    assert (r.visibility() != 0).any() and (r.shadow_maps() != 1.0).any()
     # uniforms.num_instances = 0: nothing is culled or drawn
     b = bytearray(bytes(u))
     b[532:536] = (0).to_bytes(4, "little")
@@ -137,6 +146,7 @@ def test_zero_instances(native):
     st = r.status()
     assert st.visible_instances[0] == 0 and st.visible_opaque[0] == 0
     assert (r.visibility() == 0).all()
+    assert (r.shadow_maps() == 1.0).all()
 
 
 def _camera_at_surface(lh, scene, inst_index, gap):
