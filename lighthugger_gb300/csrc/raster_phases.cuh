@@ -651,6 +651,11 @@ __device__ void phase_raster(const FrameDev& f, uint32_t view_begin, uint32_t n_
     const bool dynamic = dyn_base < units;
     uint32_t pending = 0;
     if (dynamic && lane == 0) pending = atomicAdd(claim_word, batch);
+    // A warp's units only increase (its static window, then claims that
+    // increase over time), so the view search starts at the previous unit's
+    // view: with many views (probes) a search from view 0 is a chain of
+    // dependent shared-memory loads per unit.
+    uint32_t v = 0;
     for (;;) {
         if (unit >= unit_end) {
             if (!dynamic) break;
@@ -662,7 +667,7 @@ __device__ void phase_raster(const FrameDev& f, uint32_t view_begin, uint32_t n_
         }
         const uint32_t item = unit / split, part = unit % split;
         unit++;
-        uint32_t v = 0;
+        if (item < s_prefix[v]) v = 0;  // not expected; keeps the search exact regardless
         while (item >= s_prefix[v + 1]) v++;
         const uint32_t view = view_begin + v;
         const ViewDev* vw = f.views + view;
