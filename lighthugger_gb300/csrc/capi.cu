@@ -314,7 +314,7 @@ lh_status upload_frame_constants(lh_ctx* c, const Uniforms* u, const Uniforms* p
 
 // The frame's kernels, all stream ordered (capturable).  The default is the
 // per-stage schedule for every frame: with the multi-view raster at four
-// blocks per SM it measured 3.54 ms against 3.65 ms for the persistent
+// blocks per SM it measured 3.15 ms against 3.22 ms for the persistent
 // launch on main + 32 probes + 4 cascades at 2048^2.  `batched` (a frame with
 // probe views) is kept for schedules that depend on it.
 uint32_t frame_schedule(const lh_ctx* c, bool batched) {
