@@ -235,9 +235,10 @@ lh_status lh_get_tuning(lh_ctx* ctx, lh_tuning* tuning);
 
 /* Per-stage timing with CUDA events recorded on the frame's stream (the
  * replacement of the reference's Tracy GPU zones, src/rendering.cpp:41-42,
- * 140-492).  Stages: 0 clear, 1 cull instances, 2 cull meshlets, 3 raster,
- * 4 depth reduce + cascade fit, 5 shadow instance cull, 6 shadow meshlet
- * cull, 7 shadow raster, 8 resolve. */
+ * 140-492).  Stages: 0 frame start (uniforms, counters), 1 cull instances
+ * (with the visibility targets' clear), 2 cull meshlets, 3 raster, 4 depth
+ * reduce + cascade fit, 5 shadow instance cull (with the shadow maps'
+ * clear), 6 shadow meshlet cull, 7 shadow raster, 8 resolve. */
 #define LH_N_STAGES 9
 lh_status lh_set_profiling(lh_ctx* ctx, int enable);
 /* Milliseconds of each stage of the last profiled frame (synchronises). */

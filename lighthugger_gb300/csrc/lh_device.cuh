@@ -220,7 +220,7 @@ __device__ __forceinline__ bool cull_cone_orthographic(const Uniforms& u, const 
 // ------------------------------------------------------------------ rasterisation rules
 // Outcode bits: 1 z > w (or w <= 0), 2 z < 0, 4 x > g*w, 8 x < -g*w,
 // 16 y > g*w, 32 y < -g*w; 64 = a non-finite coordinate (the triangle is
-// dropped).  Any other bit sends the triangle to the clipper.
+// dropped).  Any other bit has the triangle clipped (clip_triangle).
 __device__ __forceinline__ uint32_t outcode(f4 v) {
     if (!(isfinite(v.x) && isfinite(v.y) && isfinite(v.z) && isfinite(v.w))) return 64u;
     uint32_t c = 0;
