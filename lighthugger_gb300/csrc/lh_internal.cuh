@@ -62,7 +62,8 @@ struct ViewDev {
 };
 
 // Triangle handed to the chunked raster path: its set-up (orientation
-// normalised, pixel bounds) and the first of its 16 x 64-pixel chunks.
+// normalised, pixel bounds) and the first of its chunks (kChunkRows x
+// chunk_cols<KIND>() pixels).
 struct BigTri {
     int32_t X0, Y0, X1, Y1, X2, Y2;
     float z0, s1, s2;
@@ -71,8 +72,24 @@ struct BigTri {
     uint32_t bias;
     int32_t px0, px1, py0, py1;
 };
-constexpr int32_t kChunkRows = 16;
-constexpr int32_t kChunkCols = 64;
+// Chunk of a big triangle (one warp): rows x columns of pixels.  The
+// visibility pass uses 16 x 32 (raster stage 0.332 -> 0.326 ms against
+// 16 x 64), the shadow pass 16 x 64 (0.099 ms against 0.103 ms at 16 x 32);
+// 8 x 64 was slower for both.
+#ifndef LH_CHUNK_ROWS
+#define LH_CHUNK_ROWS 16
+#endif
+#ifndef LH_CHUNK_COLS_VIS
+#define LH_CHUNK_COLS_VIS 32
+#endif
+#ifndef LH_CHUNK_COLS_SHADOW
+#define LH_CHUNK_COLS_SHADOW 64
+#endif
+constexpr int32_t kChunkRows = LH_CHUNK_ROWS;
+template <int KIND>
+__host__ __device__ constexpr int32_t chunk_cols() {
+    return KIND == 0 ? LH_CHUNK_COLS_VIS : LH_CHUNK_COLS_SHADOW;
+}
 
 // Per-frame scratch words (zeroed at frame start; the raster words again
 // before each raster pass).

@@ -199,8 +199,9 @@ __device__ __forceinline__ void load_transform(const Instance* inst, lh_mat4& m)
 // (the packed single-pass append of prefix_sum.glsl:17-30): the triangle's
 // index and its first chunk come from the same word, so chunk bases ascend
 // with the index and the band kernel finds a chunk's triangle by binary search.
+template <int KIND>
 __device__ __forceinline__ unsigned long long big_chunks(const TriSetup& t) {
-    const uint32_t nbx = (uint32_t)(t.px1 - t.px0) / kChunkCols + 1;
+    const uint32_t nbx = (uint32_t)(t.px1 - t.px0) / chunk_cols<KIND>() + 1;
     const uint32_t nby = (uint32_t)(t.py1 - t.py0) / kChunkRows + 1;
     return (unsigned long long)nbx * nby;
 }
@@ -227,8 +228,9 @@ __device__ void store_big(const FrameDev& f, const TriSetup& t, uint32_t view, u
     f.big_base[idx] = (uint32_t)base;
 }
 // One thread's triangle.
+template <int KIND>
 __device__ void push_big(const FrameDev& f, const TriSetup& t, uint32_t view) {
-    const unsigned long long n = big_chunks(t);
+    const unsigned long long n = big_chunks<KIND>(t);
     const unsigned long long old =
         atomicAdd(reinterpret_cast<unsigned long long*>(f.status + kStBigPacked), (1ull << 40) | n);
     store_big(f, t, view, old, n);
@@ -238,7 +240,7 @@ __device__ void push_big(const FrameDev& f, const TriSetup& t, uint32_t view) {
 // lane the running total below it).  The word's low 40 bits cannot carry into
 // the count: a sum reaching 2^32 chunks is flagged and dropped.
 __device__ void push_big_warp(const FrameDev& f, const TriSetup& t, uint32_t view, bool big, uint32_t lane) {
-    const unsigned long long n = big ? big_chunks(t) : 0ull;
+    const unsigned long long n = big ? big_chunks<1>(t) : 0ull;
     const unsigned long long mine = big ? (1ull << 40) | n : 0ull;
     unsigned long long incl = mine;
 #pragma unroll
@@ -333,7 +335,7 @@ __device__ __noinline__ void clip_triangle(const FrameDev& f, uint32_t view, uin
             TriSetup st;
             if (make_setup(a, b, c, id, W, H, st)) {
                 if (alpha) st.bias |= kBiasAlpha;
-                push_big(f, st, it.view);
+                push_big<KIND>(f, st, it.view);
             }
         }
     }
@@ -574,7 +576,7 @@ __device__ __forceinline__ void raster_meshlet(const FrameDev& f, const MeshletW
                         } else if (KIND == 1) {
                             big = true;  // appended below, one atomic per warp
                         } else {
-                            push_big(f, st, w.view);
+                            push_big<KIND>(f, st, w.view);
                         }
                     }
                 }
@@ -757,7 +759,8 @@ __device__ __noinline__ void raster_chunk_alpha(const FrameDev& f, const BigTri*
         }
 }
 
-// One warp per 16 x 64-pixel chunk of a big triangle; chunks whose
+// One warp per chunk of a big triangle (16 x 32 pixels in the visibility
+// pass, 16 x 64 in the shadow pass: chunk_cols); chunks whose
 // rectangle lies outside one edge are skipped whole.
 template <int KIND>
 __device__ void phase_raster_big(const FrameDev& f) {
@@ -802,7 +805,7 @@ __device__ void phase_raster_big(const FrameDev& f) {
         }
         c++;
         const BigTri b = f.big[i];
-        const uint32_t nbx = (uint32_t)(b.px1 - b.px0) / kChunkCols + 1;
+        const uint32_t nbx = (uint32_t)(b.px1 - b.px0) / chunk_cols<KIND>() + 1;
         const uint32_t nby = (uint32_t)(b.py1 - b.py0) / kChunkRows + 1;
         const uint32_t base = f.big_base[i];
         const unsigned long long local = (c - 1u) - base;
@@ -811,7 +814,7 @@ __device__ void phase_raster_big(const FrameDev& f) {
         t_base = base;
         t_end = base + nbx * nby;
         const int32_t cx = (int32_t)(local % nbx), cy = (int32_t)(local / nbx);
-        const int32_t x0 = b.px0 + cx * kChunkCols, x1 = min(b.px1, x0 + kChunkCols - 1);
+        const int32_t x0 = b.px0 + cx * chunk_cols<KIND>(), x1 = min(b.px1, x0 + chunk_cols<KIND>() - 1);
         const int32_t y0 = b.py0 + cy * kChunkRows, y1 = min(b.py1, y0 + kChunkRows - 1);
         if (edge_rejects(b.X1, b.Y1, b.X2, b.Y2, x0, x1, y0, y1, b.bias & 1u) ||
             edge_rejects(b.X2, b.Y2, b.X0, b.Y0, x0, x1, y0, y1, (b.bias >> 1) & 1u) ||
