@@ -2,7 +2,8 @@
 
 The raster kernels split triangles into three bins by the pixel count of
 their bounding box -- rasterised by one lane (<= small_px), by one warp
-(<= medium_px), or cut into 16 x 64-pixel chunks spread over all warps --,
+(<= medium_px), or cut into chunks of 16 x 32 (visibility) or 16 x 64
+(shadow) pixels spread over all warps --,
 claim `raster_batch` meshlets per atomic, and a batched frame can run per
 stage or as one persistent launch.  None of this
 changes a single output bit; it only moves time.  `tune()` times frames of
