@@ -37,6 +37,16 @@ namespace {
 
 constexpr int kRasterWarps = 8;
 
+// Upper bound of the warp bin in the shadow pass (0: the tuning's medium_px
+// for both passes).  A shadow launch has about one unit per warp, so a warp
+// that rasterises a run of 33-128-pixel triangles one after another sets the
+// launch's time; sent to the chunk kernel instead, they spread over all
+// warps: shadow raster stage 0.099 -> 0.087 ms at 32 (0.096 ms at 64) for the
+// four 1024^2 cascades of the 4,096-instance frame.
+#ifndef LH_SHADOW_MEDIUM_PX
+#define LH_SHADOW_MEDIUM_PX 32
+#endif
+
 struct RasterTune {
     uint32_t small_px;   // lane path up to this many bbox pixels
     uint32_t medium_px;  // warp path up to this many; larger: band queue
@@ -571,7 +581,8 @@ __device__ __forceinline__ void raster_meshlet(const FrameDev& f, const MeshletW
                         if (npx <= tune.small_px) {
                             if (ALPHA) raster_lane_alpha<KIND>(f, st, w.target, W, as);
                             else raster_lane<KIND>(st, w.target, W);
-                        } else if (npx <= tune.medium_px) {
+                        } else if (npx <= (KIND == 1 && LH_SHADOW_MEDIUM_PX ? min(tune.medium_px, (uint32_t)LH_SHADOW_MEDIUM_PX)
+                                                                            : tune.medium_px)) {
                             medium = true;
                         } else if (KIND == 1) {
                             big = true;  // appended below, one atomic per warp
