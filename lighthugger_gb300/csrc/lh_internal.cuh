@@ -74,8 +74,9 @@ struct BigTri {
 };
 // Chunk of a big triangle (one warp): rows x columns of pixels.  The
 // visibility pass uses 16 x 32 (raster stage 0.332 -> 0.326 ms against
-// 16 x 64), the shadow pass 16 x 64 (0.099 ms against 0.103 ms at 16 x 32);
-// 8 x 64 was slower for both.
+// 16 x 64), the shadow pass 16 x 64 (0.099 ms against 0.103 ms at 16 x 32;
+// 0.088 against 0.092 ms once the shadow pass lost its warp bin); 8 x 64 was
+// slower for both.
 #ifndef LH_CHUNK_ROWS
 #define LH_CHUNK_ROWS 16
 #endif
