@@ -198,6 +198,17 @@ lh_status lh_frame_graph_backward(lh_ctx* ctx, const Uniforms* uniforms, const U
                                   uint64_t d_grad_hdr, const lh_grad_targets* targets, void* stream,
                                   lh_frame_out* out);
 
+/* Device address (float4[height][width], linear RGBA) of the context's copy
+ * of texture `index`, the texels every frame, the alpha test and the adjoint
+ * sample; made by lh_set_scene from the caller's RGBA8 texels (sRGB
+ * decoded, / 255).  Writing float4 values there, stream ordered before a
+ * frame, changes what the following frames sample until the next
+ * lh_set_scene -- how a differentiable caller applies texel parameters whose
+ * gradients lh_resolve_backward writes (lh_grad_targets.texture_grads).  The
+ * reference samples its bindless images instead; no counterpart there. */
+lh_status lh_get_texture_linear(lh_ctx* ctx, uint32_t index, uint64_t* d_texels, uint32_t* width,
+                                uint32_t* height);
+
 /* Display transform of the last frame's HDR image (display_transform.comp:
  * 5-81): the tony_mc_mapface encoding stimulus / (stimulus + 1) into a 48^3
  * LUT sampled trilinearly (clamp to edge) at texel centres, the cascade
@@ -255,12 +266,47 @@ lh_status lh_get_stage_times(lh_ctx* ctx, float* ms, uint32_t n);
  * lh_frame's main-view sector.  `d_flags` (optional, device) receives
  * LH_FLAG_* bits.  The kernel's scratch is a fixed array inside the library
  * of about 33 KB per GPU, so n_instances is limited to 1,048,576
- * (LH_ERR_CAPACITY beyond).  The first call on a device looks up that
- * array's address and should come before any stream capture; all calls share
- * the array, so calls that overlap on the GPU race -- serialise them. */
+ * (LH_ERR_CAPACITY beyond).  A call outside stream capture looks up that
+ * array's address on the current device; a call during capture reuses the
+ * address found by the last call outside capture (LH_ERR_UNSUPPORTED if there
+ * was none), so the first call on a device should come before any stream
+ * capture.  All calls share the array, so calls that overlap on the GPU
+ * race -- serialise them.  Every block ORs the flags it raises into d_flags
+ * itself (LH_FLAG_TIMEOUT, LH_FLAG_INSTANCE_OVERFLOW); with more visible
+ * instances than `capacity` the counter holds the true count and entries
+ * stop at `capacity`. */
 lh_status lh_cull_instances_noalloc(const Instance* d_instances, uint32_t n_instances,
                                     const Uniforms* host_uniforms, uint8_t* d_sector, uint32_t capacity,
                                     uint32_t* d_flags, void* stream);
+
+/* Diagnostic: run one of the library's bounded device-side waits -- the
+ * decoupled look-back of the culls (LH_WAIT_LOOKBACK), the grid barrier of
+ * the persistent frame kernel (LH_WAIT_GRID_BARRIER) or the mbarrier wait of
+ * the TMA-staged resolve (LH_WAIT_MBARRIER) -- in a one-block launch whose
+ * condition is met at once (`satisfied` != 0) or never (a predecessor that
+ * never publishes, a block that never arrives, an arrival that never comes),
+ * polling at most `poll_limit` times (1 .. 2^22).  `d_words`: 8 device u64
+ * words, zeroed by the call; once the stream has run it, word 3 (low 32
+ * bits) holds LH_FLAG_TIMEOUT if the wait expired and word 4 the wait's
+ * result (the look-back's exclusive prefix: 5 from its predecessor, or 0
+ * when that never published; else 1 when the wait completed).  Checks the
+ * failure path of the frame kernels without a fault or a hang.  No
+ * counterpart in the reference. */
+#define LH_WAIT_LOOKBACK 0u
+#define LH_WAIT_GRID_BARRIER 1u
+#define LH_WAIT_MBARRIER 2u
+lh_status lh_check_bounded_wait(uint32_t which, uint32_t poll_limit, uint32_t satisfied, uint64_t* d_words,
+                                void* stream);
+
+/* Throughput probe of the raster's depth test (no counterpart in the
+ * reference, whose depth test is fixed-function): `reps` passes of 64-bit
+ * max reductions (red.relaxed.gpu.global.max.u64, no return) over the
+ * n_words words at d_words -- each pass one reduction per word, to word i
+ * (`scattered` 0: a warp covers 256 contiguous bytes) or to a pseudo-random
+ * word (1: every lane its own cache line).  Time it with events on `stream`:
+ * n_words * reps / seconds is the reductions-per-second ceiling the raster's
+ * fragments are measured against.  The buffer's contents are overwritten. */
+lh_status lh_probe_red_u64(uint64_t* d_words, uint64_t n_words, uint32_t scattered, uint32_t reps, void* stream);
 
 /* The plain frame (as lh_frame) followed by a copy of the HDR image (width *
  * height pixels of 16 bytes, 8 with LH_CONFIG_HDR_RGBA16F) to `host_hdr`,

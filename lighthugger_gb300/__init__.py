@@ -31,6 +31,9 @@ FLAG_QUEUE_OVERFLOW = 0x4
 FLAG_TIMEOUT = 0x8
 FLAG_BAD_MESHLET = 0x10
 FLAG_NO_DEPTH = 0x20
+FLAG_SLOT_OVERFLOW = 0x40
+
+WAIT_LOOKBACK, WAIT_GRID_BARRIER, WAIT_MBARRIER = 0, 1, 2
 
 STAGES = ["clear", "cull_instances", "cull_meshlets", "raster", "depth_fit", "shadow_cull_instances",
           "shadow_cull_meshlets", "shadow_raster", "resolve"]
@@ -160,10 +163,16 @@ def lib():
     L.lh_scene_destroy.argtypes = [P]
     L.lh_scene_destroy.restype = None
     L.lh_make_uniforms.argtypes = [C.POINTER(Camera), C.POINTER(Uniforms)]
+    L.lh_cull_instances_noalloc.argtypes = [P, C.c_uint32, P, P, C.c_uint32, P, P]
+    L.lh_check_bounded_wait.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, P, P]
+    L.lh_probe_red_u64.argtypes = [P, C.c_uint64, C.c_uint32, C.c_uint32, P]
+    L.lh_get_texture_linear.argtypes = [P, C.c_uint32, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32),
+                                        C.POINTER(C.c_uint32)]
     for name in ("lh_create", "lh_set_scene", "lh_frame", "lh_frame_batched", "lh_frame_graph", "lh_get_outputs",
                  "lh_read_status",
                  "lh_download", "lh_resolve_backward", "lh_frame_graph_backward", "lh_display_transform", "lh_set_profiling", "lh_get_stage_times", "lh_set_tuning", "lh_get_tuning", "lh_scene_create", "lh_scene_describe",
-                 "lh_scene_upload", "lh_make_uniforms"):
+                 "lh_scene_upload", "lh_make_uniforms", "lh_cull_instances_noalloc", "lh_check_bounded_wait",
+                 "lh_get_texture_linear", "lh_probe_red_u64"):
         getattr(L, name).restype = C.c_int32
     _lib = L
     return L
@@ -371,6 +380,14 @@ class Renderer:
                                              grad_ptr, C.byref(targets), s, C.byref(self.out)),
                "lh_frame_graph_backward", self.ctx)
         return self.out
+
+    def texture_linear(self, index):
+        """(device address, width, height) of the context's linear float4
+        copy of texture `index` (what the frames and the adjoint sample)."""
+        a, w, h = C.c_uint64(), C.c_uint32(), C.c_uint32()
+        _check(lib().lh_get_texture_linear(self.ctx, index, C.byref(a), C.byref(w), C.byref(h)),
+               "lh_get_texture_linear", self.ctx)
+        return int(a.value), int(w.value), int(h.value)
 
     def display_transform(self, out_ptr, lut_ptr=0, stream=None):
         """RGBA8 display image of the last frame into device buffer out_ptr

@@ -22,7 +22,7 @@ LIB = os.path.join(LIBDIR, "liblh.so")
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 
-CU_SOURCES = ["cull.cu", "raster.cu", "resolve.cu", "persistent.cu", "adjoint.cu", "display.cu", "capi.cu", "noalloc.cu"]
+CU_SOURCES = ["cull.cu", "raster.cu", "resolve.cu", "persistent.cu", "adjoint.cu", "display.cu", "capi.cu", "noalloc.cu", "waits.cu", "probe.cu"]
 CPP_SOURCES = ["scene.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",

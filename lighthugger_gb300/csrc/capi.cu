@@ -65,6 +65,8 @@ struct lh_ctx {
     // device pointers into it, made by lh_set_scene
     float4* d_tex_linear = nullptr;
     const float4** d_tex_linear_ptrs = nullptr;
+    std::vector<size_t> tex_offset;    // first texel of each texture in d_tex_linear (n_textures + 1)
+    std::vector<uint32_t> tex_size;    // width, height of each texture
     // per-frame zeroed scratch (look-back words and tile claims)
     uint8_t* d_reset = nullptr;
     size_t reset_bytes = 0;
@@ -574,6 +576,12 @@ lh_status lh_set_scene(lh_ctx* c, const Instance* d_instances, uint32_t n, const
         if (e == cudaSuccess) e = dalloc(c, &c->d_tex_linear, sizeof(float4) * std::max<size_t>(1, offset[n_textures]));
         if (e == cudaSuccess) e = dalloc(c, &c->d_tex_linear_ptrs, sizeof(float4*) * std::max(1u, n_textures));
         std::vector<const float4*> ptrs(n_textures);
+        c->tex_offset = offset;
+        c->tex_size.assign(2 * (size_t)n_textures, 0u);
+        for (uint32_t i = 0; i < n_textures; i++) {
+            c->tex_size[2 * i] = textures[i].width;
+            c->tex_size[2 * i + 1] = textures[i].height;
+        }
         for (uint32_t i = 0; i < n_textures && e == cudaSuccess; i++) {
             ptrs[i] = c->d_tex_linear + offset[i];
             e = launch_linearize_texture(reinterpret_cast<const uchar4*>(textures[i].texels), c->d_tex_linear + offset[i],
@@ -849,6 +857,19 @@ lh_status lh_resolve_backward(lh_ctx* c, uint64_t d_grad_hdr, const lh_grad_targ
                                             *targets, s);
     if (e != cudaSuccess) return cuda_fail(c, e, "resolve backward");
     c->last_stream = s;
+    return LH_OK;
+}
+
+lh_status lh_get_texture_linear(lh_ctx* c, uint32_t index, uint64_t* d_texels, uint32_t* width, uint32_t* height) {
+    lh_status st = check_ctx(c);
+    if (st != LH_OK) return st;
+    if (!d_texels) return fail(c, LH_ERR_INVALID_ARGUMENT, "null output");
+    if (!c->d_reset) return fail(c, LH_ERR_NO_SCENE, "lh_set_scene was not called");
+    if (index >= c->n_textures || c->tex_offset.size() != (size_t)c->n_textures + 1)
+        return fail(c, LH_ERR_INVALID_ARGUMENT, "texture index out of range");
+    *d_texels = (uint64_t)(uintptr_t)(c->d_tex_linear + c->tex_offset[index]);
+    if (width) *width = c->tex_size[2 * (size_t)index];
+    if (height) *height = c->tex_size[2 * (size_t)index + 1];
     return LH_OK;
 }
 

@@ -37,9 +37,11 @@ __device__ __forceinline__ uint64_t ld_status(const uint64_t* p) {
 
 // Decoupled look-back by one thread: publish the tile aggregate, walk back
 // until an inclusive prefix is found, publish the tile's inclusive prefix.
-// Every wait is bounded; on expiry the status flag LH_FLAG_TIMEOUT is set and
-// the missing predecessors count as zero (no hang, results flagged).
-__device__ __noinline__ uint64_t lookback(uint64_t* status, uint32_t tile, uint64_t agg, uint32_t* flags) {
+// Every wait is bounded (`limit` polls of one predecessor's word); on expiry
+// the status flag LH_FLAG_TIMEOUT is set and the missing predecessors count
+// as zero (no hang, results flagged).
+__device__ __noinline__ uint64_t lookback(uint64_t* status, uint32_t tile, uint64_t agg, uint32_t* flags,
+                                          uint32_t limit = kSpinLimit) {
     if (tile == 0) {
         st_status(&status[0], kStatIncl | agg);
         return 0;
@@ -53,7 +55,7 @@ __device__ __noinline__ uint64_t lookback(uint64_t* status, uint32_t tile, uint6
         uint64_t s = ld_status(&status[t]);
         uint64_t fl = s >> 62;
         if (fl == 0) {
-            if (++spins >= kSpinLimit) { timed_out = true; break; }
+            if (++spins >= limit) { timed_out = true; break; }
             if (spins > 32) __nanosleep(spins > 1024 ? 256 : 32);
             continue;
         }

@@ -13,9 +13,12 @@
 // Limits and rules of use:
 //  - at most kNoAllocMaxTiles tiles of kInstTile instances (1,048,576
 //    instances); larger calls are rejected with LH_ERR_CAPACITY;
-//  - the first call on a device looks up the device address of the array
-//    (cudaGetSymbolAddress) with that device current; make that first call
-//    before any stream capture;
+//  - a call made outside stream capture looks up the device address of the
+//    array (cudaGetSymbolAddress) with the caller's device current and keeps
+//    it for that device; a call made while its stream is being captured uses
+//    the address kept by the last call outside capture, so make the first
+//    call on a device before any stream capture (after a cudaDeviceReset,
+//    or under another context, make one call outside capture again);
 //  - every call shares the one array: calls whose work overlaps on the GPU
 //    (different streams, or different host threads) race on it and give
 //    wrong results; serialise them;
@@ -32,7 +35,7 @@ namespace lh {
 namespace {
 
 constexpr uint32_t kNoAllocMaxTiles = 4096;
-constexpr uint32_t kNoAllocWords = kNoAllocMaxTiles + 32;  // look-back words + claim/flag words
+constexpr uint32_t kNoAllocWords = kNoAllocMaxTiles + 32;  // look-back words + the tile claim counter
 
 // The scratch of every call.  Host code must not use `g_cull_scratch`
 // directly: on the host it names a stand-in, not the device memory.
@@ -63,7 +66,6 @@ __global__ void __launch_bounds__(kInstTile) k_cull_instances_noalloc(const Inst
     __shared__ uint32_t s_tile;
     unsigned long long* status = scratch;                         // one word per tile
     unsigned int* claim = reinterpret_cast<unsigned int*>(scratch + kNoAllocMaxTiles);
-    unsigned int* flags = claim + 1;
     if (threadIdx.x == 0) s_tile = atomicAdd(claim, 1u);
     __syncthreads();
     const uint32_t tile = s_tile;
@@ -115,8 +117,8 @@ __global__ void __launch_bounds__(kInstTile) k_cull_instances_noalloc(const Inst
                 unsigned long long fl = s >> 62;
                 if (fl == 0) {
                     if (++spins >= kSpinLimit) {
-                        atomicOr(flags, LH_FLAG_TIMEOUT);
-                        __threadfence();
+                        // recorded by the block that timed out, whenever it does
+                        if (flags_out) atomicOr(flags_out, LH_FLAG_TIMEOUT);
                         break;
                     }
                     if (spins > 32) __nanosleep(spins > 1024 ? 256 : 32);
@@ -133,10 +135,8 @@ __global__ void __launch_bounds__(kInstTile) k_cull_instances_noalloc(const Inst
             unsigned long long total = excl + run;
             unsigned long long count = total >> 40;
             *reinterpret_cast<unsigned long long*>(sector) = (count << 32) | (uint32_t)(total & ((1ull << 40) - 1));
-            if (count > capacity) atomicOr(flags, LH_FLAG_INSTANCE_OVERFLOW);
-            if (flags_out) {
-                __threadfence();
-                atomicOr(flags_out, atomicOr(flags, 0u));
+            if (count > capacity) {
+                if (flags_out) atomicOr(flags_out, LH_FLAG_INSTANCE_OVERFLOW);
             }
         }
     }
@@ -153,23 +153,27 @@ __global__ void __launch_bounds__(kInstTile) k_cull_instances_noalloc(const Inst
     }
 }
 
-// Device address of the scratch array on the current device, looked up once
-// per device.
-lh_status scratch_for_current_device(unsigned long long** out) {
+// Device address of the scratch array on the current device.  Outside
+// stream capture it is looked up on every call (cheap, host side only), so a
+// device reset or another current context is picked up; during capture the
+// address kept by the last call outside capture on this device is used.
+lh_status scratch_for_current_device(cudaStream_t s, unsigned long long** out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return LH_ERR_CUDA;
     if (dev < 0 || dev >= kMaxDevices) return LH_ERR_UNSUPPORTED;
-    unsigned long long* p = g_scratch_ptr[dev].load(std::memory_order_acquire);
-    if (!p) {
-        std::lock_guard<std::mutex> lock(g_setup_mutex);
-        p = g_scratch_ptr[dev].load(std::memory_order_acquire);
-        if (!p) {
-            void* addr = nullptr;
-            if (cudaGetSymbolAddress(&addr, g_cull_scratch) != cudaSuccess || !addr) return LH_ERR_CUDA;
-            p = reinterpret_cast<unsigned long long*>(addr);
-            g_scratch_ptr[dev].store(p, std::memory_order_release);
-        }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) return LH_ERR_CUDA;
+    if (cs != cudaStreamCaptureStatusNone) {
+        unsigned long long* p = g_scratch_ptr[dev].load(std::memory_order_acquire);
+        if (!p) return LH_ERR_UNSUPPORTED;  // no call outside capture on this device yet
+        *out = p;
+        return LH_OK;
     }
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    void* addr = nullptr;
+    if (cudaGetSymbolAddress(&addr, g_cull_scratch) != cudaSuccess || !addr) return LH_ERR_CUDA;
+    unsigned long long* p = reinterpret_cast<unsigned long long*>(addr);
+    g_scratch_ptr[dev].store(p, std::memory_order_release);
     *out = p;
     return LH_OK;
 }
@@ -185,10 +189,10 @@ extern "C" lh_status lh_cull_instances_noalloc(const Instance* d_instances, uint
     if (((uintptr_t)d_instances & 15) || ((uintptr_t)d_sector & 7)) return LH_ERR_INVALID_ARGUMENT;
     const uint32_t tiles = (n_instances + kInstTile - 1) / kInstTile;
     if (tiles > kNoAllocMaxTiles) return LH_ERR_CAPACITY;  // more than 1,048,576 instances
-    unsigned long long* scratch = nullptr;
-    lh_status st = scratch_for_current_device(&scratch);
-    if (st != LH_OK) return st;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    unsigned long long* scratch = nullptr;
+    lh_status st = scratch_for_current_device(s, &scratch);
+    if (st != LH_OK) return st;
     // the previous call's look-back words and claim counter must not leak in
     if (cudaMemsetAsync(scratch, 0, sizeof(unsigned long long) * kNoAllocWords, s) != cudaSuccess) return LH_ERR_CUDA;
     if (tiles == 0) {

@@ -13,39 +13,32 @@
 #include "cull_phases.cuh"
 #include "frame_phases.cuh"
 #include "raster_phases.cuh"
+#include "waits.cuh"
 
 namespace lh {
 namespace {
 
-__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
-    uint32_t v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
 // Grid barrier on a counter that only grows within the launch: barrier k
 // completes when the counter reaches k * gridDim.x.  All blocks are
-// resident (cooperative launch), and the wait is bounded: on expiry
-// LH_FLAG_TIMEOUT is recorded and the block goes on (results flagged, no
-// hang).
-__device__ void grid_barrier(const FrameDev& f, uint32_t& epoch) {
+// resident (cooperative launch), and the wait is bounded: on expiry (or once
+// another block's wait has expired) LH_FLAG_TIMEOUT is recorded and the
+// barrier returns false; the kernel then stops instead of running its later
+// phases on data that no barrier ordered.
+__device__ bool grid_barrier(const FrameDev& f, uint32_t& epoch) {
+    __shared__ uint32_t s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         epoch++;
         const uint32_t target = epoch * gridDim.x;
         __threadfence();
         atomicAdd(&f.status[kStBarrier], 1u);
-        uint32_t spins = 0;
-        while (ld_acquire_u32(&f.status[kStBarrier]) < target) {
-            if (++spins >= kSpinLimit) {
-                atomicOr(&f.status[kStFlags], LH_FLAG_TIMEOUT);
-                break;
-            }
-            if (spins > 16) __nanosleep(spins > 1024 ? 256 : 32);
-        }
+        const bool ok = counter_wait(&f.status[kStBarrier], target, &f.status[kStFlags], kSpinLimit);
+        if (!ok) atomicOr(&f.status[kStFlags], LH_FLAG_TIMEOUT);
         __threadfence();
+        s_ok = ok ? 1u : 0u;
     }
     __syncthreads();
+    return s_ok != 0;
 }
 
 // Resets the raster words between the visibility and the shadow passes.
@@ -64,36 +57,36 @@ __global__ void __launch_bounds__(kPersistentThreads, 3) k_frame_persistent(Fram
     const uint32_t n_views = n_persp + 4;
     // clear every target; block 0 resets the per-view counters and the depth range
     for (uint32_t v = 0; v < n_views; v++) phase_clear_view(f, v, gtid, gstride, blockIdx.x == 0 && v == 0);
-    grid_barrier(f, epoch);
+    if (!grid_barrier(f, epoch)) return;
     const uint32_t inst_tiles = (f.n_instances + kInstTile - 1) / kInstTile;
     // visibility views: instance cull + prefix sum
     for (uint32_t vb = blockIdx.x; vb < inst_tiles * n_persp; vb += gridDim.x)
         phase_cull_instances_tile(f, vb / inst_tiles, inst_tiles);
-    grid_barrier(f, epoch);
+    if (!grid_barrier(f, epoch)) return;
     phase_cull_meshlets(f, 0, n_persp, &f.status[kStMlClaim]);
-    grid_barrier(f, epoch);
+    if (!grid_barrier(f, epoch)) return;
     phase_raster<0, false>(f, 0, n_persp, tune, &f.status[kStRasterClaim], s_raster, nullptr);
     phase_raster<0, true>(f, 0, n_persp, tune, &f.status[kStRasterClaimAlpha], s_raster, s_raster.av);
-    grid_barrier(f, epoch);
+    if (!grid_barrier(f, epoch)) return;
     phase_raster_big<0>(f);
-    grid_barrier(f, epoch);
+    if (!grid_barrier(f, epoch)) return;
     // depth range of the main view, then the cascade fit
     phase_depth_reduce(f, gtid, gstride);
-    grid_barrier(f, epoch);
+    if (!grid_barrier(f, epoch)) return;
     if (blockIdx.x == 0) {
         phase_fit(f);
         reset_raster_words(f);
     }
-    grid_barrier(f, epoch);
+    if (!grid_barrier(f, epoch)) return;
     // cascades
     for (uint32_t vb = blockIdx.x; vb < inst_tiles * 4; vb += gridDim.x)
         phase_cull_instances_tile(f, n_persp + vb / inst_tiles, inst_tiles);
-    grid_barrier(f, epoch);
+    if (!grid_barrier(f, epoch)) return;
     phase_cull_meshlets(f, n_persp, 4, &f.status[kStMlClaim]);
-    grid_barrier(f, epoch);
+    if (!grid_barrier(f, epoch)) return;
     phase_raster<1, false>(f, n_persp, 4, tune, &f.status[kStRasterClaim], s_raster, nullptr);
     phase_raster<1, true>(f, n_persp, 4, tune, &f.status[kStRasterClaimAlpha], s_raster, s_raster.av);
-    grid_barrier(f, epoch);
+    if (!grid_barrier(f, epoch)) return;
     phase_raster_big<1>(f);
 }
 

@@ -1,11 +1,15 @@
 """Differentiable lighting resolve for PyTorch.
 
 `DiffResolve(renderer, scene)` exposes the scene's vertex positions, normals,
-uvs and per-record base-colour factors as flat float32 CUDA tensors, plus
-the light direction and colour; calling it renders one frame through the C
-ABI and returns the HDR image as a tensor whose backward is the hand-written
-adjoint (lh_resolve_backward), wrapped in a libtorch
-torch::autograd::Function (lighthugger_gb300/torch_ext/diff_resolve.cpp).
+uvs and per-record base-colour factors as flat float32 CUDA tensors, the
+linear RGBA texels of every texture (base colour; metallic-roughness, whose
+green channel is the roughness and blue the metalness,
+render_geometry.comp:233-236), plus the light direction and colour; calling
+it renders one frame through the C ABI and returns the HDR image as a tensor
+whose backward is the hand-written adjoint (lh_resolve_backward), wrapped in
+a libtorch torch::autograd::Function
+(lighthugger_gb300/torch_ext/diff_resolve.cpp).  Forward and backward run on
+PyTorch's current CUDA stream.
 
 Visibility is held fixed: the backward differentiates the lighting of the
 forward's visibility buffer (triangle IDs, cascades and shadow-map compare
@@ -39,7 +43,7 @@ def extension():
     build_dir = os.path.join(_HERE, "_build", "torch_ext")
     os.makedirs(build_dir, exist_ok=True)
     lib()  # the C ABI library must be there
-    _ext = load(name="lh_torch_ext", sources=[os.path.join(_HERE, "torch_ext", "diff_resolve.cpp")],
+    _ext = load(name="lh_torch_ext", sources=[os.path.join(_HERE, "torch_ext", "diff_resolve.cpp")], with_cuda=True,
                 extra_include_paths=[os.path.join(_ROOT, "include"), os.path.join(cuda_home, "include")],
                 extra_cflags=["-O2"],
                 extra_ldflags=["-L" + os.path.dirname(LIB_PATH), "-l:liblh.so",
@@ -111,6 +115,20 @@ class DiffResolve:
         self.normals = torch.from_numpy(np.concatenate(nrm)).to(device).requires_grad_()
         self.uvs = torch.from_numpy(np.concatenate(uvs)).to(device).requires_grad_()
         self.base_color_factor = torch.from_numpy(np.stack(bcf)).to(device).requires_grad_()
+        # textures: the context's linear copies (what the kernels sample)
+        tex, tex_layout = [], []
+        for i in range(scene.desc.n_textures):
+            addr, w, h = renderer.texture_linear(i)
+            host = np.empty(w * h * 4, np.float32)
+            _check(lib().lh_download(renderer.ctx, host.ctypes.data, addr, host.nbytes), "lh_download", renderer.ctx)
+            tex.append(host)
+            tex_layout.append([w * h, addr])
+        self.texture_layout = torch.tensor(np.array(tex_layout, np.uint64).reshape(-1, 2).view(np.int64),
+                                           dtype=torch.int64)
+        self.texture_shapes = [(int(renderer.texture_linear(i)[2]), int(renderer.texture_linear(i)[1]))
+                               for i in range(scene.desc.n_textures)]
+        flat = np.concatenate(tex) if tex else np.zeros(0, np.float32)
+        self.textures = torch.from_numpy(flat).to(device).requires_grad_()
         f = uniforms_fields(scene.uniforms)
         self.light_dir = torch.tensor(f["sun_dir"], dtype=torch.float32, device=device).requires_grad_()
         self.light_color = torch.tensor(f["sun_intensity"], dtype=torch.float32, device=device).requires_grad_()
@@ -118,12 +136,23 @@ class DiffResolve:
     def parameters(self):
         return {"positions": self.positions, "normals": self.normals, "uvs": self.uvs,
                 "base_color_factor": self.base_color_factor, "light_dir": self.light_dir,
-                "light_color": self.light_color}
+                "light_color": self.light_color, "textures": self.textures}
+
+    def texture_offset(self, index):
+        """First float of texture `index` in `textures` (4 floats per texel)."""
+        return 4 * int(self.texture_layout[:index, 0].sum())
+
+    def texture_view(self, tensor, index):
+        """[h, w, 4] view of texture `index` inside a tensor shaped like
+        `textures` (the parameter itself or its gradient)."""
+        h, w = self.texture_shapes[index]
+        o = self.texture_offset(index)
+        return tensor[o:o + 4 * w * h].view(h, w, 4)
 
     def __call__(self, uniforms=None):
         torch = self.torch
         u = uniforms if uniforms is not None else self.scene.uniforms
         ub = torch.from_numpy(np.frombuffer(bytes(u), np.uint8).copy())
         return extension().resolve(self.renderer.ctx.value, ub, self.mesh_layout, self.record_layout,
-                                   self.instance_record, self.light_dir, self.light_color, self.positions,
-                                   self.normals, self.uvs, self.base_color_factor)
+                                   self.instance_record, self.texture_layout, self.light_dir, self.light_color,
+                                   self.positions, self.normals, self.uvs, self.base_color_factor, self.textures)

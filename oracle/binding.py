@@ -19,7 +19,7 @@ class FrameDesc(C.Structure):
     _fields_ = [("instances", C.c_void_p), ("n_instances", C.c_uint32), ("textures", C.c_void_p),
                 ("n_textures", C.c_uint32), ("uniforms", C.c_void_p), ("shadow_size", C.c_uint32),
                 ("max_instances", C.c_uint32), ("max_draws", C.c_uint32), ("threads", C.c_int32),
-                ("stages", C.c_uint32)]
+                ("stages", C.c_uint32), ("texture_linear", C.c_void_p)]
 
 
 class FrameOut(C.Structure):
@@ -49,6 +49,9 @@ def lib():
         L.lho_display_transform.restype = C.c_int
         L.lho_resolve_f64.argtypes = [C.POINTER(FrameDesc), C.POINTER(FrameOut), C.c_void_p]
         L.lho_resolve_f64.restype = C.c_int
+        L.lho_resolve_f64_pixels.argtypes = [C.POINTER(FrameDesc), C.POINTER(FrameOut), C.c_void_p, C.c_uint32,
+                                             C.c_void_p]
+        L.lho_resolve_f64_pixels.restype = C.c_int
         _lib = L
     return _lib
 
@@ -152,6 +155,29 @@ def resolve_f64(frame):
     if st != 0:
         raise RuntimeError("lho_resolve_f64 failed: %d" % st)
     return out
+
+
+def resolve_f64_pixels(frame, xy):
+    """FP64 resolve of the listed pixels (int array [n, 2] of x, y): [n, 4]."""
+    xy = np.ascontiguousarray(xy, dtype=np.uint32).reshape(-1, 2)
+    out = np.zeros((len(xy), 4), np.float64)
+    st = lib().lho_resolve_f64_pixels(C.byref(frame.desc), C.byref(frame.out), xy.ctypes.data, len(xy),
+                                      out.ctypes.data)
+    if st != 0:
+        raise RuntimeError("lho_resolve_f64_pixels failed: %d" % st)
+    return out
+
+
+def set_linear_textures(frame, textures):
+    """Sample the given linear RGBA float32 arrays (one per texture, [h, w, 4]
+    or flat; None keeps that texture's RGBA8 texels) in the frame's later
+    float64 resolves.  The arrays are kept alive by the frame and may be
+    changed in place between resolves."""
+    arrs = [None if t is None else np.ascontiguousarray(t, dtype=np.float32) for t in textures]
+    table = (C.c_void_p * max(1, len(arrs)))(*[None if a is None else a.ctypes.data for a in arrs])
+    frame._linear = (arrs, table)
+    frame.desc.texture_linear = C.cast(table, C.c_void_p)
+    return arrs
 
 
 def raster_triangle(clip, tri_id, kind, width, height, target=None):

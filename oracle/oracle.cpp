@@ -776,9 +776,15 @@ template <class T> static Tex4<T> sample_repeat(const lho_frame_desc* d, uint32_
     int64_t W = t.width, H = t.height;
     int64_t ia = ((i0 % W) + W) % W, ib = (((i0 + 1) % W) + W) % W;
     int64_t ja = ((j0 % H) + H) % H, jb = (((j0 + 1) % H) + H) % H;
+    const float* lin = d->texture_linear ? d->texture_linear[index] : nullptr;
     auto texel = [&](int64_t i, int64_t j) {
-        const uint8_t* p = tex + ((size_t)j * W + i) * 4;
         Tex4<T> r;
+        if (lin) {
+            const float* q = lin + ((size_t)j * W + i) * 4;
+            r.r = (T)q[0]; r.g = (T)q[1]; r.b = (T)q[2]; r.a = (T)q[3];
+            return r;
+        }
+        const uint8_t* p = tex + ((size_t)j * W + i) * 4;
         if (t.srgb) { r.r = (T)srgb_table[p[0]]; r.g = (T)srgb_table[p[1]]; r.b = (T)srgb_table[p[2]]; }
         else { r.r = (T)p[0] / (T)255; r.g = (T)p[1] / (T)255; r.b = (T)p[2] / (T)255; }
         r.a = (T)p[3] / (T)255;
@@ -1254,6 +1260,24 @@ int lho_resolve_f64(const lho_frame_desc* d, const lho_frame_out* in, double* hd
                 double* p = hdr64 + ((size_t)y * W + x) * 4;
                 p[0] = c.x; p[1] = c.y; p[2] = c.z; p[3] = c.w;
             }
+    });
+    return LH_OK;
+}
+
+int lho_resolve_f64_pixels(const lho_frame_desc* d, const lho_frame_out* in, const uint32_t* xy, uint32_t n,
+                           double* hdr64) {
+    if (!d || !in || !hdr64 || (n && !xy)) return LH_ERR_INVALID_ARGUMENT;
+    init_srgb();
+    const uint32_t W = d->uniforms->window_size.x, H = d->uniforms->window_size.y;
+    for (uint32_t i = 0; i < n; i++)
+        if (xy[2 * i] >= W || xy[2 * i + 1] >= H) return LH_ERR_INVALID_ARGUMENT;
+    Pool pool(d->threads);
+    pool.run(n, 16, [&](size_t b, size_t e) {
+        for (size_t i = b; i < e; i++) {
+            V4<double> c = resolve_pixel<double>(d, in, xy[2 * i], xy[2 * i + 1]);
+            double* p = hdr64 + i * 4;
+            p[0] = c.x; p[1] = c.y; p[2] = c.z; p[3] = c.w;
+        }
     });
     return LH_OK;
 }

@@ -11,8 +11,8 @@
  * Vulkan renderer with no tests, golden vectors or CPU path, and it cannot be
  * built or run here (no Vulkan, glslc or graphics stack, empty submodules).
  * The oracle is pinned instead by hand-derived known-answer tests
- * (tests/test_oracle_known_answers.py) and by the fixtures under
- * tests/golden/.
+ * (tests/test_oracle_known_answers.py) and by its float64 twin of the
+ * resolve (lho_resolve_f64).
  *
  * Evaluation-order contract (shared with the CUDA kernels so that integer,
  * visibility and depth results can be bit exact): every float operation is a
@@ -57,6 +57,11 @@ typedef struct lho_frame_desc {
     uint32_t max_draws;
     int32_t threads;             /* <= 0: all hardware threads */
     uint32_t stages;
+    /* optional (may be null; entries may be null): per texture, width*height
+     * linear RGBA floats sampled in place of its RGBA8 texels -- the values
+     * the kernels sample (sRGB decoded, / 255), so that the float64 resolve
+     * can be differentiated with respect to a texel */
+    const float* const* texture_linear;
 } lho_frame_desc;
 
 /* All buffers are caller allocated, in the layouts lh_frame_out documents:
@@ -108,6 +113,11 @@ int lho_display_transform(const float* hdr, uint32_t width, uint32_t height, con
  * statements); same inputs as lho_frame with visibility and shadow maps
  * already filled in `out`. */
 int lho_resolve_f64(const lho_frame_desc* desc, const lho_frame_out* in, double* hdr64);
+
+/* The same for the n pixels listed in xy (x, y pairs); hdr64 receives 4
+ * doubles per listed pixel. */
+int lho_resolve_f64_pixels(const lho_frame_desc* desc, const lho_frame_out* in, const uint32_t* xy, uint32_t n,
+                           double* hdr64);
 
 #ifdef __cplusplus
 }

@@ -2,9 +2,12 @@
 reference gradient: central differences (h = 1e-4) of the FP64 forward
 resolve over the same float buffers, visibility held fixed, upstream
 gradient N(0,1) on interior pixels (>= 2 px inside their triangle) and zero
-elsewhere.  Parameters: vertex positions, normals and uvs of triangles under
-those pixels, per-material base-colour factors, light direction and colour.
-Relative error bound 1e-3."""
+elsewhere.  Workload: the differentiable-resolve configuration at its full
+size (2,048 instances of 4 meshes, 512 x 512).  Parameters: vertex positions,
+normals and uvs of triangles under those pixels, per-material base-colour
+factors, light direction and colour, and texels -- base-colour texels and the
+metallic-roughness texel whose green channel is the roughness and blue the
+metalness (render_geometry.comp:233-236).  Relative error bound 1e-3."""
 import ctypes as C
 
 import numpy as np
@@ -61,7 +64,7 @@ class HostScene:
         return self.float_view(info_addr + 92, 3)
 
 
-def _smooth_pixels(oracle, fr, hs, trials=4, h=1e-4):
+def _smooth_pixels(oracle, fr, hs, textures, trials=4, h=1e-4):
     """Pixels whose FP64 radiance responds smoothly to joint random
     perturbations of every parameter (no clamp, texel centre, face sign,
     cascade or shadow-compare switch within reach): the second difference
@@ -71,6 +74,7 @@ def _smooth_pixels(oracle, fr, hs, trials=4, h=1e-4):
     for a in hs.infos:
         arrays += list(hs.vertex_arrays(a)) + [hs.bcf_view(a)]
     arrays.append(np.ctypeslib.as_array((C.c_float * 140).from_address(C.addressof(fr._ubuf)))[127:133])
+    arrays += list(textures)
     base = oracle.resolve_f64(fr)[..., :3]
     ok = np.ones(base.shape[:2], bool)
     for _ in range(trials):
@@ -89,29 +93,50 @@ def _smooth_pixels(oracle, fr, hs, trials=4, h=1e-4):
     return ok
 
 
+def _texture_linear(r, n_textures):
+    """The context's linear float4 copies of the textures (what the kernels
+    sample), as float32 [h, w, 4] host arrays."""
+    out = []
+    for i in range(n_textures):
+        addr, w, h = r.texture_linear(i)
+        out.append(r.download(addr, w * h * 16, np.float32).reshape(h, w, 4).copy())
+    return out
+
+
 def test_adjoint_matches_fp64_central_differences(native, oracle):
     import torch
     lh = native
-    scene = lh.Scene(4, width=256, height=256, n_instances=512).upload(0)
+    scene = lh.Scene(4).upload(0)
     d = scene.desc
-    cfg = lh.Config(width=d.width, height=d.height, shadow_size=1024, max_instances=1024, max_draws=200000)
+    assert (d.n_instances, d.width, d.height) == (2048, 512, 512)
+    cfg = lh.Config(width=d.width, height=d.height, shadow_size=d.shadow_size, max_instances=max(1024, d.n_instances),
+                    max_draws=400000)
     r = lh.Renderer(cfg)
     r.set_scene(scene)
     u = scene.uniforms
     r.frame(u)
-    fr = oracle.run_scene(scene, shadow_size=1024, max_instances=1024, max_draws=200000, uniforms=u)
+    fr = oracle.run_scene(scene, shadow_size=d.shadow_size, max_instances=max(1024, d.n_instances),
+                          max_draws=400000, uniforms=u)
     vis = fr.vis
     assert np.array_equal(r.visibility(), vis)
     hs = HostScene(scene)
-    interior = _interior_pixels(vis) & _smooth_pixels(oracle, fr, hs)
+    # the FP64 resolve samples the very texels the kernels sample; with them
+    # in place of the RGBA8 decode it must not change
+    tex = _texture_linear(r, d.n_textures)
+    before = oracle.resolve_f64(fr)
+    tex = oracle.set_linear_textures(fr, tex)
+    assert np.array_equal(oracle.resolve_f64(fr), before)
+    interior = _interior_pixels(vis) & _smooth_pixels(oracle, fr, hs, tex)
     rng = np.random.default_rng(11)
     ys, xs = np.nonzero(interior)
-    assert len(ys) > 200, "too few interior pixels: %d" % len(ys)
-    pick = rng.choice(len(ys), size=min(600, len(ys)), replace=False)
+    assert len(ys) > 400, "too few interior pixels: %d" % len(ys)
+    pick = rng.choice(len(ys), size=min(800, len(ys)), replace=False)
     G = np.zeros((d.height, d.width, 4), np.float32)
     G[ys[pick], xs[pick], :3] = rng.normal(size=(len(pick), 3)).astype(np.float32)
+    xy = np.stack([xs[pick], ys[pick]], axis=1)
+    Gp = G[ys[pick], xs[pick], :3].astype(np.float64)
 
-    # ---- GPU adjoint into per-mesh buffers
+    # ---- GPU adjoint into per-mesh and per-texture buffers
     info_addrs = sorted(hs.infos)
     dev = torch.device("cuda")
     bufs = {}
@@ -126,23 +151,23 @@ def test_adjoint_matches_fp64_central_differences(native, oracle):
     inst_rec = np.array([rec_dev.data_ptr() + 32 * info_addrs.index(int(a)) for a in hs.inst["mesh_info_address"]],
                         np.uint64)
     inst_rec_dev = torch.from_numpy(inst_rec.view(np.int64)).to(dev)
+    tex_grads = [torch.zeros(t.size, device=dev) for t in tex]
+    tex_tab = torch.tensor([t.data_ptr() for t in tex_grads], dtype=torch.int64, device=dev)
     light = torch.zeros(8, device=dev)
     g_dev = torch.from_numpy(G).to(dev)
-    t = lh.GradTargets(instance_grads=inst_rec_dev.data_ptr(), texture_grads=0, light_dir=light.data_ptr(),
-                       light_color=light.data_ptr() + 16)
+    t = lh.GradTargets(instance_grads=inst_rec_dev.data_ptr(), texture_grads=tex_tab.data_ptr(),
+                       light_dir=light.data_ptr(), light_color=light.data_ptr() + 16)
     torch.cuda.synchronize()
     st = lh.lib().lh_resolve_backward(r.ctx, g_dev.data_ptr(), C.byref(t), None)
     assert st == 0
     torch.cuda.synchronize()
     gpu = {a: {k: v.cpu().numpy().astype(np.float64) for k, v in b.items()} for a, b in bufs.items()}
     gl = light.cpu().numpy().astype(np.float64)
+    gtex = [g.cpu().numpy().astype(np.float64).reshape(tx.shape) for g, tx in zip(tex_grads, tex)]
 
-    # ---- FP64 reference: L(theta) = sum G . hdr64
-    Gd = G.astype(np.float64)
-
+    # ---- FP64 reference: L(theta) = sum G . hdr64 over the picked pixels
     def loss():
-        h = oracle.resolve_f64(fr)
-        return float((h[..., :3] * Gd[..., :3]).sum())
+        return float((oracle.resolve_f64_pixels(fr, xy)[:, :3] * Gp).sum())
 
     def fd(arr, i, h):
         """Central difference of L in arr[i] (a float32 view) with exact steps."""
@@ -171,7 +196,6 @@ def test_adjoint_matches_fp64_central_differences(native, oracle):
         checks.append((kind, got, ref))
 
     # vertices of triangles under picked pixels
-    uf = lh.uniforms_fields(u)
     vis_p = vis[ys[pick], xs[pick]]
     slots = (vis_p & np.uint64(0xFFFFFF)).astype(np.int64)
     tris = (vis_p >> np.uint64(24) & np.uint64(0xFF)).astype(np.int64)
@@ -205,11 +229,37 @@ def test_adjoint_matches_fp64_central_differences(native, oracle):
         record("light_dir", gl[c], g, ok)
         g, ok = fd(ub, 130 + c, 1e-4)  # sun_intensity at byte 520
         record("light_color", gl[4 + c], g, ok)
+    # texels: per texture the few with the largest GPU gradient.  1 x 1
+    # textures are the metallic-roughness ones (green = roughness, blue =
+    # metalness); the 256 x 256 ones the base colours (rgb)
+    kinds = {"roughness": 0, "metalness": 0, "base_color_texel": 0}
+    for i, (tx, gt) in enumerate(zip(tex, gtex)):
+        h_, w_ = tx.shape[:2]
+        flat = tx.reshape(-1)
+        gflat = gt.reshape(-1)
+        if h_ * w_ == 1:
+            for ch, kind in ((1, "roughness"), (2, "metalness")):
+                if gflat[ch] == 0.0 or kinds[kind] >= 6:
+                    continue  # material not under a picked pixel / enough checks
+                g, ok = fd(flat, ch, 1e-4)
+                record(kind, gflat[ch], g, ok)
+                kinds[kind] += 1
+        elif kinds["base_color_texel"] < 24:
+            rgb = np.abs(gt[..., :3]).reshape(-1)
+            for k in np.argsort(rgb)[::-1][:4]:
+                if rgb[k] == 0.0:
+                    break
+                j = (k // 3) * 4 + k % 3
+                g, ok = fd(flat, j, 1e-4)
+                record("base_color_texel", gflat[j], g, ok)
+                kinds["base_color_texel"] += 1
 
-    assert len(checks) >= 40, "only %d checks (%d skipped)" % (len(checks), skipped)
+    assert len(checks) >= 60, "only %d checks (%d skipped)" % (len(checks), skipped)
     by_kind = {}
     for kind, got, ref in checks:
         by_kind.setdefault(kind, []).append((got, ref))
+    for kind in ("roughness", "base_color_texel", "position", "normal", "uv", "light_dir", "light_color"):
+        assert len(by_kind.get(kind, [])) >= 2, "too few %s checks: %s" % (kind, {k: len(v) for k, v in by_kind.items()})
     report = []
     for kind, lst in by_kind.items():
         refs_ = np.array([b for a, b in lst])
@@ -220,4 +270,5 @@ def test_adjoint_matches_fp64_central_differences(native, oracle):
             if err > REL_TOL:
                 report.append("%s: gpu %.8g fp64 %.8g rel %.2e" % (kind, got, ref, err))
     assert not report, "\n".join(report[:20]) + "\n(%d checks, %d skipped)" % (len(checks), skipped)
-    print("adjoint: %d checks, %d skipped, worst relative error %.2e" % (len(checks), skipped, worst))
+    print("adjoint: %d checks (%s), %d skipped, worst relative error %.2e" % (
+        len(checks), {k: len(v) for k, v in by_kind.items()}, skipped, worst))

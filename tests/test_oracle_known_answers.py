@@ -149,7 +149,8 @@ def test_depth_range_reduction(native, oracle):
 
 def test_resolve_float_vs_float64(native, oracle):
     """The oracle's float resolve against its float64 twin: the HDR error of
-    the reference's float math itself (stated in the design doc)."""
+    the reference's float math itself, bounded at its 99th percentile over
+    covered pixels."""
     scene = native.Scene(1, width=320, height=180)
     fr = oracle.run_scene(scene, shadow_size=512)
     h64 = oracle.resolve_f64(fr)
