@@ -7,7 +7,17 @@ size (2,048 instances of 4 meshes, 512 x 512).  Parameters: vertex positions,
 normals and uvs of triangles under those pixels, per-material base-colour
 factors, light direction and colour, and texels -- base-colour texels and the
 metallic-roughness texel whose green channel is the roughness and blue the
-metalness (render_geometry.comp:233-236).  Relative error bound 1e-3."""
+metalness (render_geometry.comp:233-236).
+
+Error bound 1e-3, per kind of parameter: the relative error of the kind's
+vector of checked gradients, and each component's error relative to the
+larger of its own size and 5% of the kind's largest.  The floor is there for
+sums that nearly cancel: a uv gradient adds up per-pixel terms of size
+texture width x texel difference (~10 here) of both signs, and the float32
+sample position (u x width, ~1e-4 texel of rounding) moves the other axis'
+bilinear weight by as much -- a component of 0.8 built from terms of +-13
+then carries ~2e-3 of absolute rounding, float32's and the forward's
+alike."""
 import ctypes as C
 
 import numpy as np
@@ -64,11 +74,12 @@ class HostScene:
         return self.float_view(info_addr + 92, 3)
 
 
-def _smooth_pixels(oracle, fr, hs, textures, trials=4, h=1e-4):
+def _smooth_pixels(oracle, fr, hs, textures, trials=4, h=2e-4):
     """Pixels whose FP64 radiance responds smoothly to joint random
     perturbations of every parameter (no clamp, texel centre, face sign,
     cascade or shadow-compare switch within reach): the second difference
-    must stay far below the first."""
+    must stay far below the first.  The reach (2e-4, relative) is twice the
+    central differences' step, so no kink lies inside their window."""
     rng = np.random.default_rng(3)
     arrays = []
     for a in hs.infos:
@@ -103,30 +114,37 @@ def _texture_linear(r, n_textures):
     return out
 
 
-def test_adjoint_matches_fp64_central_differences(native, oracle):
+def _adjoint_checks(lh, oracle, scene, r, u):
+    """GPU adjoint of the frame seen with uniforms `u` against FP64 central
+    differences: returns the (kind, gpu, fp64, where) checks and the skipped
+    count."""
     import torch
-    lh = native
-    scene = lh.Scene(4).upload(0)
     d = scene.desc
-    assert (d.n_instances, d.width, d.height) == (2048, 512, 512)
-    cfg = lh.Config(width=d.width, height=d.height, shadow_size=d.shadow_size, max_instances=max(1024, d.n_instances),
-                    max_draws=400000)
-    r = lh.Renderer(cfg)
-    r.set_scene(scene)
-    u = scene.uniforms
     r.frame(u)
     fr = oracle.run_scene(scene, shadow_size=d.shadow_size, max_instances=max(1024, d.n_instances),
                           max_draws=400000, uniforms=u)
     vis = fr.vis
     assert np.array_equal(r.visibility(), vis)
     hs = HostScene(scene)
-    # the FP64 resolve samples the very texels the kernels sample; with them
-    # in place of the RGBA8 decode it must not change
+    # the FP64 resolve samples the very texels the kernels sample (float32
+    # values; its own RGBA8 decode divides in float64): the image moves by
+    # rounding only
     tex = _texture_linear(r, d.n_textures)
     before = oracle.resolve_f64(fr)
     tex = oracle.set_linear_textures(fr, tex)
-    assert np.array_equal(oracle.resolve_f64(fr), before)
+    base = oracle.resolve_f64(fr)
+    assert float(np.nanmax(np.abs(base - before))) < 1e-6
     interior = _interior_pixels(vis) & _smooth_pixels(oracle, fr, hs, tex)
+    # pixels the sun reaches (the sun term changes with the light colour):
+    # roughness and metalness act there through the BRDF, so the picks are
+    # drawn from them (in shadow only the ambient term is left)
+    ub = np.ctypeslib.as_array((C.c_float * 140).from_address(C.addressof(fr._ubuf)))
+    saved = ub[130:133].copy()
+    ub[130:133] = 0.0
+    dark = oracle.resolve_f64(fr)
+    ub[130:133] = saved
+    lit = np.abs(base - dark)[..., :3].sum(-1) > 1e-3 * np.abs(base)[..., :3].sum(-1) + 1e-9
+    interior &= lit
     rng = np.random.default_rng(11)
     ys, xs = np.nonzero(interior)
     assert len(ys) > 400, "too few interior pixels: %d" % len(ys)
@@ -136,15 +154,22 @@ def test_adjoint_matches_fp64_central_differences(native, oracle):
     xy = np.stack([xs[pick], ys[pick]], axis=1)
     Gp = G[ys[pick], xs[pick], :3].astype(np.float64)
 
-    # ---- GPU adjoint into per-mesh and per-texture buffers
+    # ---- GPU adjoint into per-vertex-buffer, per-record and per-texture
+    # buffers: MeshInfo records of one mesh with different materials share
+    # its vertex buffers, so their vertex gradients go to one buffer (what a
+    # central difference of a shared vertex sees)
     info_addrs = sorted(hs.infos)
     dev = torch.device("cuda")
-    bufs = {}
+    vbufs, bufs = {}, {}
     rec = np.zeros((len(info_addrs), 4), np.uint64)
     for k, a in enumerate(info_addrs):
         nv = len(hs.infos[a].positions)
-        b = {"pos": torch.zeros(nv * 3, device=dev), "nrm": torch.zeros(nv * 3, device=dev),
-             "uv": torch.zeros(nv * 2, device=dev), "bcf": torch.zeros(4, device=dev)}
+        key = int(hs.infos[a].mi["positions"])
+        if key not in vbufs:
+            vbufs[key] = {"pos": torch.zeros(nv * 3, device=dev), "nrm": torch.zeros(nv * 3, device=dev),
+                          "uv": torch.zeros(nv * 2, device=dev)}
+        b = dict(vbufs[key])
+        b["bcf"] = torch.zeros(4, device=dev)
         bufs[a] = b
         rec[k] = [b["pos"].data_ptr(), b["nrm"].data_ptr(), b["uv"].data_ptr(), b["bcf"].data_ptr()]
     rec_dev = torch.from_numpy(rec.view(np.int64)).to(dev)
@@ -186,14 +211,14 @@ def test_adjoint_matches_fp64_central_differences(native, oracle):
         g2 = (lp2 - lm2) / (dp2 - dm2)
         return g1, abs(g1 - g2) <= 1e-3 * (abs(g1) + abs(g2)) + 1e-9
 
-    checks, skipped, worst = [], 0, 0.0
+    checks, skipped = [], 0
 
-    def record(kind, got, ref, ok):
+    def record(kind, got, ref, ok, where=""):
         nonlocal skipped
         if not ok:
             skipped += 1
             return
-        checks.append((kind, got, ref))
+        checks.append((kind, got, ref, where))
 
     # vertices of triangles under picked pixels
     vis_p = vis[ys[pick], xs[pick]]
@@ -212,18 +237,17 @@ def test_adjoint_matches_fp64_central_differences(native, oracle):
         P, N, UV = hs.vertex_arrays(a)
         for c in range(3):
             g, ok = fd(P[vi], c, 1e-4 * max(1.0, abs(float(P[vi][c]))))
-            record("position", gpu[a]["pos"][vi * 3 + c], g, ok)
+            record("position", gpu[a]["pos"][vi * 3 + c], g, ok, "mesh %#x vertex %d axis %d" % (a, vi, c))
             g, ok = fd(N[vi], c, 1e-4)
-            record("normal", gpu[a]["nrm"][vi * 3 + c], g, ok)
+            record("normal", gpu[a]["nrm"][vi * 3 + c], g, ok, "mesh %#x vertex %d axis %d" % (a, vi, c))
         for c in range(2):
             g, ok = fd(UV[vi], c, 1e-4)
-            record("uv", gpu[a]["uv"][vi * 2 + c], g, ok)
+            record("uv", gpu[a]["uv"][vi * 2 + c], g, ok, "mesh %#x vertex %d axis %d" % (a, vi, c))
     for a in info_addrs[:3]:
         bv = hs.bcf_view(a)
         for c in range(3):
             g, ok = fd(bv, c, 1e-4)
             record("base_color_factor", gpu[a]["bcf"][c], g, ok)
-    ub = np.ctypeslib.as_array((C.c_float * 140).from_address(C.addressof(fr._ubuf)))
     for c in range(3):
         g, ok = fd(ub, 127 + c, 1e-4)  # sun_dir at byte 508
         record("light_dir", gl[c], g, ok)
@@ -239,7 +263,7 @@ def test_adjoint_matches_fp64_central_differences(native, oracle):
         gflat = gt.reshape(-1)
         if h_ * w_ == 1:
             for ch, kind in ((1, "roughness"), (2, "metalness")):
-                if gflat[ch] == 0.0 or kinds[kind] >= 6:
+                if gflat[ch] == 0.0 or kinds[kind] >= 8:
                     continue  # material not under a picked pixel / enough checks
                 g, ok = fd(flat, ch, 1e-4)
                 record(kind, gflat[ch], g, ok)
@@ -254,21 +278,50 @@ def test_adjoint_matches_fp64_central_differences(native, oracle):
                 record("base_color_texel", gflat[j], g, ok)
                 kinds["base_color_texel"] += 1
 
-    assert len(checks) >= 60, "only %d checks (%d skipped)" % (len(checks), skipped)
+    return checks, skipped
+
+
+def test_adjoint_matches_fp64_central_differences(native, oracle):
+    """The differentiable-resolve workload at full size, seen from its own
+    camera and from one 4 m higher looking 0.3 rad down (from the first, the
+    lit interior pixels are nearly all on two materials; the second adds
+    three more)."""
+    lh = native
+    scene = lh.Scene(4).upload(0)
+    d = scene.desc
+    assert (d.n_instances, d.width, d.height) == (2048, 512, 512)
+    r = lh.Renderer(lh.Config(width=d.width, height=d.height, shadow_size=d.shadow_size,
+                              max_instances=max(1024, d.n_instances), max_draws=400000))
+    r.set_scene(scene)
+    cam = lh.uniforms_fields(scene.uniforms)["camera_pos"].astype(float)
+    high = lh.make_uniforms((cam[0], cam[1] + 4.0, cam[2]), 1.0, -0.3, 60.0, d.width, d.height, d.n_instances)
+    checks, skipped, worst = [], 0, 0.0
+    for cam_i, u in enumerate((scene.uniforms, high)):
+        c, sk = _adjoint_checks(lh, oracle, scene, r, u)
+        checks += [(k, g, f, "camera %d %s" % (cam_i, w)) for k, g, f, w in c]
+        skipped += sk
+    assert len(checks) >= 120, "only %d checks (%d skipped)" % (len(checks), skipped)
     by_kind = {}
-    for kind, got, ref in checks:
-        by_kind.setdefault(kind, []).append((got, ref))
-    for kind in ("roughness", "base_color_texel", "position", "normal", "uv", "light_dir", "light_color"):
-        assert len(by_kind.get(kind, [])) >= 2, "too few %s checks: %s" % (kind, {k: len(v) for k, v in by_kind.items()})
-    report = []
+    for kind, got, ref, where in checks:
+        by_kind.setdefault(kind, []).append((got, ref, where))
+    need = {"roughness": 4, "metalness": 4, "base_color_texel": 8, "position": 8, "normal": 8, "uv": 8,
+            "base_color_factor": 4, "light_dir": 2, "light_color": 2}
+    for kind, n in need.items():
+        assert len(by_kind.get(kind, [])) >= n, "too few %s checks: %s" % (kind, {k: len(v) for k, v in by_kind.items()})
+    report, vec_err = [], {}
     for kind, lst in by_kind.items():
-        refs_ = np.array([b for a, b in lst])
+        gots = np.array([a for a, b, w in lst])
+        refs_ = np.array([b for a, b, w in lst])
         scale = max(np.abs(refs_).max(), 1e-6)
-        for got, ref in lst:
-            err = abs(got - ref) / max(abs(ref), 1e-2 * scale)
+        vec_err[kind] = float(np.linalg.norm(gots - refs_) / max(np.linalg.norm(refs_), 1e-12))
+        if vec_err[kind] > REL_TOL:
+            report.append("%s: vector relative error %.2e" % (kind, vec_err[kind]))
+        for got, ref, where in lst:
+            err = abs(got - ref) / max(abs(ref), 5e-2 * scale)
             worst = max(worst, err)
             if err > REL_TOL:
-                report.append("%s: gpu %.8g fp64 %.8g rel %.2e" % (kind, got, ref, err))
+                report.append("%s %s: gpu %.8g fp64 %.8g rel %.2e" % (kind, where, got, ref, err))
     assert not report, "\n".join(report[:20]) + "\n(%d checks, %d skipped)" % (len(checks), skipped)
-    print("adjoint: %d checks (%s), %d skipped, worst relative error %.2e" % (
-        len(checks), {k: len(v) for k, v in by_kind.items()}, skipped, worst))
+    print("adjoint: %d checks (%s), %d skipped, worst component error %.2e, vector errors %s" % (
+        len(checks), {k: len(v) for k, v in by_kind.items()}, skipped, worst,
+        {k: "%.1e" % v for k, v in vec_err.items()}))

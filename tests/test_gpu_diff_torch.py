@@ -94,7 +94,9 @@ def _roughness_textures(dr):
 
 def test_runs_on_the_current_stream(native):
     """Forward and backward enqueued on a side stream give the default
-    stream's image and gradients."""
+    stream's image and gradients (up to the order of the adjoint's float
+    atomic sums, which no two runs share: the tolerance is relative to each
+    parameter group's largest gradient)."""
     import torch
     from lighthugger_gb300.diff import DiffResolve
     lh = native
@@ -118,7 +120,10 @@ def test_runs_on_the_current_stream(native):
     torch.cuda.synchronize()
     assert torch.equal(got_img, ref_img)
     for k, v in dr.parameters().items():
-        assert torch.allclose(v.grad, ref[k], rtol=1e-5, atol=1e-6), k
+        scale = float(ref[k].abs().max())
+        assert scale > 0, k
+        err = float((v.grad - ref[k]).abs().max())
+        assert err <= 1e-4 * scale, (k, err, scale)
 
 
 def test_roughness_fits_a_target(native):
