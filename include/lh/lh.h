@@ -118,6 +118,8 @@ typedef struct lh_device_status {
     uint32_t visible_alpha_clip[40]; /* per view: num_alpha_clip */
     uint32_t big_triangles;          /* triangles sent to the tiled raster path */
     uint32_t clipped_triangles;      /* triangles clipped (last raster pass) */
+    uint32_t fragments[2];           /* fragments written this frame (one 64-bit depth-test reduction
+                                        each): [0] visibility views, [1] shadow views */
 } lh_device_status;
 
 typedef struct lh_ctx lh_ctx;

@@ -74,7 +74,7 @@ class DeviceStatus(C.Structure):
     _fields_ = [("flags", C.c_uint32), ("n_views", C.c_uint32), ("visible_instances", C.c_uint32 * 40),
                 ("candidate_meshlets", C.c_uint32 * 40), ("visible_opaque", C.c_uint32 * 40),
                 ("visible_alpha_clip", C.c_uint32 * 40), ("big_triangles", C.c_uint32),
-                ("clipped_triangles", C.c_uint32)]
+                ("clipped_triangles", C.c_uint32), ("fragments", C.c_uint32 * 2)]
 
 
 SCHEDULE_DEFAULT, SCHEDULE_PER_STAGE, SCHEDULE_PERSISTENT, SCHEDULE_PER_VIEW = 0, 1, 2, 3

@@ -828,6 +828,8 @@ lh_status lh_read_status(lh_ctx* c, lh_device_status* out) {
     out->flags = words[kStFlags];
     out->big_triangles = words[kStBigPacked + 1] >> 8;  // high word of the packed u64: count << 8
     out->clipped_triangles = words[kStClipCount];
+    out->fragments[0] = words[kStFragVis];
+    out->fragments[1] = words[kStFragShadow];
     out->n_views = c->n_views_last;
     for (uint32_t v = 0; v < c->n_views_last && v < 40; v++) {
         unsigned long long counter = 0;

@@ -105,6 +105,8 @@ enum StatusWord : uint32_t {
     kStBarrier = 7,    // grid barrier of the persistent kernel
     kStBigPacked = 8,  // u64 (words 8-9): big-triangle count << 40 | chunk count
     kStRasterClaimAlpha = 10,  // raster claims of the alpha-clip class
+    kStFragVis = 11,     // fragments written this frame, visibility views (statistics)
+    kStFragShadow = 12,  // the same, shadow views
     kStWords = 16
 };
 

@@ -364,27 +364,36 @@ __device__ __forceinline__ AlphaTri alpha_of(const TriSetup& t, const AlphaSrc& 
     return alpha_setup(as.av[t.verts & 0xFFu], as.av[(t.verts >> 8) & 0xFFu], as.av[(t.verts >> 16) & 0xFFu], as.tex);
 }
 
+// The bbox pixels of one triangle by one lane; `nfrag` counts the fragments
+// written (depth-test reductions issued).
 template <int KIND>
-__device__ __forceinline__ void raster_lane(const TriSetup& t, void* target, uint32_t W) {
+__device__ __forceinline__ void raster_lane(const TriSetup& t, void* target, uint32_t W, uint32_t& nfrag) {
     if (t.bias & 8u) {
         const EdgeSteps es = edge_steps(t);
         for (int32_t ry = 0; ry <= t.py1 - t.py0; ry++)
             for (int32_t rx = 0; rx <= t.px1 - t.px0; rx++) {
                 float d;
-                if (cover_step(t, es, rx, ry, d)) write_fragment<KIND>(target, W, t.px0 + rx, t.py0 + ry, d, t.id);
+                if (cover_step(t, es, rx, ry, d)) {
+                    write_fragment<KIND>(target, W, t.px0 + rx, t.py0 + ry, d, t.id);
+                    nfrag++;
+                }
             }
         return;
     }
     for (int32_t py = t.py0; py <= t.py1; py++)
         for (int32_t px = t.px0; px <= t.px1; px++) {
             float d;
-            if (cover(t, px, py, d)) write_fragment<KIND>(target, W, px, py, d, t.id);
+            if (cover(t, px, py, d)) {
+                write_fragment<KIND>(target, W, px, py, d, t.id);
+                nfrag++;
+            }
         }
 }
 
 // All lanes of a warp cover the pixels of one triangle's bbox.
 template <int KIND>
-__device__ __forceinline__ void raster_warp(const TriSetup& t, void* target, uint32_t W, uint32_t lane) {
+__device__ __forceinline__ void raster_warp(const TriSetup& t, void* target, uint32_t W, uint32_t lane,
+                                            uint32_t& nfrag) {
     const uint32_t w = (uint32_t)(t.px1 - t.px0 + 1);
     const uint32_t npx = w * (uint32_t)(t.py1 - t.py0 + 1);
     const float inv_w = 1.0f / (float)w;
@@ -395,7 +404,10 @@ __device__ __forceinline__ void raster_warp(const TriSetup& t, void* target, uin
         else if (rx >= (int32_t)w) { ry++; rx -= (int32_t)w; }
         int32_t px = t.px0 + rx, py = t.py0 + ry;
         float d;
-        if (cover(t, px, py, d)) write_fragment<KIND>(target, W, px, py, d, t.id);
+        if (cover(t, px, py, d)) {
+            write_fragment<KIND>(target, W, px, py, d, t.id);
+            nfrag++;
+        }
     }
 }
 
@@ -403,24 +415,29 @@ __device__ __forceinline__ void raster_warp(const TriSetup& t, void* target, uin
 // state stays out of the register allocation of the opaque paths (the
 // launch bounds cap the whole call tree; alpha triangles are the rare case).
 template <int KIND>
-__device__ __noinline__ void raster_lane_alpha(const FrameDev& f, const TriSetup& t, void* target, uint32_t W,
-                                               const AlphaSrc& as) {
+__device__ __noinline__ uint32_t raster_lane_alpha(const FrameDev& f, const TriSetup& t, void* target, uint32_t W,
+                                                   const AlphaSrc& as) {
     const AlphaTri at = alpha_of(t, as);
+    uint32_t n = 0;
     for (int32_t py = t.py0; py <= t.py1; py++)
         for (int32_t px = t.px0; px <= t.px1; px++) {
             float d;
-            if (cover(t, px, py, d) && alpha_pass(f, at, px, py, W, as.H))
+            if (cover(t, px, py, d) && alpha_pass(f, at, px, py, W, as.H)) {
                 write_fragment<KIND>(target, W, px, py, d, t.id);
+                n++;
+            }
         }
+    return n;
 }
 
 template <int KIND>
-__device__ __noinline__ void raster_warp_alpha(const FrameDev& f, const TriSetup& t, void* target, uint32_t W,
-                                               uint32_t lane, const AlphaSrc& as) {
+__device__ __noinline__ uint32_t raster_warp_alpha(const FrameDev& f, const TriSetup& t, void* target, uint32_t W,
+                                                   uint32_t lane, const AlphaSrc& as) {
     const uint32_t w = (uint32_t)(t.px1 - t.px0 + 1);
     const uint32_t npx = w * (uint32_t)(t.py1 - t.py0 + 1);
     const float inv_w = 1.0f / (float)w;
     const AlphaTri at = alpha_of(t, as);
+    uint32_t n = 0;
     for (uint32_t p = lane; p < npx; p += 32) {
         int32_t ry = (int32_t)(((float)p + 0.5f) * inv_w);
         int32_t rx = (int32_t)p - ry * (int32_t)w;
@@ -428,8 +445,12 @@ __device__ __noinline__ void raster_warp_alpha(const FrameDev& f, const TriSetup
         else if (rx >= (int32_t)w) { ry++; rx -= (int32_t)w; }
         int32_t px = t.px0 + rx, py = t.py0 + ry;
         float d;
-        if (cover(t, px, py, d) && alpha_pass(f, at, px, py, W, as.H)) write_fragment<KIND>(target, W, px, py, d, t.id);
+        if (cover(t, px, py, d) && alpha_pass(f, at, px, py, W, as.H)) {
+            write_fragment<KIND>(target, W, px, py, d, t.id);
+            n++;
+        }
     }
+    return n;
 }
 
 __device__ __forceinline__ TriSetup shfl_setup(const TriSetup& s, int src) {
@@ -473,7 +494,8 @@ struct MeshletWork {
 // ALPHA: the alpha-clip class (double sided, alpha tested per fragment).
 template <int KIND, bool ALPHA>
 __device__ __forceinline__ void raster_meshlet(const FrameDev& f, const MeshletWork w, RasterTune tune, SnapV* sv,
-                                               uint8_t* so, uint32_t* micro_words, AlphaVert* av, uint32_t lane) {
+                                               uint8_t* so, uint32_t* micro_words, AlphaVert* av, uint32_t lane,
+                                               uint32_t& nfrag) {
     const uint32_t nv = w.nv, nt = w.nt, W = w.W, H = w.H;
     const MeshInfoRaster& mi = w.mi;
     AlphaSrc as{av, 0u, H};
@@ -579,8 +601,8 @@ __device__ __forceinline__ void raster_meshlet(const FrameDev& f, const MeshletW
                         }
                         uint32_t npx = (uint32_t)(st.px1 - st.px0 + 1) * (uint32_t)(st.py1 - st.py0 + 1);
                         if (npx <= tune.small_px) {
-                            if (ALPHA) raster_lane_alpha<KIND>(f, st, w.target, W, as);
-                            else raster_lane<KIND>(st, w.target, W);
+                            if (ALPHA) nfrag += raster_lane_alpha<KIND>(f, st, w.target, W, as);
+                            else raster_lane<KIND>(st, w.target, W, nfrag);
                         } else if (npx <= (KIND == 1 && LH_SHADOW_MEDIUM_PX ? min(tune.medium_px, (uint32_t)LH_SHADOW_MEDIUM_PX)
                                                                             : tune.medium_px)) {
                             medium = true;
@@ -601,11 +623,19 @@ __device__ __forceinline__ void raster_meshlet(const FrameDev& f, const MeshletW
             int src = __ffs(mask) - 1;
             mask &= mask - 1;
             TriSetup b = shfl_setup(st, src);
-            if (ALPHA) raster_warp_alpha<KIND>(f, b, w.target, W, lane, as);
-            else raster_warp<KIND>(b, w.target, W, lane);
+            if (ALPHA) nfrag += raster_warp_alpha<KIND>(f, b, w.target, W, lane, as);
+            else raster_warp<KIND>(b, w.target, W, lane, nfrag);
         }
     }
     __syncwarp();
+}
+
+// Adds the warp's fragment count to the frame's statistics word of the
+// pass (visibility or shadow views); called by every lane of the warp.
+template <int KIND>
+__device__ __forceinline__ void count_fragments(const FrameDev& f, uint32_t nfrag) {
+    const uint32_t total = __reduce_add_sync(0xFFFFFFFFu, nfrag);
+    if ((threadIdx.x & 31) == 0 && total) atomicAdd(&f.status[KIND == 0 ? kStFragVis : kStFragShadow], total);
 }
 
 // One warp per visible meshlet of views [view_begin, view_begin + n_views)
@@ -669,6 +699,7 @@ __device__ void phase_raster(const FrameDev& f, uint32_t view_begin, uint32_t n_
     // view: with many views (probes) a search from view 0 is a chain of
     // dependent shared-memory loads per unit.
     uint32_t v = 0;
+    uint32_t nfrag = 0;  // fragments this lane wrote
     for (;;) {
         if (unit >= unit_end) {
             if (!dynamic) break;
@@ -709,8 +740,9 @@ __device__ void phase_raster(const FrameDev& f, uint32_t view_begin, uint32_t n_
         }
         if (part * 32u >= nt) continue;  // this quarter holds no triangles
         const MeshletWork w{view, slot, part, split, nv, nt, W, H, target, hw, hh, &s_vp[v], transform, mi, 0u, 0u, inst};
-        raster_meshlet<KIND, ALPHA>(f, w, tune, sv, so, s_micro[warp], ALPHA ? s_av[warp] : nullptr, lane);
+        raster_meshlet<KIND, ALPHA>(f, w, tune, sv, so, s_micro[warp], ALPHA ? s_av[warp] : nullptr, lane, nfrag);
     }
+    count_fragments<KIND>(f, nfrag);
 }
 
 // Edge function of edge a->b at pixel centre (px, py).
@@ -751,8 +783,8 @@ __device__ __forceinline__ uint32_t upper_bound_warp(const uint32_t* base, uint3
 // passed as its queue entry: a reference to the caller's copy would keep
 // that copy in local memory on the opaque path too.
 template <int KIND>
-__device__ __noinline__ void raster_chunk_alpha(const FrameDev& f, const BigTri* entry, int32_t x0, int32_t x1,
-                                                int32_t y0, int32_t y1, uint32_t lane) {
+__device__ __noinline__ uint32_t raster_chunk_alpha(const FrameDev& f, const BigTri* entry, int32_t x0, int32_t x1,
+                                                    int32_t y0, int32_t y1, uint32_t lane) {
     const BigTri b = *entry;
     const ViewDev* vw = f.views + b.view;
     void* target = vw->target;
@@ -763,11 +795,16 @@ __device__ __noinline__ void raster_chunk_alpha(const FrameDev& f, const BigTri*
     t.z0 = b.z0; t.s1 = b.s1; t.s2 = b.s2;
     t.id = b.id;
     t.bias = b.bias;
+    uint32_t n = 0;
     for (int32_t py = y0; py <= y1; py++)
         for (int32_t px = x0 + (int32_t)lane; px <= x1; px += 32) {
             float d;
-            if (cover(t, px, py, d) && alpha_pass(f, at, px, py, W, H)) write_fragment<KIND>(target, W, px, py, d, t.id);
+            if (cover(t, px, py, d) && alpha_pass(f, at, px, py, W, H)) {
+                write_fragment<KIND>(target, W, px, py, d, t.id);
+                n++;
+            }
         }
+    return n;
 }
 
 // One warp per chunk of a big triangle (16 x 32 pixels in the visibility
@@ -790,6 +827,7 @@ __device__ void phase_raster_big(const FrameDev& f) {
     uint32_t t_idx = 0, t_base = 1, t_end = 0;  // chunk range [t_base, t_end) of triangle t_idx (empty at first)
     uint32_t c = (uint32_t)min((uint64_t)gwarp * kChunkBatch, (uint64_t)total32);
     uint32_t c_end = (uint32_t)min((uint64_t)gwarp * kChunkBatch + kChunkBatch, (uint64_t)total32);
+    uint32_t nfrag = 0;
     for (;;) {
         if (c >= c_end) {
             if (dyn_base >= total32) break;
@@ -835,7 +873,7 @@ __device__ void phase_raster_big(const FrameDev& f) {
         void* target = vw->target;
         const uint32_t W = vw->width;
         if (b.bias & kBiasAlpha) {
-            raster_chunk_alpha<KIND>(f, f.big + i, x0, x1, y0, y1, lane);
+            nfrag += raster_chunk_alpha<KIND>(f, f.big + i, x0, x1, y0, y1, lane);
             continue;
         }
         // edge functions at the top of the lane's column, then one add per
@@ -857,6 +895,7 @@ __device__ void phase_raster_big(const FrameDev& f) {
                     d = d > 0.0f ? d : 0.0f;
                     d = d < 1.0f ? d : 1.0f;
                     write_fragment<KIND>(target, W, px, py, d, b.id);
+                    nfrag++;
                 }
             }
             continue;
@@ -873,9 +912,11 @@ __device__ void phase_raster_big(const FrameDev& f) {
                 d = d > 0.0f ? d : 0.0f;
                 d = d < 1.0f ? d : 1.0f;
                 write_fragment<KIND>(target, W, px, py, d, b.id);
+                nfrag++;
             }
         }
     }
+    count_fragments<KIND>(f, nfrag);
 }
 
 }  // namespace

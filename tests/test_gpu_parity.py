@@ -92,6 +92,10 @@ def test_config2_full_parity(native, oracle):
     scene, r, fr, st, cap = _run(native, oracle, 2)
     stats = _assert_parity(r, fr, 200000, cap, st)
     assert stats["covered"] > 100000
+    # the raster's fragment counters (its depth-test reductions) equal the
+    # oracle's covered, alpha-passed fragments of the same frame
+    rs = fr.raster_stats
+    assert (st.fragments[0], st.fragments[1]) == (rs["visibility"]["fragments"], rs["shadow"]["fragments"])
 
 
 def test_overflow_capacities_flagged(native, oracle):
