@@ -44,13 +44,22 @@ INSTANCE_BYTES = 112
 MESHLET_BYTES = 56
 PREFIX_ENTRY_BYTES = 8
 DRAW_WRITE_BYTES = 8 + 16
+RASTER_DRAW_BYTES = 48       # the raster draw record written per visible meshlet, read by the raster
 VIS_PIXEL_BYTES = 8
 HDR_PIXEL_BYTES = 16
-# dram__bytes_read.sum + dram__bytes_write.sum of one k_resolve launch of the
-# config-2 frame, from an ncu --set full capture of this bench's plain frame
-# (17.841 MB read + 2.6 KB written); traffic below the algorithmic bytes
-# means the kernel found its inputs in L2
-RESOLVE_TRAFFIC_C2 = 17.841152e6 + 2.56e3
+RASTER_TRI_BYTES = 3 + 0.52 * (4 + 12)  # micro indices + ~0.52 unique vertices (index + fp32 position)
+FRAGMENT_BYTES = 8           # one 64-bit depth-test reduction per fragment
+# Per-kernel DRAM bytes of the workload, from the committed ncu capture
+# summary (profiles/dram_bytes_c2_frame.txt: command, commit, one line per
+# kernel); `traffic` in the roofline is read from there, never measured here.
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "dram_bytes_c2_frame.txt")
+STAGE_KERNELS = {
+    "raster": ("k_raster<0, 3>", "k_raster_alpha<0>", "k_raster_big<0>", "k_hiz", "k_occlusion_filter"),
+    "shadow_raster": ("k_raster<1, 3>", "k_raster_alpha<1>", "k_raster_big<1>"),
+    "resolve": ("k_resolve<1>",),
+    "cull_meshlets": ("k_cull_meshlets",),
+    "depth_fit": ("k_depth_reduce_fit",),
+}
 
 
 def _env_rank():
@@ -106,6 +115,50 @@ def _measured_peak_hbm():
         return 6800.0, "fallback"
 
 
+def committed_traffic(stage):
+    """DRAM bytes per frame of a stage's kernels from the committed capture
+    summary, with the summary's provenance line; (None, None) if absent."""
+    try:
+        with open(TRAFFIC_FILE) as f:
+            lines = f.read().splitlines()
+    except OSError:
+        return None, None
+    source = next((l[2:].strip() for l in lines if l.startswith("# capture:")), TRAFFIC_FILE)
+    per = {}
+    for l in lines:
+        if not l.strip() or l.startswith("#"):
+            continue
+        name, rd, wr = l.rsplit(None, 2)
+        per[name.strip()] = float(rd) + float(wr)
+    names = [n for n in STAGE_KERNELS.get(stage, ()) if n in per]
+    if not names:
+        return None, None
+    return sum(per[n] for n in names), "profiles/dram_bytes_c2_frame.txt: " + source
+
+
+def atomic_peak(lh, torch, stream, mib=16, reps=16):
+    """Reductions per second of the raster's depth-test instruction
+    (lh_probe_red_u64) over a buffer the size of the visibility target, both
+    patterns, best of 4, CUDA events on `stream`."""
+    L = lh.lib()
+    n = mib * 1024 * 1024 // 8
+    buf = torch.zeros(n, dtype=torch.int64, device="cuda")
+    out = {"buffer_mib": mib}
+    for name, scattered in (("contiguous", 0), ("scattered", 1)):
+        best = 0.0
+        for _ in range(4):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                a.record(stream)
+            lh._check(L.lh_probe_red_u64(buf.data_ptr(), n, scattered, reps, stream.cuda_stream), "lh_probe_red_u64")
+            with torch.cuda.stream(stream):
+                b.record(stream)
+            torch.cuda.synchronize()
+            best = max(best, n * reps / (a.elapsed_time(b) * 1e-3))
+        out[name + "_per_s"] = best
+    return out
+
+
 def reduce_max_over_ranks(value, device=None):
     """Max of a per-rank float over the process group (identity with one rank)."""
     import torch
@@ -120,14 +173,32 @@ def reduce_max_over_ranks(value, device=None):
 def cpu_oracle_frames(scene, frames, threads=0):
     from oracle import binding as ob
     d = scene.desc
-    times, stages = [], []
+    times, stages, fr = [], [], None
     for _ in range(frames):
         fr = ob.run_scene(scene, shadow_size=d.shadow_size, max_instances=max(1024, d.n_instances), threads=threads)
         times.append(fr.stage_ms["total"])
         stages.append(fr.stage_ms)
     n_threads = int(stages[-1]["threads"]) if stages else 0
     s = sorted(times)
-    return s[len(s) // 2], n_threads, stages[-1] if stages else {}
+    return s[len(s) // 2], n_threads, stages[-1] if stages else {}, fr
+
+
+def hdr_error_vs_f64(gpu_hdr, fr):
+    """The GPU image against the oracle's float64 resolve of the same
+    visibility (and the oracle's own float32 image against it), over the
+    covered pixels: max and 99th percentile of the absolute error."""
+    import numpy as np
+    from oracle import binding as ob
+    h64 = ob.resolve_f64(fr)[..., :3]
+    cov = (fr.vis >> np.uint64(32)) != 0
+    out = {"pixels": int(cov.sum())}
+    for name, img in (("gpu", gpu_hdr), ("oracle_f32", fr.hdr)):
+        e = np.abs(img[..., :3].astype(np.float64) - h64)[cov]
+        out[name + "_max_abs"] = float(e.max()) if e.size else 0.0
+        out[name + "_p99_abs"] = float(np.percentile(e, 99)) if e.size else 0.0
+    out["gpu_vs_oracle_f32_max_abs"] = float(np.abs(gpu_hdr[..., :3].astype(np.float64) -
+                                                    fr.hdr[..., :3].astype(np.float64)).max())
+    return out
 
 
 def run_reference(args):
@@ -272,12 +343,15 @@ def run_gpu(args):
             e2e_times.append((t1 - t0) * 1e3)
     e2e_serial_ms = sum(e2e_times) / len(e2e_times)
 
-    # roofline: the dominant stage among the HBM-bound ones
+    # rooflines.  Algorithmic bytes per stage (the per-unit figures above
+    # times this frame's units), over each stage's CUDA-event time
+    st = r.status()
     vis_inst = st.visible_instances[0]
     cand = st.candidate_meshlets[0]
     vis_ml = st.visible_opaque[0] + st.visible_alpha_clip[0]
     cand_sh = sum(st.candidate_meshlets[1:5])
-    vis_sh = sum(st.visible_opaque[1:5])
+    vis_sh = sum(st.visible_opaque[1:5]) + sum(st.visible_alpha_clip[1:5])
+    frag_main, frag_shadow = int(st.fragments[0]), int(st.fragments[1])
     # resolve: visibility words read, HDR written, plus what it gathers once:
     # the 4 shadow layers, the textures, and the geometry of the triangles
     # left in the visibility buffer (micro indices, ~0.52 unique vertices per
@@ -285,43 +359,67 @@ def run_gpu(args):
     vis_ids = np.unique(r.visibility().reshape(-1) & np.uint64(0xFFFFFFFF))
     shown_tris = int(vis_ids.size)
     tex_bytes = sum(int(d.host_textures[i].width) * int(d.host_textures[i].height) * 4 for i in range(d.n_textures))
+    tri_main, tri_shadow = visible_triangles(r, st, 0), sum(visible_triangles(r, st, v) for v in range(1, 5))
     algo = {
-        "cull_meshlets": cand * (MESHLET_BYTES + PREFIX_ENTRY_BYTES) + vis_ml * DRAW_WRITE_BYTES,
-        "shadow_cull_meshlets": cand_sh * (MESHLET_BYTES + PREFIX_ENTRY_BYTES) + vis_sh * DRAW_WRITE_BYTES,
+        "cull_instances": d.n_instances * INSTANCE_BYTES + vis_inst * PREFIX_ENTRY_BYTES,
+        "cull_meshlets": cand * (MESHLET_BYTES + PREFIX_ENTRY_BYTES) + vis_ml * (DRAW_WRITE_BYTES + RASTER_DRAW_BYTES),
+        "raster": int(tri_main * RASTER_TRI_BYTES) + frag_main * FRAGMENT_BYTES + vis_ml * RASTER_DRAW_BYTES,
+        "depth_fit": npx * VIS_PIXEL_BYTES,
+        "shadow_cull_meshlets": cand_sh * (MESHLET_BYTES + PREFIX_ENTRY_BYTES) +
+        vis_sh * (DRAW_WRITE_BYTES + RASTER_DRAW_BYTES),
+        "shadow_raster": int(tri_shadow * RASTER_TRI_BYTES) + frag_shadow * FRAGMENT_BYTES + vis_sh * RASTER_DRAW_BYTES,
         "resolve": npx * (VIS_PIXEL_BYTES + HDR_PIXEL_BYTES) + 4 * d.shadow_size ** 2 * 4 + tex_bytes +
         int(shown_tris * (3 + 0.52 * (4 + 32))),
-        "depth_fit": npx * VIS_PIXEL_BYTES,
-        "clear": npx * 8 + 4 * d.shadow_size ** 2 * 4,
     }
-    dom = max(algo, key=lambda k: stage_ms.get(k, 0.0))
-    tri_main, tri_shadow = visible_triangles(r, st, 0), sum(visible_triangles(r, st, v) for v in range(1, 5))
     peak, peak_kind = _measured_peak_hbm()
-    achieved = algo[dom] / (stage_ms[dom] * 1e-3) / 1e9 if stage_ms.get(dom) else 0.0
+    per_stage = {}
+    for k, b in algo.items():
+        t = stage_ms.get(k, 0.0)
+        if t > 0:
+            gbs = b / (t * 1e-3) / 1e9
+            per_stage[k] = {"ms": round(t, 4), "algorithmic_bytes": int(b), "achieved_gbs": round(gbs, 1),
+                            "frac": round(gbs / peak, 4)}
+    dom = max(algo, key=lambda k: stage_ms.get(k, 0.0))  # the dominant stage
+    achieved = algo[dom] / (stage_ms[dom] * 1e-3) / 1e9
+    traffic, traffic_src = committed_traffic(dom) if args.config == 2 else (None, None)
+    atom = atomic_peak(lh, torch, stream)
+    red_rate = frag_main / (stage_ms["raster"] * 1e-3)
     tri_total = d.total_triangles
+    tune = r.tuning()
     line = {
         "metric": METRIC, "value": ms, "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded procedural scene, seed %d)" % scene.seed,
         "config": {"workload": _workload_name(args.config, d), "l2": "flushed between frames (256 MiB write)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "gtri_per_s": tri_total / (ms * 1e-3) / 1e9,
+        # the visibility raster's rate over the triangles of the visible meshlets
+        "gtri_per_s": tri_main / (stage_ms["raster"] * 1e-3) / 1e9,
+        # the whole frame over the scene's triangles before culling
+        "scene_gtri_per_s_before_culling": tri_total / (ms * 1e-3) / 1e9,
         "visible_meshlets": vis_ml, "candidate_meshlets": cand, "visible_instances": vis_inst,
         "shadow_visible_meshlets": [int(st.visible_opaque[k]) for k in range(1, 5)],
         "big_triangles_last_pass": int(st.big_triangles), "clipped_triangles_last_pass": int(st.clipped_triangles),
         "stage_ms": {k: round(v, 4) for k, v in stage_ms.items()},
         "launch_ms": launch_ms,
         "raster": {"visible_triangles": tri_main, "shadow_triangles": tri_shadow,
+                   "fragments": frag_main, "shadow_fragments": frag_shadow,
                    "gtri_per_s": tri_main / (stage_ms["raster"] * 1e-3) / 1e9,
-                   "shadow_gtri_per_s": tri_shadow / (stage_ms["shadow_raster"] * 1e-3) / 1e9},
+                   "shadow_gtri_per_s": tri_shadow / (stage_ms["shadow_raster"] * 1e-3) / 1e9,
+                   "fragments_per_s": red_rate,
+                   # fragments are 64-bit reductions: against the probe's ceiling
+                   "atomic_frac_of_scattered_peak": red_rate / atom["scattered_per_s"],
+                   "atomic_peak": atom},
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": 560 + 8, "d2h_bytes_per_step": npx * 16,
                 "pipelined": True, "serial_value": e2e_serial_ms},
         # per frame: clear; 2 x (cull instances, cull meshlets, raster opaque,
         # raster alpha clip, chunks); depth + fit; resolve
         "gpu_launches": 13 * args.steps,
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": RESOLVE_TRAFFIC_C2 if (dom == "resolve" and args.config == 2) else None,
-                     "algorithmic_bytes": algo[dom]},
+        "roofline": {"bound": "hbm", "kernel": dom + " stage (" + ", ".join(STAGE_KERNELS.get(dom, (dom,))) + ")",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": (peak_kind + " (MEASURED_PEAKS.json hbm_gbs)") if peak_kind == "measured"
+                     else peak_kind,
+                     "traffic": traffic, "traffic_source": traffic_src, "algorithmic_bytes": int(algo[dom])},
+        "per_stage_roofline": per_stage,
         "status_flags": int(st.flags),
     }
     if clk:
@@ -331,10 +429,13 @@ def run_gpu(args):
     if args.differentiable:
         line["differentiable"] = bench_differentiable(lh, torch, args, local_rank)
     if rank == 0 and args.cpu_frames > 0:
-        med, threads, stages = cpu_oracle_frames(scene, args.cpu_frames)
+        gpu_hdr = r.hdr()
+        med, threads, stages, fr = cpu_oracle_frames(scene, args.cpu_frames)
         line["cpu_baseline"] = {"value": med, "unit": "ms", "cores": threads, "kind": "port",
                                 "sample": "median of %d full frames of the workload" % args.cpu_frames,
                                 "speedup_vs_gpu_frame": med / ms}
+        # the HDR's error against the float64 resolve of the same frame
+        line["hdr_error_vs_f64"] = hdr_error_vs_f64(gpu_hdr, fr)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
