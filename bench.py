@@ -412,8 +412,13 @@ def run_gpu(args):
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": 560 + 8, "d2h_bytes_per_step": npx * 16,
                 "pipelined": True, "serial_value": e2e_serial_ms},
         # per frame: clear; 2 x (cull instances, cull meshlets, raster opaque,
-        # raster alpha clip, chunks); depth + fit; resolve
-        "gpu_launches": 13 * args.steps,
+        # raster alpha clip, chunks); depth + fit; resolve; with the occlusion
+        # raster the visibility view adds the occluder pass, its chunks, the
+        # hierarchical depth and the depth test of the other meshlets
+        "gpu_launches": (13 + (4 if tune.occlusion_px else 0)) * args.steps,
+        "occlusion": {"occluder_px": int(tune.occlusion_px), "occluders": int(st.occlusion[0]),
+                      "survivors_opaque": int(st.occlusion[1]), "survivors_alpha": int(st.occlusion[2]),
+                      "visible_opaque": int(st.visible_opaque[0])},
         "roofline": {"bound": "hbm", "kernel": dom + " stage (" + ", ".join(STAGE_KERNELS.get(dom, (dom,))) + ")",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": (peak_kind + " (MEASURED_PEAKS.json hbm_gbs)") if peak_kind == "measured"

@@ -120,6 +120,9 @@ typedef struct lh_device_status {
     uint32_t clipped_triangles;      /* triangles clipped (last raster pass) */
     uint32_t fragments[2];           /* fragments written this frame (one 64-bit depth-test reduction
                                         each): [0] visibility views, [1] shadow views */
+    uint32_t occlusion[3];           /* main view, two-pass occlusion raster: occluder meshlets, then the
+                                        opaque and alpha-clip meshlets that survived the depth test (the
+                                        rest of the visible ones were skipped); 0 without occlusion */
 } lh_device_status;
 
 typedef struct lh_ctx lh_ctx;
@@ -241,6 +244,11 @@ typedef struct lh_tuning {
     uint32_t schedule;        /* LH_SCHEDULE_* */
     uint32_t raster_batch;    /* meshlets a raster warp claims per atomic (0: 4 when the views hold more than
                                  256 meshlets per warp of the grid, else 1) */
+    uint32_t occlusion_px;    /* two-pass occlusion raster of the visibility views: opaque meshlets whose
+                                 bounding sphere projects to a radius above this many pixels are drawn
+                                 first, the hierarchical depth of what they wrote is built, and every other
+                                 meshlet whose sphere lies behind it is skipped (no counterpart in the
+                                 reference; results identical).  0: one pass, no occlusion test */
 } lh_tuning;
 
 lh_status lh_set_tuning(lh_ctx* ctx, const lh_tuning* tuning);

@@ -74,7 +74,8 @@ class DeviceStatus(C.Structure):
     _fields_ = [("flags", C.c_uint32), ("n_views", C.c_uint32), ("visible_instances", C.c_uint32 * 40),
                 ("candidate_meshlets", C.c_uint32 * 40), ("visible_opaque", C.c_uint32 * 40),
                 ("visible_alpha_clip", C.c_uint32 * 40), ("big_triangles", C.c_uint32),
-                ("clipped_triangles", C.c_uint32), ("fragments", C.c_uint32 * 2)]
+                ("clipped_triangles", C.c_uint32), ("fragments", C.c_uint32 * 2),
+                ("occlusion", C.c_uint32 * 3)]
 
 
 SCHEDULE_DEFAULT, SCHEDULE_PER_STAGE, SCHEDULE_PERSISTENT, SCHEDULE_PER_VIEW = 0, 1, 2, 3
@@ -83,7 +84,7 @@ CONFIG_HDR_RGBA16F = 1  # lh_config.flags: the HDR image in RGBA16F
 
 class Tuning(C.Structure):
     _fields_ = [("small_px", C.c_uint32), ("medium_px", C.c_uint32), ("cull_blocks_per_sm", C.c_float),
-                ("schedule", C.c_uint32), ("raster_batch", C.c_uint32)]
+                ("schedule", C.c_uint32), ("raster_batch", C.c_uint32), ("occlusion_px", C.c_uint32)]
 
 
 class MeshGrads(C.Structure):
@@ -316,8 +317,11 @@ class Renderer:
                "lh_set_scene", self.ctx)
         self.scene = scene
 
-    def set_tuning(self, small_px=None, medium_px=None, cull_blocks_per_sm=None, schedule=None, raster_batch=None):
+    def set_tuning(self, small_px=None, medium_px=None, cull_blocks_per_sm=None, schedule=None, raster_batch=None,
+                   occlusion_px=None):
         t = self.tuning()
+        if occlusion_px is not None:
+            t.occlusion_px = occlusion_px
         if schedule is not None:
             t.schedule = schedule
         if raster_batch is not None:

@@ -51,6 +51,9 @@ struct lh_ctx {
     uint8_t* d_sectors = nullptr;
     MeshletReference* d_refs = nullptr;
     RasterDraw* d_rdraws = nullptr;  // the raster's per-slot draw records
+    uint32_t* d_lists = nullptr;     // occlusion lists of the visibility views (3 * max_draws words each)
+    uint32_t* d_hiz = nullptr;       // hierarchical depth of the visibility views (pool)
+    size_t hiz_words = 0;
     uint8_t* d_draws = nullptr;
     uint64_t* d_vis = nullptr;
     float* d_shadow = nullptr;
@@ -197,7 +200,8 @@ void build_views(lh_ctx* c, uint32_t n_probes, const Uniforms* probe_uniforms) {
     uint32_t n_views = 5 + n_probes;
     uint32_t n_inst_tiles = (c->n_instances + kInstTile - 1) / kInstTile + 1;
     uint32_t ml_tiles = (uint32_t)((c->scene_meshlets + kMlTile - 1) / kMlTile) + 1;
-    size_t per_view = align_up(16 + 8 * (size_t)n_inst_tiles + 8 * (size_t)ml_tiles, 256);
+    size_t per_view = align_up(4 * kClaimWords + 8 * (size_t)n_inst_tiles + 8 * (size_t)ml_tiles, 256);
+    size_t hiz_used = 0;
     for (uint32_t v = 0; v < n_views; v++) {
         ViewDev vw{};
         bool cascade = v >= 1 + n_probes;
@@ -227,9 +231,21 @@ void build_views(lh_ctx* c, uint32_t n_probes, const Uniforms* probe_uniforms) {
         vw.section_base = v * 2 * cfg.max_draws;
         uint8_t* r = c->d_reset + kStWords * 4 + v * per_view;
         vw.claim = reinterpret_cast<uint32_t*>(r);
-        vw.inst_status = reinterpret_cast<uint64_t*>(r + 16);
-        vw.ml_status = reinterpret_cast<uint64_t*>(r + 16 + 8 * (size_t)n_inst_tiles);
+        vw.inst_status = reinterpret_cast<uint64_t*>(r + 4 * kClaimWords);
+        vw.ml_status = reinterpret_cast<uint64_t*>(r + 4 * kClaimWords + 8 * (size_t)n_inst_tiles);
         vw.ml_tile_cap = ml_tiles;
+        if (!cascade) {
+            // occlusion lists, and the view's hierarchical depth from the
+            // pool while it lasts (a view without one culls nothing)
+            vw.lists = c->d_lists + (size_t)v * 3 * cfg.max_draws;
+            vw.hiz_rx = (vw.width + kHizRegion - 1) / kHizRegion;
+            vw.hiz_ry = (vw.height + kHizRegion - 1) / kHizRegion;
+            const size_t words = (size_t)vw.hiz_rx * vw.hiz_ry * 65;
+            if (hiz_used + words <= c->hiz_words) {
+                vw.hiz = c->d_hiz + hiz_used;
+                hiz_used += align_up(words, 64);
+            }
+        }
         c->h_views.push_back(vw);
     }
 }
@@ -237,7 +253,7 @@ void build_views(lh_ctx* c, uint32_t n_probes, const Uniforms* probe_uniforms) {
 size_t reset_bytes_for(const lh_ctx* c) {
     uint32_t n_inst_tiles = (c->n_instances + kInstTile - 1) / kInstTile + 1;
     uint32_t ml_tiles = (uint32_t)((c->scene_meshlets + kMlTile - 1) / kMlTile) + 1;
-    size_t per_view = align_up(16 + 8 * (size_t)n_inst_tiles + 8 * (size_t)ml_tiles, 256);
+    size_t per_view = align_up(4 * kClaimWords + 8 * (size_t)n_inst_tiles + 8 * (size_t)ml_tiles, 256);
     return align_up(kStWords * 4, 256) + per_view * c->max_views;
 }
 
@@ -265,6 +281,7 @@ FrameDev frame_dev(const lh_ctx* c, uint32_t n_views, uint32_t n_instances) {
     f.uniforms = c->d_uniforms;
     f.frame_consts = c->d_consts;
     f.srgb_lut = c->d_srgb;
+    f.occlusion_px = c->tuning.occlusion_px;
     return f;
 }
 
@@ -470,7 +487,7 @@ lh_status lh_create(const lh_config* config, lh_ctx** out) {
     if (!c) return LH_ERR_OUT_OF_MEMORY;
     c->cfg = cfg;
     c->device = cfg.device;
-    c->tuning = lh_tuning{32u, 128u, 2.0f, LH_SCHEDULE_DEFAULT, 0u};
+    c->tuning = lh_tuning{32u, 128u, 2.0f, LH_SCHEDULE_DEFAULT, 0u, 128u};
     cudaError_t e = cudaSetDevice(c->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device);
     c->max_views = 5 + cfg.max_probes;
@@ -488,6 +505,13 @@ lh_status lh_create(const lh_config* config, lh_ctx** out) {
     if (e == cudaSuccess) e = dalloc(c, &c->d_sectors, c->sector_bytes * c->max_views);
     if (e == cudaSuccess) e = dalloc(c, &c->d_refs, sizeof(MeshletReference) * 2 * (size_t)cfg.max_draws * c->max_views);
     if (e == cudaSuccess) e = dalloc(c, &c->d_rdraws, sizeof(RasterDraw) * 2 * (size_t)cfg.max_draws * c->max_views);
+    if (e == cudaSuccess) e = dalloc(c, &c->d_lists, sizeof(uint32_t) * 3 * (size_t)cfg.max_draws * (1 + cfg.max_probes));
+    // hierarchical depth: the main view, and the probes' total pixels in 64 x
+    // 64 regions with room for each probe's partial regions
+    c->hiz_words = align_up(((W + kHizRegion - 1) / kHizRegion) * ((H + kHizRegion - 1) / kHizRegion) * 65, 64) +
+                   ((size_t)cfg.max_probe_pixels / (kHizRegion * kHizRegion) * 4 + 32 * (size_t)cfg.max_probes) * 65 +
+                   64 * (size_t)cfg.max_probes;
+    if (e == cudaSuccess) e = dalloc(c, &c->d_hiz, sizeof(uint32_t) * c->hiz_words);
     if (e == cudaSuccess) e = dalloc(c, &c->d_draws, c->draw_bytes * c->max_views);
     if (e == cudaSuccess) e = dalloc(c, &c->d_vis, W * H * 8);
     if (e == cudaSuccess) e = dalloc(c, &c->d_shadow, 4 * S * S * 4);
@@ -830,6 +854,14 @@ lh_status lh_read_status(lh_ctx* c, lh_device_status* out) {
     out->clipped_triangles = words[kStClipCount];
     out->fragments[0] = words[kStFragVis];
     out->fragments[1] = words[kStFragShadow];
+    if (!c->h_views.empty() && c->tuning.occlusion_px) {
+        uint32_t claim[kClaimWords];
+        e = cudaMemcpy(claim, c->h_views[0].claim, sizeof(claim), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_fail(c, e, "status read");
+        out->occlusion[0] = claim[kClaimOccluders];
+        out->occlusion[1] = claim[kClaimSurvivorsOpaque];
+        out->occlusion[2] = claim[kClaimSurvivorsAlpha];
+    }
     out->n_views = c->n_views_last;
     for (uint32_t v = 0; v < c->n_views_last && v < 40; v++) {
         unsigned long long counter = 0;
@@ -951,7 +983,8 @@ void lh_destroy(lh_ctx* c) {
 lh_status lh_set_tuning(lh_ctx* c, const lh_tuning* t) {
     if (!c || !t) return LH_ERR_INVALID_ARGUMENT;
     if (t->small_px > 4096 || t->medium_px < t->small_px || !(t->cull_blocks_per_sm > 0.0f) ||
-        t->cull_blocks_per_sm > 64.0f || t->schedule > LH_SCHEDULE_PER_VIEW || t->raster_batch > 64)
+        t->cull_blocks_per_sm > 64.0f || t->schedule > LH_SCHEDULE_PER_VIEW || t->raster_batch > 64 ||
+        t->occlusion_px > 65536)
         return LH_ERR_INVALID_ARGUMENT;
     c->tuning = *t;
     return LH_OK;

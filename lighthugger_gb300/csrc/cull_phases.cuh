@@ -69,9 +69,30 @@ __device__ __noinline__ uint64_t lookback(uint64_t* status, uint32_t tile, uint6
 }
 
 
+// Radius of a ball of radius r after the linear part of `m` (columns 0..2):
+// r times a bound of the largest singular value, sqrt of Gershgorin's bound
+// on the eigenvalues of M^T M (exact for orthogonal columns, an upper bound
+// for any matrix), widened by 2^-16 for the rounding of the float sums.
+__device__ __forceinline__ float bounding_radius(const float4 (&c)[4], float r) {
+    const float n0 = c[0].x * c[0].x + c[0].y * c[0].y + c[0].z * c[0].z;
+    const float n1 = c[1].x * c[1].x + c[1].y * c[1].y + c[1].z * c[1].z;
+    const float n2 = c[2].x * c[2].x + c[2].y * c[2].y + c[2].z * c[2].z;
+    const float d01 = fabsf(c[0].x * c[1].x + c[0].y * c[1].y + c[0].z * c[1].z);
+    const float d02 = fabsf(c[0].x * c[2].x + c[0].y * c[2].y + c[0].z * c[2].z);
+    const float d12 = fabsf(c[1].x * c[2].x + c[1].y * c[2].y + c[1].z * c[2].z);
+    const float lam = fmaxf(fmaxf(n0 + d01 + d02, n1 + d01 + d12), n2 + d02 + d12);
+    return r * sqrtf(lam) * (1.0f + 1.0f / 65536.0f);
+}
+
 // The raster's record of a visible meshlet (the scene records it reads were
-// loaded moments earlier by the same thread, so these loads mostly hit).
-__device__ __forceinline__ RasterDraw raster_draw_of(const FrameDev& f, MeshletReference ref) {
+// loaded moments earlier by the same thread, so these loads mostly hit):
+// the addresses of its vertex data, its world-space bounding sphere, and --
+// in a visibility view with occlusion culling -- whether it is an occluder:
+// opaque, with a projected sphere radius above f.occlusion_px pixels (or
+// reaching the camera plane).  Occluders are appended to the view's
+// occluder list (any order: the raster is order independent).
+__device__ __forceinline__ RasterDraw raster_draw_of(const FrameDev& f, const ViewDev* vw, const Uniforms& u,
+                                                     MeshletReference ref, bool alpha, uint32_t slot) {
     const Instance* inst = f.instances + ref.instance_index;
     const unsigned long long* mw = reinterpret_cast<const unsigned long long*>(__ldg(&inst->mesh_info_address));
     const uint64_t positions = __ldg(mw + 0), indices = __ldg(mw + 1), micro = __ldg(mw + 4), meshlets = __ldg(mw + 5);
@@ -86,6 +107,33 @@ __device__ __forceinline__ RasterDraw raster_draw_of(const FrameDev& f, MeshletR
     r.instance = ref.instance_index;
     // counts = triangle_count | index_count << 8
     r.bits = ((counts >> 8) & 0xFFu) | ((counts & 0xFFu) << 8) | (mflags << 16);
+    // world sphere: transform * centre, radius through the linear part
+    float4 tc[4];
+    const float4* tsrc = reinterpret_cast<const float4*>(inst);
+#pragma unroll
+    for (int c = 0; c < 4; c++) tc[c] = __ldg(tsrc + c);
+    const float* mls = reinterpret_cast<const float*>(ml) + 7;  // Meshlet.bounding_sphere at byte 28
+    const float bx = __ldg(mls), by = __ldg(mls + 1), bz = __ldg(mls + 2), br = __ldg(mls + 3);
+    const float wx = ((tc[0].x * bx + tc[1].x * by) + tc[2].x * bz) + tc[3].x;
+    const float wy = ((tc[0].y * bx + tc[1].y * by) + tc[2].y * bz) + tc[3].y;
+    const float wz = ((tc[0].z * bx + tc[1].z * by) + tc[2].z * bz) + tc[3].z;
+    // plus 8 ulps of the largest coordinate: the raster's float world
+    // positions of the vertices, rounded like this centre, stay inside
+    const float R = bounding_radius(tc, br) + fmaxf(fmaxf(fabsf(wx), fabsf(wy)), fabsf(wz)) * (1.0f / 1048576.0f);
+    r.sphere[0] = wx;
+    r.sphere[1] = wy;
+    r.sphere[2] = wz;
+    r.sphere[3] = R;
+    if (f.occlusion_px && !alpha && vw->kind == kViewVisibility && vw->lists) {
+        const lh_mat4& pv = u.combined_perspective_view;
+        const float w = ((pv.cols[0].w * wx + pv.cols[1].w * wy) + pv.cols[2].w * wz) + pv.cols[3].w;
+        const float focal_px = fabsf(u.perspective.cols[1].y) * 0.5f * (float)vw->height;
+        if (!(w > R) || R * focal_px > (float)f.occlusion_px * (w - R)) {
+            r.bits |= kDrawOccluder;
+            const uint32_t pos = atomicAdd(&vw->claim[kClaimOccluders], 1u);
+            if (pos < f.max_draws) vw->lists[pos] = slot;
+        }
+    }
     return r;
 }
 
@@ -432,7 +480,7 @@ __device__ void phase_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint
             dc.firstInstance = vw->section_base + slot;
             draws[slot] = dc;
             out_refs[slot] = refs[k];
-            vw->rdraws[slot] = raster_draw_of(f, refs[k]);
+            vw->rdraws[slot] = raster_draw_of(f, vw, s_u, refs[k], cl == 2u, slot);
         }
         __syncthreads();
     }

@@ -40,9 +40,34 @@ struct __align__(16) RasterDraw {
     uint64_t indices;    // MeshInfo.indices + Meshlet.index_offset elements
     uint64_t micro;      // MeshInfo.micro_indices + Meshlet.triangle_offset
     uint32_t instance;   // MeshletReference.instance_index
-    uint32_t bits;       // index_count | triangle_count << 8 | MeshInfo.flags << 16
+    uint32_t bits;       // index_count | triangle_count << 8 | MeshInfo.flags << 16 | kDrawOccluder
+    float sphere[4];     // world-space sphere holding every vertex of the meshlet (centre, radius)
 };
-static_assert(sizeof(RasterDraw) == 32, "RasterDraw layout");
+static_assert(sizeof(RasterDraw) == 48, "RasterDraw layout");
+// RasterDraw::bits: the meshlet is rasterised in the occluder pass (a
+// visibility view with occlusion culling, opaque, large on screen).
+constexpr uint32_t kDrawOccluder = 1u << 31;
+
+// Per-view lists of the two-pass occlusion raster of visibility views
+// (ViewDev::lists, 3 * max_draws words): draw slots of the occluders, then
+// of the opaque and the alpha-clip meshlets that survive the hierarchical
+// depth test.  Their counts are ViewDev::claim[kClaimOccluders ...].
+enum RasterList : uint32_t { kListAll = 0, kListOccluders = 1, kListSurvivors = 2 };
+enum ClaimWord : uint32_t {
+    kClaimInstTiles = 0,
+    kClaimMeshletTiles = 1,
+    kClaimOccluders = 2,       // entries of the occluder list
+    kClaimSurvivorsOpaque = 3,
+    kClaimSurvivorsAlpha = 4,
+    kClaimWords = 8
+};
+// Hierarchical depth of a visibility view (ViewDev::hiz): level 0 holds the
+// minimum depth bits of every 8 x 8-pixel tile, level 1 of every 64 x 64
+// region, over the pixels written by the occluder pass (0 where a pixel has
+// no fragment: a tile with an empty pixel culls nothing).  Regions are
+// hiz_rx x hiz_ry; level 0 is row major with hiz_rx * 8 tiles per row,
+// level 1 follows it.
+constexpr uint32_t kHizTile = 8, kHizRegion = 64;
 
 struct ViewDev {
     uint32_t kind;
@@ -56,9 +81,12 @@ struct ViewDev {
     void* target;               // u64 visibility or u32 depth
     uint64_t* inst_status;      // per-frame zeroed look-back words, instance cull
     uint64_t* ml_status;        // per-frame zeroed look-back words, meshlet cull
-    uint32_t* claim;            // per-frame zeroed: [0] instance tiles, [1] meshlet tiles
+    uint32_t* claim;            // per-frame zeroed kClaimWords: tile claims, occlusion list counts
     uint32_t section_base;      // firstInstance offset of this view's reference section
     uint32_t ml_tile_cap;       // capacity of ml_status
+    uint32_t* lists;            // visibility views: occluder / survivor draw-slot lists (3 * max_draws)
+    uint32_t* hiz;              // visibility views with occlusion culling: hierarchical depth, else null
+    uint32_t hiz_rx, hiz_ry;    // 64 x 64-pixel regions of the view
 };
 
 // Triangle handed to the chunked raster path: its set-up (orientation
@@ -133,6 +161,7 @@ struct FrameDev {
     const Uniforms* uniforms;   // main view
     const float* frame_consts;  // [0] pow(0.5, split), [1] pow(0.75, split)
     const float* srgb_lut;      // 256 entries
+    uint32_t occlusion_px;      // occluder threshold (projected sphere radius, pixels); 0: no occlusion culling
 };
 
 // Launch `kernel` with programmatic stream serialisation: its blocks may
@@ -186,6 +215,11 @@ cudaError_t launch_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint32_
 // Raster all views [view_begin, view_begin + n_views) of one kind (kViewVisibility
 // or kViewShadow): the opaque and alpha-clip classes (clipping inline), then
 // the band kernel.
+// With f.occlusion_px set, the visibility raster runs in two passes: the
+// occluders, the hierarchical depth of what they wrote, the depth test of
+// every other visible meshlet's bounding sphere against it, then the
+// survivors (results identical: a skipped meshlet could not have won any
+// pixel's depth test).
 cudaError_t launch_raster_kind(const FrameDev& f, uint32_t view_begin, uint32_t n_views, int kind, uint32_t small_px,
                                uint32_t medium_px, uint32_t raster_batch, cudaStream_t s, int sms);
 cudaError_t launch_depth_reduce_fit(const FrameDev& f, cudaStream_t s, int sms);

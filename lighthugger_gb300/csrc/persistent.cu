@@ -65,8 +65,24 @@ __global__ void __launch_bounds__(kPersistentThreads, 3) k_frame_persistent(Fram
     if (!grid_barrier(f, epoch)) return;
     phase_cull_meshlets(f, 0, n_persp, &f.status[kStMlClaim]);
     if (!grid_barrier(f, epoch)) return;
-    phase_raster<0, false>(f, 0, n_persp, tune, &f.status[kStRasterClaim], s_raster, nullptr);
-    phase_raster<0, true>(f, 0, n_persp, tune, &f.status[kStRasterClaimAlpha], s_raster, s_raster.av);
+    if (f.occlusion_px) {
+        // occluders and their chunks, hierarchical depth, the depth test of
+        // the other meshlets, then the survivors
+        phase_raster<0, false>(f, 0, n_persp, tune, &f.status[kStRasterClaim], s_raster, nullptr, kListOccluders);
+        if (!grid_barrier(f, epoch)) return;
+        phase_raster_big<0>(f);
+        if (!grid_barrier(f, epoch)) return;
+        phase_hiz(f, 0, n_persp);
+        if (!grid_barrier(f, epoch)) return;
+        phase_occlusion_filter(f, 0, n_persp, gtid, gstride);
+        if (!grid_barrier(f, epoch)) return;
+        phase_raster<0, false>(f, 0, n_persp, tune, &f.status[kStRasterClaim], s_raster, nullptr, kListSurvivors);
+        phase_raster<0, true>(f, 0, n_persp, tune, &f.status[kStRasterClaimAlpha], s_raster, s_raster.av,
+                              kListSurvivors);
+    } else {
+        phase_raster<0, false>(f, 0, n_persp, tune, &f.status[kStRasterClaim], s_raster, nullptr);
+        phase_raster<0, true>(f, 0, n_persp, tune, &f.status[kStRasterClaimAlpha], s_raster, s_raster.av);
+    }
     if (!grid_barrier(f, epoch)) return;
     phase_raster_big<0>(f);
     if (!grid_barrier(f, epoch)) return;

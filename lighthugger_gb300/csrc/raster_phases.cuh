@@ -638,14 +638,30 @@ __device__ __forceinline__ void count_fragments(const FrameDev& f, uint32_t nfra
     if ((threadIdx.x & 31) == 0 && total) atomicAdd(&f.status[KIND == 0 ? kStFragVis : kStFragShadow], total);
 }
 
+// Meshlets of view `vw` a raster pass covers: every visible one of the class
+// (kListAll), or the entries of one of the view's occlusion lists.
+__device__ __forceinline__ uint32_t raster_list_count(const FrameDev& f, const ViewDev* vw, bool alpha, uint32_t list) {
+    if (list == kListAll) return min(reinterpret_cast<const uint32_t*>(vw->draws)[alpha ? 1 : 0], f.max_draws);
+    const uint32_t w = list == kListOccluders ? kClaimOccluders : (alpha ? kClaimSurvivorsAlpha : kClaimSurvivorsOpaque);
+    return min(*reinterpret_cast<const volatile uint32_t*>(&vw->claim[w]), f.max_draws);
+}
+__device__ __forceinline__ uint32_t raster_list_slot(const FrameDev& f, const ViewDev* vw, bool alpha, uint32_t list,
+                                                     uint32_t local) {
+    if (list == kListAll) return alpha ? f.max_draws + local : local;
+    const uint32_t k = list == kListOccluders ? 0u : (alpha ? 2u : 1u);
+    return __ldcg(vw->lists + (size_t)k * f.max_draws + local);
+}
+
 // One warp per visible meshlet of views [view_begin, view_begin + n_views)
 // of one draw class (opaque, or ALPHA: alpha clip), claimed from
-// `claim_word`.  Persistent: returns when the claims run out.  The classes
-// are separate instantiations (separate launches) so that the opaque path
-// carries none of the alpha test's state.
+// `claim_word`; `list` selects all of them or one occlusion list.
+// Persistent: returns when the claims run out.  The classes are separate
+// instantiations (separate launches) so that the opaque path carries none
+// of the alpha test's state.
 template <int KIND, bool ALPHA>
 __device__ void phase_raster(const FrameDev& f, uint32_t view_begin, uint32_t n_views, RasterTune tune,
-                             uint32_t* claim_word, RasterSmem& sm, AlphaVert (*s_av)[MAX_MESHLET_UNIQUE_VERTICES]) {
+                             uint32_t* claim_word, RasterSmem& sm, AlphaVert (*s_av)[MAX_MESHLET_UNIQUE_VERTICES],
+                             uint32_t list = kListAll) {
     uint32_t* s_prefix = sm.prefix;
     lh_mat4* s_vp = sm.vp;
     SnapV(*s_v)[MAX_MESHLET_UNIQUE_VERTICES] = sm.v;
@@ -656,9 +672,8 @@ __device__ void phase_raster(const FrameDev& f, uint32_t view_begin, uint32_t n_
     if (threadIdx.x == 0) {
         uint32_t run = 0;
         for (uint32_t v = 0; v < n_views; v++) {
-            const uint32_t* cnt = reinterpret_cast<const uint32_t*>(f.views[view_begin + v].draws);
             s_prefix[v] = run;
-            run += min(cnt[ALPHA ? 1 : 0], md);
+            run += raster_list_count(f, f.views + view_begin + v, ALPHA, list);
         }
         s_prefix[n_views] = run;
     }
@@ -716,7 +731,7 @@ __device__ void phase_raster(const FrameDev& f, uint32_t view_begin, uint32_t n_
         const uint32_t view = view_begin + v;
         const ViewDev* vw = f.views + view;
         const uint32_t local = item - s_prefix[v];
-        const uint32_t slot = ALPHA ? md + local : local;
+        const uint32_t slot = raster_list_slot(f, vw, ALPHA, list, local);
         // the slot's draw record (written by the meshlet cull): the index and
         // micro-index addresses come offset to the meshlet already
         const RasterDraw rd = vw->rdraws[slot];
@@ -917,6 +932,182 @@ __device__ void phase_raster_big(const FrameDev& f) {
         }
     }
     count_fragments<KIND>(f, nfrag);
+}
+
+// ------------------------------------------------------------ occlusion
+// Hierarchical depth of the visibility views [view_begin, view_begin +
+// n_views) that cull by occlusion, after the occluder pass: one block of 256
+// threads per 64 x 64-pixel region (regions of all these views numbered one
+// after another), claimed round robin by the grid.  Warp w takes pixel rows
+// 8w .. 8w + 7 of the region in two 32-pixel halves, keeps the minimum depth
+// bits of each lane's column, then of each 8 x 8 tile (lanes in groups of
+// 8); the block takes the region's minimum over its 64 tiles.  Pixels
+// outside the view do not count; a pixel without a fragment is depth 0.
+__device__ void phase_hiz(const FrameDev& f, uint32_t view_begin, uint32_t n_views) {
+    __shared__ uint32_t s_region_min[8];
+    __shared__ uint32_t s_first[kMaxViews + 1];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();  // shared memory may still be in use by a previous phase of the block
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (uint32_t v = 0; v < n_views; v++) {
+            const ViewDev* vw = f.views + view_begin + v;
+            s_first[v] = run;
+            if (vw->kind == kViewVisibility && vw->hiz) run += vw->hiz_rx * vw->hiz_ry;
+        }
+        s_first[n_views] = run;
+    }
+    __syncthreads();
+    const uint32_t total = s_first[n_views];
+    uint32_t v = 0;
+    for (uint32_t region = blockIdx.x; region < total; region += gridDim.x) {
+        while (region >= s_first[v + 1]) v++;
+        const ViewDev* vw = f.views + view_begin + v;
+        const uint32_t r = region - s_first[v], rx = r % vw->hiz_rx, ry = r / vw->hiz_rx;
+        const uint32_t W = vw->width, H = vw->height;
+        const uint64_t* vis = reinterpret_cast<const uint64_t*>(vw->target);
+        uint32_t* level0 = vw->hiz;
+        const uint32_t pitch0 = vw->hiz_rx * 8u;
+        uint32_t wmin = 0xFFFFFFFFu;
+#pragma unroll
+        for (uint32_t half = 0; half < 2; half++) {
+            const uint32_t x = rx * kHizRegion + half * 32u + lane;
+            uint32_t m = 0xFFFFFFFFu;
+#pragma unroll
+            for (uint32_t k = 0; k < 8; k++) {
+                const uint32_t y = ry * kHizRegion + warp * 8u + k;
+                if (x < W && y < H) m = min(m, (uint32_t)(__ldcg(vis + (size_t)y * W + x) >> 32));
+            }
+            m = min(m, __shfl_xor_sync(0xFFFFFFFFu, m, 1));
+            m = min(m, __shfl_xor_sync(0xFFFFFFFFu, m, 2));
+            m = min(m, __shfl_xor_sync(0xFFFFFFFFu, m, 4));
+            if ((lane & 7u) == 0) level0[(size_t)(ry * 8u + warp) * pitch0 + rx * 8u + half * 4u + (lane >> 3)] = m;
+            wmin = min(wmin, m);
+        }
+        wmin = __reduce_min_sync(0xFFFFFFFFu, wmin);
+        if (lane == 0) s_region_min[warp] = wmin;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t m = s_region_min[0];
+            for (uint32_t k = 1; k < 8; k++) m = min(m, s_region_min[k]);
+            level0[(size_t)pitch0 * vw->hiz_ry * 8u + r] = m;  // level 1
+        }
+        __syncthreads();
+    }
+}
+
+// True when no fragment of a meshlet inside the world sphere `sp` can pass
+// the depth test against what the view holds already: every 8 x 8 tile (or
+// 64 x 64 region) its screen box touches has a minimum depth above the
+// largest depth the sphere can reach.  The box and that depth come from the
+// 8 corners of the sphere's axis-aligned box through the view's matrix,
+// widened by 2 pixels and by 1/128 of the depth (the kernels' float
+// rounding of the vertices is far below both); a corner at or behind the
+// camera plane culls nothing.  Exact: a culled meshlet's every fragment
+// would have lost the atomicMax (its depth strictly below the pixel's).
+__device__ __forceinline__ bool hiz_occluded(const ViewDev* vw, const lh_mat4& pv, const float (&sp)[4]) {
+    const f4 cc = mul(pv, f4{sp[0], sp[1], sp[2], 1.0f});
+    const float r = sp[3];
+    const f4 a{pv.cols[0].x * r, pv.cols[0].y * r, pv.cols[0].z * r, pv.cols[0].w * r};
+    const f4 b{pv.cols[1].x * r, pv.cols[1].y * r, pv.cols[1].z * r, pv.cols[1].w * r};
+    const f4 d{pv.cols[2].x * r, pv.cols[2].y * r, pv.cols[2].z * r, pv.cols[2].w * r};
+    const float hw = (float)vw->width * 0.5f, hh = (float)vw->height * 0.5f;
+    float x0 = 3.0e38f, x1 = -3.0e38f, y0 = 3.0e38f, y1 = -3.0e38f, zmax = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const float sa = (k & 1) ? 1.0f : -1.0f, sb = (k & 2) ? 1.0f : -1.0f, sd = (k & 4) ? 1.0f : -1.0f;
+        const float cw = cc.w + sa * a.w + sb * b.w + sd * d.w;
+        if (!(cw > 1e-6f)) return false;
+        const float cx = cc.x + sa * a.x + sb * b.x + sd * d.x;
+        const float cy = cc.y + sa * a.y + sb * b.y + sd * d.y;
+        const float cz = cc.z + sa * a.z + sb * b.z + sd * d.z;
+        const float px = (cx / cw) * hw + hw, py = (cy / cw) * hh + hh, pz = cz / cw;
+        x0 = fminf(x0, px);
+        x1 = fmaxf(x1, px);
+        y0 = fminf(y0, py);
+        y1 = fmaxf(y1, py);
+        zmax = fmaxf(zmax, pz);
+    }
+    if (!(zmax >= 0.0f) || !(x1 >= x0) || !(y1 >= y0)) return false;  // NaN
+    const float zt = zmax + zmax * (1.0f / 128.0f);
+    if (!(zt < 1.0f)) return false;
+    const uint32_t zbits = __float_as_uint(zt);
+    const int32_t W = (int32_t)vw->width, H = (int32_t)vw->height;
+    // the box, widened and clamped to [-1, W] x [-1, H] before conversion
+    auto px_lo = [](float v, float lim) { return fminf(fmaxf(floorf(v) - 2.0f, -1.0f), lim); };
+    auto px_hi = [](float v, float lim) { return fminf(fmaxf(ceilf(v) + 2.0f, -1.0f), lim); };
+    const int32_t ix0 = max((int32_t)px_lo(x0, (float)W), 0), ix1 = min((int32_t)px_hi(x1, (float)W), W - 1);
+    const int32_t iy0 = max((int32_t)px_lo(y0, (float)H), 0), iy1 = min((int32_t)px_hi(y1, (float)H), H - 1);
+    if (ix0 > ix1 || iy0 > iy1) return true;  // no pixel centre of the view in reach
+    const uint32_t pitch0 = vw->hiz_rx * 8u;
+    const uint32_t* level0 = vw->hiz;
+    int32_t tx0 = ix0 >> 3, tx1 = ix1 >> 3, ty0 = iy0 >> 3, ty1 = iy1 >> 3;
+    if ((tx1 - tx0 + 1) * (ty1 - ty0 + 1) <= 16) {
+        for (int32_t ty = ty0; ty <= ty1; ty++)
+            for (int32_t tx = tx0; tx <= tx1; tx++)
+                if (__ldcg(level0 + (size_t)ty * pitch0 + tx) <= zbits) return false;
+        return true;
+    }
+    const uint32_t* level1 = level0 + (size_t)pitch0 * vw->hiz_ry * 8u;
+    tx0 = ix0 >> 6, tx1 = ix1 >> 6, ty0 = iy0 >> 6, ty1 = iy1 >> 6;
+    if ((tx1 - tx0 + 1) * (ty1 - ty0 + 1) > 16) return false;
+    for (int32_t ty = ty0; ty <= ty1; ty++)
+        for (int32_t tx = tx0; tx <= tx1; tx++)
+            if (__ldcg(level1 + (size_t)ty * vw->hiz_rx + tx) <= zbits) return false;
+    return true;
+}
+
+// After the hierarchical depth: every visible meshlet of the visibility
+// views that is not an occluder (opaque, then alpha clip) is tested against
+// it, and the survivors go to the view's survivor lists for the second
+// raster pass (warp-aggregated appends, any order).  Threads stride over
+// the (view, meshlet) pairs.  Also resets the raster's claim and big-triangle
+// words for that pass (nothing of the occluder pass runs any more).
+__device__ void phase_occlusion_filter(const FrameDev& f, uint32_t view_begin, uint32_t n_views, uint64_t gtid,
+                                       uint64_t gstride) {
+    const uint32_t md = f.max_draws, lane = threadIdx.x & 31;
+    if (gtid == 0) {
+        f.status[kStRasterClaim] = 0u;
+        f.status[kStBigClaim] = 0u;
+        *reinterpret_cast<unsigned long long*>(f.status + kStBigPacked) = 0ull;
+    }
+    for (uint32_t v = 0; v < n_views; v++) {
+        const ViewDev* vw = f.views + view_begin + v;
+        if (vw->kind != kViewVisibility || !vw->lists) continue;
+        const uint32_t* cnt = reinterpret_cast<const uint32_t*>(vw->draws);
+        const uint32_t nop = min(cnt[0], md), nal = min(cnt[1], md);
+        const lh_mat4& pv = vw->uniforms->combined_perspective_view;
+        const uint64_t n = (uint64_t)nop + nal;
+        // whole warps iterate together (the appends are warp collectives)
+        for (uint64_t base = gtid - lane; base < n; base += gstride) {
+            const uint64_t i = base + lane;
+            bool keep = false, alpha = false;
+            uint32_t slot = 0;
+            if (i < n) {
+                alpha = i >= nop;
+                slot = alpha ? md + (uint32_t)(i - nop) : (uint32_t)i;
+                const RasterDraw* rd = vw->rdraws + slot;
+                const uint32_t bits = __ldcg(&rd->bits);
+                if (!(bits & kDrawOccluder)) {
+                    const float4 sp4 = __ldcg(reinterpret_cast<const float4*>(rd->sphere));
+                    const float sp[4] = {sp4.x, sp4.y, sp4.z, sp4.w};
+                    keep = !vw->hiz || !hiz_occluded(vw, pv, sp);
+                }
+            }
+#pragma unroll
+            for (int cl = 0; cl < 2; cl++) {
+                const bool mine = keep && (alpha == (cl == 1));
+                const uint32_t m = __ballot_sync(0xFFFFFFFFu, mine);
+                if (!m) continue;
+                const uint32_t leader = __ffs(m) - 1;
+                uint32_t first = 0;
+                if (lane == leader) first = atomicAdd(&vw->claim[cl ? kClaimSurvivorsAlpha : kClaimSurvivorsOpaque], __popc(m));
+                first = __shfl_sync(0xFFFFFFFFu, first, leader);
+                const uint32_t pos = first + __popc(m & ((1u << lane) - 1u));
+                if (mine && pos < md) vw->lists[(size_t)(cl ? 2u : 1u) * md + pos] = slot;
+            }
+        }
+    }
 }
 
 }  // namespace

@@ -92,10 +92,52 @@ def test_config2_full_parity(native, oracle):
     scene, r, fr, st, cap = _run(native, oracle, 2)
     stats = _assert_parity(r, fr, 200000, cap, st)
     assert stats["covered"] > 100000
-    # the raster's fragment counters (its depth-test reductions) equal the
+    # without the occlusion test every visible meshlet is rasterised: the
+    # raster's fragment counters (its depth-test reductions) then equal the
     # oracle's covered, alpha-passed fragments of the same frame
+    r.set_tuning(occlusion_px=0)
+    r.frame(scene.uniforms)
+    st0 = r.status()
+    _assert_parity(r, fr, 200000, cap, st0)
     rs = fr.raster_stats
-    assert (st.fragments[0], st.fragments[1]) == (rs["visibility"]["fragments"], rs["shadow"]["fragments"])
+    assert (st0.fragments[0], st0.fragments[1]) == (rs["visibility"]["fragments"], rs["shadow"]["fragments"])
+    # with it, the skipped meshlets' fragments are never issued
+    assert st.fragments[0] < st0.fragments[0] and st.fragments[1] == st0.fragments[1]
+
+
+def test_occlusion_raster_is_exact(native, oracle):
+    """The two-pass occlusion raster (occluders, hierarchical depth, depth
+    test of every other meshlet's sphere, survivors) gives the same bits as
+    the one-pass raster and the oracle, at several occluder thresholds, and
+    at the large configuration it skips most meshlets."""
+    lh = native
+    scene = lh.Scene(2).upload(0)
+    d = scene.desc
+    cap = max(1024, d.n_instances)
+    r = lh.Renderer(lh.Config(width=d.width, height=d.height, shadow_size=d.shadow_size, max_instances=cap,
+                              max_draws=200000))
+    r.set_scene(scene)
+    u = scene.uniforms
+    fr = oracle.run_scene(scene, shadow_size=d.shadow_size, max_instances=cap, max_draws=200000)
+    outs = {}
+    for px in (0, 4, 32, 128, 1024):
+        r.set_tuning(occlusion_px=px)
+        r.frame(u)
+        st = r.status()
+        assert st.flags == 0, (px, hex(st.flags))
+        errors, stats = compare_frame(r, fr, 200000, cap)
+        assert not errors, (px, errors)
+        outs[px] = (r.visibility(), r.hdr(), r.shadow_maps(), st)
+        if px:
+            occ, surv_op, surv_al = (int(x) for x in st.occlusion)
+            assert 0 < occ < st.visible_opaque[0]
+            assert surv_op + occ <= st.visible_opaque[0] and surv_al <= st.visible_alpha_clip[0]
+    for px in (4, 32, 128, 1024):
+        assert np.array_equal(outs[px][0], outs[0][0]) and np.array_equal(outs[px][2], outs[0][2])
+        assert np.array_equal(outs[px][1], outs[0][1])
+    st = outs[128][3]
+    # the near object hides most of the view: most meshlets never reach the raster
+    assert st.occlusion[0] + st.occlusion[1] < 0.2 * st.visible_opaque[0], list(st.occlusion)
 
 
 def test_overflow_capacities_flagged(native, oracle):
