@@ -433,6 +433,8 @@ def run_gpu(args):
         line["batched"] = bench_batched(lh, torch, args, local_rank)
     if args.differentiable:
         line["differentiable"] = bench_differentiable(lh, torch, args, local_rank)
+    if args.stress:
+        line["stress"] = bench_stress(lh, torch, args, local_rank)
     if rank == 0 and args.cpu_frames > 0:
         gpu_hdr = r.hdr()
         med, threads, stages, fr = cpu_oracle_frames(scene, args.cpu_frames)
@@ -581,6 +583,86 @@ def bench_differentiable(lh, torch, args, device):
             "resolve_forward_ms": f_ms, "resolve_backward_ms": b_ms, "bwd_over_fwd": b_ms / f_ms}
 
 
+def bench_stress(lh, torch, args, device):
+    """Stress workload (100,000 instances of 16 meshes up to 500k triangles,
+    ~40M candidate meshlets, 3840x2160 + 4 cascades at 1024^2): the frame
+    replayed from its CUDA graph, its stages, and the frame with the resolve
+    adjoint captured in the same graph (lh_frame_graph_backward); CUDA events
+    on one stream, L2 flushed between steps."""
+    import ctypes as C
+    import numpy as np
+    from lighthugger_gb300.diff import _scene_records
+    scene = lh.Scene(5, seed=args.seed).upload(device)
+    d = scene.desc
+    r = lh.Renderer(lh.Config(width=d.width, height=d.height, shadow_size=d.shadow_size, max_instances=d.n_instances,
+                              max_draws=6000000, max_big_triangles=1 << 22, device=device))
+    r.set_scene(scene)
+    stream = torch.cuda.Stream()
+    sptr = stream.cuda_stream
+    u = scene.uniforms
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    dev = torch.device("cuda", device)
+    recs, inst = _scene_records(scene)
+    total_v = sum(m.vertices for m in recs)
+    g_pos, g_nrm = torch.zeros(total_v * 3, device=dev), torch.zeros(total_v * 3, device=dev)
+    g_uv, g_bcf = torch.zeros(total_v * 2, device=dev), torch.zeros(len(recs) * 4, device=dev)
+    rows, first = [], 0
+    for k, m in enumerate(recs):
+        rows.append([g_pos.data_ptr() + 12 * first, g_nrm.data_ptr() + 12 * first, g_uv.data_ptr() + 8 * first,
+                     g_bcf.data_ptr() + 16 * k])
+        first += m.vertices
+    rec_dev = torch.tensor(np.array(rows, np.uint64).view(np.int64), device=dev)
+    inst_rec = torch.tensor(rec_dev.data_ptr() + 32 * inst.astype(np.int64), device=dev)
+    tex_grads = [torch.zeros(d.host_textures[i].width * d.host_textures[i].height * 4, device=dev)
+                 for i in range(d.n_textures)]
+    tex_tab = torch.tensor([t.data_ptr() for t in tex_grads], dtype=torch.int64, device=dev)
+    light = torch.zeros(8, device=dev)
+    grad = torch.randn(d.height, d.width, 4, device=dev, generator=torch.Generator(device=dev).manual_seed(3))
+    t = lh.GradTargets(instance_grads=inst_rec.data_ptr(), texture_grads=tex_tab.data_ptr(),
+                       light_dir=light.data_ptr(), light_color=light.data_ptr() + 16)
+
+    def timed(run, steps):
+        for _ in range(max(3, args.warmup)):
+            run()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for i in range(steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(i))
+                ev[i][0].record(stream)
+            run()
+            with torch.cuda.stream(stream):
+                ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in ev) / steps
+
+    steps = max(3, min(args.steps, 10))
+    frame_ms = timed(lambda: r.frame_graph(u, None, 0, stream=sptr), steps)
+    both_ms = timed(lambda: r.frame_graph_backward(u, None, 0, grad.data_ptr(), t, stream=sptr), steps)
+    r.set_profiling(True)
+    r.frame(u, stream=sptr)
+    stage_ms = r.stage_times()
+    r.set_profiling(False)
+    st = r.status()
+    out = {"workload": "%d instances of %d meshes, %.1fM triangles before culling, %dx%d + 4 cascades %d^2" % (
+        d.n_instances, d.n_meshes, d.total_triangles / 1e6, d.width, d.height, d.shadow_size),
+        "frame_graph_ms": frame_ms, "frame_and_backward_graph_ms": both_ms,
+        "backward_ms": both_ms - frame_ms,
+        "stage_ms": {k: round(v, 4) for k, v in stage_ms.items()},
+        "candidate_meshlets": int(st.candidate_meshlets[0]), "visible_instances": int(st.visible_instances[0]),
+        "visible_meshlets": int(st.visible_opaque[0] + st.visible_alpha_clip[0]),
+        "shadow_candidate_meshlets": int(sum(st.candidate_meshlets[1:5])),
+        "fragments": int(st.fragments[0]), "shadow_fragments": int(st.fragments[1]),
+        "fragments_per_s": st.fragments[0] / (stage_ms["raster"] * 1e-3) if stage_ms["raster"] else None,
+        # prefix-sum scale: candidate meshlets looked up per second by the meshlet cull
+        "meshlet_cull_candidates_per_s": st.candidate_meshlets[0] / (stage_ms["cull_meshlets"] * 1e-3)
+        if stage_ms["cull_meshlets"] else None,
+        "occlusion": {"occluders": int(st.occlusion[0]), "survivors_opaque": int(st.occlusion[1]),
+                      "survivors_alpha": int(st.occlusion[2])},
+        "status_flags": int(st.flags), "steps": steps}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -592,6 +674,7 @@ def main():
     ap.add_argument("--cpu-frames", type=int, default=3)
     ap.add_argument("--batched", type=int, default=1, help="also time the batched multi-view frame (config 3)")
     ap.add_argument("--differentiable", type=int, default=1, help="also time the resolve adjoint (config 4)")
+    ap.add_argument("--stress", type=int, default=1, help="also time the stress workload (config 5)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

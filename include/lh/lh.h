@@ -249,6 +249,10 @@ typedef struct lh_tuning {
                                  first, the hierarchical depth of what they wrote is built, and every other
                                  meshlet whose sphere lies behind it is skipped (no counterpart in the
                                  reference; results identical).  0: one pass, no occlusion test */
+    uint32_t chunk_rows[2];   /* pixel rows of a big-triangle chunk (one warp) in the visibility / shadow
+                                 pass: 4, 8, 16 or 32 */
+    uint32_t chunk_cols[2];   /* its columns: 32, 64 or 128 */
+    uint32_t backward_rows;   /* pixel rows of a resolve-adjoint tile (one warp per row): 4, 8 or 16 */
 } lh_tuning;
 
 lh_status lh_set_tuning(lh_ctx* ctx, const lh_tuning* tuning);

@@ -84,7 +84,14 @@ CONFIG_HDR_RGBA16F = 1  # lh_config.flags: the HDR image in RGBA16F
 
 class Tuning(C.Structure):
     _fields_ = [("small_px", C.c_uint32), ("medium_px", C.c_uint32), ("cull_blocks_per_sm", C.c_float),
-                ("schedule", C.c_uint32), ("raster_batch", C.c_uint32), ("occlusion_px", C.c_uint32)]
+                ("schedule", C.c_uint32), ("raster_batch", C.c_uint32), ("occlusion_px", C.c_uint32),
+                ("chunk_rows", C.c_uint32 * 2), ("chunk_cols", C.c_uint32 * 2), ("backward_rows", C.c_uint32)]
+
+    def as_dict(self):
+        return {"small_px": self.small_px, "medium_px": self.medium_px, "cull_blocks_per_sm": self.cull_blocks_per_sm,
+                "schedule": self.schedule, "raster_batch": self.raster_batch, "occlusion_px": self.occlusion_px,
+                "chunk_rows": list(self.chunk_rows), "chunk_cols": list(self.chunk_cols),
+                "backward_rows": self.backward_rows}
 
 
 class MeshGrads(C.Structure):
@@ -318,10 +325,18 @@ class Renderer:
         self.scene = scene
 
     def set_tuning(self, small_px=None, medium_px=None, cull_blocks_per_sm=None, schedule=None, raster_batch=None,
-                   occlusion_px=None):
+                   occlusion_px=None, chunk_rows=None, chunk_cols=None, backward_rows=None):
+        """Set the given launch-shape knobs (lh_tuning); chunk_rows / chunk_cols
+        are pairs (visibility pass, shadow pass)."""
         t = self.tuning()
         if occlusion_px is not None:
             t.occlusion_px = occlusion_px
+        if chunk_rows is not None:
+            t.chunk_rows[0], t.chunk_rows[1] = chunk_rows
+        if chunk_cols is not None:
+            t.chunk_cols[0], t.chunk_cols[1] = chunk_cols
+        if backward_rows is not None:
+            t.backward_rows = backward_rows
         if schedule is not None:
             t.schedule = schedule
         if raster_batch is not None:

@@ -1,16 +1,24 @@
-"""Autotuner of the launch shape: raster bin thresholds and the schedule.
+"""Autotuner of the launch shape (lh_tuning).
 
-The raster kernels split triangles into three bins by the pixel count of
-their bounding box -- rasterised by one lane (<= small_px), by one warp
-(<= medium_px), or cut into chunks of 16 x 32 (visibility) or 16 x 64
-(shadow) pixels spread over all warps --,
-claim `raster_batch` meshlets per atomic, and a batched frame can run per
-stage or as one persistent launch.  None of this
-changes a single output bit; it only moves time.  `tune()` times frames of
-the given workload with CUDA events for every candidate and keeps the
-fastest; results are cached per GPU name and workload signature in
-lighthugger_gb300/_build/tuning.json.
+The knobs, none of which changes a single output bit (they only move time):
+
+- occlusion_px: the two-pass occlusion raster's occluder threshold
+  (projected sphere radius in pixels; 0 = one pass without occlusion test);
+- small_px / medium_px: the raster's bins by bounding-box pixels -- one lane
+  (<= small_px), one warp (<= medium_px), or chunks spread over all warps;
+- chunk_rows / chunk_cols: the chunk (tile) shape of big triangles, per pass
+  (visibility, shadow);
+- raster_batch: meshlets a raster warp claims per atomic;
+- schedule: per stage or one persistent launch (batched frames);
+- backward_rows: rows of a resolve-adjoint tile (tune_backward).
+
+`tune()` times frames of the given workload with CUDA events and keeps the
+fastest, one group of knobs at a time (coordinate descent from the current
+tuning, groups in the order above); results are cached per GPU, target
+sizes, scene (instances, triangles, seed) and camera (a hash of the
+Uniforms) in lighthugger_gb300/_build/tuning.json.
 """
+import hashlib
 import itertools
 import json
 import os
@@ -18,32 +26,40 @@ import os
 _HERE = os.path.dirname(os.path.abspath(__file__))
 CACHE = os.path.join(_HERE, "_build", "tuning.json")
 
-SMALL = (4, 8, 16, 32)
-MEDIUM = (64, 128, 256, 512, 1024)
-BATCH = (1, 2, 4, 8)
+OCCLUSION = (0, 64, 128, 256, 512)
+SMALL = (16, 32)
+MEDIUM = (64, 128, 256)
+CHUNK = ((16, 32), (16, 64), (8, 64), (32, 32))  # (rows, columns)
+BATCH = (0, 1, 2, 4)
+BACKWARD_ROWS = (4, 8, 16)
+KNOBS = ("small_px", "medium_px", "schedule", "raster_batch", "occlusion_px", "chunk_rows", "chunk_cols")
 
 
-def _signature(renderer, n_probes, batched):
+def signature(renderer, uniforms, n_probes, batched):
+    """Cache key: GPU, target sizes, scene and camera of the workload."""
     import torch
     c = renderer.config
-    return "%s|%dx%d|s%d|p%d|%s" % (torch.cuda.get_device_name(), c.width, c.height, c.shadow_size, n_probes,
-                                    "batched" if batched else "plain")
+    d = renderer.scene.desc if getattr(renderer, "scene", None) is not None else None
+    scene = "i%d|t%d|seed%d" % (d.n_instances, d.total_triangles, d.seed) if d is not None else "noscene"
+    cam = hashlib.sha1(bytes(uniforms)).hexdigest()[:12]
+    return "%s|%dx%d|s%d|p%d|%s|%s|cam%s" % (torch.cuda.get_device_name(), c.width, c.height, c.shadow_size,
+                                            n_probes, "batched" if batched else "plain", scene, cam)
 
 
-def _load():
+def _load(path):
     try:
-        with open(CACHE) as f:
+        with open(path) as f:
             return json.load(f)
     except Exception:
         return {}
 
 
-def _save(cache):
-    os.makedirs(os.path.dirname(CACHE), exist_ok=True)
-    tmp = CACHE + ".tmp%d" % os.getpid()
+def _save(cache, path):
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    tmp = path + ".tmp%d" % os.getpid()
     with open(tmp, "w") as f:
         json.dump(cache, f, indent=1, sort_keys=True)
-    os.replace(tmp, CACHE)
+    os.replace(tmp, path)
 
 
 def time_frames(renderer, run, frames, stream):
@@ -63,17 +79,30 @@ def time_frames(renderer, run, frames, stream):
     return a.elapsed_time(b) / frames
 
 
-def tune(renderer, uniforms, probes=None, n_probes=0, batched=False, frames=4, use_cache=True, stream=None):
+def _apply(renderer, t):
+    renderer.set_tuning(**{k: t[k] for k in KNOBS})
+
+
+def _label(t):
+    return "occ%d/bins%d-%d/chunk%dx%d,%dx%d/batch%d/sched%d" % (
+        t["occlusion_px"], t["small_px"], t["medium_px"], t["chunk_rows"][0], t["chunk_cols"][0], t["chunk_rows"][1],
+        t["chunk_cols"][1], t["raster_batch"], t["schedule"])
+
+
+def tune(renderer, uniforms, probes=None, n_probes=0, batched=False, frames=4, use_cache=True, stream=None,
+         cache_path=None, digest=None):
     """Pick and apply the fastest tuning for this workload; returns
-    (tuning dict, {candidate: ms})."""
+    (tuning dict with its "ms", {candidate label: ms}).  `digest`, if given,
+    is called after each candidate's frames and its result stored per label
+    in the returned results under "digests" (tests compare them)."""
     import torch
     from . import SCHEDULE_PER_STAGE, SCHEDULE_PERSISTENT
-    key = _signature(renderer, n_probes, batched)
-    cache = _load() if use_cache else {}
+    path = cache_path or CACHE
+    key = signature(renderer, uniforms, n_probes, batched)
+    cache = _load(path) if use_cache else {}
     if key in cache:
         best = cache[key]
-        renderer.set_tuning(small_px=best["small_px"], medium_px=best["medium_px"], schedule=best["schedule"],
-                            raster_batch=best.get("raster_batch", 0))
+        _apply(renderer, best)
         return best, {}
     stream = stream or torch.cuda.Stream()
     sptr = stream.cuda_stream
@@ -83,28 +112,64 @@ def tune(renderer, uniforms, probes=None, n_probes=0, batched=False, frames=4, u
     else:
         run = lambda: renderer.frame_graph(uniforms, None, 0, stream=sptr)
         schedules = (SCHEDULE_PER_STAGE,)
-    results = {}
-    best, best_ms = None, float("inf")
-    # bins and schedule first (automatic claim batch), then the claim batch
-    for sched, small, medium in itertools.product(schedules, SMALL, MEDIUM):
-        if medium < small:
-            continue
-        renderer.set_tuning(small_px=small, medium_px=medium, schedule=sched, raster_batch=0)
+    cur = renderer.tuning().as_dict()
+    best = {k: cur[k] for k in KNOBS}
+    results, digests = {}, {}
+    best_ms = [float("inf")]
+
+    def measure(cand):
+        label = _label(cand)
+        if label in results:
+            return results[label]
+        _apply(renderer, cand)
         ms = time_frames(renderer, run, frames, stream)
-        results["%d/%d/%d/0" % (sched, small, medium)] = ms
-        if ms < best_ms:
-            best_ms, best = ms, {"small_px": small, "medium_px": medium, "schedule": sched, "raster_batch": 0, "ms": ms}
-    for batch in BATCH:
-        renderer.set_tuning(small_px=best["small_px"], medium_px=best["medium_px"], schedule=best["schedule"],
-                            raster_batch=batch)
-        ms = time_frames(renderer, run, frames, stream)
-        results["%d/%d/%d/%d" % (best["schedule"], best["small_px"], best["medium_px"], batch)] = ms
-        if ms < best_ms:
-            best_ms = ms
-            best = dict(best, raster_batch=batch, ms=ms)
-    renderer.set_tuning(small_px=best["small_px"], medium_px=best["medium_px"], schedule=best["schedule"],
-                        raster_batch=best["raster_batch"])
+        results[label] = ms
+        if digest is not None:
+            digests[label] = digest()
+        return ms
+
+    def descend(options):
+        nonlocal best
+        for change in options:
+            cand = dict(best, **change)
+            ms = measure(cand)
+            if ms < best_ms[0]:
+                best_ms[0], best = ms, cand
+
+    best_ms[0] = measure(best)
+    descend({"occlusion_px": v} for v in OCCLUSION)
+    descend({"small_px": a, "medium_px": b} for a, b in itertools.product(SMALL, MEDIUM))
+    descend({"chunk_rows": [r, best["chunk_rows"][1]], "chunk_cols": [c, best["chunk_cols"][1]]} for r, c in CHUNK)
+    descend({"chunk_rows": [best["chunk_rows"][0], r], "chunk_cols": [best["chunk_cols"][0], c]} for r, c in CHUNK)
+    descend({"raster_batch": v} for v in BATCH)
+    descend({"schedule": v} for v in schedules)
+    _apply(renderer, best)
+    best = dict(best, ms=best_ms[0])
     if use_cache:
         cache[key] = best
-        _save(cache)
+        _save(cache, path)
+    if digest is not None:
+        results["digests"] = digests
+    return best, results
+
+
+def tune_backward(renderer, grad_ptr, targets, frames=4, stream=None):
+    """Pick and apply the fastest adjoint tile (backward_rows) for the last
+    frame's resolve adjoint; returns (rows, {rows: ms})."""
+    import ctypes as C
+    import torch
+    from . import _check, lib
+    stream = stream or torch.cuda.Stream()
+    sptr = stream.cuda_stream
+
+    def run():
+        _check(lib().lh_resolve_backward(renderer.ctx, grad_ptr, C.byref(targets), C.c_void_p(sptr)),
+               "lh_resolve_backward", renderer.ctx)
+
+    results = {}
+    for rows in BACKWARD_ROWS:
+        renderer.set_tuning(backward_rows=rows)
+        results[rows] = time_frames(renderer, run, frames, stream)
+    best = min(results, key=results.get)
+    renderer.set_tuning(backward_rows=best)
     return best, results

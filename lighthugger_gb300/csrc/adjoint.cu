@@ -70,16 +70,13 @@ struct DeviceSampler {
 };
 
 constexpr uint32_t kFull = 0xFFFFFFFFu;
-// Launch shape: tiles of 32 x kBwdRows pixels, one warp per row, and the
-// blocks per SM the register budget is cut for (2: 128 registers a thread).
-#ifndef LH_BWD_ROWS
-#define LH_BWD_ROWS 8
-#endif
+// Launch shape: tiles of 32 x ROWS pixels (ROWS = 4, 8 or 16, chosen at run
+// time through lh_tuning.backward_rows), one warp per row, and the threads
+// per SM the register budget is cut for (LH_BWD_MIN_BLOCKS blocks of 8 rows:
+// 512 threads, 128 registers a thread, at every ROWS).
 #ifndef LH_BWD_MIN_BLOCKS
 #define LH_BWD_MIN_BLOCKS 2
 #endif
-constexpr int kBwdRows = LH_BWD_ROWS;
-constexpr int kBwdThreads = 32 * kBwdRows;
 constexpr uint32_t kCacheSlots = 256;     // shared-memory accumulators of hot gradient addresses
 constexpr uint32_t kSmallTexture = 64;    // textures of at most this many texels go through them
 
@@ -367,14 +364,15 @@ __device__ __forceinline__ void rel_columns(const FrameDev& f, uint32_t tid, flo
 // over the triangle's run of pixels in the warp's row before the atomics;
 // the light gradients stay in registers until block end; base-colour
 // factors and small textures accumulate in the block's HotCache.
-__global__ void __launch_bounds__(kBwdThreads, LH_BWD_MIN_BLOCKS)
+template <int ROWS>
+__global__ void __launch_bounds__(32 * ROWS, LH_BWD_MIN_BLOCKS * 8 / ROWS)
     k_resolve_backward(FrameDev f, const float4* grad, lh_grad_targets t, uint32_t tiles_x, uint32_t n_tiles) {
     __shared__ HotCache cache;
-    __shared__ float s_light[kBwdThreads / 32][6];
+    __shared__ float s_light[ROWS][6];
     pdl_enter();
     __shared__ __align__(16) FrameMats s_mats;
     const uint32_t tid = threadIdx.y * 32 + threadIdx.x;
-    for (uint32_t s = tid; s < kCacheSlots; s += kBwdThreads) {
+    for (uint32_t s = tid; s < kCacheSlots; s += 32 * ROWS) {
         cache.key[s] = 0ull;
         cache.sum[s] = 0.0f;
     }
@@ -385,7 +383,7 @@ __global__ void __launch_bounds__(kBwdThreads, LH_BWD_MIN_BLOCKS)
     float acc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     const uint64_t* tex_targets = reinterpret_cast<const uint64_t*>(t.texture_grads);
     for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-        const uint32_t x = (tile % tiles_x) * 32 + threadIdx.x, y = (tile / tiles_x) * kBwdRows + threadIdx.y;
+        const uint32_t x = (tile % tiles_x) * 32 + threadIdx.x, y = (tile / tiles_x) * ROWS + threadIdx.y;
         PixelGrad<float> g;
         PixelOut o;
         DeviceFixed fx;
@@ -499,34 +497,45 @@ __global__ void __launch_bounds__(kBwdThreads, LH_BWD_MIN_BLOCKS)
     __syncthreads();
     if (tid < 6) {
         float s = 0.0f;
-        for (int w = 0; w < kBwdThreads / 32; w++) s += s_light[w][tid];
+        for (int w = 0; w < ROWS; w++) s += s_light[w][tid];
         float* dst = tid < 3 ? reinterpret_cast<float*>(t.light_dir) : reinterpret_cast<float*>(t.light_color);
         if (dst) atomicAdd(dst + (tid % 3), s);
     }
-    for (uint32_t s = tid; s < kCacheSlots; s += kBwdThreads)
+    for (uint32_t s = tid; s < kCacheSlots; s += 32 * ROWS)
         if (cache.key[s]) atomicAdd(reinterpret_cast<float*>(cache.key[s]), cache.sum[s]);
 }
 
-int g_backward_blocks_per_sm = -1;
+int g_backward_blocks_per_sm[3] = {-1, -1, -1};
 
-}  // namespace
-
-cudaError_t launch_resolve_backward(const FrameDev& f, uint32_t width, uint32_t height, const float4* grad,
-                                    const lh_grad_targets& t, cudaStream_t s) {
-    if (g_backward_blocks_per_sm < 0) {
+template <int ROWS>
+cudaError_t launch_backward_rows(const FrameDev& f, uint32_t width, uint32_t height, const float4* grad,
+                                 const lh_grad_targets& t, cudaStream_t s, int& blocks_per_sm) {
+    if (blocks_per_sm < 0) {
         int n = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_resolve_backward, kBwdThreads, 0) != cudaSuccess) n = 1;
-        g_backward_blocks_per_sm = n > 0 ? n : 1;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_resolve_backward<ROWS>, 32 * ROWS, 0) != cudaSuccess)
+            n = 1;
+        blocks_per_sm = n > 0 ? n : 1;
     }
     int dev = 0, sms = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
-    const uint32_t tiles_x = (width + 31) / 32, tiles_y = (height + kBwdRows - 1) / kBwdRows;
+    const uint32_t tiles_x = (width + 31) / 32, tiles_y = (height + ROWS - 1) / ROWS;
     const uint32_t n_tiles = tiles_x * tiles_y;
     if (n_tiles == 0) return cudaSuccess;
-    const uint32_t grid = std::min<uint32_t>(n_tiles, (uint32_t)(sms * g_backward_blocks_per_sm));
-    return launch_pdl(k_resolve_backward, dim3(grid), dim3(32, kBwdRows), s, f, grad, t, tiles_x, n_tiles);
+    const uint32_t grid = std::min<uint32_t>(n_tiles, (uint32_t)(sms * blocks_per_sm));
+    return launch_pdl(k_resolve_backward<ROWS>, dim3(grid), dim3(32, ROWS), s, f, grad, t, tiles_x, n_tiles);
+}
+
+}  // namespace
+
+cudaError_t launch_resolve_backward(const FrameDev& f, uint32_t width, uint32_t height, const float4* grad,
+                                    const lh_grad_targets& t, cudaStream_t s) {
+    switch (f.backward_rows) {
+        case 4: return launch_backward_rows<4>(f, width, height, grad, t, s, g_backward_blocks_per_sm[0]);
+        case 16: return launch_backward_rows<16>(f, width, height, grad, t, s, g_backward_blocks_per_sm[2]);
+        default: return launch_backward_rows<8>(f, width, height, grad, t, s, g_backward_blocks_per_sm[1]);
+    }
 }
 
 }  // namespace lh

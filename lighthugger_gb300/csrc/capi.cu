@@ -282,6 +282,11 @@ FrameDev frame_dev(const lh_ctx* c, uint32_t n_views, uint32_t n_instances) {
     f.frame_consts = c->d_consts;
     f.srgb_lut = c->d_srgb;
     f.occlusion_px = c->tuning.occlusion_px;
+    for (int k = 0; k < 2; k++) {
+        f.chunk_shift[k][0] = (uint32_t)__builtin_ctz(c->tuning.chunk_rows[k]);
+        f.chunk_shift[k][1] = (uint32_t)__builtin_ctz(c->tuning.chunk_cols[k]);
+    }
+    f.backward_rows = c->tuning.backward_rows;
     return f;
 }
 
@@ -487,7 +492,7 @@ lh_status lh_create(const lh_config* config, lh_ctx** out) {
     if (!c) return LH_ERR_OUT_OF_MEMORY;
     c->cfg = cfg;
     c->device = cfg.device;
-    c->tuning = lh_tuning{32u, 128u, 2.0f, LH_SCHEDULE_DEFAULT, 0u, 128u};
+    c->tuning = lh_tuning{32u, 128u, 2.0f, LH_SCHEDULE_DEFAULT, 0u, 256u, {16u, 16u}, {32u, 64u}, 8u};
     cudaError_t e = cudaSetDevice(c->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device);
     c->max_views = 5 + cfg.max_probes;
@@ -986,6 +991,10 @@ lh_status lh_set_tuning(lh_ctx* c, const lh_tuning* t) {
         t->cull_blocks_per_sm > 64.0f || t->schedule > LH_SCHEDULE_PER_VIEW || t->raster_batch > 64 ||
         t->occlusion_px > 65536)
         return LH_ERR_INVALID_ARGUMENT;
+    auto pow2_in = [](uint32_t v, uint32_t lo, uint32_t hi) { return v >= lo && v <= hi && (v & (v - 1)) == 0; };
+    for (int k = 0; k < 2; k++)
+        if (!pow2_in(t->chunk_rows[k], 4, 32) || !pow2_in(t->chunk_cols[k], 32, 128)) return LH_ERR_INVALID_ARGUMENT;
+    if (!pow2_in(t->backward_rows, 4, 16)) return LH_ERR_INVALID_ARGUMENT;
     c->tuning = *t;
     return LH_OK;
 }

@@ -90,8 +90,8 @@ struct ViewDev {
 };
 
 // Triangle handed to the chunked raster path: its set-up (orientation
-// normalised, pixel bounds) and the first of its chunks (kChunkRows x
-// chunk_cols<KIND>() pixels).
+// normalised, pixel bounds) and its pixel bounds, cut into chunks of
+// FrameDev::chunk_shift.
 struct BigTri {
     int32_t X0, Y0, X1, Y1, X2, Y2;
     float z0, s1, s2;
@@ -100,25 +100,11 @@ struct BigTri {
     uint32_t bias;
     int32_t px0, px1, py0, py1;
 };
-// Chunk of a big triangle (one warp): rows x columns of pixels.  The
-// visibility pass uses 16 x 32 (raster stage 0.332 -> 0.326 ms against
-// 16 x 64), the shadow pass 16 x 64 (0.099 ms against 0.103 ms at 16 x 32;
-// 0.088 against 0.092 ms once the shadow pass lost its warp bin); 8 x 64 was
-// slower for both.
-#ifndef LH_CHUNK_ROWS
-#define LH_CHUNK_ROWS 16
-#endif
-#ifndef LH_CHUNK_COLS_VIS
-#define LH_CHUNK_COLS_VIS 32
-#endif
-#ifndef LH_CHUNK_COLS_SHADOW
-#define LH_CHUNK_COLS_SHADOW 64
-#endif
-constexpr int32_t kChunkRows = LH_CHUNK_ROWS;
-template <int KIND>
-__host__ __device__ constexpr int32_t chunk_cols() {
-    return KIND == 0 ? LH_CHUNK_COLS_VIS : LH_CHUNK_COLS_SHADOW;
-}
+// Chunk of a big triangle (one warp): rows x columns of pixels, powers of
+// two chosen per pass at run time (lh_tuning.chunk_rows / chunk_cols, by
+// the autotuner): FrameDev::chunk_shift holds their log2.  Measured by hand
+// before: the visibility pass at 16 x 32 (raster stage 0.332 -> 0.326 ms
+// against 16 x 64), the shadow pass at 16 x 64 (0.088 against 0.092 ms).
 
 // Per-frame scratch words (zeroed at frame start; the raster words again
 // before each raster pass).
@@ -162,6 +148,8 @@ struct FrameDev {
     const float* frame_consts;  // [0] pow(0.5, split), [1] pow(0.75, split)
     const float* srgb_lut;      // 256 entries
     uint32_t occlusion_px;      // occluder threshold (projected sphere radius, pixels); 0: no occlusion culling
+    uint32_t chunk_shift[2][2]; // [pass: visibility, shadow][log2 rows, log2 columns] of a big-triangle chunk
+    uint32_t backward_rows;     // pixel rows of a resolve-adjoint tile: 4, 8 or 16
 };
 
 // Launch `kernel` with programmatic stream serialisation: its blocks may

@@ -210,9 +210,9 @@ __device__ __forceinline__ void load_transform(const Instance* inst, lh_mat4& m)
 // index and its first chunk come from the same word, so chunk bases ascend
 // with the index and the band kernel finds a chunk's triangle by binary search.
 template <int KIND>
-__device__ __forceinline__ unsigned long long big_chunks(const TriSetup& t) {
-    const uint32_t nbx = (uint32_t)(t.px1 - t.px0) / chunk_cols<KIND>() + 1;
-    const uint32_t nby = (uint32_t)(t.py1 - t.py0) / kChunkRows + 1;
+__device__ __forceinline__ unsigned long long big_chunks(const FrameDev& f, const TriSetup& t) {
+    const uint32_t nbx = ((uint32_t)(t.px1 - t.px0) >> f.chunk_shift[KIND][1]) + 1;
+    const uint32_t nby = ((uint32_t)(t.py1 - t.py0) >> f.chunk_shift[KIND][0]) + 1;
     return (unsigned long long)nbx * nby;
 }
 // Store the queue entry of a triangle of n chunks whose packed word (before
@@ -240,7 +240,7 @@ __device__ void store_big(const FrameDev& f, const TriSetup& t, uint32_t view, u
 // One thread's triangle.
 template <int KIND>
 __device__ void push_big(const FrameDev& f, const TriSetup& t, uint32_t view) {
-    const unsigned long long n = big_chunks<KIND>(t);
+    const unsigned long long n = big_chunks<KIND>(f, t);
     const unsigned long long old =
         atomicAdd(reinterpret_cast<unsigned long long*>(f.status + kStBigPacked), (1ull << 40) | n);
     store_big(f, t, view, old, n);
@@ -250,7 +250,7 @@ __device__ void push_big(const FrameDev& f, const TriSetup& t, uint32_t view) {
 // lane the running total below it).  The word's low 40 bits cannot carry into
 // the count: a sum reaching 2^32 chunks is flagged and dropped.
 __device__ void push_big_warp(const FrameDev& f, const TriSetup& t, uint32_t view, bool big, uint32_t lane) {
-    const unsigned long long n = big ? big_chunks<1>(t) : 0ull;
+    const unsigned long long n = big ? big_chunks<1>(f, t) : 0ull;
     const unsigned long long mine = big ? (1ull << 40) | n : 0ull;
     unsigned long long incl = mine;
 #pragma unroll
@@ -822,9 +822,9 @@ __device__ __noinline__ uint32_t raster_chunk_alpha(const FrameDev& f, const Big
     return n;
 }
 
-// One warp per chunk of a big triangle (16 x 32 pixels in the visibility
-// pass, 16 x 64 in the shadow pass: chunk_cols); chunks whose
-// rectangle lies outside one edge are skipped whole.
+// One warp per chunk of a big triangle (rows x columns of f.chunk_shift;
+// 16 x 32 pixels in the visibility pass and 16 x 64 in the shadow pass by
+// default); chunks whose rectangle lies outside one edge are skipped whole.
 template <int KIND>
 __device__ void phase_raster_big(const FrameDev& f) {
     const unsigned long long packed = *reinterpret_cast<volatile unsigned long long*>(f.status + kStBigPacked);
@@ -869,8 +869,9 @@ __device__ void phase_raster_big(const FrameDev& f) {
         }
         c++;
         const BigTri b = f.big[i];
-        const uint32_t nbx = (uint32_t)(b.px1 - b.px0) / chunk_cols<KIND>() + 1;
-        const uint32_t nby = (uint32_t)(b.py1 - b.py0) / kChunkRows + 1;
+        const uint32_t rs = f.chunk_shift[KIND][0], cs = f.chunk_shift[KIND][1];
+        const uint32_t nbx = ((uint32_t)(b.px1 - b.px0) >> cs) + 1;
+        const uint32_t nby = ((uint32_t)(b.py1 - b.py0) >> rs) + 1;
         const uint32_t base = f.big_base[i];
         const unsigned long long local = (c - 1u) - base;
         if (local >= (unsigned long long)nbx * nby) continue;  // chunk of a dropped triangle
@@ -878,8 +879,8 @@ __device__ void phase_raster_big(const FrameDev& f) {
         t_base = base;
         t_end = base + nbx * nby;
         const int32_t cx = (int32_t)(local % nbx), cy = (int32_t)(local / nbx);
-        const int32_t x0 = b.px0 + cx * chunk_cols<KIND>(), x1 = min(b.px1, x0 + chunk_cols<KIND>() - 1);
-        const int32_t y0 = b.py0 + cy * kChunkRows, y1 = min(b.py1, y0 + kChunkRows - 1);
+        const int32_t x0 = b.px0 + (cx << cs), x1 = min(b.px1, x0 + (1 << cs) - 1);
+        const int32_t y0 = b.py0 + (cy << rs), y1 = min(b.py1, y0 + (1 << rs) - 1);
         if (edge_rejects(b.X1, b.Y1, b.X2, b.Y2, x0, x1, y0, y1, b.bias & 1u) ||
             edge_rejects(b.X2, b.Y2, b.X0, b.Y0, x0, x1, y0, y1, (b.bias >> 1) & 1u) ||
             edge_rejects(b.X0, b.Y0, b.X1, b.Y1, x0, x1, y0, y1, (b.bias >> 2) & 1u))
