@@ -19,10 +19,16 @@ struct Tex4 { float r, g, b, a; };
 
 // Bilinear filtering of level 0 with repeat addressing, over the texture's
 // linear float4 copy.
+// A 1 x 1 texture (the scenes' constant materials) returns its texel: the
+// bilinear blend of four copies of one value is that value up to rounding.
 __device__ Tex4 sample_repeat(const FrameDev& f, uint32_t index, f2 uv) {
     if (index >= f.n_textures) return {0.0f, 0.0f, 0.0f, 0.0f};
     const lh_texture t = f.textures[index];
     const float4* tex = f.tex_linear[index];
+    if (t.width == 1 && t.height == 1) {
+        const float4 p = __ldg(tex);
+        return Tex4{p.x, p.y, p.z, p.w};
+    }
     float u = uv.x * (float)t.width - 0.5f, v = uv.y * (float)t.height - 0.5f;
     if (!(fabsf(u) < 1e9f)) u = 0.0f;
     if (!(fabsf(v) < 1e9f)) v = 0.0f;
@@ -68,10 +74,14 @@ __device__ float sample_shadow(const FrameDev& f, f2 uv, float layer_f, float re
 
 // The 9-tap PCF of render_geometry.comp:200-214 at shadow coordinate
 // (sx, sy), reference depth `ref`: the sum of sample_shadow over the taps
-// at offsets (ox, oy) / 1024, ox outer, oy inner (the same sum, in the same
-// order).  When the taps' texel columns and rows are consecutive (a
-// 1024-texel cascade: the offsets are one texel apart) the 4 x 4 texels they
-// share are compared once -- 16 loads instead of 36; otherwise tap by tap.
+// at offsets (ox, oy) / 1024.  When the taps' texel columns and rows are
+// consecutive (a 1024-texel cascade: the offsets are one texel apart) the
+// 4 x 4 texels they share are compared once -- 16 loads instead of 36 -- and
+// the sum is taken in separable form: tap (ox, oy) weighs its 2 x 2 texels by
+// (1 - a_ox, a_ox) x (1 - b_oy, b_oy), so texel (i, j) of the window carries
+// CX(i) * CY(j) with CX = (1 - a_0, a_0 + 1 - a_1, a_1 + 1 - a_2, a_2) and CY
+// alike: the same compare results, the same weights, summed in another
+// order (float rounding only).  Otherwise tap by tap.
 __device__ float pcf9(const FrameDev& f, float sx, float sy, float layer_f, float ref) {
     const uint32_t S = f.shadow_size;
     float ax[3], ay[3];
@@ -103,18 +113,16 @@ __device__ float pcf9(const FrameDev& f, float sx, float sy, float layer_f, floa
         // no texel passes: every tap is 0 * (finite, non-negative weights)
         // summed, exactly +0
         if (bits == 0u) return 0.0f;
+        const float cx[4] = {1.0f - ax[0], ax[0] + (1.0f - ax[1]), ax[1] + (1.0f - ax[2]), ax[2]};
+        const float cy[4] = {1.0f - ay[0], ay[0] + (1.0f - ay[1]), ay[1] + (1.0f - ay[2]), ay[2]};
         float sum = 0.0f;
 #pragma unroll
-        for (int ox = 0; ox < 3; ox++)
-#pragma unroll
-            for (int oy = 0; oy < 3; oy++) {
-                const float a = ax[ox], b = ay[oy];
-                const uint32_t q = bits >> (4 * oy + ox);
-                const float c00 = (q & 1u) ? 1.0f : 0.0f, c10 = (q & 2u) ? 1.0f : 0.0f;
-                const float c01 = (q & 16u) ? 1.0f : 0.0f, c11 = (q & 32u) ? 1.0f : 0.0f;
-                const float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
-                sum += ((c00 * w00 + c10 * w10) + c01 * w01) + c11 * w11;
-            }
+        for (int r = 0; r < 4; r++) {
+            const uint32_t q = bits >> (4 * r);
+            const float row = (((q & 1u) ? cx[0] : 0.0f) + ((q & 2u) ? cx[1] : 0.0f)) +
+                              (((q & 4u) ? cx[2] : 0.0f) + ((q & 8u) ? cx[3] : 0.0f));
+            sum = __fmaf_rn(row, cy[r], sum);
+        }
         return sum;
     }
     float sum = 0.0f;
@@ -302,12 +310,89 @@ __device__ __noinline__ f3 apply_normal_map(const FrameDev& f, uint32_t tex, f2 
                         (tt.z * mn.x + bb.z * mn.y) + normal.z * mn.z});
 }
 
+// Vertex k of triangle `packed` (tri << 24 | draw slot) of the main view as
+// the lighting reads it -- world position, clip position (PV times it),
+// normalised raw normal, uv times the texture scale -- in the arithmetic
+// and order the lighting has always used.
+__device__ __forceinline__ void load_vertex(const FrameDev& f, uint32_t packed, uint32_t k, f3& p, f4& c, f3& n,
+                                            float& us, float& vs) {
+    const uint32_t slot = packed & ((1u << 24) - 1u), tri = packed >> 24;
+    const RasterDraw rd = f.views[0].rdraws[slot];
+    const Instance* inst = f.instances + rd.instance;
+    const MeshInfo* mip = mesh_info_of(inst);
+    const uint32_t flags = rd.bits >> 16;
+    const uint32_t vi = __ldg(reinterpret_cast<const uint8_t*>(rd.micro) + tri * 3 + k);
+    const uint32_t idx = (flags & MESH_INFO_FLAGS_32_BIT_INDICES)
+                             ? __ldg(reinterpret_cast<const uint32_t*>(rd.indices) + vi)
+                             : __ldg(reinterpret_cast<const uint16_t*>(rd.indices) + vi);
+    p = world_pos(inst->transform, load_position(rd.positions, flags, idx));
+    c = mul(f.uniforms->combined_perspective_view, f4{p.x, p.y, p.z, 1.0f});
+    n = fast_normalize(load_normal_raw(__ldg(&mip->normals), flags, idx));
+    const f2 uv = load_uv_raw(__ldg(&mip->uvs), flags, idx);
+    us = uv.x * __ldg(&mip->texture_scale.x);
+    vs = uv.y * __ldg(&mip->texture_scale.y);
+}
+
+constexpr uint32_t kShareTris = 10;  // distinct triangles a warp row shares vertex work for
+
+// The vertex stage of a warp's 32 pixels (called by all lanes).  Neighbouring
+// pixels mostly show one triangle (1.26 distinct triangles per 32-pixel row
+// on average in the large workload), so the distinct triangles' vertices are
+// computed once, one vertex per lane -- lanes 3k, 3k + 1, 3k + 2 for the
+// k-th distinct triangle -- into the warp's shared-memory slots (3 float4 a
+// vertex: p.xyz n.x | c.xyzw | n.yz us vs), at a third of the vertex work of
+// every pixel computing its own three.  Returns the pixel's first slot, or
+// -1 when the row holds more than kShareTris distinct triangles (each pixel
+// then computes its own at use).
+__device__ __forceinline__ int32_t share_vertices(const FrameDev& f, bool covered, uint32_t packed, uint32_t* s_keys,
+                                                  float4* s_vert) {
+    const uint32_t lane = threadIdx.x;
+    const uint32_t key = covered ? packed : 0xFFFFFFFFu;
+    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+    const uint32_t leader = __ffs(peers) - 1;
+    const uint32_t leaders = __ballot_sync(0xFFFFFFFFu, covered && lane == leader);
+    const uint32_t n = __popc(leaders);
+    if (n > kShareTris) return -1;
+    const uint32_t rank = __popc(leaders & ((1u << leader) - 1u));  // the pixel's distinct-triangle index
+    if (covered && lane == leader) s_keys[rank] = packed;
+    __syncwarp();
+    if (lane < 3 * n) {
+        f3 p, nv;
+        f4 c;
+        float us, vs;
+        load_vertex(f, s_keys[lane / 3], lane % 3, p, c, nv, us, vs);
+        s_vert[3 * lane] = make_float4(p.x, p.y, p.z, nv.x);
+        s_vert[3 * lane + 1] = make_float4(c.x, c.y, c.z, c.w);
+        s_vert[3 * lane + 2] = make_float4(nv.y, nv.z, us, vs);
+    }
+    __syncwarp();
+    return (int32_t)(3 * rank);
+}
+
+// Vertex k of the pixel's triangle: from the warp's slots, or computed.
+__device__ __forceinline__ void pixel_vertex(const FrameDev& f, const float4* s_vert, int32_t base, uint32_t packed,
+                                             uint32_t k, f3& p, f4& c, f3& n, float& us, float& vs) {
+    if (base < 0) {
+        load_vertex(f, packed, k, p, c, n, us, vs);
+        return;
+    }
+    const float4 a = s_vert[3 * (base + k)], b = s_vert[3 * (base + k) + 1], d = s_vert[3 * (base + k) + 2];
+    p = f3{a.x, a.y, a.z};
+    c = f4{b.x, b.y, b.z, b.w};
+    n = f3{a.w, d.x, d.y};
+    us = d.z;
+    vs = d.w;
+}
+
 // `clock_slot`: the thread's shared-memory word for the clock view's start
-// time (kept out of registers).
+// time (kept out of registers).  Called by all lanes of the warp (the vertex
+// stage is a warp collective); `in_view` false for lanes past the image.
 __device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uint32_t y, unsigned long long vis,
-                                              long long* clock_slot) {
+                                              bool in_view, long long* clock_slot, uint32_t* s_keys, float4* s_vert) {
     const Uniforms& u = *f.uniforms;
-    if (u.debug == 4) *clock_slot = clock64();
+    if (in_view && u.debug == 4) *clock_slot = clock64();
+    const int32_t vbase = share_vertices(f, in_view && u2f((uint32_t)(vis >> 32)) != 0.0f, (uint32_t)vis, s_keys, s_vert);
+    if (!in_view) return;
     const uint32_t W = u.window_size.x, H = u.window_size.y;
     const f2 ndc{(float)x / (float)W * 2.0f - 1.0f, (float)y / (float)H * 2.0f - 1.0f};
     const size_t pix = (size_t)y * W + x;
@@ -322,38 +407,24 @@ __device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uin
     }
     const uint32_t packed = (uint32_t)vis;
     const uint32_t slot = packed & ((1u << 24) - 1u), tri = packed >> 24;
-    // the slot's draw record (written by the meshlet cull) carries the index
-    // and micro-index addresses of the meshlet: the micro indices load in
-    // parallel with the instance and its MeshInfo instead of after them
+    // the slot's draw record (written by the meshlet cull): instance and
+    // MeshInfo flags; the vertices came from the warp's vertex stage
     const RasterDraw rd = f.views[0].rdraws[slot];
     const Instance* inst = f.instances + rd.instance;
     const MeshInfoResolve mi = load_mesh_info_resolve(mesh_info_of(inst));
-    const uint8_t* micro = reinterpret_cast<const uint8_t*>(rd.micro) + tri * 3;
     const uint32_t flags = rd.bits >> 16;
-    uint32_t idx[3];
-    for (int k = 0; k < 3; k++) {
-        const uint32_t vi = __ldg(micro + k);
-        idx[k] = (flags & MESH_INFO_FLAGS_32_BIT_INDICES) ? __ldg(reinterpret_cast<const uint32_t*>(rd.indices) + vi)
-                                                          : __ldg(reinterpret_cast<const uint16_t*>(rd.indices) + vi);
-    }
-    const lh_mat4& T = inst->transform;
-    f3 pa = world_pos(T, load_position(rd.positions, flags, idx[0]));
-    f3 pb = world_pos(T, load_position(rd.positions, flags, idx[1]));
-    f3 pc = world_pos(T, load_position(rd.positions, flags, idx[2]));
+    f3 pa, pb, pc, na, nb, nc;
+    f4 ca, cb, cc;
+    f3 us, vs;
+    pixel_vertex(f, s_vert, vbase, packed, 0, pa, ca, na, us.x, vs.x);
+    pixel_vertex(f, s_vert, vbase, packed, 1, pb, cb, nb, us.y, vs.y);
+    pixel_vertex(f, s_vert, vbase, packed, 2, pc, cc, nc, us.z, vs.z);
     const lh_mat4& PV = u.combined_perspective_view;
-    const Bary bary = calc_full_bary<false>(mul(PV, f4{pa.x, pa.y, pa.z, 1.0f}), mul(PV, f4{pb.x, pb.y, pb.z, 1.0f}),
-                                            mul(PV, f4{pc.x, pc.y, pc.z, 1.0f}), ndc, f2{(float)W, (float)H});
+    const Bary bary = calc_full_bary<false>(ca, cb, cc, ndc, f2{(float)W, (float)H});
     const f3 world{dot(f3{pa.x, pb.x, pc.x}, bary.lambda), dot(f3{pa.y, pb.y, pc.y}, bary.lambda),
                    dot(f3{pa.z, pb.z, pc.z}, bary.lambda)};
-    f2 ua = load_uv_raw(mi.uvs, flags, idx[0]), ub = load_uv_raw(mi.uvs, flags, idx[1]),
-       uc = load_uv_raw(mi.uvs, flags, idx[2]);
-    f2 ts{mi.texture_scale.x, mi.texture_scale.y};
-    const f3 us{ua.x * ts.x, ub.x * ts.x, uc.x * ts.x}, vs{ua.y * ts.y, ub.y * ts.y, uc.y * ts.y};
     f2 uv{dot(us, bary.lambda) + mi.texture_offset.x, dot(vs, bary.lambda) + mi.texture_offset.y};
     f3 view_vector = normalize(ld3(u.camera_pos) - world);
-    f3 na = fast_normalize(load_normal_raw(mi.normals, flags, idx[0]));
-    f3 nb = fast_normalize(load_normal_raw(mi.normals, flags, idx[1]));
-    f3 nc = fast_normalize(load_normal_raw(mi.normals, flags, idx[2]));
     f3 normal{interp_deriv(bary, na.x, nb.x, nc.x).x, interp_deriv(bary, na.y, nb.y, nc.y).x,
               interp_deriv(bary, na.z, nb.z, nc.z).x};
     normal = fast_normalize(mul3(inst->normal_transform, normal));
@@ -426,6 +497,8 @@ __global__ void __launch_bounds__(kResolveWarps * 32, LH_RESOLVE_MIN_BLOCKS)
     __shared__ __align__(8) uint64_t s_bar[kResolveWarps][kResolveStages];
     pdl_enter();
     __shared__ long long s_clock[kResolveWarps][32];
+    __shared__ uint32_t s_keys[kResolveWarps][kShareTris];
+    __shared__ __align__(16) float4 s_vert[kResolveWarps][3 * 3 * kShareTris];
     const uint32_t W = f.uniforms->window_size.x, H = f.uniforms->window_size.y;
     const uint32_t lane = threadIdx.x, warp = threadIdx.y;
     unsigned long long(*vis_buf)[kStripCols] = s_vis[warp];
@@ -477,11 +550,12 @@ __global__ void __launch_bounds__(kResolveWarps * 32, LH_RESOLVE_MIN_BLOCKS)
 #pragma unroll 1
         for (uint32_t j = 0; j < kStripCols / 32; j++) {
             const uint32_t x = (uint32_t)x0 + 32 * j + lane;
-            if (x >= W) continue;
+            const bool in_view = x < W;  // every lane takes part: the vertex stage is a warp collective
             const unsigned long long vis =
-                kTma ? vis_buf[st][32 * j + lane]
-                     : __ldcs(reinterpret_cast<const unsigned long long*>(f.visibility) + (size_t)y * W + x);
-            resolve_pixel(f, x, (uint32_t)y, vis, &s_clock[warp][lane]);
+                !in_view ? 0ull
+                         : kTma ? vis_buf[st][32 * j + lane]
+                                : __ldcs(reinterpret_cast<const unsigned long long*>(f.visibility) + (size_t)y * W + x);
+            resolve_pixel(f, x, (uint32_t)y, vis, in_view, &s_clock[warp][lane], s_keys[warp], s_vert[warp]);
         }
         if (kTma) {
             __syncwarp();  // stage st is free again; the other stage's strip is already in flight
