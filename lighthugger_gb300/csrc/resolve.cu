@@ -387,8 +387,10 @@ __device__ __forceinline__ void pixel_vertex(const FrameDev& f, const float4* s_
 // `clock_slot`: the thread's shared-memory word for the clock view's start
 // time (kept out of registers).  Called by all lanes of the warp (the vertex
 // stage is a warp collective); `in_view` false for lanes past the image.
+// `s_uvs`: the block's shared copy of the 4 cascades' uv-space matrices.
 __device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uint32_t y, unsigned long long vis,
-                                              bool in_view, long long* clock_slot, uint32_t* s_keys, float4* s_vert) {
+                                              bool in_view, long long* clock_slot, uint32_t* s_keys, float4* s_vert,
+                                              const lh_mat4* s_uvs) {
     const Uniforms& u = *f.uniforms;
     if (in_view && u.debug == 4) *clock_slot = clock64();
     const int32_t vbase = share_vertices(f, in_view && u2f((uint32_t)(vis >> 32)) != 0.0f, (uint32_t)vis, s_keys, s_vert);
@@ -441,7 +443,7 @@ __device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uin
     uint32_t ci;
     f4 sc{0.0f, 0.0f, 0.0f, 0.0f};
     for (ci = 0; ci < 4; ci++) {
-        sc = mul(f.misc->uv_space_shadow_matrices[ci], f4{world.x, world.y, world.z, 1.0f});
+        sc = mul(s_uvs[ci], f4{world.x, world.y, world.z, 1.0f});
         float ox = sc.x - 0.5f, oy = sc.y - 0.5f;
         if (fabsf(ox) < 0.5f && fabsf(oy) < 0.5f) break;
     }
@@ -459,11 +461,12 @@ __device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uin
         store_hdr(f.hdr, f.hdr_half, pix, o.x, o.y, o.z);
         return;
     }
+    // The reference's 9-term sum has zero coefficients but sh[0] and sh[2]:
+    // for a finite normal each zero term is +-0, and adding +-0 leaves a sum
+    // unchanged, so the sum is bit for bit sh0 + sh0 * n.y.
     const float amb_level = 0.025f;
-    const f3 zero{0.0f, 0.0f, 0.0f}, sh0{amb_level, amb_level, amb_level};
-    f3 amb = ((((((((sh0 + zero * normal.x) + sh0 * normal.y) + zero * normal.z) + zero * (normal.x * normal.z)) +
-                  zero * (normal.z * normal.y)) + zero * (normal.y * normal.x)) +
-               zero * (3.0f * normal.z * normal.z - 1.0f)) + zero * (normal.x * normal.x - normal.y * normal.y));
+    const f3 sh0{amb_level, amb_level, amb_level};
+    f3 amb = sh0 + sh0 * normal.y;
     f3 ambient = amb * (base * (1.0f - metallic));
     float sun_intensity = kPi * shadow_sum;
     // Uniforms.sun_intensity is the light colour (1,1,1 in the reference, whose
@@ -498,9 +501,16 @@ __global__ void __launch_bounds__(kResolveWarps * 32, LH_RESOLVE_MIN_BLOCKS)
     pdl_enter();
     __shared__ long long s_clock[kResolveWarps][32];
     __shared__ uint32_t s_keys[kResolveWarps][kShareTris];
+    __shared__ __align__(16) lh_mat4 s_uvs[4];
     __shared__ __align__(16) float4 s_vert[kResolveWarps][3 * 3 * kShareTris];
     const uint32_t W = f.uniforms->window_size.x, H = f.uniforms->window_size.y;
     const uint32_t lane = threadIdx.x, warp = threadIdx.y;
+    // the cascades' matrices, read by every pixel's cascade selection
+    if (warp < 2) {  // 64 floats
+        const float* src = &f.misc->uv_space_shadow_matrices[0].cols[0].x;
+        reinterpret_cast<float*>(s_uvs)[warp * 32 + lane] = src[warp * 32 + lane];
+    }
+    __syncthreads();
     unsigned long long(*vis_buf)[kStripCols] = s_vis[warp];
     uint64_t* bar = s_bar[warp];
     constexpr uint32_t kRowBytes = kStripCols * 8;
@@ -555,7 +565,7 @@ __global__ void __launch_bounds__(kResolveWarps * 32, LH_RESOLVE_MIN_BLOCKS)
                 !in_view ? 0ull
                          : kTma ? vis_buf[st][32 * j + lane]
                                 : __ldcs(reinterpret_cast<const unsigned long long*>(f.visibility) + (size_t)y * W + x);
-            resolve_pixel(f, x, (uint32_t)y, vis, in_view, &s_clock[warp][lane], s_keys[warp], s_vert[warp]);
+            resolve_pixel(f, x, (uint32_t)y, vis, in_view, &s_clock[warp][lane], s_keys[warp], s_vert[warp], s_uvs);
         }
         if (kTma) {
             __syncwarp();  // stage st is free again; the other stage's strip is already in flight
