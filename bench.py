@@ -240,6 +240,19 @@ def _workload_name(cfg, d):
         names.get(cfg, str(cfg)), d.n_instances, d.total_triangles / 1e6, d.width, d.height, d.shadow_size)
 
 
+def _autotune(r, u, stream, args, probes=None, n_probes=0, frames=4):
+    """The launch shape the autotuner picks for this workload (it times
+    frames of each candidate before anything here is timed; no candidate
+    changes a result bit): {"candidates": n, "tuning_ms": wall ms} or None."""
+    if not args.tune:
+        return None
+    from lighthugger_gb300 import autotune
+    t0 = time.perf_counter()
+    _, results = autotune.tune(r, u, probes, n_probes, batched=n_probes > 0, frames=frames, use_cache=False,
+                               stream=stream)
+    return {"candidates": len(results), "tuning_ms": round((time.perf_counter() - t0) * 1e3, 1)}
+
+
 def run_gpu(args):
     import numpy as np
     import torch
@@ -262,6 +275,7 @@ def run_gpu(args):
     sptr = stream.cuda_stream
     u = scene.uniforms
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    tune_results = _autotune(r, u, stream, args, frames=10)
     for _ in range(max(3, args.warmup)):
         r.frame(u, stream=sptr)
     torch.cuda.synchronize()
@@ -416,6 +430,7 @@ def run_gpu(args):
         # raster the visibility view adds the occluder pass, its chunks, the
         # hierarchical depth and the depth test of the other meshlets
         "gpu_launches": (13 + (4 if tune.occlusion_px else 0)) * args.steps,
+        "tuning": dict(tune.as_dict(), autotuned=tune_results),
         "occlusion": {"occluder_px": int(tune.occlusion_px), "occluders": int(st.occlusion[0]),
                       "survivors_opaque": int(st.occlusion[1]), "survivors_alpha": int(st.occlusion[2]),
                       "visible_opaque": int(st.visible_opaque[0])},
@@ -486,6 +501,8 @@ def bench_batched(lh, torch, args, device):
     u = scene.uniforms
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     out = {"workload": "main %dx%d + %d probes (%d px) + 4 cascades %d^2" % (d.width, d.height, n, px, d.shadow_size)}
+    out["autotuned"] = _autotune(r, u, stream, args, probes, n, frames=2)
+    out["tuning"] = r.tuning().as_dict()
     for name, sched, graph in (("persistent_graph", lh.SCHEDULE_PERSISTENT, True),
                                ("per_stage_graph", lh.SCHEDULE_PER_STAGE, True),
                                ("per_stage_launches", lh.SCHEDULE_PER_STAGE, False),
@@ -601,6 +618,7 @@ def bench_stress(lh, torch, args, device):
     sptr = stream.cuda_stream
     u = scene.uniforms
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    autotuned = _autotune(r, u, stream, args, frames=2)
     dev = torch.device("cuda", device)
     recs, inst = _scene_records(scene)
     total_v = sum(m.vertices for m in recs)
@@ -659,6 +677,7 @@ def bench_stress(lh, torch, args, device):
         if stage_ms["cull_meshlets"] else None,
         "occlusion": {"occluders": int(st.occlusion[0]), "survivors_opaque": int(st.occlusion[1]),
                       "survivors_alpha": int(st.occlusion[2])},
+        "tuning": dict(r.tuning().as_dict(), autotuned=autotuned),
         "status_flags": int(st.flags), "steps": steps}
     return out
 
@@ -675,6 +694,7 @@ def main():
     ap.add_argument("--batched", type=int, default=1, help="also time the batched multi-view frame (config 3)")
     ap.add_argument("--differentiable", type=int, default=1, help="also time the resolve adjoint (config 4)")
     ap.add_argument("--stress", type=int, default=1, help="also time the stress workload (config 5)")
+    ap.add_argument("--tune", type=int, default=1, help="autotune the launch shape of each workload before timing it")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

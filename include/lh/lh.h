@@ -239,7 +239,8 @@ lh_status lh_read_status(lh_ctx* ctx, lh_device_status* out);
 #define LH_SCHEDULE_PER_VIEW 3   /* each view's cull and raster launched on its own (the reference's per-cascade loop) */
 typedef struct lh_tuning {
     uint32_t small_px;        /* a lane rasterises triangles whose bbox has <= small_px pixels */
-    uint32_t medium_px;       /* the warp rasterises up to medium_px; larger go to 16 x 64-pixel chunks */
+    uint32_t medium_px;       /* the warp rasterises up to medium_px; larger go to chunks (chunk_rows x
+                                 chunk_cols pixels, one warp each) */
     float cull_blocks_per_sm; /* meshlet-cull blocks per SM (per-stage schedule); blocks per SM (persistent) */
     uint32_t schedule;        /* LH_SCHEDULE_* */
     uint32_t raster_batch;    /* meshlets a raster warp claims per atomic (0: 4 when the views hold more than
@@ -251,9 +252,11 @@ typedef struct lh_tuning {
                                  reference; results identical).  0: one pass, no occlusion test */
     uint32_t chunk_rows[2];   /* pixel rows of a big-triangle chunk (one warp) in the visibility / shadow
                                  pass: 4, 8, 16 or 32 */
-    uint32_t chunk_cols[2];   /* its columns: 32, 64 or 128 */
+    uint32_t chunk_cols[2];   /* its columns: 32, 64, 128 or 256 */
     uint32_t backward_rows;   /* pixel rows of a resolve-adjoint tile (one warp per row): 4, 8 or 16 */
 } lh_tuning;
+/* lh_create's tuning: bins 16 / 64, occluders above 128 px, chunks of
+ * 16 x 128 (visibility) and 32 x 64 (shadow) pixels, adjoint tiles of 8 rows. */
 
 lh_status lh_set_tuning(lh_ctx* ctx, const lh_tuning* tuning);
 lh_status lh_get_tuning(lh_ctx* ctx, lh_tuning* tuning);

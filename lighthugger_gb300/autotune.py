@@ -29,7 +29,7 @@ CACHE = os.path.join(_HERE, "_build", "tuning.json")
 OCCLUSION = (0, 64, 128, 256, 512)
 SMALL = (16, 32)
 MEDIUM = (64, 128, 256)
-CHUNK = ((16, 32), (16, 64), (8, 64), (32, 32))  # (rows, columns)
+CHUNK = ((16, 32), (16, 64), (32, 64), (16, 128), (32, 128), (32, 256))  # (rows, columns)
 BATCH = (0, 1, 2, 4)
 BACKWARD_ROWS = (4, 8, 16)
 KNOBS = ("small_px", "medium_px", "schedule", "raster_batch", "occlusion_px", "chunk_rows", "chunk_cols")

@@ -492,7 +492,7 @@ lh_status lh_create(const lh_config* config, lh_ctx** out) {
     if (!c) return LH_ERR_OUT_OF_MEMORY;
     c->cfg = cfg;
     c->device = cfg.device;
-    c->tuning = lh_tuning{32u, 128u, 2.0f, LH_SCHEDULE_DEFAULT, 0u, 256u, {16u, 16u}, {32u, 64u}, 8u};
+    c->tuning = lh_tuning{16u, 64u, 2.0f, LH_SCHEDULE_DEFAULT, 0u, 128u, {16u, 32u}, {128u, 64u}, 8u};
     cudaError_t e = cudaSetDevice(c->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device);
     c->max_views = 5 + cfg.max_probes;
@@ -993,7 +993,7 @@ lh_status lh_set_tuning(lh_ctx* c, const lh_tuning* t) {
         return LH_ERR_INVALID_ARGUMENT;
     auto pow2_in = [](uint32_t v, uint32_t lo, uint32_t hi) { return v >= lo && v <= hi && (v & (v - 1)) == 0; };
     for (int k = 0; k < 2; k++)
-        if (!pow2_in(t->chunk_rows[k], 4, 32) || !pow2_in(t->chunk_cols[k], 32, 128)) return LH_ERR_INVALID_ARGUMENT;
+        if (!pow2_in(t->chunk_rows[k], 4, 32) || !pow2_in(t->chunk_cols[k], 32, 256)) return LH_ERR_INVALID_ARGUMENT;
     if (!pow2_in(t->backward_rows, 4, 16)) return LH_ERR_INVALID_ARGUMENT;
     c->tuning = *t;
     return LH_OK;

@@ -61,6 +61,23 @@ LH_IF_HD float i64_to_f32_rn(int64_t v) {
     return bits_to_float(sign | ((uint32_t)(e + 127) << 23) | ((uint32_t)q & 0x7FFFFFu));
 }
 
+// Round-to-nearest-even conversion of 0 <= v < 2^46 with FP32 adds only:
+// v = a * 2^23 + b with a, b < 2^23; each part is an exact float (placed in
+// the significand of 2^46, resp. 2^23, and that power subtracted), so the
+// one rounding of their sum is the rounding of v.
+LH_IF_HD float u46_to_f32_rn(uint64_t v) {
+    const float fa = bits_to_float(0x56800000u | (uint32_t)(v >> 23)) - 70368744177664.0f;
+    const float fb = bits_to_float(0x4B000000u | ((uint32_t)v & 0x7FFFFFu)) - 8388608.0f;
+    return fa + fb;
+}
+
+// The same for any unsigned 32-bit v (its high part v >> 23 has 9 bits).
+LH_IF_HD float u32_to_f32_rn(uint32_t v) {
+    const float fa = bits_to_float(0x56800000u | (v >> 23)) - 70368744177664.0f;
+    const float fb = bits_to_float(0x4B000000u | (v & 0x7FFFFFu)) - 8388608.0f;
+    return fa + fb;
+}
+
 // Round-to-nearest-even conversion of a signed 32-bit integer: values below
 // 2^22 in magnitude are placed in the significand of 1.5 * 2^23 (exact: one
 // integer add and one float subtract), the rest take the general routine.

@@ -102,9 +102,7 @@ struct BigTri {
 };
 // Chunk of a big triangle (one warp): rows x columns of pixels, powers of
 // two chosen per pass at run time (lh_tuning.chunk_rows / chunk_cols, by
-// the autotuner): FrameDev::chunk_shift holds their log2.  Measured by hand
-// before: the visibility pass at 16 x 32 (raster stage 0.332 -> 0.326 ms
-// against 16 x 64), the shadow pass at 16 x 64 (0.088 against 0.092 ms).
+// the autotuner; at most 32 x 256): FrameDev::chunk_shift holds their log2.
 
 // Per-frame scratch words (zeroed at frame start; the raster words again
 // before each raster pass).

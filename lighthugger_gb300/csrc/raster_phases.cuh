@@ -19,16 +19,21 @@
 //                 memory; then one lane per triangle does set-up and face
 //                 culling.  Triangles covering <= `small` pixel centres are
 //                 rasterised by their lane, up to `medium` by the whole warp,
-//                 larger ones go to a queue of 16-row bands.  A triangle
-//                 that needs clipping is clipped by its lane
+//                 larger ones go to a queue of chunks (tiles of the bbox).
+//                 A triangle that needs clipping is clipped by its lane
 //                 (Sutherland-Hodgman in clip space against 0 <= z <= w and
-//                 the guard band, fan triangulation) into the band queue.
-//  k_raster_big   one warp per band.
+//                 the guard band, fan triangulation) into the chunk queue.
+//  k_raster_big   one warp per chunk: each row's run of covered pixels
+//                 from the three edge functions, the runs walked row by
+//                 row or compacted across the warp.
 // The depth test is an atomicMax of (depth bits << 32 | packed ID) for the
 // visibility buffer and an atomicMin of depth bits for shadow maps, so the
 // result does not depend on the order of the work.
 #pragma once
 
+#include <type_traits>
+
+#include "edge_run.cuh"
 #include "lh_device.cuh"
 #include "lh_internal.cuh"
 
@@ -49,7 +54,7 @@ constexpr int kRasterWarps = 8;
 
 struct RasterTune {
     uint32_t small_px;   // lane path up to this many bbox pixels
-    uint32_t medium_px;  // warp path up to this many; larger: band queue
+    uint32_t medium_px;  // warp path up to this many; larger: chunk queue
     uint32_t batch;      // meshlets claimed per atomic (0: automatic)
 };
 
@@ -166,7 +171,7 @@ __device__ __forceinline__ bool alpha_pass(const FrameDev& f, const AlphaTri& t,
 }
 
 // The alpha set-up of triangle `id` (packed tri / draw slot) of view
-// `view`, from the scene buffers (the band and clip paths).
+// `view`, from the scene buffers (the chunk and clip paths).
 __device__ AlphaTri alpha_tri_global(const FrameDev& f, uint32_t view, uint32_t id) {
     const ViewDev* vw = f.views + view;
     const uint32_t slot = id & ((1u << 24) - 1u), tri = id >> 24;
@@ -208,7 +213,7 @@ __device__ __forceinline__ void load_transform(const Instance* inst, lh_mat4& m)
 // Append big triangles with 64-bit atomics of {triangles:hi24, chunks:lo40}
 // (the packed single-pass append of prefix_sum.glsl:17-30): the triangle's
 // index and its first chunk come from the same word, so chunk bases ascend
-// with the index and the band kernel finds a chunk's triangle by binary search.
+// with the index and the chunk kernel finds a chunk's triangle by binary search.
 template <int KIND>
 __device__ __forceinline__ unsigned long long big_chunks(const FrameDev& f, const TriSetup& t) {
     const uint32_t nbx = ((uint32_t)(t.px1 - t.px0) >> f.chunk_shift[KIND][1]) + 1;
@@ -773,6 +778,180 @@ __device__ __forceinline__ bool edge_rejects(int32_t ax, int32_t ay, int32_t bx,
            edge_at(ax, ay, bx, by, x0, y1) < bias && edge_at(ax, ay, bx, by, x1, y1) < bias;
 }
 
+// Edge values of a chunk's covered pixels, by the triangle's doubled area
+// 2A (= e12 + e20 + e01 at every point, so no covered pixel's value exceeds
+// it): kEdge32 below 2^31 (32-bit arithmetic, exact modulo 2^32 and so
+// exact for these values), kEdge46 below 2^46 (64-bit, FP32-add
+// conversion), kEdge64 beyond (the conversion instruction).
+enum EdgeMode { kEdge32 = 0, kEdge46 = 1, kEdge64 = 2 };
+template <int MODE>
+struct EdgeVal {
+    using T = typename std::conditional<MODE == kEdge32, uint32_t, int64_t>::type;
+};
+template <int MODE>
+__device__ __forceinline__ float covered_to_float(typename EdgeVal<MODE>::T v) {
+    if (MODE == kEdge32) return u32_to_f32_rn((uint32_t)v);
+    if (MODE == kEdge46) return u46_to_f32_rn((uint64_t)v);
+    return __ll2float_rn((int64_t)v);
+}
+template <int MODE>
+__device__ __forceinline__ typename EdgeVal<MODE>::T shfl_edge(typename EdgeVal<MODE>::T v, uint32_t src) {
+    if (MODE == kEdge32) return (uint32_t)__shfl_sync(0xFFFFFFFFu, (uint32_t)v, src);
+    return (int64_t)__shfl_sync(0xFFFFFFFFu, (unsigned long long)v, src);
+}
+
+// A covered pixel: depth from its two edge values (the per-pixel test's
+// arithmetic), then the depth test at linear pixel index `pix`.
+template <int KIND, int MODE>
+__device__ __forceinline__ void chunk_fragment(const BigTri& b, void* target, uint32_t pix,
+                                               typename EdgeVal<MODE>::T a20, typename EdgeVal<MODE>::T a01) {
+    float d = (b.z0 + covered_to_float<MODE>(a20) * b.s1) + covered_to_float<MODE>(a01) * b.s2;
+    d = d > 0.0f ? d : 0.0f;
+    d = d < 1.0f ? d : 1.0f;
+    if (KIND == 0) {
+        const unsigned long long key = ((unsigned long long)f2u(d) << 32) | b.id;
+        asm volatile("red.relaxed.gpu.global.max.u64 [%0], %1;" ::"l"(reinterpret_cast<unsigned long long*>(target) + pix),
+                     "l"(key));
+    } else {
+        asm volatile("red.relaxed.gpu.global.min.u32 [%0], %1;" ::"l"(reinterpret_cast<uint32_t*>(target) + pix),
+                     "r"(f2u(d)));
+    }
+}
+
+// Row by row: the warp's lanes along each run (long runs).  Lane r holds
+// row r's run: its length, the linear index of its first pixel and the two
+// edge values there.
+template <int KIND, int MODE>
+__device__ __forceinline__ uint32_t chunk_rows(const BigTri& b, void* target, uint32_t rows, uint32_t lane, int32_t len,
+                                               uint32_t pix_first, typename EdgeVal<MODE>::T f20,
+                                               typename EdgeVal<MODE>::T f01, typename EdgeVal<MODE>::T dx20,
+                                               typename EdgeVal<MODE>::T dx01) {
+    using T = typename EdgeVal<MODE>::T;
+    uint32_t nfrag = 0;
+    for (uint32_t r = 0; r < rows; r++) {
+        const int32_t l = __shfl_sync(0xFFFFFFFFu, len, r);
+        if (l == 0) continue;
+        uint32_t pix = __shfl_sync(0xFFFFFFFFu, pix_first, r) + lane;
+        T a20 = shfl_edge<MODE>(f20, r) + (T)lane * dx20, a01 = shfl_edge<MODE>(f01, r) + (T)lane * dx01;
+        for (int32_t k = (int32_t)lane; k < l; k += 32, pix += 32, a20 += 32 * dx20, a01 += 32 * dx01) {
+            chunk_fragment<KIND, MODE>(b, target, pix, a20, a01);
+            nfrag++;
+        }
+    }
+    return nfrag;
+}
+
+// Compacted: the covered pixels of all rows numbered one after another,
+// 32 consecutive per step, one per lane (short runs: slivers, corners).  A
+// lane finds the row of its pixel number p by binary search of the runs'
+// first numbers (an empty row shares the next row's first number, so the
+// last row whose first number is <= p holds p); lane r holds, for row r,
+// the linear index and edge values extrapolated to p = 0.
+template <int KIND, int MODE>
+__device__ __forceinline__ uint32_t chunk_compact(const BigTri& b, void* target, uint32_t rows, uint32_t lane,
+                                                  int32_t total, int32_t pre, uint32_t pix_zero,
+                                                  typename EdgeVal<MODE>::T z20, typename EdgeVal<MODE>::T z01,
+                                                  typename EdgeVal<MODE>::T dx20, typename EdgeVal<MODE>::T dx01) {
+    using T = typename EdgeVal<MODE>::T;
+    uint32_t nfrag = 0;
+    for (int32_t base = 0; base < total; base += 32) {
+        const int32_t p = base + (int32_t)lane;
+        uint32_t r = 0;
+#pragma unroll
+        for (uint32_t bit = 16; bit; bit >>= 1) {
+            const uint32_t c = r + bit;
+            const int32_t s = __shfl_sync(0xFFFFFFFFu, pre, c & 31u);
+            if (c < rows && s <= p) r = c;
+        }
+        const uint32_t pix = (uint32_t)p + __shfl_sync(0xFFFFFFFFu, pix_zero, r);
+        const T a20 = shfl_edge<MODE>(z20, r) + (T)p * dx20, a01 = shfl_edge<MODE>(z01, r) + (T)p * dx01;
+        if (p < total) {
+            chunk_fragment<KIND, MODE>(b, target, pix, a20, a01);
+            nfrag++;
+        }
+    }
+    return nfrag;
+}
+
+// Per-row run state of a chunk, then the cheaper of the two walks.
+template <int KIND, int MODE>
+__device__ __forceinline__ uint32_t chunk_walk(const BigTri& b, void* target, uint32_t W, int32_t x0, int32_t y0,
+                                               uint32_t rows, uint32_t lane, int32_t lo, int32_t len, int32_t pre,
+                                               int32_t total, int64_t e20, int64_t e01, int64_t dx20, int64_t dx01) {
+    using T = typename EdgeVal<MODE>::T;
+    // steps of the row walk (plus a row's own cost) against the compacted
+    // walk's, whose steps cost about twice as much
+    const uint32_t row_steps = __reduce_add_sync(0xFFFFFFFFu, (uint32_t)(len + 31) >> 5);
+    const uint32_t nonempty = __popc(__ballot_sync(0xFFFFFFFFu, len > 0));
+    const uint32_t pix_row = (uint32_t)(y0 + (int32_t)lane) * W + (uint32_t)x0;
+    if (row_steps + nonempty / 4u <= 2u * (uint32_t)((total + 31) >> 5))
+        return chunk_rows<KIND, MODE>(b, target, rows, lane, len, pix_row + (uint32_t)lo, (T)(e20 + (int64_t)lo * dx20),
+                                      (T)(e01 + (int64_t)lo * dx01), (T)dx20, (T)dx01);
+    return chunk_compact<KIND, MODE>(b, target, rows, lane, total, pre, pix_row + (uint32_t)(lo - pre),
+                                     (T)(e20 + (int64_t)(lo - pre) * dx20), (T)(e01 + (int64_t)(lo - pre) * dx01),
+                                     (T)dx20, (T)dx01);
+}
+
+// The pixels [x0, x1] x [y0, y1] (at most 32 rows of at most 256) of an
+// opaque big triangle, by the whole warp.  Lane r finds the run of covered
+// pixels of row y0 + r (the three edges' runs intersected, clip_run); the
+// runs are walked row by row when they are long, else compacted (every lane
+// of a step on a covered pixel).  Either walk forms, at every pixel, the
+// very integers the per-pixel test forms, so coverage and depth are the
+// same; a step's pixels lie in one or two rows, so its reductions stay
+// coalesced.  Returns the fragments written.
+struct ChunkSteps {  // a triangle's edge steps along x and their reciprocals
+    int64_t dx12, dx20, dx01;
+    float inv12, inv20, inv01;
+};
+__device__ __forceinline__ ChunkSteps chunk_steps(const BigTri& b) {
+    ChunkSteps k;
+    k.dx12 = (int64_t)(b.Y2 - b.Y1) * 256;
+    k.dx20 = (int64_t)(b.Y0 - b.Y2) * 256;
+    k.dx01 = (int64_t)(b.Y1 - b.Y0) * 256;
+    k.inv12 = run_inv_step(b.Y2 - b.Y1);
+    k.inv20 = run_inv_step(b.Y0 - b.Y2);
+    k.inv01 = run_inv_step(b.Y1 - b.Y0);
+    return k;
+}
+
+template <int KIND>
+__device__ __forceinline__ uint32_t raster_chunk_runs(const BigTri& b, const ChunkSteps& k, int32_t x0, int32_t x1,
+                                                      int32_t y0, int32_t y1, uint32_t lane, void* target, uint32_t W) {
+    const int32_t n = x1 - x0 + 1;
+    const uint32_t rows = (uint32_t)(y1 - y0 + 1);
+    const int64_t dx20 = k.dx20, dx01 = k.dx01;
+    int32_t lo = 0, hi = -1;
+    int64_t e12 = 0, e20 = 0, e01 = 0;
+    if (lane < rows) {
+        const int32_t y = y0 + (int32_t)lane;
+        e12 = edge_at(b.X1, b.Y1, b.X2, b.Y2, x0, y);
+        e20 = edge_at(b.X2, b.Y2, b.X0, b.Y0, x0, y);
+        e01 = edge_at(b.X0, b.Y0, b.X1, b.Y1, x0, y);
+        hi = n - 1;
+        clip_run(e12, k.dx12, b.bias & 1u, n, k.inv12, lo, hi);
+        clip_run(e20, dx20, (b.bias >> 1) & 1u, n, k.inv20, lo, hi);
+        clip_run(e01, dx01, (b.bias >> 2) & 1u, n, k.inv01, lo, hi);
+    }
+    const int32_t len = hi >= lo ? hi - lo + 1 : 0;
+    int32_t incl = len;
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        const int32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const int32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    if (total == 0) return 0;
+    const int32_t pre = incl - len;
+    // 2A: the sum of the three edge functions, the same at every point
+    const uint64_t area2 = (uint64_t)__shfl_sync(0xFFFFFFFFu, (unsigned long long)(e12 + e20 + e01), 0);
+    if (area2 < (1ull << 31))
+        return chunk_walk<KIND, kEdge32>(b, target, W, x0, y0, rows, lane, lo, len, pre, total, e20, e01, dx20, dx01);
+    if (area2 < (1ull << 46))
+        return chunk_walk<KIND, kEdge46>(b, target, W, x0, y0, rows, lane, lo, len, pre, total, e20, e01, dx20, dx01);
+    return chunk_walk<KIND, kEdge64>(b, target, W, x0, y0, rows, lane, lo, len, pre, total, e20, e01, dx20, dx01);
+}
+
 // Number of entries of the ascending array base[0, n) that are <= c (the
 // upper bound), found by the whole warp: 32 probes per round narrow the
 // range 32-fold, so a queue of 16k triangles takes 3 dependent loads instead
@@ -822,11 +1001,25 @@ __device__ __noinline__ uint32_t raster_chunk_alpha(const FrameDev& f, const Big
     return n;
 }
 
-// One warp per chunk of a big triangle (rows x columns of f.chunk_shift;
-// 16 x 32 pixels in the visibility pass and 16 x 64 in the shadow pass by
-// default); chunks whose rectangle lies outside one edge are skipped whole.
+// One warp per chunk of a big triangle (rows x columns of f.chunk_shift,
+// at most 32 x 256 pixels): opaque chunks by runs of covered pixels
+// (raster_chunk_runs), alpha-tested ones pixel by pixel, skipped whole when
+// their rectangle lies outside one edge.
 template <int KIND>
 __device__ void phase_raster_big(const FrameDev& f) {
+    // the views' targets and widths, read once per block
+    __shared__ unsigned long long s_target[kMaxViews];
+    __shared__ uint32_t s_width[kMaxViews];
+    // each warp's current triangle (kept in shared memory, not registers,
+    // between its chunks; blocks of kRasterWarps warps)
+    __shared__ BigTri s_tri[kRasterWarps];
+    __shared__ ChunkSteps s_steps[kRasterWarps];
+    __syncthreads();  // a previous call of this phase in the block may still read them
+    for (uint32_t v = threadIdx.x; v < f.n_views; v += blockDim.x) {
+        s_target[v] = reinterpret_cast<unsigned long long>(f.views[v].target);
+        s_width[v] = f.views[v].width;
+    }
+    __syncthreads();
     const unsigned long long packed = *reinterpret_cast<volatile unsigned long long*>(f.status + kStBigPacked);
     const uint32_t ntri = (uint32_t)min((unsigned long long)f.big_cap, packed >> 40);
     const unsigned long long total = packed & ((1ull << 40) - 1);
@@ -839,9 +1032,16 @@ __device__ void phase_raster_big(const FrameDev& f) {
     const uint32_t warps_total = gridDim.x * (blockDim.x >> 5);
     const uint32_t gwarp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const uint64_t dyn_base = (uint64_t)warps_total * kChunkBatch;
-    uint32_t t_idx = 0, t_base = 1, t_end = 0;  // chunk range [t_base, t_end) of triangle t_idx (empty at first)
+    const uint32_t rs = f.chunk_shift[KIND][0], cs = f.chunk_shift[KIND][1];
     uint32_t c = (uint32_t)min((uint64_t)gwarp * kChunkBatch, (uint64_t)total32);
     uint32_t c_end = (uint32_t)min((uint64_t)gwarp * kChunkBatch + kChunkBatch, (uint64_t)total32);
+    // the current triangle, kept while consecutive chunks belong to it:
+    // its entry, chunk range [t_base, t_end), chunk columns and steps, and
+    // the coordinates of the last chunk taken (number c_last)
+    uint32_t t_idx = 0, t_base = 1, t_end = 0, nbx = 1, c_last = 0xFFFFFFFFu;
+    int32_t cx = 0, cy = 0;
+    BigTri& b = s_tri[threadIdx.x >> 5];
+    ChunkSteps& ks = s_steps[threadIdx.x >> 5];
     uint32_t nfrag = 0;
     for (;;) {
         if (c >= c_end) {
@@ -854,83 +1054,61 @@ __device__ void phase_raster_big(const FrameDev& f) {
             c = (uint32_t)first;
             c_end = (uint32_t)min(first + kChunkBatch, (uint64_t)total32);
         }
-        // the chunk's triangle: the previous chunk's while c stays in its
-        // range (consecutive claims), else a 32-ary search of the bases
-        uint32_t i;
         if (c >= t_base && c < t_end) {
-            i = t_idx;
+            // the same triangle: the next chunk in row order, or any other
+            if (c == c_last + 1u) {
+                if (++cx == (int32_t)nbx) {
+                    cx = 0;
+                    cy++;
+                }
+            } else {
+                cx = (int32_t)((c - t_base) % nbx);
+                cy = (int32_t)((c - t_base) / nbx);
+            }
         } else {
+            // another triangle: a 32-ary search of the bases
             const uint32_t first = upper_bound_warp(f.big_base, ntri, c, lane);
             if (first == 0) {
                 c++;
                 continue;
             }
-            i = first - 1;
+            const uint32_t i = first - 1;
+            const BigTri nb = f.big[i];
+            const uint32_t base = f.big_base[i];
+            const uint32_t nx = ((uint32_t)(nb.px1 - nb.px0) >> cs) + 1;
+            const uint32_t ny = ((uint32_t)(nb.py1 - nb.py0) >> rs) + 1;
+            if ((unsigned long long)(c - base) >= (unsigned long long)nx * ny) {  // chunk of a dropped triangle
+                c++;
+                continue;
+            }
+            __syncwarp();  // every lane is done with the previous triangle
+            if (lane == 0) {
+                b = nb;
+                ks = chunk_steps(nb);
+            }
+            __syncwarp();
+            t_idx = i;
+            t_base = base;
+            t_end = base + nx * ny;
+            nbx = nx;
+            cx = (int32_t)((c - base) % nx);
+            cy = (int32_t)((c - base) / nx);
         }
+        c_last = c;
         c++;
-        const BigTri b = f.big[i];
-        const uint32_t rs = f.chunk_shift[KIND][0], cs = f.chunk_shift[KIND][1];
-        const uint32_t nbx = ((uint32_t)(b.px1 - b.px0) >> cs) + 1;
-        const uint32_t nby = ((uint32_t)(b.py1 - b.py0) >> rs) + 1;
-        const uint32_t base = f.big_base[i];
-        const unsigned long long local = (c - 1u) - base;
-        if (local >= (unsigned long long)nbx * nby) continue;  // chunk of a dropped triangle
-        t_idx = i;
-        t_base = base;
-        t_end = base + nbx * nby;
-        const int32_t cx = (int32_t)(local % nbx), cy = (int32_t)(local / nbx);
         const int32_t x0 = b.px0 + (cx << cs), x1 = min(b.px1, x0 + (1 << cs) - 1);
         const int32_t y0 = b.py0 + (cy << rs), y1 = min(b.py1, y0 + (1 << rs) - 1);
-        if (edge_rejects(b.X1, b.Y1, b.X2, b.Y2, x0, x1, y0, y1, b.bias & 1u) ||
-            edge_rejects(b.X2, b.Y2, b.X0, b.Y0, x0, x1, y0, y1, (b.bias >> 1) & 1u) ||
-            edge_rejects(b.X0, b.Y0, b.X1, b.Y1, x0, x1, y0, y1, (b.bias >> 2) & 1u))
-            continue;
-        const ViewDev* vw = f.views + b.view;
-        void* target = vw->target;
-        const uint32_t W = vw->width;
+        void* target = reinterpret_cast<void*>(s_target[b.view]);
+        const uint32_t W = s_width[b.view];
         if (b.bias & kBiasAlpha) {
-            nfrag += raster_chunk_alpha<KIND>(f, f.big + i, x0, x1, y0, y1, lane);
+            if (edge_rejects(b.X1, b.Y1, b.X2, b.Y2, x0, x1, y0, y1, b.bias & 1u) ||
+                edge_rejects(b.X2, b.Y2, b.X0, b.Y0, x0, x1, y0, y1, (b.bias >> 1) & 1u) ||
+                edge_rejects(b.X0, b.Y0, b.X1, b.Y1, x0, x1, y0, y1, (b.bias >> 2) & 1u))
+                continue;
+            nfrag += raster_chunk_alpha<KIND>(f, f.big + t_idx, x0, x1, y0, y1, lane);
             continue;
         }
-        // edge functions at the top of the lane's column, then one add per
-        // row (the same integers cover() forms, so the same coverage/depth);
-        // 32-bit when the triangle's edge products fit (bias bit 3: every
-        // value in its bbox, and one row step beyond, stays below 2^31)
-        if (b.bias & 8u) {
-            const int32_t d12 = -(b.X2 - b.X1) * 256, d20 = -(b.X0 - b.X2) * 256, d01 = -(b.X1 - b.X0) * 256;
-            const int32_t b12 = b.bias & 1u, b20 = (b.bias >> 1) & 1u, b01 = (b.bias >> 2) & 1u;
-            const int32_t Py0 = y0 * 256 + 128;
-            for (int32_t px = x0 + (int32_t)lane; px <= x1; px += 32) {
-                const int32_t Px = px * 256 + 128;
-                int32_t e12 = (b.Y2 - b.Y1) * (Px - b.X1) - (b.X2 - b.X1) * (Py0 - b.Y1);
-                int32_t e20 = (b.Y0 - b.Y2) * (Px - b.X2) - (b.X0 - b.X2) * (Py0 - b.Y2);
-                int32_t e01 = (b.Y1 - b.Y0) * (Px - b.X0) - (b.X1 - b.X0) * (Py0 - b.Y0);
-                for (int32_t py = y0; py <= y1; py++, e12 += d12, e20 += d20, e01 += d01) {
-                    if (e12 < b12 || e20 < b20 || e01 < b01) continue;
-                    float d = (b.z0 + i32_to_f32_rn(e20) * b.s1) + i32_to_f32_rn(e01) * b.s2;
-                    d = d > 0.0f ? d : 0.0f;
-                    d = d < 1.0f ? d : 1.0f;
-                    write_fragment<KIND>(target, W, px, py, d, b.id);
-                    nfrag++;
-                }
-            }
-            continue;
-        }
-        const int64_t d12 = -(int64_t)(b.X2 - b.X1) * 256, d20 = -(int64_t)(b.X0 - b.X2) * 256,
-                      d01 = -(int64_t)(b.X1 - b.X0) * 256;
-        const int64_t b12 = b.bias & 1u, b20 = (b.bias >> 1) & 1u, b01 = (b.bias >> 2) & 1u;
-        for (int32_t px = x0 + (int32_t)lane; px <= x1; px += 32) {
-            int64_t e12 = edge_at(b.X1, b.Y1, b.X2, b.Y2, px, y0), e20 = edge_at(b.X2, b.Y2, b.X0, b.Y0, px, y0),
-                    e01 = edge_at(b.X0, b.Y0, b.X1, b.Y1, px, y0);
-            for (int32_t py = y0; py <= y1; py++, e12 += d12, e20 += d20, e01 += d01) {
-                if (e12 < b12 || e20 < b20 || e01 < b01) continue;
-                float d = (b.z0 + edge_to_float(e20) * b.s1) + edge_to_float(e01) * b.s2;
-                d = d > 0.0f ? d : 0.0f;
-                d = d < 1.0f ? d : 1.0f;
-                write_fragment<KIND>(target, W, px, py, d, b.id);
-                nfrag++;
-            }
-        }
+        nfrag += raster_chunk_runs<KIND>(b, ks, x0, x1, y0, y1, lane, target, W);
     }
     count_fragments<KIND>(f, nfrag);
 }

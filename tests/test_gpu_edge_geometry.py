@@ -93,3 +93,36 @@ def test_edge_geometry_parity(native, oracle, camera):
     assert stats["covered"] > 0.2 * w * h
     if camera == "near":
         assert fr.raster_stats["visibility"]["clipped"] > 0
+
+
+_ORACLE_FRAMES = {}
+
+
+@pytest.mark.parametrize("camera", ["front", "near"])
+@pytest.mark.parametrize("shape", [(4, 32, 32, 256), (32, 256, 8, 64), (16, 128, 32, 32)])
+def test_edge_geometry_all_triangles_in_chunks(native, oracle, camera, shape):
+    """Every triangle with a pixel in its box through the big-triangle chunks
+    (lane and warp bins off), at chunk shapes from 4 x 32 to 32 x 256 pixels:
+    the chunks' runs of covered pixels give the oracle's visibility buffer
+    and shadow maps bit for bit (slivers, ties, sub-pixel and clipped
+    triangles included)."""
+    lh = native
+    pos, tris = _edge_mesh()
+    w, h = 640, 480
+    if camera == "front":
+        u = lh.make_uniforms((0.0, 0.0, -2.4), 1.5707963, 0.0, 60.0, w, h, 3)
+    else:
+        u = lh.make_uniforms((0.05, -0.1, -0.012), 1.5707963, 0.35, 100.0, w, h, 3)
+    scene = lh.Scene.from_mesh(pos, tris, _transforms(), u).upload(0)
+    r = lh.Renderer(lh.Config(width=w, height=h, shadow_size=1024, max_instances=16, max_draws=200000))
+    r.set_scene(scene)
+    r.set_tuning(small_px=0, medium_px=0, chunk_rows=[shape[0], shape[2]], chunk_cols=[shape[1], shape[3]])
+    r.frame(scene.uniforms)
+    st = r.status()
+    assert st.flags == 0, hex(st.flags)
+    assert st.big_triangles > 1000
+    if camera not in _ORACLE_FRAMES:
+        _ORACLE_FRAMES[camera] = oracle.run_scene(scene, shadow_size=1024, max_instances=16, max_draws=200000)
+    fr = _ORACLE_FRAMES[camera]
+    errors, stats = compare_frame(r, fr, 200000, 16)
+    assert not errors, "\n".join(errors) + " %s" % stats

@@ -18,3 +18,16 @@ def test_conversions_round_like_the_conversion_instructions():
         r = subprocess.run([exe], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "bad 0" in r.stdout
+
+
+def test_edge_runs_hold_exactly_the_covered_pixels():
+    """lighthugger_gb300/csrc/edge_run.cuh (the big-triangle chunks' runs of
+    covered pixels) against the per-pixel edge tests, host-compiled."""
+    src = os.path.join(ROOT, "tests", "native", "edge_run_check.cpp")
+    with tempfile.TemporaryDirectory() as d:
+        exe = os.path.join(d, "edge_run_check")
+        subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I",
+                        os.path.join(ROOT, "lighthugger_gb300", "csrc"), src, "-o", exe], check=True)
+        r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "bad 0" in r.stdout
