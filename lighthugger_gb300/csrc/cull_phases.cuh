@@ -35,36 +35,58 @@ __device__ __forceinline__ uint64_t ld_status(const uint64_t* p) {
     return v;
 }
 
-// Decoupled look-back by one thread: publish the tile aggregate, walk back
-// until an inclusive prefix is found, publish the tile's inclusive prefix.
-// Every wait is bounded (`limit` polls of one predecessor's word); on expiry
-// the status flag LH_FLAG_TIMEOUT is set and the missing predecessors count
-// as zero (no hang, results flagged).
-__device__ __noinline__ uint64_t lookback(uint64_t* status, uint32_t tile, uint64_t agg, uint32_t* flags,
-                                          uint32_t limit = kSpinLimit) {
+// Decoupled look-back by one warp (every lane calls it; the result is the
+// same on all): publish the tile aggregate, then read the status words of
+// the 32 preceding tiles at once, lane i the (i + 1)-th predecessor.  When
+// one of them holds an inclusive prefix, the nearest one ends the walk: the
+// aggregates of the tiles after it and that prefix sum to the exclusive
+// prefix; when none does (all 32 ready), their aggregates are added and the
+// window moves 32 tiles back.  Words before tile 0 read as an inclusive 0.
+// Publishes the tile's inclusive prefix.  The payloads add field-wise.
+// Every wait is bounded (`limit` polls of the window); on expiry the status
+// flag LH_FLAG_TIMEOUT is set and the missing predecessors count as zero (no
+// hang, results flagged).
+__device__ __forceinline__ uint64_t warp_sum_u64(uint64_t v) {
+#pragma unroll
+    for (uint32_t o = 16; o; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    return v;
+}
+__device__ __noinline__ uint64_t lookback_warp(uint64_t* status, uint32_t tile, uint64_t agg, uint32_t* flags,
+                                               uint32_t limit = kSpinLimit) {
+    const uint32_t lane = threadIdx.x & 31;
     if (tile == 0) {
-        st_status(&status[0], kStatIncl | agg);
+        if (lane == 0) st_status(&status[0], kStatIncl | agg);
         return 0;
     }
-    st_status(&status[tile], kStatAgg | agg);
+    if (lane == 0) st_status(&status[tile], kStatAgg | agg);
     uint64_t excl = 0;
-    int64_t t = (int64_t)tile - 1;
+    int64_t base = (int64_t)tile - 1;  // the window's nearest predecessor
     uint32_t spins = 0;
     bool timed_out = false;
-    while (t >= 0) {
-        uint64_t s = ld_status(&status[t]);
-        uint64_t fl = s >> 62;
-        if (fl == 0) {
-            if (++spins >= limit) { timed_out = true; break; }
-            if (spins > 32) __nanosleep(spins > 1024 ? 256 : 32);
-            continue;
+    for (;;) {
+        const int64_t t = base - (int64_t)lane;
+        const uint64_t s = t >= 0 ? ld_status(&status[t]) : kStatIncl;
+        const uint32_t fl = (uint32_t)(s >> 62);
+        const uint32_t incl = __ballot_sync(0xFFFFFFFFu, fl == 2u);
+        const uint32_t not_ready = __ballot_sync(0xFFFFFFFFu, fl == 0u);
+        const uint32_t first = incl ? (uint32_t)(__ffs(incl) - 1) : 31u;
+        const uint32_t need = first == 31u ? 0xFFFFFFFFu : (2u << first) - 1u;  // lanes 0 .. first
+        if (not_ready & need) {
+            if (++spins < limit) {
+                if (spins > 32) __nanosleep(spins > 1024 ? 256 : 32);
+                continue;
+            }
+            timed_out = true;  // the missing words count as zero
         }
-        excl += s & kPayloadMask;
-        if (fl == 2) break;
-        --t;
+        excl += warp_sum_u64(lane <= first && fl != 0u ? (s & kPayloadMask) : 0ull);
+        if (incl || timed_out) break;
+        base -= 32;
+        spins = 0;
     }
-    if (timed_out) atomicOr(&flags[kStFlags], LH_FLAG_TIMEOUT);
-    st_status(&status[tile], kStatIncl | (excl + agg));
+    if (lane == 0) {
+        if (timed_out) atomicOr(&flags[kStFlags], LH_FLAG_TIMEOUT);
+        st_status(&status[tile], kStatIncl | (excl + agg));
+    }
     return excl;
 }
 
@@ -214,16 +236,18 @@ __device__ void phase_cull_instances_tile(const FrameDev& f, uint32_t view, uint
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (lane == 31) s_warp[warp] = incl;
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (warp == 0) {
         uint64_t run = 0;
-        for (uint32_t w = 0; w < kInstTile / 32; w++) {
-            uint64_t t = s_warp[w];
-            s_warp[w] = run;
-            run += t;
-        }
-        uint64_t excl = lookback(vw->inst_status, tile, run, f.status);
-        s_excl = excl;
-        if (tile == n_tiles - 1) {
+        if (lane == 0)
+            for (uint32_t w = 0; w < kInstTile / 32; w++) {
+                uint64_t t = s_warp[w];
+                s_warp[w] = run;
+                run += t;
+            }
+        run = __shfl_sync(0xFFFFFFFFu, run, 0);
+        const uint64_t excl = lookback_warp(vw->inst_status, tile, run, f.status);
+        if (lane == 0) s_excl = excl;
+        if (lane == 0 && tile == n_tiles - 1) {
             uint64_t total = excl + run;
             uint64_t count = total >> 40;
             *reinterpret_cast<unsigned long long*>(vw->sector) = (count << 32) | (uint32_t)(total & kSum40);
@@ -441,9 +465,9 @@ __device__ void phase_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint
                 if (lane == 31) s_tot[cl] = incl;
             }
             __syncwarp();
+            const uint64_t agg = ((uint64_t)s_tot[0] << 31) | (uint64_t)s_tot[1];
+            const uint64_t excl = lookback_warp(vw->ml_status, tile, agg, f.status);
             if (lane == 0) {
-                uint64_t agg = ((uint64_t)s_tot[0] << 31) | (uint64_t)s_tot[1];
-                uint64_t excl = lookback(vw->ml_status, tile, agg, f.status);
                 s_excl = excl;
                 if (tile == n_tiles - 1) {
                     uint64_t tot = excl + agg;

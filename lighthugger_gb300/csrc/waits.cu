@@ -22,11 +22,11 @@ __global__ void k_check_wait(uint32_t which, uint32_t limit, uint32_t satisfied,
     __shared__ uint64_t bar;
     uint32_t* flags = reinterpret_cast<uint32_t*>(words + 3);
     if (which == LH_WAIT_LOOKBACK) {
-        if (threadIdx.x == 0) {
-            // tile 1 looks back at tile 0, which publishes 5 or never
-            if (satisfied) st_status(reinterpret_cast<uint64_t*>(&words[0]), kStatIncl | 5u);
-            words[4] = lookback(reinterpret_cast<uint64_t*>(words), 1, 7, flags, limit);
-        }
+        // tile 1 looks back (the whole warp) at tile 0, which publishes 5 or never
+        if (satisfied && threadIdx.x == 0) st_status(reinterpret_cast<uint64_t*>(&words[0]), kStatIncl | 5u);
+        __syncwarp();
+        const uint64_t excl = lookback_warp(reinterpret_cast<uint64_t*>(words), 1, 7, flags, limit);
+        if (threadIdx.x == 0) words[4] = excl;
     } else if (which == LH_WAIT_GRID_BARRIER) {
         if (threadIdx.x == 0) {
             // this block arrives; a second block that never launches would be needed
