@@ -254,8 +254,9 @@ __device__ void push_big(const FrameDev& f, const TriSetup& t, uint32_t view) {
 // one atomic per warp (a warp scan of the lanes' {1, chunks} words gives each
 // lane the running total below it).  The word's low 40 bits cannot carry into
 // the count: a sum reaching 2^32 chunks is flagged and dropped.
+template <int KIND>
 __device__ void push_big_warp(const FrameDev& f, const TriSetup& t, uint32_t view, bool big, uint32_t lane) {
-    const unsigned long long n = big ? big_chunks<1>(f, t) : 0ull;
+    const unsigned long long n = big ? big_chunks<KIND>(f, t) : 0ull;
     const unsigned long long mine = big ? (1ull << 40) | n : 0ull;
     unsigned long long incl = mine;
 #pragma unroll
@@ -611,18 +612,17 @@ __device__ __forceinline__ void raster_meshlet(const FrameDev& f, const MeshletW
                         } else if (npx <= (KIND == 1 && LH_SHADOW_MEDIUM_PX ? min(tune.medium_px, (uint32_t)LH_SHADOW_MEDIUM_PX)
                                                                             : tune.medium_px)) {
                             medium = true;
-                        } else if (KIND == 1) {
-                            big = true;  // appended below, one atomic per warp
                         } else {
-                            push_big<KIND>(f, st, w.view);
+                            big = true;  // appended below, one atomic per warp
                         }
                     }
                 }
             }
         }
-        // shadow views: few meshlets with many big triangles each, whose
-        // appends would queue on the one counter word
-        if (KIND == 1 && __any_sync(0xFFFFFFFFu, big)) push_big_warp(f, st, w.view, big, lane);
+        // one atomic per warp on the queue's counter word: shadow views and
+        // the occluder pass hold few meshlets with many big triangles each,
+        // whose appends would otherwise queue on that one word
+        if (__any_sync(0xFFFFFFFFu, big)) push_big_warp<KIND>(f, st, w.view, big, lane);
         uint32_t mask = __ballot_sync(0xFFFFFFFFu, medium);
         while (mask) {
             int src = __ffs(mask) - 1;
