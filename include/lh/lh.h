@@ -255,8 +255,9 @@ typedef struct lh_tuning {
     uint32_t chunk_cols[2];   /* its columns: 32, 64, 128 or 256 */
     uint32_t backward_rows;   /* pixel rows of a resolve-adjoint tile (one warp per row): 4, 8 or 16 */
 } lh_tuning;
-/* lh_create's tuning: bins 16 / 64, occluders above 128 px, chunks of
- * 16 x 128 (visibility) and 32 x 64 (shadow) pixels, adjoint tiles of 8 rows. */
+/* lh_create's tuning: lane bin 32 pixels and no warp bin (medium_px 32),
+ * occluders above 128 px, chunks of 16 x 128 (visibility) and 32 x 64
+ * (shadow) pixels, adjoint tiles of 8 rows. */
 
 lh_status lh_set_tuning(lh_ctx* ctx, const lh_tuning* tuning);
 lh_status lh_get_tuning(lh_ctx* ctx, lh_tuning* tuning);

@@ -5,7 +5,8 @@ The knobs, none of which changes a single output bit (they only move time):
 - occlusion_px: the two-pass occlusion raster's occluder threshold
   (projected sphere radius in pixels; 0 = one pass without occlusion test);
 - small_px / medium_px: the raster's bins by bounding-box pixels -- one lane
-  (<= small_px), one warp (<= medium_px), or chunks spread over all warps;
+  (<= small_px), one warp (<= medium_px; equal to small_px: no warp bin), or
+  chunks spread over all warps;
 - chunk_rows / chunk_cols: the chunk (tile) shape of big triangles, per pass
   (visibility, shadow);
 - raster_batch: meshlets a raster warp claims per atomic;
@@ -19,7 +20,6 @@ sizes, scene (instances, triangles, seed) and camera (a hash of the
 Uniforms) in lighthugger_gb300/_build/tuning.json.
 """
 import hashlib
-import itertools
 import json
 import os
 
@@ -27,8 +27,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 CACHE = os.path.join(_HERE, "_build", "tuning.json")
 
 OCCLUSION = (0, 64, 128, 256, 512)
-SMALL = (16, 32)
-MEDIUM = (64, 128, 256)
+BINS = ((32, 32), (16, 16), (16, 64), (32, 64), (32, 128), (16, 128))  # (small_px, medium_px)
 CHUNK = ((16, 32), (16, 64), (32, 64), (16, 128), (32, 128), (32, 256))  # (rows, columns)
 BATCH = (0, 1, 2, 4)
 BACKWARD_ROWS = (4, 8, 16)
@@ -138,7 +137,7 @@ def tune(renderer, uniforms, probes=None, n_probes=0, batched=False, frames=4, u
 
     best_ms[0] = measure(best)
     descend({"occlusion_px": v} for v in OCCLUSION)
-    descend({"small_px": a, "medium_px": b} for a, b in itertools.product(SMALL, MEDIUM))
+    descend({"small_px": a, "medium_px": b} for a, b in BINS)
     descend({"chunk_rows": [r, best["chunk_rows"][1]], "chunk_cols": [c, best["chunk_cols"][1]]} for r, c in CHUNK)
     descend({"chunk_rows": [best["chunk_rows"][0], r], "chunk_cols": [best["chunk_cols"][0], c]} for r, c in CHUNK)
     descend({"raster_batch": v} for v in BATCH)
