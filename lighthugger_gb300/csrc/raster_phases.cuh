@@ -781,8 +781,9 @@ __device__ __forceinline__ bool edge_rejects(int32_t ax, int32_t ay, int32_t bx,
 // Edge values of a chunk's covered pixels, by the triangle's doubled area
 // 2A (= e12 + e20 + e01 at every point, so no covered pixel's value exceeds
 // it): kEdge32 below 2^31 (32-bit arithmetic, exact modulo 2^32 and so
-// exact for these values), kEdge46 below 2^46 (64-bit, FP32-add
-// conversion), kEdge64 beyond (the conversion instruction).
+// exact for these values; the 32-bit conversion instruction), kEdge46 below
+// 2^46 (64-bit, FP32-add conversion), kEdge64 beyond (the 64-bit conversion
+// instruction).
 enum EdgeMode { kEdge32 = 0, kEdge46 = 1, kEdge64 = 2 };
 template <int MODE>
 struct EdgeVal {
@@ -790,7 +791,7 @@ struct EdgeVal {
 };
 template <int MODE>
 __device__ __forceinline__ float covered_to_float(typename EdgeVal<MODE>::T v) {
-    if (MODE == kEdge32) return u32_to_f32_rn((uint32_t)v);
+    if (MODE == kEdge32) return __uint2float_rn((uint32_t)v);
     if (MODE == kEdge46) return u46_to_f32_rn((uint64_t)v);
     return __ll2float_rn((int64_t)v);
 }
@@ -800,16 +801,22 @@ __device__ __forceinline__ typename EdgeVal<MODE>::T shfl_edge(typename EdgeVal<
     return (int64_t)__shfl_sync(0xFFFFFFFFu, (unsigned long long)v, src);
 }
 
+// The triangle's depth plane and ID, held in registers during a walk.
+struct ChunkDepth {
+    float z0, s1, s2;
+    uint32_t id;
+};
+
 // A covered pixel: depth from its two edge values (the per-pixel test's
 // arithmetic), then the depth test at linear pixel index `pix`.
 template <int KIND, int MODE>
-__device__ __forceinline__ void chunk_fragment(const BigTri& b, void* target, uint32_t pix,
+__device__ __forceinline__ void chunk_fragment(const ChunkDepth& t, void* target, uint32_t pix,
                                                typename EdgeVal<MODE>::T a20, typename EdgeVal<MODE>::T a01) {
-    float d = (b.z0 + covered_to_float<MODE>(a20) * b.s1) + covered_to_float<MODE>(a01) * b.s2;
+    float d = (t.z0 + covered_to_float<MODE>(a20) * t.s1) + covered_to_float<MODE>(a01) * t.s2;
     d = d > 0.0f ? d : 0.0f;
     d = d < 1.0f ? d : 1.0f;
     if (KIND == 0) {
-        const unsigned long long key = ((unsigned long long)f2u(d) << 32) | b.id;
+        const unsigned long long key = ((unsigned long long)f2u(d) << 32) | t.id;
         asm volatile("red.relaxed.gpu.global.max.u64 [%0], %1;" ::"l"(reinterpret_cast<unsigned long long*>(target) + pix),
                      "l"(key));
     } else {
@@ -822,19 +829,20 @@ __device__ __forceinline__ void chunk_fragment(const BigTri& b, void* target, ui
 // row r's run: its length, the linear index of its first pixel and the two
 // edge values there.
 template <int KIND, int MODE>
-__device__ __forceinline__ uint32_t chunk_rows(const BigTri& b, void* target, uint32_t rows, uint32_t lane, int32_t len,
-                                               uint32_t pix_first, typename EdgeVal<MODE>::T f20,
+__device__ __forceinline__ uint32_t chunk_rows(const ChunkDepth& t, void* target, uint32_t rows, uint32_t lane,
+                                               int32_t len, uint32_t pix_first, typename EdgeVal<MODE>::T f20,
                                                typename EdgeVal<MODE>::T f01, typename EdgeVal<MODE>::T dx20,
                                                typename EdgeVal<MODE>::T dx01) {
     using T = typename EdgeVal<MODE>::T;
     uint32_t nfrag = 0;
+    const T step20 = 32 * dx20, step01 = 32 * dx01;
     for (uint32_t r = 0; r < rows; r++) {
         const int32_t l = __shfl_sync(0xFFFFFFFFu, len, r);
         if (l == 0) continue;
         uint32_t pix = __shfl_sync(0xFFFFFFFFu, pix_first, r) + lane;
         T a20 = shfl_edge<MODE>(f20, r) + (T)lane * dx20, a01 = shfl_edge<MODE>(f01, r) + (T)lane * dx01;
-        for (int32_t k = (int32_t)lane; k < l; k += 32, pix += 32, a20 += 32 * dx20, a01 += 32 * dx01) {
-            chunk_fragment<KIND, MODE>(b, target, pix, a20, a01);
+        for (int32_t k = (int32_t)lane; k < l; k += 32, pix += 32, a20 += step20, a01 += step01) {
+            chunk_fragment<KIND, MODE>(t, target, pix, a20, a01);
             nfrag++;
         }
     }
@@ -842,31 +850,33 @@ __device__ __forceinline__ uint32_t chunk_rows(const BigTri& b, void* target, ui
 }
 
 // Compacted: the covered pixels of all rows numbered one after another,
-// 32 consecutive per step, one per lane (short runs: slivers, corners).  A
-// lane finds the row of its pixel number p by binary search of the runs'
-// first numbers (an empty row shares the next row's first number, so the
-// last row whose first number is <= p holds p); lane r holds, for row r,
-// the linear index and edge values extrapolated to p = 0.
+// 32 consecutive per step, one per lane (short runs: slivers, corners).
+// The non-empty rows are ranked in row order and lane k holds the k-th
+// one's run: its first number, and the linear index and edge values
+// extrapolated to number 0.  A step over numbers [base, base + 32) marks
+// the runs that start inside it in one word (a warp OR of one bit per
+// run), so a lane's run is the last one started at or before its number:
+// the runs started before the step plus those marked up to its own bit.
 template <int KIND, int MODE>
-__device__ __forceinline__ uint32_t chunk_compact(const BigTri& b, void* target, uint32_t rows, uint32_t lane,
-                                                  int32_t total, int32_t pre, uint32_t pix_zero,
-                                                  typename EdgeVal<MODE>::T z20, typename EdgeVal<MODE>::T z01,
-                                                  typename EdgeVal<MODE>::T dx20, typename EdgeVal<MODE>::T dx01) {
+__device__ __forceinline__ uint32_t chunk_compact(const ChunkDepth& t, void* target, uint32_t lane, int32_t total,
+                                                  int32_t first, uint32_t pix_zero, typename EdgeVal<MODE>::T z20,
+                                                  typename EdgeVal<MODE>::T z01, typename EdgeVal<MODE>::T dx20,
+                                                  typename EdgeVal<MODE>::T dx01, uint32_t nonempty) {
     using T = typename EdgeVal<MODE>::T;
     uint32_t nfrag = 0;
+    const uint32_t upto_me = 0xFFFFFFFFu >> (31u - lane);  // bits 0 .. lane
+    int32_t before = 0;  // runs started before the step
     for (int32_t base = 0; base < total; base += 32) {
+        const uint32_t off = (uint32_t)(first - base);
+        const uint32_t starts = __reduce_or_sync(0xFFFFFFFFu, lane < nonempty && off < 32u ? 1u << off : 0u);
+        const int32_t k = before + __popc(starts & upto_me) - 1;  // the lane's run
+        before += __popc(starts);
         const int32_t p = base + (int32_t)lane;
-        uint32_t r = 0;
-#pragma unroll
-        for (uint32_t bit = 16; bit; bit >>= 1) {
-            const uint32_t c = r + bit;
-            const int32_t s = __shfl_sync(0xFFFFFFFFu, pre, c & 31u);
-            if (c < rows && s <= p) r = c;
-        }
-        const uint32_t pix = (uint32_t)p + __shfl_sync(0xFFFFFFFFu, pix_zero, r);
-        const T a20 = shfl_edge<MODE>(z20, r) + (T)p * dx20, a01 = shfl_edge<MODE>(z01, r) + (T)p * dx01;
+        const uint32_t src = (uint32_t)k & 31u;
+        const uint32_t pix = (uint32_t)p + __shfl_sync(0xFFFFFFFFu, pix_zero, src);
+        const T a20 = shfl_edge<MODE>(z20, src) + (T)p * dx20, a01 = shfl_edge<MODE>(z01, src) + (T)p * dx01;
         if (p < total) {
-            chunk_fragment<KIND, MODE>(b, target, pix, a20, a01);
+            chunk_fragment<KIND, MODE>(t, target, pix, a20, a01);
             nfrag++;
         }
     }
@@ -879,17 +889,24 @@ __device__ __forceinline__ uint32_t chunk_walk(const BigTri& b, void* target, ui
                                                uint32_t rows, uint32_t lane, int32_t lo, int32_t len, int32_t pre,
                                                int32_t total, int64_t e20, int64_t e01, int64_t dx20, int64_t dx01) {
     using T = typename EdgeVal<MODE>::T;
+    const ChunkDepth t{b.z0, b.s1, b.s2, b.id};
     // steps of the row walk (plus a row's own cost) against the compacted
     // walk's, whose steps cost about twice as much
     const uint32_t row_steps = __reduce_add_sync(0xFFFFFFFFu, (uint32_t)(len + 31) >> 5);
-    const uint32_t nonempty = __popc(__ballot_sync(0xFFFFFFFFu, len > 0));
+    const uint32_t ne_mask = __ballot_sync(0xFFFFFFFFu, len > 0);
+    const uint32_t nonempty = __popc(ne_mask);
     const uint32_t pix_row = (uint32_t)(y0 + (int32_t)lane) * W + (uint32_t)x0;
     if (row_steps + nonempty / 4u <= 2u * (uint32_t)((total + 31) >> 5))
-        return chunk_rows<KIND, MODE>(b, target, rows, lane, len, pix_row + (uint32_t)lo, (T)(e20 + (int64_t)lo * dx20),
+        return chunk_rows<KIND, MODE>(t, target, rows, lane, len, pix_row + (uint32_t)lo, (T)(e20 + (int64_t)lo * dx20),
                                       (T)(e01 + (int64_t)lo * dx01), (T)dx20, (T)dx01);
-    return chunk_compact<KIND, MODE>(b, target, rows, lane, total, pre, pix_row + (uint32_t)(lo - pre),
-                                     (T)(e20 + (int64_t)(lo - pre) * dx20), (T)(e01 + (int64_t)(lo - pre) * dx01),
-                                     (T)dx20, (T)dx01);
+    // rank the non-empty rows: lane k takes the k-th one's values
+    const uint32_t src = __fns(ne_mask, 0, (int32_t)lane + 1);  // 0xFFFFFFFF past the last
+    const uint32_t s = src < 32u ? src : 0u;
+    const int32_t first = __shfl_sync(0xFFFFFFFFu, pre, s);
+    const uint32_t pix_zero = __shfl_sync(0xFFFFFFFFu, pix_row + (uint32_t)(lo - pre), s);
+    const T z20 = shfl_edge<MODE>((T)(e20 + (int64_t)(lo - pre) * dx20), s);
+    const T z01 = shfl_edge<MODE>((T)(e01 + (int64_t)(lo - pre) * dx01), s);
+    return chunk_compact<KIND, MODE>(t, target, lane, total, first, pix_zero, z20, z01, (T)dx20, (T)dx01, nonempty);
 }
 
 // The pixels [x0, x1] x [y0, y1] (at most 32 rows of at most 256) of an
@@ -1066,13 +1083,23 @@ __device__ void phase_raster_big(const FrameDev& f) {
                 cy = (int32_t)((c - t_base) / nbx);
             }
         } else {
-            // another triangle: a 32-ary search of the bases
-            const uint32_t first = upper_bound_warp(f.big_base, ntri, c, lane);
-            if (first == 0) {
-                c++;
-                continue;
+            // another triangle: the queue's next one when c lies in its
+            // range (chunk numbers ascend with the entries), else a 32-ary
+            // search of the bases
+            uint32_t i = 0xFFFFFFFFu;
+            if (c >= t_end && t_end > t_base && t_idx + 1u < ntri) {
+                const uint32_t b1 = f.big_base[t_idx + 1u];
+                const uint32_t b2 = t_idx + 2u < ntri ? f.big_base[t_idx + 2u] : total32;
+                if (c >= b1 && c < b2) i = t_idx + 1u;
             }
-            const uint32_t i = first - 1;
+            if (i == 0xFFFFFFFFu) {
+                const uint32_t first = upper_bound_warp(f.big_base, ntri, c, lane);
+                if (first == 0) {
+                    c++;
+                    continue;
+                }
+                i = first - 1;
+            }
             const BigTri nb = f.big[i];
             const uint32_t base = f.big_base[i];
             const uint32_t nx = ((uint32_t)(nb.px1 - nb.px0) >> cs) + 1;
