@@ -1022,14 +1022,24 @@ __device__ __noinline__ uint32_t raster_chunk_alpha(const FrameDev& f, const Big
 // at most 32 x 256 pixels): opaque chunks by runs of covered pixels
 // (raster_chunk_runs), alpha-tested ones pixel by pixel, skipped whole when
 // their rectangle lies outside one edge.
+// Asynchronous 16-byte copy global -> shared through L2 (cp.async.cg), and
+// the wait for the issuing thread's copies.
+__device__ __forceinline__ void cp_async16_cg(void* smem, const void* gmem) {
+    const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 template <int KIND>
 __device__ void phase_raster_big(const FrameDev& f) {
     // the views' targets and widths, read once per block
     __shared__ unsigned long long s_target[kMaxViews];
     __shared__ uint32_t s_width[kMaxViews];
-    // each warp's current triangle (kept in shared memory, not registers,
-    // between its chunks; blocks of kRasterWarps warps)
-    __shared__ BigTri s_tri[kRasterWarps];
+    // each warp's current triangle and the queue's next one (copied ahead
+    // with cp.async while the current one's chunks are walked), kept in
+    // shared memory, not registers; blocks of kRasterWarps warps
+    __shared__ __align__(16) BigTri s_tri[kRasterWarps][2];
     __shared__ ChunkSteps s_steps[kRasterWarps];
     __syncthreads();  // a previous call of this phase in the block may still read them
     for (uint32_t v = threadIdx.x; v < f.n_views; v += blockDim.x) {
@@ -1040,25 +1050,26 @@ __device__ void phase_raster_big(const FrameDev& f) {
     const unsigned long long packed = *reinterpret_cast<volatile unsigned long long*>(f.status + kStBigPacked);
     const uint32_t ntri = (uint32_t)min((unsigned long long)f.big_cap, packed >> 40);
     const unsigned long long total = packed & ((1ull << 40) - 1);
-    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (ntri == 0) return;
     constexpr uint32_t kChunkBatch = 4;  // chunks claimed per atomic
     // chunk numbers fit 32 bits (push_big drops triangles beyond)
     const uint32_t total32 = (uint32_t)min(total, 0xFFFFFFFFull);
     // static first batch per warp, then claims from warps * kChunkBatch on
     const uint32_t warps_total = gridDim.x * (blockDim.x >> 5);
-    const uint32_t gwarp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const uint32_t gwarp = blockIdx.x * (blockDim.x >> 5) + w;
     const uint64_t dyn_base = (uint64_t)warps_total * kChunkBatch;
     const uint32_t rs = f.chunk_shift[KIND][0], cs = f.chunk_shift[KIND][1];
     uint32_t c = (uint32_t)min((uint64_t)gwarp * kChunkBatch, (uint64_t)total32);
     uint32_t c_end = (uint32_t)min((uint64_t)gwarp * kChunkBatch + kChunkBatch, (uint64_t)total32);
     // the current triangle, kept while consecutive chunks belong to it:
-    // its entry, chunk range [t_base, t_end), chunk columns and steps, and
-    // the coordinates of the last chunk taken (number c_last)
-    uint32_t t_idx = 0, t_base = 1, t_end = 0, nbx = 1, c_last = 0xFFFFFFFFu;
+    // its entry, chunk range [t_base, t_end), chunk columns, shared-memory
+    // slot, and the coordinates of the last chunk taken (number c_last);
+    // the copied-ahead next entry (index pre_idx, chunk range [pb1, pb2))
+    uint32_t t_idx = 0, t_base = 1, t_end = 0, nbx = 1, c_last = 0xFFFFFFFFu, slot = 0;
+    uint32_t pre_idx = 0xFFFFFFFFu, pb1 = 0, pb2 = 0;
     int32_t cx = 0, cy = 0;
-    BigTri& b = s_tri[threadIdx.x >> 5];
-    ChunkSteps& ks = s_steps[threadIdx.x >> 5];
+    const ChunkSteps& ks = s_steps[w];
     uint32_t nfrag = 0;
     for (;;) {
         if (c >= c_end) {
@@ -1083,46 +1094,64 @@ __device__ void phase_raster_big(const FrameDev& f) {
                 cy = (int32_t)((c - t_base) / nbx);
             }
         } else {
-            // another triangle: the queue's next one when c lies in its
-            // range (chunk numbers ascend with the entries), else a 32-ary
-            // search of the bases
-            uint32_t i = 0xFFFFFFFFu;
-            if (c >= t_end && t_end > t_base && t_idx + 1u < ntri) {
-                const uint32_t b1 = f.big_base[t_idx + 1u];
-                const uint32_t b2 = t_idx + 2u < ntri ? f.big_base[t_idx + 2u] : total32;
-                if (c >= b1 && c < b2) i = t_idx + 1u;
-            }
-            if (i == 0xFFFFFFFFu) {
+            // another triangle: the copied-ahead next entry when c lies in
+            // its range (chunk numbers ascend with the entries), else a
+            // 32-ary search of the bases and a load
+            __syncwarp();  // every lane is done with the current slot
+            uint32_t i, base;
+            if (pre_idx != 0xFFFFFFFFu && c >= pb1 && c < pb2) {
+                i = pre_idx;
+                base = pb1;
+                cp_async_wait_all();
+                __syncwarp();
+                slot ^= 1u;
+            } else {
                 const uint32_t first = upper_bound_warp(f.big_base, ntri, c, lane);
                 if (first == 0) {
                     c++;
                     continue;
                 }
                 i = first - 1;
+                const BigTri nb = f.big[i];
+                base = f.big_base[i];
+                if (lane == 0) s_tri[w][slot] = nb;
+                __syncwarp();
             }
-            const BigTri nb = f.big[i];
-            const uint32_t base = f.big_base[i];
+            const BigTri& nb = s_tri[w][slot];
             const uint32_t nx = ((uint32_t)(nb.px1 - nb.px0) >> cs) + 1;
             const uint32_t ny = ((uint32_t)(nb.py1 - nb.py0) >> rs) + 1;
             if ((unsigned long long)(c - base) >= (unsigned long long)nx * ny) {  // chunk of a dropped triangle
+                t_base = 1;  // the slot no longer holds the current triangle
+                t_end = 0;
+                pre_idx = 0xFFFFFFFFu;
                 c++;
                 continue;
             }
-            __syncwarp();  // every lane is done with the previous triangle
-            if (lane == 0) {
-                b = nb;
-                ks = chunk_steps(nb);
-            }
-            __syncwarp();
+            if (lane == 0) s_steps[w] = chunk_steps(nb);
             t_idx = i;
             t_base = base;
             t_end = base + nx * ny;
             nbx = nx;
             cx = (int32_t)((c - base) % nx);
             cy = (int32_t)((c - base) / nx);
+            // copy the queue's next entry into the other slot meanwhile
+            pre_idx = 0xFFFFFFFFu;
+            if (i + 1u < ntri) {
+                if (lane < 4) {
+                    cp_async_wait_all();  // a copy still in flight to that slot
+                    cp_async16_cg(reinterpret_cast<char*>(&s_tri[w][slot ^ 1u]) + 16 * lane,
+                                  reinterpret_cast<const char*>(f.big + i + 1u) + 16 * lane);
+                    cp_async_commit();
+                }
+                pb1 = f.big_base[i + 1u];
+                pb2 = i + 2u < ntri ? f.big_base[i + 2u] : total32;
+                pre_idx = i + 1u;
+            }
+            __syncwarp();
         }
         c_last = c;
         c++;
+        const BigTri& b = s_tri[w][slot];
         const int32_t x0 = b.px0 + (cx << cs), x1 = min(b.px1, x0 + (1 << cs) - 1);
         const int32_t y0 = b.py0 + (cy << rs), y1 = min(b.py1, y0 + (1 << rs) - 1);
         void* target = reinterpret_cast<void*>(s_target[b.view]);
@@ -1137,6 +1166,7 @@ __device__ void phase_raster_big(const FrameDev& f) {
         }
         nfrag += raster_chunk_runs<KIND>(b, ks, x0, x1, y0, y1, lane, target, W);
     }
+    cp_async_wait_all();  // no copy outlives the phase
     count_fragments<KIND>(f, nfrag);
 }
 
