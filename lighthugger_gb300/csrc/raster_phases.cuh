@@ -42,6 +42,12 @@ namespace {
 
 constexpr int kRasterWarps = 8;
 
+// Chunks of big triangles a warp claims per atomic (build knob; large
+// frame 0.395 ms at 2, 0.397 at 4, 0.425 at 1, 0.464 at 8).
+#ifndef LH_CHUNK_BATCH
+#define LH_CHUNK_BATCH 2
+#endif
+
 // Upper bound of the warp bin in the shadow pass (0: the tuning's medium_px
 // for both passes).  A shadow launch has about one unit per warp, so a warp
 // that rasterises a run of 33-128-pixel triangles one after another sets the
@@ -1052,7 +1058,7 @@ __device__ void phase_raster_big(const FrameDev& f) {
     const unsigned long long total = packed & ((1ull << 40) - 1);
     const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (ntri == 0) return;
-    constexpr uint32_t kChunkBatch = 4;  // chunks claimed per atomic
+    constexpr uint32_t kChunkBatch = LH_CHUNK_BATCH;  // chunks claimed per atomic
     // chunk numbers fit 32 bits (push_big drops triangles beyond)
     const uint32_t total32 = (uint32_t)min(total, 0xFFFFFFFFull);
     // static first batch per warp, then claims from warps * kChunkBatch on
