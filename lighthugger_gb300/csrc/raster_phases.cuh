@@ -678,7 +678,6 @@ __device__ void phase_raster(const FrameDev& f, uint32_t view_begin, uint32_t n_
     SnapV(*s_v)[MAX_MESHLET_UNIQUE_VERTICES] = sm.v;
     uint8_t(*s_oc)[MAX_MESHLET_UNIQUE_VERTICES] = sm.oc;
     uint32_t(*s_micro)[kMicroWords] = sm.micro;
-    const uint32_t md = f.max_draws;
     __syncthreads();  // `sm` may still be in use by a previous phase of the block
     if (threadIdx.x == 0) {
         uint32_t run = 0;
