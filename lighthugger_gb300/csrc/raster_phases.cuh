@@ -1282,20 +1282,30 @@ __device__ __forceinline__ bool hiz_occluded(const ViewDev* vw, const lh_mat4& p
     if (ix0 > ix1 || iy0 > iy1) return true;  // no pixel centre of the view in reach
     const uint32_t pitch0 = vw->hiz_rx * 8u;
     const uint32_t* level0 = vw->hiz;
+    // the ≤ 16 tiles (or regions) under the box, loaded all at once (no
+    // load waits on the previous one's compare), then their minimum
+    auto box_min = [](const uint32_t* level, uint32_t pitch, int32_t tx0, int32_t tx1, int32_t ty0, int32_t ty1) {
+        const int32_t n = (tx1 - tx0 + 1) * (ty1 - ty0 + 1);
+        uint32_t m = 0xFFFFFFFFu;
+        int32_t tx = tx0, ty = ty0;
+#pragma unroll
+        for (int32_t k = 0; k < 16; k++) {
+            if (k < n) {
+                m = min(m, __ldcg(level + (size_t)ty * pitch + tx));
+                if (++tx > tx1) {
+                    tx = tx0;
+                    ty++;
+                }
+            }
+        }
+        return m;
+    };
     int32_t tx0 = ix0 >> 3, tx1 = ix1 >> 3, ty0 = iy0 >> 3, ty1 = iy1 >> 3;
-    if ((tx1 - tx0 + 1) * (ty1 - ty0 + 1) <= 16) {
-        for (int32_t ty = ty0; ty <= ty1; ty++)
-            for (int32_t tx = tx0; tx <= tx1; tx++)
-                if (__ldcg(level0 + (size_t)ty * pitch0 + tx) <= zbits) return false;
-        return true;
-    }
+    if ((tx1 - tx0 + 1) * (ty1 - ty0 + 1) <= 16) return box_min(level0, pitch0, tx0, tx1, ty0, ty1) > zbits;
     const uint32_t* level1 = level0 + (size_t)pitch0 * vw->hiz_ry * 8u;
     tx0 = ix0 >> 6, tx1 = ix1 >> 6, ty0 = iy0 >> 6, ty1 = iy1 >> 6;
     if ((tx1 - tx0 + 1) * (ty1 - ty0 + 1) > 16) return false;
-    for (int32_t ty = ty0; ty <= ty1; ty++)
-        for (int32_t tx = tx0; tx <= tx1; tx++)
-            if (__ldcg(level1 + (size_t)ty * vw->hiz_rx + tx) <= zbits) return false;
-    return true;
+    return box_min(level1, vw->hiz_rx, tx0, tx1, ty0, ty1) > zbits;
 }
 
 // After the hierarchical depth: every visible meshlet of the visibility
