@@ -1338,9 +1338,10 @@ __device__ void phase_occlusion_filter(const FrameDev& f, uint32_t view_begin, u
                 alpha = i >= nop;
                 slot = alpha ? md + (uint32_t)(i - nop) : (uint32_t)i;
                 const RasterDraw* rd = vw->rdraws + slot;
+                // both loads issued together (one round trip)
                 const uint32_t bits = __ldcg(&rd->bits);
+                const float4 sp4 = __ldcg(reinterpret_cast<const float4*>(rd->sphere));
                 if (!(bits & kDrawOccluder)) {
-                    const float4 sp4 = __ldcg(reinterpret_cast<const float4*>(rd->sphere));
                     const float sp[4] = {sp4.x, sp4.y, sp4.z, sp4.w};
                     keep = !vw->hiz || !hiz_occluded(vw, pv, sp);
                 }

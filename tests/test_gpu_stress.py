@@ -42,6 +42,26 @@ def test_stress_parity(native, stress, schedule):
     assert st.candidate_meshlets[0] > 5_000_000
 
 
+def test_stress_reduced_parity(native, oracle):
+    """The stress scene's meshes at a quarter of its instances, 1920 x 1080
+    + 4 cascades: bit exact against the oracle (a stress-shaped case small
+    enough for a full profiler capture)."""
+    lh = native
+    scene = lh.Scene(5, n_instances=25000, width=1920, height=1080).upload(0)
+    d = scene.desc
+    md = 2000000
+    r = lh.Renderer(lh.Config(width=d.width, height=d.height, shadow_size=d.shadow_size, max_instances=d.n_instances,
+                              max_draws=md, max_big_triangles=1 << 21))
+    r.set_scene(scene)
+    r.frame(scene.uniforms)
+    st = r.status()
+    assert st.flags == 0, hex(st.flags)
+    fr = oracle.run_scene(scene, shadow_size=d.shadow_size, max_instances=d.n_instances, max_draws=md)
+    errors, stats = compare_frame(r, fr, md, d.n_instances)
+    assert not errors, "\n".join(errors) + " %s" % stats
+    assert st.candidate_meshlets[0] > 1_000_000
+
+
 def _grad_targets(lh, scene, torch):
     """Gradient buffers for every mesh record, texture and the light, and the
     GradTargets that point at them."""
