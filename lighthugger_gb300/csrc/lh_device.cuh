@@ -236,11 +236,18 @@ __device__ __forceinline__ uint32_t outcode(f4 v) {
 
 struct SnapV { int32_t X, Y; float z; };
 
-// Viewport transform + snap to 1/256 pixel (round to nearest even).
+// Viewport transform + snap to 1/256 pixel (round to nearest even).  An
+// orthographic view (the shadow cascades) has w = 1 exactly, and x / 1 = x
+// for every x: the divides only run when they can change a bit.
 __device__ __forceinline__ SnapV snap(f4 v, float hw, float hh) {
-    float ndx = v.x / v.w, ndy = v.y / v.w;
+    float ndx = v.x, ndy = v.y;
     SnapV s;
-    s.z = v.z / v.w;
+    s.z = v.z;
+    if (v.w != 1.0f) {
+        ndx = v.x / v.w;
+        ndy = v.y / v.w;
+        s.z = v.z / v.w;
+    }
     float xf = ndx * hw + hw, yf = ndy * hh + hh;
     s.X = __float2int_rn(xf * 256.0f);
     s.Y = __float2int_rn(yf * 256.0f);
@@ -310,7 +317,8 @@ __device__ __forceinline__ void finish_setup(SnapV v0, SnapV v1, SnapV v2, int64
     t.py0 = b.py0;
     t.py1 = b.py1;
     t.X0 = v0.X; t.Y0 = v0.Y; t.X1 = v1.X; t.Y1 = v1.Y; t.X2 = v2.X; t.Y2 = v2.Y;
-    float fA = __ll2float_rn(A);
+    // A > 0 (round to nearest even either way; FP32 adds below 2^46)
+    const float fA = A < (1ll << 46) ? u46_to_f32_rn((uint64_t)A) : __ll2float_rn(A);
     t.z0 = v0.z;
     t.s1 = (v1.z - v0.z) / fA;
     t.s2 = (v2.z - v0.z) / fA;

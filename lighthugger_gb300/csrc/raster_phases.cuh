@@ -1057,11 +1057,14 @@ __device__ void phase_raster_big(const FrameDev& f) {
     const unsigned long long total = packed & ((1ull << 40) - 1);
     const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (ntri == 0) return;
-    constexpr uint32_t kChunkBatch = LH_CHUNK_BATCH;  // chunks claimed per atomic
     // chunk numbers fit 32 bits (push_big drops triangles beyond)
     const uint32_t total32 = (uint32_t)min(total, 0xFFFFFFFFull);
-    // static first batch per warp, then claims from warps * kChunkBatch on
+    // static first batch per warp, then claims from warps * kChunkBatch on;
+    // chunks claimed per atomic: LH_CHUNK_BATCH, or 16 when the queue holds
+    // more than 256 chunks per warp (millions of chunks would otherwise
+    // queue on the one claim word)
     const uint32_t warps_total = gridDim.x * (blockDim.x >> 5);
+    const uint32_t kChunkBatch = total32 > 256u * warps_total ? 16u : (uint32_t)LH_CHUNK_BATCH;
     const uint32_t gwarp = blockIdx.x * (blockDim.x >> 5) + w;
     const uint64_t dyn_base = (uint64_t)warps_total * kChunkBatch;
     const uint32_t rs = f.chunk_shift[KIND][0], cs = f.chunk_shift[KIND][1];
