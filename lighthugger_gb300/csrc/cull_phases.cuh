@@ -22,6 +22,7 @@
 
 #include "lh_device.cuh"
 #include "lh_internal.cuh"
+#include "sphere_box.cuh"
 
 namespace lh {
 namespace {
@@ -114,7 +115,8 @@ __device__ __forceinline__ float bounding_radius(const float4 (&c)[4], float r) 
 // reaching the camera plane).  Occluders are appended to the view's
 // occluder list (any order: the raster is order independent).
 __device__ __forceinline__ RasterDraw raster_draw_of(const FrameDev& f, const ViewDev* vw, const Uniforms& u,
-                                                     MeshletReference ref, bool alpha, uint32_t slot) {
+                                                     const lh_mat4& vp, MeshletReference ref, bool alpha,
+                                                     uint32_t slot) {
     const Instance* inst = f.instances + ref.instance_index;
     const unsigned long long* mw = reinterpret_cast<const unsigned long long*>(__ldg(&inst->mesh_info_address));
     const uint64_t positions = __ldg(mw + 0), indices = __ldg(mw + 1), micro = __ldg(mw + 4), meshlets = __ldg(mw + 5);
@@ -146,6 +148,13 @@ __device__ __forceinline__ RasterDraw raster_draw_of(const FrameDev& f, const Vi
     r.sphere[1] = wy;
     r.sphere[2] = wz;
     r.sphere[3] = R;
+    // small views (probes): a meshlet whose sphere reaches no pixel centre
+    // is common there, and the raster skips it before its vertices (in
+    // large views the test would cost the cull more than it saves)
+    if (vw->width * vw->height <= kNoCentreTestPixels && sphere_misses_centres(vp, wx, wy, wz, R, vw->width, vw->height)) {
+        r.bits |= kDrawNoCentre;
+        return r;
+    }
     if (f.occlusion_px && !alpha && vw->kind == kViewVisibility && vw->lists) {
         const lh_mat4& pv = u.combined_perspective_view;
         const float w = ((pv.cols[0].w * wx + pv.cols[1].w * wy) + pv.cols[2].w * wz) + pv.cols[3].w;
@@ -504,7 +513,9 @@ __device__ void phase_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint
             dc.firstInstance = vw->section_base + slot;
             draws[slot] = dc;
             out_refs[slot] = refs[k];
-            vw->rdraws[slot] = raster_draw_of(f, vw, s_u, refs[k], cl == 2u, slot);
+            vw->rdraws[slot] = raster_draw_of(f, vw, s_u, kind == kViewVisibility ? s_u.combined_perspective_view
+                                                                                  : s_m.shadow_matrices[cascade],
+                                              refs[k], cl == 2u, slot);
         }
         __syncthreads();
     }

@@ -40,13 +40,15 @@ struct __align__(16) RasterDraw {
     uint64_t indices;    // MeshInfo.indices + Meshlet.index_offset elements
     uint64_t micro;      // MeshInfo.micro_indices + Meshlet.triangle_offset
     uint32_t instance;   // MeshletReference.instance_index
-    uint32_t bits;       // index_count | triangle_count << 8 | MeshInfo.flags << 16 | kDrawOccluder
+    uint32_t bits;       // index_count | triangle_count << 8 | MeshInfo.flags << 16 | kDrawNoCentre | kDrawOccluder
     float sphere[4];     // world-space sphere holding every vertex of the meshlet (centre, radius)
 };
 static_assert(sizeof(RasterDraw) == 48, "RasterDraw layout");
 // RasterDraw::bits: the meshlet is rasterised in the occluder pass (a
 // visibility view with occlusion culling, opaque, large on screen).
 constexpr uint32_t kDrawOccluder = 1u << 31;
+constexpr uint32_t kDrawNoCentre = 1u << 30;  // the world sphere reaches no pixel centre of the view
+constexpr uint32_t kNoCentreTestPixels = 512u * 512u;  // views up to this size test it (sphere_box.cuh)
 
 // Per-view lists of the two-pass occlusion raster of visibility views
 // (ViewDev::lists, 3 * max_draws words): draw slots of the occluders, then

@@ -764,6 +764,7 @@ __device__ void phase_raster(const FrameDev& f, uint32_t view_begin, uint32_t n_
             continue;
         }
         if (part * 32u >= nt) continue;  // this quarter holds no triangles
+        if (rd.bits & kDrawNoCentre) continue;  // no pixel centre in reach of its sphere
         const MeshletWork w{view, slot, part, split, nv, nt, W, H, target, hw, hh, &s_vp[v], transform, mi, 0u, 0u, inst};
         raster_meshlet<KIND, ALPHA>(f, w, tune, sv, so, s_micro[warp], ALPHA ? s_av[warp] : nullptr, lane, nfrag);
     }
@@ -1344,7 +1345,7 @@ __device__ void phase_occlusion_filter(const FrameDev& f, uint32_t view_begin, u
                 // both loads issued together (one round trip)
                 const uint32_t bits = __ldcg(&rd->bits);
                 const float4 sp4 = __ldcg(reinterpret_cast<const float4*>(rd->sphere));
-                if (!(bits & kDrawOccluder)) {
+                if (!(bits & (kDrawOccluder | kDrawNoCentre))) {
                     const float sp[4] = {sp4.x, sp4.y, sp4.z, sp4.w};
                     keep = !vw->hiz || !hiz_occluded(vw, pv, sp);
                 }

@@ -31,3 +31,18 @@ def test_edge_runs_hold_exactly_the_covered_pixels():
         r = subprocess.run([exe], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "bad 0" in r.stdout
+
+
+def test_sphere_box_skips_only_meshlets_without_pixel_centres():
+    """lighthugger_gb300/csrc/sphere_box.cuh (the raster's skip of meshlets
+    whose world sphere reaches no pixel centre): sampled points of every
+    skipped sphere, through the raster's transform and snap, reach none."""
+    src = os.path.join(ROOT, "tests", "native", "sphere_box_check.cpp")
+    with tempfile.TemporaryDirectory() as d:
+        exe = os.path.join(d, "sphere_box_check")
+        subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I",
+                        os.path.join(ROOT, "lighthugger_gb300", "csrc"), "-I", os.path.join(ROOT, "include"), src,
+                        "-o", exe], check=True)
+        r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "bad 0" in r.stdout
