@@ -577,6 +577,13 @@ def bench_differentiable(lh, torch, args, device):
     grad = torch.randn(d.height, d.width, 4, device=dev)
     t = lh.GradTargets(instance_grads=inst_rec.data_ptr(), texture_grads=tex_tab.data_ptr(),
                        light_dir=light.data_ptr(), light_color=light.data_ptr() + 16)
+    tuned = None
+    if args.tune:
+        # the adjoint's tile rows picked by the autotuner (before timing)
+        from lighthugger_gb300 import autotune
+        r.frame(u, stream=sptr)
+        rows, res = autotune.tune_backward(r, grad.data_ptr(), t, frames=4, stream=stream)
+        tuned = {"backward_rows": rows, "ms": {str(k): round(v, 4) for k, v in res.items()}}
     r.set_profiling(True)
     fwd, bwd = [], []
     for i in range(max(3, args.warmup) + args.steps):
@@ -597,7 +604,8 @@ def bench_differentiable(lh, torch, args, device):
     f_ms, b_ms = sum(fwd) / len(fwd), sum(bwd) / len(bwd)
     return {"workload": "%d instances of %d meshes, %dx%d, visibility fixed" % (d.n_instances, d.n_meshes, d.width,
                                                                                  d.height),
-            "resolve_forward_ms": f_ms, "resolve_backward_ms": b_ms, "bwd_over_fwd": b_ms / f_ms}
+            "resolve_forward_ms": f_ms, "resolve_backward_ms": b_ms, "bwd_over_fwd": b_ms / f_ms,
+            "backward_rows": int(r.tuning().backward_rows), "autotuned": tuned}
 
 
 def bench_stress(lh, torch, args, device):
