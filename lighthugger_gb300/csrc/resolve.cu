@@ -483,7 +483,10 @@ __device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uin
 #endif
 constexpr uint32_t kResolveWarps = 8;   // warps per block = rows of a strip
 constexpr uint32_t kStripCols = 128;    // a strip: 128 x 8 pixels (4 tiles of 32 x 8)
-constexpr uint32_t kResolveStages = 2;  // strips in flight per warp
+#ifndef LH_RESOLVE_STAGES
+#define LH_RESOLVE_STAGES 2
+#endif
+constexpr uint32_t kResolveStages = LH_RESOLVE_STAGES;  // strips in flight per warp (build knob)
 
 // One thread per pixel over 128 x 8-pixel strips, one warp per strip row
 // (four 32-pixel steps); a grid of resident blocks strides over the strips,
