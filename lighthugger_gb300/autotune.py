@@ -26,7 +26,7 @@ import os
 _HERE = os.path.dirname(os.path.abspath(__file__))
 CACHE = os.path.join(_HERE, "_build", "tuning.json")
 
-OCCLUSION = (0, 64, 128, 256, 512)
+OCCLUSION = (0, 16, 32, 64, 128, 256, 512)
 BINS = ((32, 32), (16, 16), (16, 64), (32, 64), (32, 128), (16, 128))  # (small_px, medium_px)
 CHUNK = ((16, 32), (16, 64), (32, 64), (16, 128), (32, 128), (32, 256))  # (rows, columns)
 BATCH = (0, 1, 2, 4)
