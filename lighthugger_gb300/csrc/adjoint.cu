@@ -214,21 +214,22 @@ __device__ __forceinline__ void pixel_backward(const FrameDev& f, const float4* 
     const float4 gp = __ldcs(grad + (size_t)y * W + x);
     const uint32_t packed = (uint32_t)vis;
     const uint32_t slot = packed & ((1u << 24) - 1u), tri = packed >> 24;
-    const MeshletReference ref = f.views[0].refs[slot];
-    const Instance* inst = f.instances + ref.instance_index;
+    // the slot's draw record (written by the meshlet cull): the instance and
+    // the index / micro-index addresses already offset to the meshlet, so
+    // the vertex loads do not wait on the reference, MeshInfo and Meshlet
+    const RasterDraw rd = f.views[0].rdraws[slot];
+    const Instance* inst = f.instances + rd.instance;
     const MeshInfoResolve mi = load_mesh_info_resolve(mesh_info_of(inst));
-    const Meshlet* ml = reinterpret_cast<const Meshlet*>(mi.meshlets) + ref.meshlet_index;
-    const uint32_t tri_off = __ldg(&ml->triangle_offset), idx_off = __ldg(&ml->index_offset);
-    const uint8_t* micro = reinterpret_cast<const uint8_t*>(mi.micro_indices) + tri_off + tri * 3;
+    const uint8_t* micro = reinterpret_cast<const uint8_t*>(rd.micro) + tri * 3;
     const uint32_t flags = mi.flags;
     for (int k = 0; k < 3; k++) {
-        uint32_t vi = idx_off + __ldg(micro + k);
-        o.idx[k] = (flags & MESH_INFO_FLAGS_32_BIT_INDICES) ? __ldg(reinterpret_cast<const uint32_t*>(mi.indices) + vi)
-                                                            : __ldg(reinterpret_cast<const uint16_t*>(mi.indices) + vi);
+        const uint32_t vi = __ldg(micro + k);
+        o.idx[k] = (flags & MESH_INFO_FLAGS_32_BIT_INDICES) ? __ldg(reinterpret_cast<const uint32_t*>(rd.indices) + vi)
+                                                            : __ldg(reinterpret_cast<const uint16_t*>(rd.indices) + vi);
     }
     const lh_mat4& T = inst->transform;
     for (int k = 0; k < 3; k++) {
-        f3 w = world_pos(T, load_position(mi.positions, flags, o.idx[k]));
+        f3 w = world_pos(T, load_position(rd.positions, flags, o.idx[k]));
         p.W[k] = {w.x, w.y, w.z};
         f3 nr = load_normal_raw(mi.normals, flags, o.idx[k]);
         p.N[k] = {nr.x, nr.y, nr.z};
@@ -292,7 +293,7 @@ __device__ __forceinline__ void pixel_backward(const FrameDev& f, const float4* 
     o.packed = packed;
     o.inst = inst;
     o.rec = t.instance_grads ? reinterpret_cast<const lh_mesh_grads*>(
-                                   reinterpret_cast<const uint64_t*>(t.instance_grads)[ref.instance_index])
+                                   reinterpret_cast<const uint64_t*>(t.instance_grads)[rd.instance])
                              : nullptr;
 }
 
