@@ -42,10 +42,15 @@ def test_stress_parity(native, stress, schedule):
     assert st.candidate_meshlets[0] > 5_000_000
 
 
-def test_stress_reduced_parity(native, oracle):
+_REDUCED = {}
+
+
+@pytest.mark.parametrize("occlusion_px", [128, 16])
+def test_stress_reduced_parity(native, oracle, occlusion_px):
     """The stress scene's meshes at a quarter of its instances, 1920 x 1080
     + 4 cascades: bit exact against the oracle (a stress-shaped case small
-    enough for a full profiler capture)."""
+    enough for a full profiler capture), with few occluders and with many
+    (16 px: most tested meshlets are small and take the per-pixel test)."""
     lh = native
     scene = lh.Scene(5, n_instances=25000, width=1920, height=1080).upload(0)
     d = scene.desc
@@ -53,13 +58,17 @@ def test_stress_reduced_parity(native, oracle):
     r = lh.Renderer(lh.Config(width=d.width, height=d.height, shadow_size=d.shadow_size, max_instances=d.n_instances,
                               max_draws=md, max_big_triangles=1 << 21))
     r.set_scene(scene)
+    r.set_tuning(occlusion_px=occlusion_px)
     r.frame(scene.uniforms)
     st = r.status()
     assert st.flags == 0, hex(st.flags)
-    fr = oracle.run_scene(scene, shadow_size=d.shadow_size, max_instances=d.n_instances, max_draws=md)
-    errors, stats = compare_frame(r, fr, md, d.n_instances)
+    if "fr" not in _REDUCED:
+        _REDUCED["fr"] = oracle.run_scene(scene, shadow_size=d.shadow_size, max_instances=d.n_instances, max_draws=md)
+    errors, stats = compare_frame(r, _REDUCED["fr"], md, d.n_instances)
     assert not errors, "\n".join(errors) + " %s" % stats
     assert st.candidate_meshlets[0] > 1_000_000
+    if occlusion_px == 16:
+        assert st.occlusion[0] > 10_000 and st.occlusion[1] < st.visible_opaque[0] - st.occlusion[0]
 
 
 def _grad_targets(lh, scene, torch):
