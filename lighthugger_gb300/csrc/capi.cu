@@ -92,8 +92,11 @@ struct lh_ctx {
     // stage timing
     bool profiling = false;
     cudaEvent_t stage_ev[LH_N_STAGES + 1] = {};
-    // graph
+    // graph (plain frames keep the template graph and its frame-start node,
+    // whose kernel parameters carry each replay's uniforms)
     cudaGraphExec_t graph_exec = nullptr;
+    cudaGraph_t graph_template = nullptr;
+    cudaGraphNode_t graph_clear_node = nullptr;
     uint32_t graph_probes = 0;
     uint32_t graph_instances = 0;
     lh_tuning graph_tuning{};
@@ -161,11 +164,18 @@ cudaError_t dalloc(lh_ctx* c, T** out, size_t bytes) {
     return cudaSuccess;
 }
 
+void drop_graph(lh_ctx* c) {
+    if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+    c->graph_exec = nullptr;
+    if (c->graph_template) cudaGraphDestroy(c->graph_template);
+    c->graph_template = nullptr;
+    c->graph_clear_node = nullptr;
+}
+
 void free_all(lh_ctx* c) {
     for (auto& ev : c->stage_ev)
         if (ev) { cudaEventDestroy(ev); ev = nullptr; }
-    if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
-    c->graph_exec = nullptr;
+    drop_graph(c);
     if (c->capture_stream) cudaStreamDestroy(c->capture_stream);
     c->capture_stream = nullptr;
     for (auto& a : c->allocs) cudaFree(a.p);
@@ -317,6 +327,19 @@ void fill_frame_constants(const lh_ctx* c, const Uniforms* u, const Uniforms* pr
     // uniform-only terms, evaluated here in double and rounded to float.
     consts[0] = (float)std::pow(0.5, (double)u->cascade_split_pow);
     consts[1] = (float)std::pow(0.75, (double)u->cascade_split_pow);
+}
+
+// A plain frame's start parameters: the main view's uniforms and frame
+// constants, and the per-frame scratch the frame-start kernel zeroes.
+FrameStart make_frame_start(lh_ctx* c, const Uniforms* u) {
+    FrameStart start;
+    std::memset(&start, 0, sizeof(start));
+    fill_frame_constants(c, u, nullptr, 0, &start.u, start.consts);
+    start.d_uniforms = c->d_uniforms;
+    start.d_consts = c->d_consts;
+    start.reset = reinterpret_cast<uint4*>(c->d_reset);
+    start.reset_words = c->reset_bytes / sizeof(uint4);
+    return start;
 }
 
 lh_status upload_frame_constants(lh_ctx* c, const Uniforms* u, const Uniforms* probes, uint32_t n_probes,
@@ -564,10 +587,7 @@ lh_status lh_set_scene(lh_ctx* c, const Instance* d_instances, uint32_t n, const
         if (!textures[i].texels || !textures[i].width || !textures[i].height || (textures[i].texels & 3))
             return fail(c, LH_ERR_INVALID_ARGUMENT, "bad texture descriptor");
     cudaError_t e = cudaSuccess;
-    if (c->graph_exec) {
-        cudaGraphExecDestroy(c->graph_exec);
-        c->graph_exec = nullptr;
-    }
+    drop_graph(c);
     c->instances = d_instances;
     c->n_instances = n;
     // total candidate meshlets bounds the look-back scratch
@@ -704,13 +724,7 @@ static lh_status frame_impl(lh_ctx* c, const Uniforms* u, const Uniforms* probes
     uint32_t n_inst = std::min(u->num_instances, c->n_instances);
     if (n_probes == 0 && frame_schedule(c, false) != LH_SCHEDULE_PERSISTENT) {
         // one main view: its uniforms ride on the clear launch
-        FrameStart start;
-        std::memset(&start, 0, sizeof(start));
-        fill_frame_constants(c, u, nullptr, 0, &start.u, start.consts);
-        start.d_uniforms = c->d_uniforms;
-        start.d_consts = c->d_consts;
-        start.reset = reinterpret_cast<uint4*>(c->d_reset);
-        start.reset_words = c->reset_bytes / sizeof(uint4);
+        const FrameStart start = make_frame_start(c, u);
         if ((st = enqueue_frame(c, n_probes, n_inst, batched, s, &start)) != LH_OK) return st;
     } else {
         if ((st = upload_frame_constants(c, u, probes, n_probes, s)) != LH_OK) return st;
@@ -749,22 +763,19 @@ lh_status frame_graph_impl(lh_ctx* c, const Uniforms* u, const Uniforms* probes,
         e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return cuda_fail(c, e, "stream sync");
         if ((st = prepare_views(c, probes, n_probes)) != LH_OK) return st;
-        if (c->graph_exec) {
-            cudaGraphExecDestroy(c->graph_exec);
-            c->graph_exec = nullptr;
-        }
+        drop_graph(c);
     }
     const bool tuning_changed = std::memcmp(&c->graph_tuning, &c->tuning, sizeof(lh_tuning)) != 0;
     const GraphBackward none{};
     const GraphBackward& want = bw ? *bw : none;
     const bool backward_changed = std::memcmp(&c->graph_backward, &want, sizeof(GraphBackward)) != 0;
+    // one main view with a frame-start launch: its uniforms ride on that
+    // kernel node's parameters (no copy before the replay)
+    const bool plain = n_probes == 0 && frame_schedule(c, false) != LH_SCHEDULE_PERSISTENT;
     if (until_resolve && (n_probes || bw)) return fail(c, LH_ERR_INVALID_ARGUMENT, "readback graph of a plain frame only");
     if (!c->graph_exec || c->graph_probes != n_probes || c->graph_instances != n_inst || tuning_changed ||
         backward_changed || c->graph_until_resolve != until_resolve) {
-        if (c->graph_exec) {
-            cudaGraphExecDestroy(c->graph_exec);
-            c->graph_exec = nullptr;
-        }
+        drop_graph(c);
         if (!c->capture_stream) {
             e = cudaStreamCreateWithFlags(&c->capture_stream, cudaStreamNonBlocking);
             if (e != cudaSuccess) return cuda_fail(c, e, "capture stream");
@@ -772,7 +783,12 @@ lh_status frame_graph_impl(lh_ctx* c, const Uniforms* u, const Uniforms* probes,
         e = cudaStreamBeginCapture(c->capture_stream, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) return cuda_fail(c, e, "begin capture");
         c->capturing = true;
-        st = enqueue_frame(c, n_probes, n_inst, true, c->capture_stream, nullptr, !until_resolve);
+        if (plain) {
+            const FrameStart start = make_frame_start(c, u);
+            st = enqueue_frame(c, n_probes, n_inst, true, c->capture_stream, &start, !until_resolve);
+        } else {
+            st = enqueue_frame(c, n_probes, n_inst, true, c->capture_stream, nullptr, !until_resolve);
+        }
         if (st == LH_OK && bw) {
             const FrameDev f = frame_dev(c, 5 + n_probes, n_inst);
             cudaError_t eb = launch_resolve_backward(f, c->cfg.width, c->cfg.height,
@@ -789,15 +805,38 @@ lh_status frame_graph_impl(lh_ctx* c, const Uniforms* u, const Uniforms* probes,
         }
         if (e != cudaSuccess) return cuda_fail(c, e, "end capture");
         e = cudaGraphInstantiate(&c->graph_exec, g, 0);
-        cudaGraphDestroy(g);
-        if (e != cudaSuccess) return cuda_fail(c, e, "graph instantiate");
+        if (e == cudaSuccess && plain) {
+            // the frame-start kernel node, updated before every replay
+            size_t n = 0;
+            e = cudaGraphGetNodes(g, nullptr, &n);
+            std::vector<cudaGraphNode_t> nodes(n);
+            if (e == cudaSuccess && n) e = cudaGraphGetNodes(g, nodes.data(), &n);
+            for (size_t i = 0; e == cudaSuccess && i < n && !c->graph_clear_node; i++)
+                if (is_clear_targets_node(nodes[i])) c->graph_clear_node = nodes[i];
+            if (e == cudaSuccess && !c->graph_clear_node) e = cudaErrorInvalidValue;
+        }
+        if (e == cudaSuccess && plain) {
+            c->graph_template = g;
+        } else {
+            cudaGraphDestroy(g);
+        }
+        if (e != cudaSuccess) {
+            drop_graph(c);
+            return cuda_fail(c, e, "graph instantiate");
+        }
         c->graph_probes = n_probes;
         c->graph_instances = n_inst;
         c->graph_tuning = c->tuning;
         c->graph_backward = want;
         c->graph_until_resolve = until_resolve;
     }
-    if ((st = upload_frame_constants(c, u, probes, n_probes, s)) != LH_OK) return st;
+    if (plain) {
+        e = set_clear_targets_node(c->graph_exec, c->graph_clear_node, frame_dev(c, 5, n_inst), c->sms,
+                                   make_frame_start(c, u));
+        if (e != cudaSuccess) return cuda_fail(c, e, "graph frame start");
+    } else if ((st = upload_frame_constants(c, u, probes, n_probes, s)) != LH_OK) {
+        return st;
+    }
     if (until_resolve) {
         e = cudaGraphLaunch(c->graph_exec, s);
         if (e == cudaSuccess) e = wait_readback(c, s);

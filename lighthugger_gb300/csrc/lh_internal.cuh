@@ -196,6 +196,9 @@ cudaError_t launch_linearize_texture(const uchar4* src, float4* dst, size_t n, u
 // launches clear the targets, each with `clear_blocks` blocks per view).
 cudaError_t launch_clear_targets(const FrameDev& f, cudaStream_t s, int sms, const FrameStart* start = nullptr,
                                  bool targets = true);
+bool is_clear_targets_node(cudaGraphNode_t node);
+cudaError_t set_clear_targets_node(cudaGraphExec_t exec, cudaGraphNode_t node, const FrameDev& f, int sms,
+                                   const FrameStart& start);
 cudaError_t launch_cull_instances(const FrameDev& f, uint32_t view_begin, uint32_t n_views, cudaStream_t s,
                                   uint32_t clear_blocks = 0);
 cudaError_t launch_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint32_t n_views, uint32_t blocks,

@@ -659,6 +659,32 @@ cudaError_t launch_clear_targets(const FrameDev& f, cudaStream_t s, int sms, con
     return launch_pdl(k_clear_targets, grid, dim3(256), s, f, none, 0u, targets ? 1u : 0u);
 }
 
+// The frame-start kernel node of a captured graph, and its parameters set
+// for the next replay: the uniforms, constants and scratch reset ride on the
+// replay's kernel parameters instead of a host-to-device copy before it.
+bool is_clear_targets_node(cudaGraphNode_t node) {
+    cudaGraphNodeType type;
+    if (cudaGraphNodeGetType(node, &type) != cudaSuccess || type != cudaGraphNodeTypeKernel) return false;
+    cudaKernelNodeParams p = {};
+    if (cudaGraphKernelNodeGetParams(node, &p) != cudaSuccess) return false;
+    return p.func == reinterpret_cast<void*>(k_clear_targets);
+}
+cudaError_t set_clear_targets_node(cudaGraphExec_t exec, cudaGraphNode_t node, const FrameDev& f, int sms,
+                                   const FrameStart& start) {
+    FrameDev fa = f;
+    FrameStart sa = start;
+    uint32_t has_start = 1u, targets = 0u;
+    void* args[4] = {&fa, &sa, &has_start, &targets};
+    cudaKernelNodeParams p = {};
+    p.func = reinterpret_cast<void*>(k_clear_targets);
+    p.gridDim = dim3((unsigned)sms, 1u);
+    p.blockDim = dim3(256);
+    p.sharedMemBytes = 0;
+    p.kernelParams = args;
+    p.extra = nullptr;
+    return cudaGraphExecKernelNodeSetParams(exec, node, &p);
+}
+
 cudaError_t launch_depth_reduce_fit(const FrameDev& f, cudaStream_t s, int sms) {
     return launch_pdl(k_depth_reduce_fit, dim3((unsigned)sms * 2), dim3(256), s, f);
 }
