@@ -330,8 +330,9 @@ def run_gpu(args):
     ms = reduce_max_over_ranks(ms, device="cuda")
 
     # e2e through the C ABI with host buffers.  Pipelined (lh_frame_readback):
-    # every frame uploads its uniforms from pinned memory and its HDR image is
-    # copied to one of two pinned host buffers while the next frame culls and
+    # every frame sends its uniforms (560 bytes) and frame constants (8) to
+    # the device as the replayed graph's frame-start kernel parameters, and
+    # its HDR image is copied to one of two pinned host buffers while the next frame culls and
     # rasterises; wall clock over the steps, from an idle GPU to the last
     # image on the host.  Serial (lh_frame + lh_download, one frame at a
     # time) is reported beside it.
