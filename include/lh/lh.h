@@ -143,7 +143,10 @@ lh_status lh_create(const lh_config* config, lh_ctx** out_ctx);
  * Texels are read here, once, into a linear float copy owned by the context
  * (16 bytes per texel; sRGB decoded), as the reference uploads its images
  * once: call lh_set_scene again after changing texel data.  Instance,
- * MeshInfo and vertex data are read by every frame. */
+ * MeshInfo and vertex data are read by every frame; whether any mesh is
+ * alpha clip (MESH_INFO_FLAGS_ALPHA_CLIP) is recorded here, so call
+ * lh_set_scene again after setting that flag on a mesh of a scene that had
+ * none. */
 lh_status lh_set_scene(lh_ctx* ctx, const Instance* d_instances, uint32_t n,
                        const lh_texture* textures, uint32_t n_textures);
 

@@ -96,6 +96,7 @@ struct lh_ctx {
     // whose kernel parameters carry each replay's uniforms)
     cudaGraphExec_t graph_exec = nullptr;
     cudaGraph_t graph_template = nullptr;
+    bool scene_alpha = true;  // some mesh is alpha clip (lh_set_scene)
     cudaGraphNode_t graph_clear_node = nullptr;
     uint32_t graph_probes = 0;
     uint32_t graph_instances = 0;
@@ -292,6 +293,7 @@ FrameDev frame_dev(const lh_ctx* c, uint32_t n_views, uint32_t n_instances) {
     f.frame_consts = c->d_consts;
     f.srgb_lut = c->d_srgb;
     f.occlusion_px = c->tuning.occlusion_px;
+    f.scene_alpha = c->scene_alpha ? 1u : 0u;
     for (int k = 0; k < 2; k++) {
         f.chunk_shift[k][0] = (uint32_t)__builtin_ctz(c->tuning.chunk_rows[k]);
         f.chunk_shift[k][1] = (uint32_t)__builtin_ctz(c->tuning.chunk_cols[k]);
@@ -591,14 +593,16 @@ lh_status lh_set_scene(lh_ctx* c, const Instance* d_instances, uint32_t n, const
     c->instances = d_instances;
     c->n_instances = n;
     // total candidate meshlets bounds the look-back scratch
+    // and whether any mesh is alpha clip (else the alpha-class launches are skipped)
     unsigned long long* d_sum = nullptr;
-    e = cudaMalloc(&d_sum, sizeof(unsigned long long));
+    e = cudaMalloc(&d_sum, 2 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = launch_sum_meshlets(d_instances, n, d_sum, 0);
-    unsigned long long total = 0;
-    if (e == cudaSuccess) e = cudaMemcpy(&total, d_sum, sizeof(total), cudaMemcpyDeviceToHost);
+    unsigned long long sums[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpy(sums, d_sum, sizeof(sums), cudaMemcpyDeviceToHost);
     if (d_sum) cudaFree(d_sum);
     if (e != cudaSuccess) return cuda_fail(c, e, "scene meshlet count");
-    c->scene_meshlets = total;
+    c->scene_meshlets = sums[0];
+    c->scene_alpha = (sums[1] & MESH_INFO_FLAGS_ALPHA_CLIP) != 0;
     // textures
     if (c->d_textures) {
         for (auto it = c->allocs.begin(); it != c->allocs.end(); ++it)

@@ -37,12 +37,21 @@ __global__ void __launch_bounds__(kMlThreads) k_cull_meshlets(FrameDev f, uint32
     phase_cull_meshlets(f, view_begin, n_views, &f.status[kStMlClaim]);
 }
 
+// out[0]: the scene's meshlets; out[1] (low word): the OR of its meshes' flags.
 __global__ void k_sum_meshlets(const Instance* inst, uint32_t n, unsigned long long* out) {
     unsigned long long acc = 0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        acc += load_mesh_info(mesh_info_of(inst + i)).num_meshlets;
+    uint32_t flags = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const MeshInfoCull mi = load_mesh_info(mesh_info_of(inst + i));
+        acc += mi.num_meshlets;
+        flags |= mi.flags;
+    }
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xFFFFFFFFu, acc, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(out, acc);
+    flags = __reduce_or_sync(0xFFFFFFFFu, flags);
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(out, acc);
+        atomicOr(reinterpret_cast<unsigned int*>(out + 1), flags);
+    }
 }
 
 }  // namespace
@@ -64,7 +73,7 @@ cudaError_t launch_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint32_
 }
 
 cudaError_t launch_sum_meshlets(const Instance* instances, uint32_t n, unsigned long long* out, cudaStream_t s) {
-    cudaError_t e = cudaMemsetAsync(out, 0, sizeof(unsigned long long), s);
+    cudaError_t e = cudaMemsetAsync(out, 0, 2 * sizeof(unsigned long long), s);
     if (e != cudaSuccess || n == 0) return e;
     k_sum_meshlets<<<(n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024, 256, 0, s>>>(instances, n, out);
     return cudaGetLastError();

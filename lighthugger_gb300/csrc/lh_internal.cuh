@@ -150,6 +150,7 @@ struct FrameDev {
     uint32_t occlusion_px;      // occluder threshold (projected sphere radius, pixels); 0: no occlusion culling
     uint32_t chunk_shift[2][2]; // [pass: visibility, shadow][log2 rows, log2 columns] of a big-triangle chunk
     uint32_t backward_rows;     // pixel rows of a resolve-adjoint tile: 4, 8 or 16
+    uint32_t scene_alpha;       // some mesh of the scene is alpha clip (else no alpha-class launch)
 };
 
 // Launch `kernel` with programmatic stream serialisation: its blocks may

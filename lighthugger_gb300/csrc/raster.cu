@@ -86,12 +86,12 @@ cudaError_t launch_raster_kind(const FrameDev& f, uint32_t view_begin, uint32_t 
             if (e == cudaSuccess)
                 e = launch_pdl(k_occlusion_filter, dim3(sms * 8), dim3(256), s, f, view_begin, n_views);
             if (e == cudaSuccess) e = opaque(kListSurvivors);
-            if (e == cudaSuccess)
+            if (e == cudaSuccess && f.scene_alpha)
                 e = launch_pdl(k_raster_alpha<0>, dim3(sms * 3), rb, s, f, view_begin, n_views, tune,
                                (uint32_t)kListSurvivors);
         } else {
             e = opaque(kListAll);
-            if (e == cudaSuccess)
+            if (e == cudaSuccess && f.scene_alpha)
                 e = launch_pdl(k_raster_alpha<0>, dim3(sms * 3), rb, s, f, view_begin, n_views, tune,
                                (uint32_t)kListAll);
         }
@@ -99,7 +99,7 @@ cudaError_t launch_raster_kind(const FrameDev& f, uint32_t view_begin, uint32_t 
     } else {
         e = launch_pdl(k_raster<1, LH_RASTER_MIN_BLOCKS>, dim3(sms * LH_RASTER_MIN_BLOCKS), rb, s, f, view_begin, n_views,
                        tune, (uint32_t)kListAll);
-        if (e == cudaSuccess)
+        if (e == cudaSuccess && f.scene_alpha)
             e = launch_pdl(k_raster_alpha<1>, dim3(sms * 3), rb, s, f, view_begin, n_views, tune, (uint32_t)kListAll);
         if (e == cudaSuccess) e = launch_pdl(k_raster_big<1>, dim3(sms * LH_RASTER_BIG_MIN_BLOCKS), dim3(256), s, f);
     }
