@@ -197,11 +197,19 @@ struct Bary { f3 lambda, ddx, ddy; };
 
 // vbuffer.glsl:11-63.  kDeriv: also the screen derivatives of lambda, which
 // only the normal-map path reads (computed there, not for every pixel).
+// A clip-space vertex as the barycentrics read it: 1 / w and the projected
+// x, y (a vertex's own terms, so the resolve's vertex stage computes them
+// once per vertex for every pixel of the triangle).
+struct ProjVertex { float inv_w; f2 n; };
+__device__ __forceinline__ ProjVertex project_vertex(f4 p) {
+    const float iw = 1.0f / p.w;
+    return {iw, f2{p.x * iw, p.y * iw}};
+}
 template <bool kDeriv>
-__device__ Bary calc_full_bary(f4 p0, f4 p1, f4 p2, f2 ndc, f2 win) {
+__device__ Bary calc_full_bary(ProjVertex v0, ProjVertex v1, ProjVertex v2, f2 ndc, f2 win) {
     Bary r;
-    f3 invW{1.0f / p0.w, 1.0f / p1.w, 1.0f / p2.w};
-    f2 n0{p0.x * invW.x, p0.y * invW.x}, n1{p1.x * invW.y, p1.y * invW.y}, n2{p2.x * invW.z, p2.y * invW.z};
+    f3 invW{v0.inv_w, v1.inv_w, v2.inv_w};
+    const f2 n0 = v0.n, n1 = v1.n, n2 = v2.n;
     f2 ca{n2.x - n1.x, n2.y - n1.y}, cb{n0.x - n1.x, n0.y - n1.y};
     float invDet = 1.0f / (ca.x * cb.y - cb.x * ca.y);
     r.ddx = f3{n1.y - n2.y, n2.y - n0.y, n0.y - n1.y} * invDet * invW;
@@ -294,8 +302,9 @@ __device__ __noinline__ f3 apply_normal_map(const FrameDev& f, uint32_t tex, f2 
           nt.b * 255.0f / 127.0f - 128.0f / 127.0f};
     // screen derivatives of the world position and uv (the same barycentrics
     // again, with their derivatives)
-    const Bary bd = calc_full_bary<true>(mul(PV, f4{pa.x, pa.y, pa.z, 1.0f}), mul(PV, f4{pb.x, pb.y, pb.z, 1.0f}),
-                                         mul(PV, f4{pc.x, pc.y, pc.z, 1.0f}), ndc, win);
+    const Bary bd = calc_full_bary<true>(project_vertex(mul(PV, f4{pa.x, pa.y, pa.z, 1.0f})),
+                                         project_vertex(mul(PV, f4{pb.x, pb.y, pb.z, 1.0f})),
+                                         project_vertex(mul(PV, f4{pc.x, pc.y, pc.z, 1.0f})), ndc, win);
     const f3 wx = interp_deriv(bd, pa.x, pb.x, pc.x), wy = interp_deriv(bd, pa.y, pb.y, pc.y),
              wz = interp_deriv(bd, pa.z, pb.z, pc.z);
     const f3 wdx{wx.y, wy.y, wz.y}, wdy{wx.z, wy.z, wz.z};
@@ -311,11 +320,11 @@ __device__ __noinline__ f3 apply_normal_map(const FrameDev& f, uint32_t tex, f2 
 }
 
 // Vertex k of triangle `packed` (tri << 24 | draw slot) of the main view as
-// the lighting reads it -- world position, clip position (PV times it),
-// normalised raw normal, uv times the texture scale -- in the arithmetic
-// and order the lighting has always used.
-__device__ __forceinline__ void load_vertex(const FrameDev& f, uint32_t packed, uint32_t k, f3& p, f4& c, f3& n,
-                                            float& us, float& vs) {
+// the lighting reads it -- world position, clip position (PV times it)
+// projected, normalised raw normal, uv times the texture scale -- in the
+// arithmetic and order the lighting has always used.
+__device__ __forceinline__ void load_vertex(const FrameDev& f, uint32_t packed, uint32_t k, f3& p, ProjVertex& c,
+                                            f3& n, float& us, float& vs) {
     const uint32_t slot = packed & ((1u << 24) - 1u), tri = packed >> 24;
     const RasterDraw rd = f.views[0].rdraws[slot];
     const Instance* inst = f.instances + rd.instance;
@@ -326,7 +335,7 @@ __device__ __forceinline__ void load_vertex(const FrameDev& f, uint32_t packed, 
                              ? __ldg(reinterpret_cast<const uint32_t*>(rd.indices) + vi)
                              : __ldg(reinterpret_cast<const uint16_t*>(rd.indices) + vi);
     p = world_pos(inst->transform, load_position(rd.positions, flags, idx));
-    c = mul(f.uniforms->combined_perspective_view, f4{p.x, p.y, p.z, 1.0f});
+    c = project_vertex(mul(f.uniforms->combined_perspective_view, f4{p.x, p.y, p.z, 1.0f}));
     n = fast_normalize(load_normal_raw(__ldg(&mip->normals), flags, idx));
     const f2 uv = load_uv_raw(__ldg(&mip->uvs), flags, idx);
     us = uv.x * __ldg(&mip->texture_scale.x);
@@ -340,7 +349,7 @@ constexpr uint32_t kShareTris = 10;  // distinct triangles a warp row shares ver
 // on average in the large workload), so the distinct triangles' vertices are
 // computed once, one vertex per lane -- lanes 3k, 3k + 1, 3k + 2 for the
 // k-th distinct triangle -- into the warp's shared-memory slots (3 float4 a
-// vertex: p.xyz n.x | c.xyzw | n.yz us vs), at a third of the vertex work of
+// vertex: p.xyz n.x | 1/w, projected x y | n.yz us vs), at a third of the vertex work of
 // every pixel computing its own three.  Returns the pixel's first slot, or
 // -1 when the row holds more than kShareTris distinct triangles (each pixel
 // then computes its own at use).
@@ -358,11 +367,11 @@ __device__ __forceinline__ int32_t share_vertices(const FrameDev& f, bool covere
     __syncwarp();
     if (lane < 3 * n) {
         f3 p, nv;
-        f4 c;
+        ProjVertex c;
         float us, vs;
         load_vertex(f, s_keys[lane / 3], lane % 3, p, c, nv, us, vs);
         s_vert[3 * lane] = make_float4(p.x, p.y, p.z, nv.x);
-        s_vert[3 * lane + 1] = make_float4(c.x, c.y, c.z, c.w);
+        s_vert[3 * lane + 1] = make_float4(c.inv_w, c.n.x, c.n.y, 0.0f);
         s_vert[3 * lane + 2] = make_float4(nv.y, nv.z, us, vs);
     }
     __syncwarp();
@@ -371,14 +380,14 @@ __device__ __forceinline__ int32_t share_vertices(const FrameDev& f, bool covere
 
 // Vertex k of the pixel's triangle: from the warp's slots, or computed.
 __device__ __forceinline__ void pixel_vertex(const FrameDev& f, const float4* s_vert, int32_t base, uint32_t packed,
-                                             uint32_t k, f3& p, f4& c, f3& n, float& us, float& vs) {
+                                             uint32_t k, f3& p, ProjVertex& c, f3& n, float& us, float& vs) {
     if (base < 0) {
         load_vertex(f, packed, k, p, c, n, us, vs);
         return;
     }
     const float4 a = s_vert[3 * (base + k)], b = s_vert[3 * (base + k) + 1], d = s_vert[3 * (base + k) + 2];
     p = f3{a.x, a.y, a.z};
-    c = f4{b.x, b.y, b.z, b.w};
+    c = ProjVertex{b.x, f2{b.y, b.z}};
     n = f3{a.w, d.x, d.y};
     us = d.z;
     vs = d.w;
@@ -416,7 +425,7 @@ __device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uin
     const MeshInfoResolve mi = load_mesh_info_resolve(mesh_info_of(inst));
     const uint32_t flags = rd.bits >> 16;
     f3 pa, pb, pc, na, nb, nc;
-    f4 ca, cb, cc;
+    ProjVertex ca, cb, cc;
     f3 us, vs;
     pixel_vertex(f, s_vert, vbase, packed, 0, pa, ca, na, us.x, vs.x);
     pixel_vertex(f, s_vert, vbase, packed, 1, pb, cb, nb, us.y, vs.y);
