@@ -53,6 +53,7 @@ FRAGMENT_BYTES = 8           # one 64-bit depth-test reduction per fragment
 # summary (profiles/dram_bytes_c2_frame.txt: command, commit, one line per
 # kernel); `traffic` in the roofline is read from there, never measured here.
 TRAFFIC_FILE = os.path.join(ROOT, "profiles", "dram_bytes_c2_frame.txt")
+# (k_raster_alpha<K> launches only for scenes with alpha-clip meshes)
 STAGE_KERNELS = {
     "raster": ("k_raster<0, 3>", "k_raster_alpha<0>", "k_raster_big<0>", "k_hiz", "k_occlusion_filter"),
     "shadow_raster": ("k_raster<1, 3>", "k_raster_alpha<1>", "k_raster_big<1>"),
@@ -115,9 +116,10 @@ def _measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def committed_traffic(stage):
+def committed_traffic(stage, alpha_scene=False):
     """DRAM bytes per frame of a stage's kernels from the committed capture
-    summary, with the summary's provenance line; (None, None) if absent."""
+    summary, with the summary's provenance line; (None, None) if absent.
+    The alpha-clip kernels count only for a scene with alpha-clip meshes."""
     try:
         with open(TRAFFIC_FILE) as f:
             lines = f.read().splitlines()
@@ -130,7 +132,7 @@ def committed_traffic(stage):
             continue
         name, rd, wr = l.rsplit(None, 2)
         per[name.strip()] = per.get(name.strip(), 0.0) + float(rd) + float(wr)  # kernels run twice add up
-    names = [n for n in STAGE_KERNELS.get(stage, ()) if n in per]
+    names = [n for n in STAGE_KERNELS.get(stage, ()) if n in per and ("alpha" not in n or alpha_scene)]
     if not names:
         return None, None
     return sum(per[n] for n in names), "profiles/dram_bytes_c2_frame.txt: " + source
@@ -396,7 +398,8 @@ def run_gpu(args):
                             "frac": round(gbs / peak, 4)}
     dom = max(algo, key=lambda k: stage_ms.get(k, 0.0))  # the dominant stage
     achieved = algo[dom] / (stage_ms[dom] * 1e-3) / 1e9
-    traffic, traffic_src = committed_traffic(dom) if args.config == 2 else (None, None)
+    traffic, traffic_src = (committed_traffic(dom, bool(scene.params.get("alpha_clip_materials")))
+                            if args.config == 2 else (None, None))
     atom = atomic_peak(lh, torch, stream)
     red_rate = frag_main / (stage_ms["raster"] * 1e-3)
     tri_total = d.total_triangles
@@ -429,13 +432,17 @@ def run_gpu(args):
         # per frame: clear; 2 x (cull instances, cull meshlets, raster opaque,
         # raster alpha clip, chunks); depth + fit; resolve; with the occlusion
         # raster the visibility view adds the occluder pass, its chunks, the
-        # hierarchical depth and the depth test of the other meshlets
-        "gpu_launches": (13 + (4 if tune.occlusion_px else 0)) * args.steps,
+        # hierarchical depth and the depth test of the other meshlets; the two
+        # alpha-clip launches only when a mesh of the scene is alpha clip
+        "gpu_launches": (13 + (4 if tune.occlusion_px else 0)
+                         - (0 if scene.params.get("alpha_clip_materials") else 2)) * args.steps,
         "tuning": dict(tune.as_dict(), autotuned=tune_results),
         "occlusion": {"occluder_px": int(tune.occlusion_px), "occluders": int(st.occlusion[0]),
                       "survivors_opaque": int(st.occlusion[1]), "survivors_alpha": int(st.occlusion[2]),
                       "visible_opaque": int(st.visible_opaque[0])},
-        "roofline": {"bound": "hbm", "kernel": dom + " stage (" + ", ".join(STAGE_KERNELS.get(dom, (dom,))) + ")",
+        "roofline": {"bound": "hbm", "kernel": dom + " stage (" + ", ".join(
+                         k for k in STAGE_KERNELS.get(dom, (dom,))
+                         if "alpha" not in k or scene.params.get("alpha_clip_materials")) + ")",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": (peak_kind + " (MEASURED_PEAKS.json hbm_gbs)") if peak_kind == "measured"
                      else peak_kind,

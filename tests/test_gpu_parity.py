@@ -87,6 +87,30 @@ def test_config2_alpha_clip_parity(native, oracle):
     assert st.visible_alpha_clip[0] > 0 and stats["covered"] > 10000
 
 
+def test_alpha_clip_scene_after_opaque_scene(native, oracle):
+    """The alpha-class raster launches are left out for a scene without
+    alpha-clip meshes; the same renderer given a scene with them (a second
+    lh_set_scene) rasterises them again, through the per-stage launches and
+    the replayed graph."""
+    lh = native
+    opaque = lh.Scene(1).upload(0)
+    alpha = lh.Scene(1, alpha_clip_materials=1).upload(0)
+    d = alpha.desc
+    cfg = lh.Config(width=d.width, height=d.height, shadow_size=d.shadow_size, max_instances=1024,
+                    max_draws=200000, device=0)
+    r = lh.Renderer(cfg)
+    r.set_scene(opaque)
+    r.frame_graph(opaque.uniforms)
+    assert r.status().visible_alpha_clip[0] == 0
+    r.set_scene(alpha)
+    fr = oracle.run_scene(alpha, shadow_size=d.shadow_size, max_instances=1024, max_draws=200000)
+    for run in (lambda: r.frame(alpha.uniforms), lambda: r.frame_graph(alpha.uniforms)):
+        run()
+        st = r.status()
+        assert st.visible_alpha_clip[0] > 0
+        _assert_parity(r, fr, 200000, 1024, st, fr.flags)
+
+
 def test_config2_full_parity(native, oracle):
     """Config 2 at full size: 4,096 instances, ~50M triangles, 1920x1080."""
     scene, r, fr, st, cap = _run(native, oracle, 2)
