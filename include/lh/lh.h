@@ -260,7 +260,8 @@ typedef struct lh_tuning {
 } lh_tuning;
 /* lh_create's tuning: lane bin 32 pixels and no warp bin (medium_px 32),
  * occluders above 128 px, chunks of 16 x 128 (visibility) and 32 x 64
- * (shadow) pixels, adjoint tiles of 8 rows. */
+ * (shadow) pixels, adjoint tiles of 8 rows, 3 meshlet-cull blocks per SM
+ * (as many as are resident at once). */
 
 lh_status lh_set_tuning(lh_ctx* ctx, const lh_tuning* tuning);
 lh_status lh_get_tuning(lh_ctx* ctx, lh_tuning* tuning);

@@ -517,7 +517,7 @@ lh_status lh_create(const lh_config* config, lh_ctx** out) {
     if (!c) return LH_ERR_OUT_OF_MEMORY;
     c->cfg = cfg;
     c->device = cfg.device;
-    c->tuning = lh_tuning{32u, 32u, 2.0f, LH_SCHEDULE_DEFAULT, 0u, 128u, {16u, 32u}, {128u, 64u}, 8u};
+    c->tuning = lh_tuning{32u, 32u, 3.0f, LH_SCHEDULE_DEFAULT, 0u, 128u, {16u, 32u}, {128u, 64u}, 8u};
     cudaError_t e = cudaSetDevice(c->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device);
     c->max_views = 5 + cfg.max_probes;

@@ -28,7 +28,14 @@ __global__ void __launch_bounds__(kInstTile) k_cull_instances(FrameDev f, uint32
 // Also zeroes the raster words of the raster launches that follow (clip
 // count, claims, reduce counter, big-triangle counter; nothing here reads
 // them).
-__global__ void __launch_bounds__(kMlThreads) k_cull_meshlets(FrameDev f, uint32_t view_begin, uint32_t n_views) {
+// Registers bounded for LH_ML_MIN_BLOCKS resident blocks per SM (build knob):
+// the launch's blocks (lh_tuning.cull_blocks_per_sm per SM, 3 by default)
+// then all run at once, one 512-candidate tile after another.
+#ifndef LH_ML_MIN_BLOCKS
+#define LH_ML_MIN_BLOCKS 3
+#endif
+__global__ void __launch_bounds__(kMlThreads, LH_ML_MIN_BLOCKS)
+    k_cull_meshlets(FrameDev f, uint32_t view_begin, uint32_t n_views) {
     pdl_enter();
     if (blockIdx.x == 0 && threadIdx.x < kStWords) {
         const uint32_t w = threadIdx.x;

@@ -396,9 +396,9 @@ __device__ void phase_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint
 
         uint32_t cls_bits = 0;  // 2 bits per item: 1 opaque, 2 alpha clip
         MeshletReference refs[kMlItems];
-        uint32_t tris[kMlItems / 4];  // triangle count per item, 8 bits each
+        uint32_t tris[(kMlItems + 3) / 4];  // triangle count per item, 8 bits each
 #pragma unroll
-        for (uint32_t k = 0; k < kMlItems / 4; k++) tris[k] = 0;
+        for (uint32_t k = 0; k < (kMlItems + 3) / 4; k++) tris[k] = 0;
 #pragma unroll
         for (uint32_t k = 0; k < kMlItems; k++) {
             const uint32_t c = t0 + k * kMlThreads + threadIdx.x;
@@ -447,16 +447,18 @@ __device__ void phase_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint
         }
         __syncthreads();
         if (warp == 0) {
-            // exclusive scan of N counts per class: PER consecutive ones per lane
+            // exclusive scan of N counts per class: PER consecutive ones on
+            // each of the first LANES lanes
             constexpr uint32_t N = kMlItems * (kMlThreads / 32);
-            constexpr uint32_t PER = N / 32;
-            static_assert(N % 32 == 0 && PER >= 1 && PER <= 4, "scan layout");
+            constexpr uint32_t PER = N >= 32 ? N / 32 : 1;
+            constexpr uint32_t LANES = N / PER;
+            static_assert(N % PER == 0 && LANES <= 32 && PER <= 4, "scan layout");
 #pragma unroll
             for (int cl = 0; cl < 2; cl++) {
                 uint32_t c[PER], s = 0;
 #pragma unroll
                 for (uint32_t i = 0; i < PER; i++) {
-                    c[i] = s_cnt[cl][PER * lane + i];
+                    c[i] = lane < LANES ? s_cnt[cl][PER * lane + i] : 0u;
                     s += c[i];
                 }
                 uint32_t incl = s;
@@ -468,7 +470,7 @@ __device__ void phase_cull_meshlets(const FrameDev& f, uint32_t view_begin, uint
                 uint32_t ex = incl - s;
 #pragma unroll
                 for (uint32_t i = 0; i < PER; i++) {
-                    s_cnt[cl][PER * lane + i] = ex;
+                    if (lane < LANES) s_cnt[cl][PER * lane + i] = ex;
                     ex += c[i];
                 }
                 if (lane == 31) s_tot[cl] = incl;

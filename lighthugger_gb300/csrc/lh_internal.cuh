@@ -14,9 +14,9 @@ constexpr uint32_t kMaxViews = 40;           // main + 4 cascades + up to 35 pro
 constexpr uint32_t kInstTile = 256;          // instances per instance-cull tile
 constexpr uint32_t kMlThreads = 256;         // threads per meshlet-cull block
 #ifndef LH_ML_ITEMS
-#define LH_ML_ITEMS 4
+#define LH_ML_ITEMS 2
 #endif
-constexpr uint32_t kMlItems = LH_ML_ITEMS;   // candidates per thread (striped; 4 or 8)
+constexpr uint32_t kMlItems = LH_ML_ITEMS;   // candidates per thread (striped; 1, 2, 4 or 8)
 constexpr uint32_t kMlTile = kMlThreads * kMlItems;
 constexpr uint32_t kSpinLimit = 1u << 22;    // bounded waits (with __nanosleep back-off)
 
