@@ -103,25 +103,21 @@ __device__ float pcf9(const FrameDev& f, float sx, float sy, float layer_f, floa
         layer = min(max(layer, 0), 3);
         const float* map = f.shadow_maps + (size_t)layer * S * S;
         auto cl = [&](int32_t i) { return i < 0 ? 0 : (i > (int32_t)S - 1 ? (int32_t)S - 1 : i); };
-        uint32_t bits = 0;  // bit 4 * row + column of the window at (ix[0], iy[0])
-#pragma unroll
-        for (int r = 0; r < 4; r++) {
-            const float* row = map + (size_t)cl(iy[0] + r) * S;
-#pragma unroll
-            for (int c = 0; c < 4; c++) bits |= (ref < __ldg(row + cl(ix[0] + c)) ? 1u : 0u) << (4 * r + c);
-        }
-        // no texel passes: every tap is 0 * (finite, non-negative weights)
-        // summed, exactly +0
-        if (bits == 0u) return 0.0f;
         const float cx[4] = {1.0f - ax[0], ax[0] + (1.0f - ax[1]), ax[1] + (1.0f - ax[2]), ax[2]};
         const float cy[4] = {1.0f - ay[0], ay[0] + (1.0f - ay[1]), ay[1] + (1.0f - ay[2]), ay[2]};
+        int32_t col[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) col[c] = cl(ix[0] + c);
+        // each row's passing texels weighted by their column weights as they
+        // are compared (a texel that fails adds +0: with no texel passing the
+        // sum is exactly +0)
         float sum = 0.0f;
 #pragma unroll
         for (int r = 0; r < 4; r++) {
-            const uint32_t q = bits >> (4 * r);
-            const float row = (((q & 1u) ? cx[0] : 0.0f) + ((q & 2u) ? cx[1] : 0.0f)) +
-                              (((q & 4u) ? cx[2] : 0.0f) + ((q & 8u) ? cx[3] : 0.0f));
-            sum = __fmaf_rn(row, cy[r], sum);
+            const float* row = map + (size_t)cl(iy[0] + r) * S;
+            const float w0 = ref < __ldg(row + col[0]) ? cx[0] : 0.0f, w1 = ref < __ldg(row + col[1]) ? cx[1] : 0.0f;
+            const float w2 = ref < __ldg(row + col[2]) ? cx[2] : 0.0f, w3 = ref < __ldg(row + col[3]) ? cx[3] : 0.0f;
+            sum = __fmaf_rn((w0 + w1) + (w2 + w3), cy[r], sum);
         }
         return sum;
     }
