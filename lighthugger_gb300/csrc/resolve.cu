@@ -36,13 +36,16 @@ __device__ Tex4 sample_repeat(const FrameDev& f, uint32_t index, f2 uv) {
     float a = u - fu, b = v - fv;
     const int32_t i0 = (int32_t)fu, j0 = (int32_t)fv;
     const int32_t W = (int32_t)t.width, H = (int32_t)t.height;
-    const int32_t ia = wrap_texel(i0, W), ib = wrap_texel(i0 + 1, W);
-    const int32_t ja = wrap_texel(j0, H), jb = wrap_texel(j0 + 1, H);
-    auto texel = [&](int32_t i, int32_t j) {
-        const float4 p = __ldg(tex + ((size_t)j * W + i));
+    // i0 + 1 wraps to the texel after i0's (or 0 past the last)
+    const int32_t ia = wrap_texel(i0, W), ib = ia + 1 == W ? 0 : ia + 1;
+    const int32_t ja = wrap_texel(j0, H), jb = ja + 1 == H ? 0 : ja + 1;
+    const float4* row_a = tex + (size_t)ja * W;
+    const float4* row_b = tex + (size_t)jb * W;
+    auto texel = [&](const float4* row, int32_t i) {
+        const float4 p = __ldg(row + i);
         return Tex4{p.x, p.y, p.z, p.w};
     };
-    Tex4 t00 = texel(ia, ja), t10 = texel(ib, ja), t01 = texel(ia, jb), t11 = texel(ib, jb);
+    Tex4 t00 = texel(row_a, ia), t10 = texel(row_a, ib), t01 = texel(row_b, ia), t11 = texel(row_b, ib);
     float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
     Tex4 r;
     r.r = ((t00.r * w00 + t10.r * w10) + t01.r * w01) + t11.r * w11;
@@ -105,13 +108,24 @@ __device__ float pcf9(const FrameDev& f, float sx, float sy, float layer_f, floa
         auto cl = [&](int32_t i) { return i < 0 ? 0 : (i > (int32_t)S - 1 ? (int32_t)S - 1 : i); };
         const float cx[4] = {1.0f - ax[0], ax[0] + (1.0f - ax[1]), ax[1] + (1.0f - ax[2]), ax[2]};
         const float cy[4] = {1.0f - ay[0], ay[0] + (1.0f - ay[1]), ay[1] + (1.0f - ay[2]), ay[2]};
-        int32_t col[4];
-#pragma unroll
-        for (int c = 0; c < 4; c++) col[c] = cl(ix[0] + c);
         // each row's passing texels weighted by their column weights as they
         // are compared (a texel that fails adds +0: with no texel passing the
         // sum is exactly +0)
         float sum = 0.0f;
+        if (ix[0] >= 0 && iy[0] >= 0 && ix[0] <= (int32_t)S - 4 && iy[0] <= (int32_t)S - 4) {
+            // the window inside the map: no clamping, four consecutive texels a row
+            const float* row = map + (size_t)iy[0] * S + ix[0];
+#pragma unroll
+            for (int r = 0; r < 4; r++, row += S) {
+                const float w0 = ref < __ldg(row) ? cx[0] : 0.0f, w1 = ref < __ldg(row + 1) ? cx[1] : 0.0f;
+                const float w2 = ref < __ldg(row + 2) ? cx[2] : 0.0f, w3 = ref < __ldg(row + 3) ? cx[3] : 0.0f;
+                sum = __fmaf_rn((w0 + w1) + (w2 + w3), cy[r], sum);
+            }
+            return sum;
+        }
+        int32_t col[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) col[c] = cl(ix[0] + c);
 #pragma unroll
         for (int r = 0; r < 4; r++) {
             const float* row = map + (size_t)cl(iy[0] + r) * S;
