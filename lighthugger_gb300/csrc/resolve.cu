@@ -357,35 +357,60 @@ constexpr uint32_t kShareTris = 10;  // distinct triangles a warp row shares ver
 // The vertex stage of a warp's 32 pixels (called by all lanes).  Neighbouring
 // pixels mostly show one triangle (1.26 distinct triangles per 32-pixel row
 // on average in the large workload), so the distinct triangles' vertices are
-// computed once, one vertex per lane -- lanes 3k, 3k + 1, 3k + 2 for the
-// k-th distinct triangle -- into the warp's shared-memory slots (3 float4 a
-// vertex: p.xyz n.x | 1/w, projected x y | n.yz us vs), at a third of the vertex work of
-// every pixel computing its own three.  Returns the pixel's first slot, or
-// -1 when the row holds more than kShareTris distinct triangles (each pixel
-// then computes its own at use).
+// computed once, one vertex per lane -- lanes 3q, 3q + 1, 3q + 2 for the q-th
+// triangle to compute -- into the warp's shared-memory slots (3 float4 a
+// vertex: p.xyz n.x | 1/w, projected x y | n.yz us vs), at a third of the
+// vertex work of every pixel computing its own three.  The slots the warp's
+// previous row segment used (`prev`, one bit a slot; s_keys holds each
+// slot's triangle) are looked up first: a triangle that continues from the
+// previous 32 pixels of the row keeps its vertices, and a segment whose
+// triangles all continue computes none.  Returns the pixel's first vertex
+// slot, or -1 when the row holds more than kShareTris distinct triangles
+// (each pixel then computes its own at use; the slots stay as they were).
 __device__ __forceinline__ int32_t share_vertices(const FrameDev& f, bool covered, uint32_t packed, uint32_t* s_keys,
-                                                  float4* s_vert) {
+                                                  float4* s_vert, uint32_t& prev) {
     const uint32_t lane = threadIdx.x;
     const uint32_t key = covered ? packed : 0xFFFFFFFFu;
     const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
     const uint32_t leader = __ffs(peers) - 1;
-    const uint32_t leaders = __ballot_sync(0xFFFFFFFFu, covered && lane == leader);
-    const uint32_t n = __popc(leaders);
-    if (n > kShareTris) return -1;
-    const uint32_t rank = __popc(leaders & ((1u << leader) - 1u));  // the pixel's distinct-triangle index
-    if (covered && lane == leader) s_keys[rank] = packed;
-    __syncwarp();
-    if (lane < 3 * n) {
-        f3 p, nv;
-        ProjVertex c;
-        float us, vs;
-        load_vertex(f, s_keys[lane / 3], lane % 3, p, c, nv, us, vs);
-        s_vert[3 * lane] = make_float4(p.x, p.y, p.z, nv.x);
-        s_vert[3 * lane + 1] = make_float4(c.inv_w, c.n.x, c.n.y, 0.0f);
-        s_vert[3 * lane + 2] = make_float4(nv.y, nv.z, us, vs);
+    const bool lead = covered && lane == leader;
+    const uint32_t leaders = __ballot_sync(0xFFFFFFFFu, lead);
+    if (__popc(leaders) > kShareTris) return -1;
+    int32_t slot = -1;
+    for (uint32_t m = prev; m; m &= m - 1) {
+        const uint32_t i = __ffs(m) - 1;
+        if (s_keys[i] == key) slot = (int32_t)i;
     }
-    __syncwarp();
-    return (int32_t)(3 * rank);
+    const bool miss = lead && slot < 0;
+    const uint32_t hits = __reduce_or_sync(0xFFFFFFFFu, lead && slot >= 0 ? 1u << slot : 0u);
+    const uint32_t misses = __ballot_sync(0xFFFFFFFFu, miss);
+    uint32_t used = hits;
+    if (misses) {
+        // the new triangles take slots that hold none of this segment's
+        const uint32_t free = ~hits & ((1u << kShareTris) - 1u);
+        if (miss) slot = (int32_t)__fns(free, 0, __popc(misses & ((1u << lane) - 1u)) + 1);
+        used |= __reduce_or_sync(0xFFFFFFFFu, miss ? 1u << slot : 0u);
+        __syncwarp();  // every lane's lookup has read s_keys, every pixel of the last segment its slots
+        if (miss) s_keys[slot] = key;
+        const uint32_t n_new = __popc(misses), q = lane / 3;
+        const uint32_t src = q < n_new ? __fns(misses, 0, q + 1) : lane;
+        const uint32_t qkey = __shfl_sync(0xFFFFFFFFu, key, src);
+        const int32_t qslot = __shfl_sync(0xFFFFFFFFu, slot, src);
+        if (q < n_new) {
+            f3 p, nv;
+            ProjVertex c;
+            float us, vs;
+            const uint32_t k = lane - 3 * q, v = 3 * (uint32_t)qslot + k;
+            load_vertex(f, qkey, k, p, c, nv, us, vs);
+            s_vert[3 * v] = make_float4(p.x, p.y, p.z, nv.x);
+            s_vert[3 * v + 1] = make_float4(c.inv_w, c.n.x, c.n.y, 0.0f);
+            s_vert[3 * v + 2] = make_float4(nv.y, nv.z, us, vs);
+        }
+        __syncwarp();
+    }
+    prev = used;
+    slot = __shfl_sync(0xFFFFFFFFu, slot, leader);
+    return covered ? 3 * slot : 0;
 }
 
 // Vertex k of the pixel's triangle: from the warp's slots, or computed.
@@ -409,10 +434,11 @@ __device__ __forceinline__ void pixel_vertex(const FrameDev& f, const float4* s_
 // `s_uvs`: the block's shared copy of the 4 cascades' uv-space matrices.
 __device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uint32_t y, unsigned long long vis,
                                               bool in_view, long long* clock_slot, uint32_t* s_keys, float4* s_vert,
-                                              const lh_mat4* s_uvs) {
+                                              uint32_t& prev, const lh_mat4* s_uvs) {
     const Uniforms& u = *f.uniforms;
     if (in_view && u.debug == 4) *clock_slot = clock64();
-    const int32_t vbase = share_vertices(f, in_view && u2f((uint32_t)(vis >> 32)) != 0.0f, (uint32_t)vis, s_keys, s_vert);
+    const int32_t vbase =
+        share_vertices(f, in_view && u2f((uint32_t)(vis >> 32)) != 0.0f, (uint32_t)vis, s_keys, s_vert, prev);
     if (!in_view) return;
     const uint32_t W = u.window_size.x, H = u.window_size.y;
     const f2 ndc{(float)x / (float)W * 2.0f - 1.0f, (float)y / (float)H * 2.0f - 1.0f};
@@ -558,6 +584,7 @@ __global__ void __launch_bounds__(kResolveWarps * 32, LH_RESOLVE_MIN_BLOCKS)
         __syncwarp();
     }
     uint32_t k = 0;
+    uint32_t prev_slots = 0;  // the vertex slots of the warp's last row segment
     for (uint32_t t = blockIdx.x; t < n_strips; t += gridDim.x, k++) {
         int32_t x0, y;
         if (!row_of(t, x0, y)) continue;  // below the image (last strip row): no load was issued
@@ -587,7 +614,8 @@ __global__ void __launch_bounds__(kResolveWarps * 32, LH_RESOLVE_MIN_BLOCKS)
                 !in_view ? 0ull
                          : kTma ? vis_buf[st][32 * j + lane]
                                 : __ldcs(reinterpret_cast<const unsigned long long*>(f.visibility) + (size_t)y * W + x);
-            resolve_pixel(f, x, (uint32_t)y, vis, in_view, &s_clock[warp][lane], s_keys[warp], s_vert[warp], s_uvs);
+            resolve_pixel(f, x, (uint32_t)y, vis, in_view, &s_clock[warp][lane], s_keys[warp], s_vert[warp], prev_slots,
+                          s_uvs);
         }
         if (kTma) {
             __syncwarp();  // stage st is free again; the other stage's strip is already in flight
