@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cstring>
 
+#include "exact_div.cuh"
 #include "frame_phases.cuh"
 #include "tma.cuh"
 
@@ -431,17 +432,20 @@ __device__ __forceinline__ void pixel_vertex(const FrameDev& f, const float4* s_
 // `clock_slot`: the thread's shared-memory word for the clock view's start
 // time (kept out of registers).  Called by all lanes of the warp (the vertex
 // stage is a warp collective); `in_view` false for lanes past the image.
-// `s_uvs`: the block's shared copy of the 4 cascades' uv-space matrices.
+// `s_uvs`: the block's shared copy of the 4 cascades' uv-space matrices;
+// `rcp_w`: 1 / window width; `ndc_y`: the row's y / H * 2 - 1.
 __device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uint32_t y, unsigned long long vis,
                                               bool in_view, long long* clock_slot, uint32_t* s_keys, float4* s_vert,
-                                              uint32_t& prev, const lh_mat4* s_uvs) {
+                                              uint32_t& prev, const lh_mat4* s_uvs, float rcp_w, float ndc_y) {
     const Uniforms& u = *f.uniforms;
     if (in_view && u.debug == 4) *clock_slot = clock64();
     const int32_t vbase =
         share_vertices(f, in_view && u2f((uint32_t)(vis >> 32)) != 0.0f, (uint32_t)vis, s_keys, s_vert, prev);
     if (!in_view) return;
     const uint32_t W = u.window_size.x, H = u.window_size.y;
-    const f2 ndc{(float)x / (float)W * 2.0f - 1.0f, (float)y / (float)H * 2.0f - 1.0f};
+    // x / W * 2 - 1 with the quotient from the reciprocal (the same bits)
+    const float qx = W <= (uint32_t)kExactDivMaxCount ? div_by_count((float)x, (float)W, rcp_w) : (float)x / (float)W;
+    const f2 ndc{qx * 2.0f - 1.0f, ndc_y};
     const size_t pix = (size_t)y * W + x;
     if (u2f((uint32_t)(vis >> 32)) == 0.0f) {
         f4 un = mul(u.perspective_inverse, f4{ndc.x, ndc.y, 0.0f, 1.0f});
@@ -585,6 +589,7 @@ __global__ void __launch_bounds__(kResolveWarps * 32, LH_RESOLVE_MIN_BLOCKS)
     }
     uint32_t k = 0;
     uint32_t prev_slots = 0;  // the vertex slots of the warp's last row segment
+    const float rcp_w = 1.0f / (float)W;
     for (uint32_t t = blockIdx.x; t < n_strips; t += gridDim.x, k++) {
         int32_t x0, y;
         if (!row_of(t, x0, y)) continue;  // below the image (last strip row): no load was issued
@@ -606,6 +611,7 @@ __global__ void __launch_bounds__(kResolveWarps * 32, LH_RESOLVE_MIN_BLOCKS)
                 break;
             }
         }
+        const float ndc_y = (float)y / (float)H * 2.0f - 1.0f;
 #pragma unroll 1
         for (uint32_t j = 0; j < kStripCols / 32; j++) {
             const uint32_t x = (uint32_t)x0 + 32 * j + lane;
@@ -615,7 +621,7 @@ __global__ void __launch_bounds__(kResolveWarps * 32, LH_RESOLVE_MIN_BLOCKS)
                          : kTma ? vis_buf[st][32 * j + lane]
                                 : __ldcs(reinterpret_cast<const unsigned long long*>(f.visibility) + (size_t)y * W + x);
             resolve_pixel(f, x, (uint32_t)y, vis, in_view, &s_clock[warp][lane], s_keys[warp], s_vert[warp], prev_slots,
-                          s_uvs);
+                          s_uvs, rcp_w, ndc_y);
         }
         if (kTma) {
             __syncwarp();  // stage st is free again; the other stage's strip is already in flight
