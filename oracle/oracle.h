@@ -12,7 +12,9 @@
  * built or run here (no Vulkan, glslc or graphics stack, empty submodules).
  * The oracle is pinned instead by hand-derived known-answer tests
  * (tests/test_oracle_known_answers.py) and by its float64 twin of the
- * resolve (lho_resolve_f64).
+ * resolve (lho_resolve_f64); its outputs on four seeded scenes are held
+ * fixed by the golden digests of tests/golden/oracle_frames.json
+ * (tests/test_golden.py).
  *
  * Evaluation-order contract (shared with the CUDA kernels so that integer,
  * visibility and depth results can be bit exact): every float operation is a
