@@ -92,8 +92,10 @@ __device__ float pcf9(const FrameDev& f, float sx, float sy, float layer_f, floa
     int32_t ix[3], iy[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        float u = (sx + (float)(k - 1) / 1024.0f) * (float)S - 0.5f;
-        float v = (sy + (float)(k - 1) / 1024.0f) * (float)S - 0.5f;
+        // (the middle tap's offset is +0: sx + 0 only turns -0 into +0, which
+        // gives the same u)
+        float u = (k == 1 ? sx : sx + (float)(k - 1) / 1024.0f) * (float)S - 0.5f;
+        float v = (k == 1 ? sy : sy + (float)(k - 1) / 1024.0f) * (float)S - 0.5f;
         if (!(fabsf(u) < 1e9f)) u = 0.0f;
         if (!(fabsf(v) < 1e9f)) v = 0.0f;
         const float fu = floorf(u), fv = floorf(v);
@@ -489,12 +491,25 @@ __device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uin
     float roughness = mr.g, metallic = mr.b;
     if (mi.normal_tex != UNUSED_TEXTURE_INDEX)
         normal = apply_normal_map(f, mi.normal_tex, uv, PV, pa, pb, pc, us, vs, ndc, f2{(float)W, (float)H}, normal);
+    // the first cascade whose uv square holds the point (x and y of each
+    // tried cascade, then z and w of the one taken -- the last tried when none
+    // holds it -- in mul's operation order: the same values as the full
+    // product per cascade)
     uint32_t ci;
+    const f4 wp{world.x, world.y, world.z, 1.0f};
     f4 sc{0.0f, 0.0f, 0.0f, 0.0f};
     for (ci = 0; ci < 4; ci++) {
-        sc = mul(s_uvs[ci], f4{world.x, world.y, world.z, 1.0f});
+        const lh_vec4 &c0 = s_uvs[ci].cols[0], &c1 = s_uvs[ci].cols[1], &c2 = s_uvs[ci].cols[2],
+                      &c3 = s_uvs[ci].cols[3];
+        sc.x = ((c0.x * wp.x + c1.x * wp.y) + c2.x * wp.z) + c3.x * wp.w;
+        sc.y = ((c0.y * wp.x + c1.y * wp.y) + c2.y * wp.z) + c3.y * wp.w;
         float ox = sc.x - 0.5f, oy = sc.y - 0.5f;
         if (fabsf(ox) < 0.5f && fabsf(oy) < 0.5f) break;
+    }
+    {
+        const lh_mat4& m = s_uvs[ci < 4 ? ci : 3];
+        sc.z = ((m.cols[0].z * wp.x + m.cols[1].z * wp.y) + m.cols[2].z * wp.z) + m.cols[3].z * wp.w;
+        sc.w = ((m.cols[0].w * wp.x + m.cols[1].w * wp.y) + m.cols[2].w * wp.z) + m.cols[3].w * wp.w;
     }
     const bool alpha = (flags & MESH_INFO_FLAGS_ALPHA_CLIP) != 0;
     const float bias = alpha ? 0.000002f : 0.0f;
@@ -502,7 +517,7 @@ __device__ __forceinline__ void resolve_pixel(const FrameDev& f, uint32_t x, uin
     // and x / 1 = x: the perspective divide only runs when it can change a bit
     if (sc.w != 1.0f) sc = f4{sc.x / sc.w, sc.y / sc.w, sc.z / sc.w, sc.w / sc.w};
     float shadow_sum = pcf9(f, sc.x, sc.y, (float)ci, sc.z - bias);
-    shadow_sum /= 9.0f;
+    shadow_sum = div_by_count(shadow_sum, 9.0f, 1.0f / 9.0f);  // shadow_sum / 9, the same bits
     if (sc.z > 1.0f) shadow_sum = 1.0f;
     // AMBIENT_SH (render_geometry.comp:40-57): only sh[0] = sh[2] = 0.025.
     if (u.debug != 0 && u.debug != 4) {

@@ -50,12 +50,13 @@ def test_sphere_box_skips_only_meshlets_without_pixel_centres():
 
 def test_column_quotient_from_the_reciprocal_is_the_ieee_quotient():
     """lighthugger_gb300/csrc/exact_div.cuh (the resolve's x / W from 1 / W
-    with Markstein's correction step) against the IEEE quotient for every
-    0 <= x <= W <= 16384, host-compiled."""
+    and its PCF sum / 9, with Markstein's correction step) against the IEEE
+    quotient for every 0 <= x <= W <= 16384 and every float in [0, 9] over
+    9, host-compiled."""
     src = os.path.join(ROOT, "tests", "native", "exact_div_check.cpp")
     with tempfile.TemporaryDirectory() as d:
         exe = os.path.join(d, "exact_div_check")
-        subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I",
+        subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-pthread", "-I",
                         os.path.join(ROOT, "lighthugger_gb300", "csrc"), src, "-o", exe], check=True)
         r = subprocess.run([exe], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
