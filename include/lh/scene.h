@@ -92,6 +92,19 @@ lh_status lh_scene_mesh_get(const lh_scene* scene, uint32_t index, lh_scene_mesh
 /* MeshInfo record index of every instance (out: n_instances entries). */
 lh_status lh_scene_instance_records(const lh_scene* scene, uint32_t* out);
 
+/* Scene dumps: a flat binary file of a scene's host copy -- the meshes'
+ * vertex, index, micro-index and Meshlet buffers, the MeshInfo and Instance
+ * records in their shared layouts (address fields stored as zero and
+ * relinked at load), the texel arrays, the camera and probe Uniforms -- so
+ * that a frame can be replayed from a file (by the oracle, or on the GPU
+ * after lh_scene_upload).  The file is in the host's byte order.
+ * lh_scene_load returns LH_ERR_INVALID_ARGUMENT for a file that is not a
+ * complete dump (wrong magic or version, truncated, an index out of range)
+ * and LH_ERR_UNSUPPORTED when the file cannot be opened; lh_scene_save
+ * returns LH_ERR_UNSUPPORTED when it cannot be written. */
+lh_status lh_scene_save(const lh_scene* scene, const char* path);
+lh_status lh_scene_load(const char* path, lh_scene** out);
+
 /* Camera as the reference's CameraParams (src/input.h:18-49) plus the
  * window; fov in degrees. */
 typedef struct lh_camera {

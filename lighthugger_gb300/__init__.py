@@ -168,6 +168,8 @@ def lib():
     L.lh_scene_create.argtypes = [C.c_uint32, C.c_uint64, C.POINTER(SceneParams), C.POINTER(P)]
     L.lh_scene_describe.argtypes = [P, C.POINTER(SceneDesc)]
     L.lh_scene_upload.argtypes = [P, C.c_int]
+    L.lh_scene_save.argtypes = [P, C.c_char_p]
+    L.lh_scene_load.argtypes = [C.c_char_p, C.POINTER(P)]
     L.lh_scene_destroy.argtypes = [P]
     L.lh_scene_destroy.restype = None
     L.lh_make_uniforms.argtypes = [C.POINTER(Camera), C.POINTER(Uniforms)]
@@ -178,7 +180,7 @@ def lib():
                                         C.POINTER(C.c_uint32)]
     for name in ("lh_create", "lh_set_scene", "lh_frame", "lh_frame_batched", "lh_frame_graph", "lh_get_outputs",
                  "lh_read_status",
-                 "lh_download", "lh_resolve_backward", "lh_frame_graph_backward", "lh_display_transform", "lh_set_profiling", "lh_get_stage_times", "lh_set_tuning", "lh_get_tuning", "lh_scene_create", "lh_scene_describe",
+                 "lh_download", "lh_resolve_backward", "lh_frame_graph_backward", "lh_display_transform", "lh_set_profiling", "lh_get_stage_times", "lh_set_tuning", "lh_get_tuning", "lh_scene_create", "lh_scene_describe", "lh_scene_save", "lh_scene_load",
                  "lh_scene_upload", "lh_make_uniforms", "lh_cull_instances_noalloc", "lh_check_bounded_wait",
                  "lh_get_texture_linear", "lh_probe_red_u64"):
         getattr(L, name).restype = C.c_int32
@@ -235,6 +237,23 @@ class Scene:
         self.handle = h
         self.params = {}
         self._describe()
+        return self
+
+    def save(self, path):
+        """Write the scene's host copy to a dump file (lh_scene_save)."""
+        _check(lib().lh_scene_save(self.handle, os.fsencode(path)), "lh_scene_save")
+
+    @classmethod
+    def load(cls, path):
+        """A scene read back from a dump file (lh_scene_load)."""
+        h = C.c_void_p()
+        _check(lib().lh_scene_load(os.fsencode(path), C.byref(h)), "lh_scene_load")
+        self = cls.__new__(cls)
+        self.handle = h
+        self.params = {}
+        self._describe()
+        self.config_id = self.desc.config_id
+        self.seed = self.desc.seed
         return self
 
     def _describe(self):

@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -885,6 +886,90 @@ static lh_status upload(lh_scene* s, const T* src, size_t bytes, uint64_t* out) 
 
 }  // namespace
 
+namespace {
+
+// ------------------------------------------------------------ scene dumps
+constexpr char kDumpMagic[8] = {'L', 'H', 'S', 'C', 'E', 'N', 'E', '\0'};
+constexpr uint32_t kDumpVersion = 1;
+
+struct DumpWriter {
+    std::vector<uint8_t> out;
+    void bytes(const void* p, size_t n) {
+        if (n) out.insert(out.end(), static_cast<const uint8_t*>(p), static_cast<const uint8_t*>(p) + n);
+    }
+    template <class T>
+    void pod(const T& v) { bytes(&v, sizeof(T)); }
+    void blob(const std::vector<uint8_t>& v) {
+        pod((uint64_t)v.size());
+        bytes(v.data(), v.size());
+    }
+};
+
+// Reads from a byte range; the first read past its end clears `ok` and every
+// later read then fails too.
+struct DumpReader {
+    const uint8_t* p;
+    size_t left;
+    bool ok = true;
+    bool bytes(void* dst, size_t n) {
+        if (!ok || n > left) return ok = false;
+        if (n) std::memcpy(dst, p, n);
+        p += n;
+        left -= n;
+        return true;
+    }
+    template <class T>
+    bool pod(T& v) { return bytes(&v, sizeof(T)); }
+    bool blob(std::vector<uint8_t>& v) {
+        uint64_t n = 0;
+        if (!pod(n) || n > left) return ok = false;
+        v.resize((size_t)n);
+        return bytes(v.data(), (size_t)n);
+    }
+    template <class T>
+    bool array(std::vector<T>& v, uint64_t n) {
+        if (!ok || n > left / sizeof(T)) return ok = false;
+        v.resize((size_t)n);
+        return bytes(v.data(), (size_t)n * sizeof(T));
+    }
+};
+
+// Every read a mesh's meshlets lead to stays inside its buffers: attribute
+// buffers hold n_vertices entries in the mesh's format, every index names a
+// vertex, every meshlet's index and micro-index ranges lie in their arrays
+// and its micro-indices name its own vertices.
+static bool dump_mesh_consistent(const BuiltMesh& m) {
+    const bool fp32 = (m.flags & MESH_INFO_FLAGS_FP32_VERTICES) != 0;
+    const bool idx32 = (m.flags & MESH_INFO_FLAGS_32_BIT_INDICES) != 0;
+    const uint64_t nv = m.n_vertices;
+    if (m.positions.size() < nv * (fp32 ? 12u : 6u) || m.normals.size() < nv * (fp32 ? 12u : 3u) ||
+        m.uvs.size() < nv * (fp32 ? 8u : 4u))
+        return false;
+    const size_t isz = idx32 ? 4u : 2u;
+    if (m.indices.size() % isz != 0 || m.meshlets.size() > 0xFFFFu) return false;
+    const size_t n_idx = m.indices.size() / isz;
+    for (size_t i = 0; i < n_idx; i++) {
+        uint32_t v = 0;
+        if (idx32) {
+            std::memcpy(&v, &m.indices[i * 4], 4);
+        } else {
+            uint16_t h;
+            std::memcpy(&h, &m.indices[i * 2], 2);
+            v = h;
+        }
+        if (v >= nv) return false;
+    }
+    for (const Meshlet& ml : m.meshlets) {
+        if ((uint64_t)ml.index_offset + ml.index_count > n_idx) return false;
+        if ((uint64_t)ml.triangle_offset + 3u * ml.triangle_count > m.micro.size()) return false;
+        for (uint32_t k = 0; k < 3u * ml.triangle_count; k++)
+            if (m.micro[ml.triangle_offset + k] >= ml.index_count) return false;
+    }
+    return true;
+}
+
+}  // namespace
+
 extern "C" {
 
 lh_status lh_make_uniforms(const lh_camera* c, Uniforms* out) {
@@ -1115,6 +1200,151 @@ lh_status lh_scene_mesh_get(const lh_scene* s, uint32_t i, lh_scene_mesh* out) {
 lh_status lh_scene_instance_records(const lh_scene* s, uint32_t* out) {
     if (!s || !out) return LH_ERR_INVALID_ARGUMENT;
     for (size_t i = 0; i < s->instance_info.size(); i++) out[i] = s->instance_info[i];
+    return LH_OK;
+}
+
+lh_status lh_scene_save(const lh_scene* s, const char* path) {
+    if (!s || !path) return LH_ERR_INVALID_ARGUMENT;
+    DumpWriter w;
+    w.bytes(kDumpMagic, sizeof(kDumpMagic));
+    w.pod(kDumpVersion);
+    w.pod((uint32_t)0);
+    w.pod(s->config_id);
+    w.pod(s->width);
+    w.pod(s->height);
+    w.pod(s->shadow_size);
+    w.pod(s->seed);
+    w.pod(s->uniforms);
+    w.pod((uint32_t)s->probes.size());
+    for (const Uniforms& u : s->probes) w.pod(u);
+    w.pod((uint32_t)s->meshes.size());
+    for (const BuiltMesh& m : s->meshes) {
+        w.pod(m.flags);
+        w.pod(m.n_vertices);
+        w.pod(m.n_triangles);
+        w.bytes(m.bounding_sphere, sizeof(m.bounding_sphere));
+        w.bytes(m.tex_scale, sizeof(m.tex_scale));
+        w.bytes(m.dequant.m, sizeof(m.dequant.m));
+        w.blob(m.positions);
+        w.blob(m.normals);
+        w.blob(m.uvs);
+        w.blob(m.indices);
+        w.blob(m.micro);
+        w.pod((uint64_t)m.meshlets.size());
+        w.bytes(m.meshlets.data(), m.meshlets.size() * sizeof(Meshlet));
+    }
+    w.pod((uint32_t)s->host_infos.size());
+    for (size_t i = 0; i < s->host_infos.size(); i++) {
+        MeshInfo mi = s->host_infos[i];
+        mi.positions = mi.indices = mi.normals = mi.uvs = mi.micro_indices = mi.meshlets = 0;
+        w.pod(mi);
+        w.pod(s->info_mesh[i]);
+    }
+    w.pod((uint32_t)s->textures.size());
+    for (const TextureData& t : s->textures) {
+        w.pod(t.w);
+        w.pod(t.h);
+        w.pod(t.srgb);
+        w.blob(t.texels);
+    }
+    w.pod((uint32_t)s->host_instances.size());
+    for (size_t i = 0; i < s->host_instances.size(); i++) {
+        Instance inst = s->host_instances[i];
+        inst.mesh_info_address = 0;
+        w.pod(inst);
+        w.pod(s->instance_info[i]);
+    }
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return LH_ERR_UNSUPPORTED;
+    const bool wrote = std::fwrite(w.out.data(), 1, w.out.size(), f) == w.out.size();
+    return std::fclose(f) == 0 && wrote ? LH_OK : LH_ERR_UNSUPPORTED;
+}
+
+lh_status lh_scene_load(const char* path, lh_scene** out) {
+    if (!path || !out) return LH_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    std::vector<uint8_t> file;
+    {
+        FILE* f = std::fopen(path, "rb");
+        if (!f) return LH_ERR_UNSUPPORTED;
+        uint8_t chunk[1 << 16];
+        size_t n;
+        while ((n = std::fread(chunk, 1, sizeof(chunk), f)) > 0) file.insert(file.end(), chunk, chunk + n);
+        const bool failed = std::ferror(f) != 0;
+        std::fclose(f);
+        if (failed) return LH_ERR_UNSUPPORTED;
+    }
+    DumpReader r{file.data(), file.size()};
+    char magic[sizeof(kDumpMagic)];
+    uint32_t version = 0, reserved = 0;
+    if (!r.bytes(magic, sizeof(magic)) || std::memcmp(magic, kDumpMagic, sizeof(magic)) != 0 || !r.pod(version) ||
+        version != kDumpVersion || !r.pod(reserved))
+        return LH_ERR_INVALID_ARGUMENT;
+    std::unique_ptr<lh_scene> s(new (std::nothrow) lh_scene());
+    if (!s) return LH_ERR_OUT_OF_MEMORY;
+    uint32_t n_probes = 0, n_meshes = 0, n_infos = 0, n_textures = 0, n_instances = 0;
+    r.pod(s->config_id);
+    r.pod(s->width);
+    r.pod(s->height);
+    r.pod(s->shadow_size);
+    r.pod(s->seed);
+    r.pod(s->uniforms);
+    r.pod(n_probes);
+    r.array(s->probes, n_probes);
+    r.pod(n_meshes);
+    if (!r.ok || n_meshes > r.left) return LH_ERR_INVALID_ARGUMENT;
+    s->meshes.resize(n_meshes);
+    for (BuiltMesh& m : s->meshes) {
+        uint64_t n_meshlets = 0;
+        r.pod(m.flags);
+        r.pod(m.n_vertices);
+        r.pod(m.n_triangles);
+        r.bytes(m.bounding_sphere, sizeof(m.bounding_sphere));
+        r.bytes(m.tex_scale, sizeof(m.tex_scale));
+        r.bytes(m.dequant.m, sizeof(m.dequant.m));
+        r.blob(m.positions);
+        r.blob(m.normals);
+        r.blob(m.uvs);
+        r.blob(m.indices);
+        r.blob(m.micro);
+        r.pod(n_meshlets);
+        r.array(m.meshlets, n_meshlets);
+        if (!r.ok || !dump_mesh_consistent(m)) return LH_ERR_INVALID_ARGUMENT;
+    }
+    r.pod(n_infos);
+    if (!r.ok || n_infos > r.left / (sizeof(MeshInfo) + 4)) return LH_ERR_INVALID_ARGUMENT;
+    s->host_infos.resize(n_infos);
+    s->info_mesh.resize(n_infos);
+    for (uint32_t i = 0; i < n_infos; i++) {
+        r.pod(s->host_infos[i]);
+        r.pod(s->info_mesh[i]);
+        if (!r.ok || s->info_mesh[i] >= n_meshes ||
+            s->host_infos[i].num_meshlets > s->meshes[s->info_mesh[i]].meshlets.size() ||
+            (s->host_infos[i].flags & ~MESH_INFO_FLAGS_ALPHA_CLIP) != s->meshes[s->info_mesh[i]].flags)
+            return LH_ERR_INVALID_ARGUMENT;
+    }
+    r.pod(n_textures);
+    if (!r.ok || n_textures > r.left) return LH_ERR_INVALID_ARGUMENT;
+    s->textures.resize(n_textures);
+    for (TextureData& t : s->textures) {
+        r.pod(t.w);
+        r.pod(t.h);
+        r.pod(t.srgb);
+        r.blob(t.texels);
+        if (!r.ok || t.w == 0 || t.h == 0 || (uint64_t)t.w * t.h * 4 != t.texels.size()) return LH_ERR_INVALID_ARGUMENT;
+    }
+    r.pod(n_instances);
+    if (!r.ok || n_instances > r.left / (sizeof(Instance) + 4)) return LH_ERR_INVALID_ARGUMENT;
+    s->host_instances.resize(n_instances);
+    s->instance_info.resize(n_instances);
+    for (uint32_t i = 0; i < n_instances; i++) {
+        r.pod(s->host_instances[i]);
+        r.pod(s->instance_info[i]);
+        if (!r.ok || s->instance_info[i] >= n_infos) return LH_ERR_INVALID_ARGUMENT;
+    }
+    if (!r.ok || r.left != 0) return LH_ERR_INVALID_ARGUMENT;
+    finish_infos(s.get());
+    *out = s.release();
     return LH_OK;
 }
 

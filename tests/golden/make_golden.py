@@ -85,9 +85,13 @@ def instances_digest(scene):
 
 
 def frame_digest(config_id, params):
-    """The oracle's frame of the scene, digested."""
+    """The oracle's frame of the config's scene, digested."""
+    return scene_digest(make_scene(config_id, params), config_id, params)
+
+
+def scene_digest(scene, config_id, params):
+    """The oracle's frame of `scene`, digested."""
     from oracle import binding as ob
-    scene = make_scene(config_id, params)
     d = scene.desc
     cap = max(1024, d.n_instances)
     fr = ob.run_scene(scene, max_instances=cap, max_draws=MAX_DRAWS)
