@@ -39,3 +39,24 @@ def test_reference_arm_other_ranks_exit_quietly():
     r = _run({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"})
     assert r.returncode == 0
     assert not [l for l in r.stdout.splitlines() if l.startswith("{")]
+
+
+def test_roofline_traffic_comes_from_the_committed_capture():
+    """The roofline's DRAM traffic is read from profiles/dram_bytes_c2_frame.txt
+    (never measured in the bench): the sum of the stage's kernels' read and
+    write bytes, the alpha-clip kernels only for a scene that has them, with
+    the capture's provenance line."""
+    sys.path.insert(0, ROOT)
+    import bench
+    per = {}
+    with open(bench.TRAFFIC_FILE) as f:
+        for line in f:
+            if line.strip() and not line.startswith("#"):
+                name, rd, wr = line.rsplit(None, 2)
+                per[name.strip()] = per.get(name.strip(), 0.0) + float(rd) + float(wr)
+    opaque, src = bench.committed_traffic("raster")
+    with_alpha, _ = bench.committed_traffic("raster", True)
+    want = sum(v for k, v in per.items() if k in bench.STAGE_KERNELS["raster"] and "alpha" not in k)
+    assert opaque == want and with_alpha == want + per.get("k_raster_alpha<0>", 0.0)
+    assert src.startswith("profiles/dram_bytes_c2_frame.txt: capture: commit")
+    assert bench.committed_traffic("no_such_stage") == (None, None)
